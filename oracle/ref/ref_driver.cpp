@@ -1,0 +1,469 @@
+// Reference-build driver for the oracle (TEST INFRASTRUCTURE ONLY).
+//
+// This translation unit is compiled together with the reference's own
+// sources (src/VX3/VX3_{Link,Voxel,Collision,Material,MaterialVoxel,
+// MaterialLink,External}.cu as host C++, plus src/old and src/VXA for the
+// VXA import path) by oracle/Makefile into oracle/_ref/libvx3ref.so.  It is
+// only used to generate golden fixtures (tests/golden/) and to pin the C
+// restatement in oracle/vx3_oracle.c; nothing shipped calls it.
+//
+// What lives here is the part of the reference that cannot be compiled on
+// the host as-is, restated call for call:
+//  * VX3_VoxelyzeKernel(CVX_Sim*) host constructor (src/VX3/VX3_VoxelyzeKernel.cu:27-105)
+//  * doTimeStep's child-kernel sequence, run as serial loops
+//    (src/VX3/VX3_VoxelyzeKernel.cu:237-359, kernels at :566-650, :682-727, :833-843)
+//  * recommendedTimeStep (:184-217), regenerateSurfaceVoxels (:495-513),
+//    updateCurrentCenterOfMass (:477-493), is_neighbor (:651-680)
+//  * the VXA read of src/VX3/VX3_SimulationManager.cu:298-308
+// Every physics function called below (VX3_Link::updateForces,
+// VX3_Voxel::timeStep, VX3_Collision::updateContactForce, ...) is the
+// reference's own code.
+//
+// Deviation (documented): the reference probes ONE random link per step for
+// strain > 100 (VX3_VoxelyzeKernel.cu:271-281); this driver checks every link,
+// which is what the GB300 kernels do as well.
+
+#include "VX3_VoxelyzeKernel.cuh"
+#include "VX3_MemoryCleaner.h"
+#include "VX_Sim.h"
+#include "XML_Rip.h"
+
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+
+// globals declared extern by src/old/VX3_MemoryCleaner.h
+bool VX3_MemoryCleaner_running = false;
+boost::mutex MemoryCleaner_mutex;
+std::vector<void *> MemoryCleaner_toBeFreedCUDAPointer;
+
+// Runtime link creation (attach) is out of scope; the reference's device-side
+// VX3_Link constructor references this member, so it must resolve.  It is
+// never reached because attach is disabled in every oracle run.
+VX3_MaterialLink *VX3_VoxelyzeKernel::combinedMaterial(VX3_MaterialVoxel *, VX3_MaterialVoxel *) { return NULL; }
+
+namespace {
+
+struct RefSim {
+    CVX_Environment env;
+    CVX_Object obj;
+    CVX_Sim sim;
+    VX3_VoxelyzeKernel *k = nullptr;
+    std::vector<VX3_Voxel *> surface;        // d_surface_voxels
+    std::vector<double> last_contact;        // contact force per voxel captured before the voxel pass
+    float last_dt = 0.0f;
+    int steps_done = 0;
+    bool diverged = false;
+};
+
+// VX3_VoxelyzeKernel.cu:27-105, restated with the public CVoxelyze accessors.
+void build_kernel(RefSim &S) {
+    CVoxelyze &Vx = S.sim.Vx;
+    VX3_VoxelyzeKernel *k = new VX3_VoxelyzeKernel();
+    S.k = k;
+    k->voxSize = Vx.voxelSize();
+
+    k->num_d_voxelMats = Vx.materialCount();
+    VcudaMalloc((void **)&k->d_voxelMats, k->num_d_voxelMats * sizeof(VX3_MaterialVoxel));
+    for (int i = 0; i < k->num_d_voxelMats; i++) k->h_voxelMats.push_back((CVX_MaterialVoxel *)Vx.material(i));
+    for (int i = 0; i < k->num_d_voxelMats; i++) {
+        VX3_MaterialVoxel tmp(k->h_voxelMats[i], k);
+        VcudaMemcpy(k->d_voxelMats + i, &tmp, sizeof(VX3_MaterialVoxel), VcudaMemcpyHostToDevice);
+    }
+
+    // link materials in order of first use by the link list
+    std::vector<CVX_MaterialLink *> lmats;
+    for (int i = 0; i < Vx.linkCount(); i++) {
+        CVX_MaterialLink *m = Vx.link(i)->mat;
+        bool seen = false;
+        for (auto *q : lmats) seen |= (q == m);
+        if (!seen) lmats.push_back(m);
+    }
+    k->num_d_linkMats = (int)lmats.size();
+    VcudaMalloc((void **)&k->d_linkMats, (k->num_d_linkMats ? k->num_d_linkMats : 1) * sizeof(VX3_MaterialLink));
+    for (int i = 0; i < k->num_d_linkMats; i++) {
+        VX3_MaterialLink tmp(lmats[i], k);
+        VcudaMemcpy(k->d_linkMats + i, &tmp, sizeof(VX3_MaterialLink), VcudaMemcpyHostToDevice);
+        k->h_linkMats.push_back(lmats[i]);
+    }
+
+    k->num_d_voxels = Vx.voxelCount();
+    VcudaMalloc((void **)&k->d_voxels, (k->num_d_voxels ? k->num_d_voxels : 1) * sizeof(VX3_Voxel));
+    for (int i = 0; i < k->num_d_voxels; i++) {
+        k->h_voxels.push_back(Vx.voxel(i));
+        k->h_lookup_voxels[Vx.voxel(i)] = k->d_voxels + i;
+    }
+    k->num_d_links = Vx.linkCount();
+    VcudaMalloc((void **)&k->d_links, (k->num_d_links ? k->num_d_links : 1) * sizeof(VX3_Link));
+    for (int i = 0; i < k->num_d_links; i++) {
+        VX3_Link tmp(Vx.link(i), k);
+        memcpy((void *)(k->d_links + i), (void *)&tmp, sizeof(VX3_Link));
+        k->h_links.push_back(Vx.link(i));
+        k->h_lookup_links[Vx.link(i)] = k->d_links + i;
+    }
+    for (int i = 0; i < k->num_d_voxels; i++) {
+        VX3_Voxel tmp(Vx.voxel(i), k);
+        memcpy((void *)(k->d_voxels + i), (void *)&tmp, sizeof(VX3_Voxel));
+        tmp.ext = NULL; // ownership moved to the array copy
+    }
+    k->DtFrac = S.sim.DtFrac;
+    k->TempEnabled = S.sim.pEnv->IsTempEnabled();
+    k->VaryTempEnabled = S.sim.pEnv->IsTempVaryEnabled();
+    k->TempBase = S.sim.pEnv->GetTempBase();
+    k->TempAmplitude = S.sim.pEnv->GetTempAmplitude();
+    k->TempPeriod = S.sim.pEnv->GetTempPeriod();
+    k->d_surface_voxels = NULL;
+
+    // CUDA_Simulation prologue (VX3_SimulationManager.cu:20-23): device vectors
+    for (int i = 0; i < k->num_d_voxelMats; i++) k->d_voxelMats[i].syncVectors();
+    for (int i = 0; i < k->num_d_linkMats; i++) k->d_linkMats[i].syncVectors();
+    for (int i = 0; i < k->num_d_voxels; i++) k->d_voxels[i].syncVectors();
+    k->currentTime = 0.0;
+    k->OptimalDt = 0.0;
+    k->CurStepCount = 0;
+    k->isSurfaceChanged = true;
+}
+
+// VX3_VoxelyzeKernel.cu:184-217
+double recommended_dt(VX3_VoxelyzeKernel *k) {
+    double MaxFreq2 = 0.0f;
+    for (int i = 0; i < k->num_d_links; i++) {
+        VX3_Link *pL = k->d_links + i;
+        double m1 = pL->pVNeg->mat->mass(), m2 = pL->pVPos->mat->mass();
+        double thisMaxFreq2 = pL->axialStiffness() / (m1 < m2 ? m1 : m2);
+        if (thisMaxFreq2 > MaxFreq2) MaxFreq2 = thisMaxFreq2;
+    }
+    if (MaxFreq2 <= 0.0f) {
+        for (int i = 0; i < k->num_d_voxels; i++) {
+            double thisMaxFreq2 = k->d_voxels[i].mat->youngsModulus() * k->d_voxels[i].mat->nomSize / k->d_voxels[i].mat->mass();
+            if (thisMaxFreq2 > MaxFreq2) MaxFreq2 = thisMaxFreq2;
+        }
+    }
+    if (MaxFreq2 <= 0.0f) return 0.0f;
+    return 1.0f / (6.283185f * sqrt(MaxFreq2));
+}
+
+// VX3_VoxelyzeKernel.cu:495-513
+void regenerate_surface(RefSim &S) {
+    VX3_VoxelyzeKernel *k = S.k;
+    S.surface.clear();
+    for (int i = 0; i < k->num_d_voxels; i++) {
+        k->d_voxels[i].updateSurface();
+        if (k->d_voxels[i].isSurface() && !k->d_voxels[i].removed) S.surface.push_back(&k->d_voxels[i]);
+    }
+}
+
+// VX3_VoxelyzeKernel.cu:651-680
+bool is_neighbor(VX3_Voxel *voxel1, VX3_Voxel *voxel2, VX3_Link *incoming_link, int depth) {
+    if (voxel1 == voxel2) return true;
+    if (depth <= 0) return false;
+    for (int i = 0; i < 6; i++) {
+        VX3_Link *L = voxel1->links[i];
+        if (L && L != incoming_link) {
+            VX3_Voxel *other = (L->pVNeg == voxel1) ? L->pVPos : L->pVNeg;
+            if (is_neighbor(other, voxel2, L, depth - 1)) return true;
+        }
+    }
+    return false;
+}
+
+// collision half of handle_collision_attachment (VX3_VoxelyzeKernel.cu:682-727)
+void collide_pair(VX3_Voxel *voxel1, VX3_Voxel *voxel2, VX3_VoxelyzeKernel *k) {
+    if (voxel1->mat->fixed && voxel2->mat->fixed) return;
+    VX3_Vec3D<double> diff = voxel1->pos - voxel2->pos;
+    double watchDistance = (voxel1->baseSizeAverage() + voxel2->baseSizeAverage()) * COLLISION_ENVELOPE_RADIUS;
+    if (diff.x > watchDistance || diff.x < -watchDistance) return;
+    if (diff.y > watchDistance || diff.y < -watchDistance) return;
+    if (diff.z > watchDistance || diff.z < -watchDistance) return;
+    if (diff.Length() > watchDistance) return;
+    if (is_neighbor(voxel1, voxel2, NULL, 1)) return;
+    if (k->EnableCollision) {
+        VX3_Collision collision(voxel1, voxel2);
+        collision.updateContactForce();
+        VX3_Vec3D<> c1 = collision.contactForce(voxel1);
+        VX3_Vec3D<> c2 = collision.contactForce(voxel2);
+        voxel1->contactForce += c1;
+        voxel2->contactForce += c2;
+    }
+}
+
+// doTimeStep (VX3_VoxelyzeKernel.cu:237-359) with dt = -1
+bool do_time_step(RefSim &S) {
+    VX3_VoxelyzeKernel *k = S.k;
+    // updateTemperature (:219-235) -> gpu_update_temperature (:625-650)
+    if (k->VaryTempEnabled && k->TempPeriod > 0) {
+        for (int i = 0; i < k->num_d_voxels; i++) {
+            VX3_Voxel *t = &k->d_voxels[i];
+            if (t->removed) continue;
+            if (t->mat->TurnOnThermalExpansionAfterThisManySeconds > k->currentTime) continue;
+            if (t->mat->fixed) continue;
+            double currentTemperature =
+                k->TempAmplitude * sin(2 * 3.1415926f * (k->currentTime / k->TempPeriod + t->phaseOffset));
+            if (!k->EnableExpansion) {
+                if (currentTemperature > 0) currentTemperature = 0;
+            }
+            t->setTemperature(currentTemperature);
+        }
+    }
+    k->CurStepCount++;
+    float dt;
+    if (!k->OptimalDt) k->OptimalDt = recommended_dt(k);
+    if (k->OptimalDt < 1e-10) k->OptimalDt = 1e-10;
+    dt = k->DtFrac * k->OptimalDt;
+    S.last_dt = dt;
+
+    // gpu_update_links (:566-581)
+    bool diverged = false;
+    for (int i = 0; i < k->num_d_links; i++) {
+        VX3_Link *t = k->d_links + i;
+        if (t->removed) continue;
+        if (t->pVPos->mat->fixed && t->pVNeg->mat->fixed) continue;
+        if (t->isDetached) continue;
+        t->updateForces();
+        if (t->axialStrain() > 100) diverged = true;
+    }
+    if (diverged) return false;
+
+    if (k->isSurfaceChanged) {
+        k->isSurfaceChanged = false;
+        regenerate_surface(S);
+    }
+    if (k->enableAttach || k->EnableCollision) {
+        // gpu_update_attach (:833-843): first in [0,S), second < first
+        int num = (int)S.surface.size();
+        for (int first = 0; first < num; first++)
+            for (int second = 0; second < first; second++) {
+                VX3_Voxel *voxel1 = S.surface[first];
+                VX3_Voxel *voxel2 = S.surface[second];
+                if (voxel1->removed || voxel2->removed) continue;
+                collide_pair(voxel1, voxel2, k);
+            }
+    }
+    S.last_contact.assign((size_t)k->num_d_voxels * 3, 0.0);
+    for (int i = 0; i < k->num_d_voxels; i++) {
+        S.last_contact[3 * i + 0] = k->d_voxels[i].contactForce.x;
+        S.last_contact[3 * i + 1] = k->d_voxels[i].contactForce.y;
+        S.last_contact[3 * i + 2] = k->d_voxels[i].contactForce.z;
+    }
+
+    // gpu_update_voxels (:582-623), physics part
+    for (int i = 0; i < k->num_d_voxels; i++) {
+        VX3_Voxel *t = &k->d_voxels[i];
+        if (t->removed) continue;
+        if (t->mat->fixed) continue;
+        t->timeStep(dt, k->currentTime, k);
+    }
+    k->currentTime += dt;
+    return true;
+}
+
+// VX3_VoxelyzeKernel.cu:477-493
+void center_of_mass(VX3_VoxelyzeKernel *k, double *out) {
+    double TotalMass = 0;
+    VX3_Vec3D<> Sum(0, 0, 0);
+    for (int i = 0; i < k->num_d_voxels; i++) {
+        if (!k->d_voxels[i].mat->isMeasured) continue;
+        double ThisMass = k->d_voxels[i].material()->mass();
+        Sum += k->d_voxels[i].position() * ThisMass;
+        TotalMass += ThisMass;
+    }
+    VX3_Vec3D<> c;
+    if (TotalMass != 0) c = Sum / TotalMass;
+    out[0] = c.x; out[1] = c.y; out[2] = c.z;
+}
+
+int vidx(VX3_VoxelyzeKernel *k, VX3_Voxel *v) { return (int)(v - k->d_voxels); }
+
+} // namespace
+
+extern "C" {
+
+// Reads a self-contained VXA document (no VXD merge) the way
+// VX3_SimulationManager::readVXD does (:298-308), then builds the kernel
+// object.  enable_collision / enable_expansion stand for the VX3-only keys
+// VXA.Simulator.AttachDetach.EnableCollision and VXA.Simulator.EnableExpansion
+// (:328, :367) that the reference reads through boost::property_tree.
+void *vx3ref_create(const char *vxa_text, int enable_collision, int enable_expansion) {
+    RefSim *S = new RefSim();
+    S->env.pObj = &S->obj;
+    S->sim.pEnv = &S->env;
+    std::string text(vxa_text);
+    CXML_Rip XML;
+    XML.fromXMLText(&text);
+    std::string msg;
+    S->sim.ReadVXA(&XML, &msg);
+    S->sim.Import(NULL, NULL, &msg);
+    build_kernel(*S);
+    S->k->EnableCollision = enable_collision != 0;
+    S->k->enableAttach = false;
+    S->k->enableDetach = false;
+    S->k->EnableExpansion = enable_expansion;
+    // CUDA_Simulation prologue (:54-57): initial COM and two recommendedTimeStep calls
+    double c[3];
+    center_of_mass(S->k, c);
+    recommended_dt(S->k);
+    return S;
+}
+
+void vx3ref_destroy(void *h) { /* the reference frees nothing reliably either; leak in tests */ (void)h; }
+
+void vx3ref_counts(void *h, int *nv, int *nl, int *nsurf) {
+    RefSim *S = (RefSim *)h;
+    *nv = S->k->num_d_voxels;
+    *nl = S->k->num_d_links;
+    *nsurf = (int)S->surface.size();
+}
+
+// returns number of steps completed (< n if the sim diverged)
+int vx3ref_step(void *h, int n) {
+    RefSim *S = (RefSim *)h;
+    int done = 0;
+    for (int i = 0; i < n; i++) {
+        if (S->diverged) break;
+        if (!do_time_step(*S)) { S->diverged = true; break; }
+        done++;
+        S->steps_done++;
+    }
+    return done;
+}
+
+double vx3ref_time(void *h) { return ((RefSim *)h)->k->currentTime; }
+float vx3ref_dt(void *h) { return ((RefSim *)h)->last_dt; }
+double vx3ref_optimal_dt(void *h) { return ((RefSim *)h)->k->OptimalDt; }
+double vx3ref_recommended_dt(void *h) { return recommended_dt(((RefSim *)h)->k); }
+double vx3ref_dtfrac(void *h) { return ((RefSim *)h)->k->DtFrac; }
+
+// pos[3n], orient[4n] (w,x,y,z), linmom[3n], angmom[3n], tempe[n], flags[n] (boolStates)
+void vx3ref_voxels(void *h, double *pos, double *orient, double *linmom, double *angmom, float *tempe, int *flags) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_voxels; i++) {
+        VX3_Voxel &v = k->d_voxels[i];
+        pos[3 * i] = v.pos.x; pos[3 * i + 1] = v.pos.y; pos[3 * i + 2] = v.pos.z;
+        orient[4 * i] = v.orient.w; orient[4 * i + 1] = v.orient.x; orient[4 * i + 2] = v.orient.y; orient[4 * i + 3] = v.orient.z;
+        linmom[3 * i] = v.linMom.x; linmom[3 * i + 1] = v.linMom.y; linmom[3 * i + 2] = v.linMom.z;
+        angmom[3 * i] = v.angMom.x; angmom[3 * i + 1] = v.angMom.y; angmom[3 * i + 2] = v.angMom.z;
+        tempe[i] = v.tempe;
+        flags[i] = v.boolStates;
+    }
+}
+
+// per voxel: material index (into the voxel material list), lattice indices, 6 link slots (-1 if none)
+void vx3ref_topology(void *h, int *mat, int *ijk, int *slots) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_voxels; i++) {
+        VX3_Voxel &v = k->d_voxels[i];
+        mat[i] = (int)(v.mat - k->d_voxelMats);
+        ijk[3 * i] = v.ix; ijk[3 * i + 1] = v.iy; ijk[3 * i + 2] = v.iz;
+        for (int d = 0; d < 6; d++) slots[6 * i + d] = v.links[d] ? (int)(v.links[d] - k->d_links) : -1;
+    }
+}
+
+// per link: neg, pos voxel index, axis, small-angle flag, bool states
+void vx3ref_link_topology(void *h, int *negpos, int *axis, int *small, int *states) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_links; i++) {
+        VX3_Link &L = k->d_links[i];
+        negpos[2 * i] = vidx(k, L.pVNeg);
+        negpos[2 * i + 1] = vidx(k, L.pVPos);
+        axis[i] = (int)L.axis;
+        small[i] = L.smallAngle ? 1 : 0;
+        states[i] = L.boolStates;
+    }
+}
+
+// per link: strain, maxStrain, restLength, pos2/angle1v/angle2v (9), forceNeg/forcePos/momentNeg/momentPos (12)
+void vx3ref_links(void *h, float *strain, float *maxstrain, double *rest, double *local9, double *forces12) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_links; i++) {
+        VX3_Link &L = k->d_links[i];
+        strain[i] = L.strain;
+        maxstrain[i] = L.maxStrain;
+        rest[i] = L.currentRestLength;
+        double *p = local9 + 9 * i;
+        p[0] = L.pos2.x; p[1] = L.pos2.y; p[2] = L.pos2.z;
+        p[3] = L.angle1v.x; p[4] = L.angle1v.y; p[5] = L.angle1v.z;
+        p[6] = L.angle2v.x; p[7] = L.angle2v.y; p[8] = L.angle2v.z;
+        double *f = forces12 + 12 * i;
+        f[0] = L.forceNeg.x; f[1] = L.forceNeg.y; f[2] = L.forceNeg.z;
+        f[3] = L.forcePos.x; f[4] = L.forcePos.y; f[5] = L.forcePos.z;
+        f[6] = L.momentNeg.x; f[7] = L.momentNeg.y; f[8] = L.momentNeg.z;
+        f[9] = L.momentPos.x; f[10] = L.momentPos.y; f[11] = L.momentPos.z;
+    }
+}
+
+// derived material constants as the kernels see them
+// voxel mats: 16 floats each: mass, massInv, sqrtMass, momentInertia, momentInertiaInv, 2xSqMxExS, 2xSqIxExSxSxS,
+//   zetaInternal, zetaGlobal, zetaCollision, muStatic, muKinetic, E, nu, alphaCTE, gravMult ; plus nomSize (double)
+void vx3ref_voxel_mats(void *h, float *f16, double *nomsize, int *fixed_measured) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_voxelMats; i++) {
+        VX3_MaterialVoxel &m = k->d_voxelMats[i];
+        float *f = f16 + 16 * i;
+        f[0] = m._mass; f[1] = m._massInverse; f[2] = m._sqrtMass; f[3] = m._momentInertia; f[4] = m._momentInertiaInverse;
+        f[5] = m._2xSqMxExS; f[6] = m._2xSqIxExSxSxS; f[7] = m.zetaInternal; f[8] = m.zetaGlobal; f[9] = m.zetaCollision;
+        f[10] = m.muStatic; f[11] = m.muKinetic; f[12] = m.E; f[13] = m.nu; f[14] = m.alphaCTE; f[15] = m.gravMult;
+        nomsize[i] = m.nomSize;
+        fixed_measured[2 * i] = m.fixed ? 1 : 0;
+        fixed_measured[2 * i + 1] = m.isMeasured ? 1 : 0;
+    }
+}
+int vx3ref_num_voxel_mats(void *h) { return ((RefSim *)h)->k->num_d_voxelMats; }
+int vx3ref_num_link_mats(void *h) { return ((RefSim *)h)->k->num_d_linkMats; }
+
+// link mats: 16 floats each: E, nu, eHat, a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp, epsilonFail, linear, alphaCTE
+void vx3ref_link_mats(void *h, float *f16, int *lmat_of_link) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_linkMats; i++) {
+        VX3_MaterialLink &m = k->d_linkMats[i];
+        float *f = f16 + 16 * i;
+        f[0] = m.E; f[1] = m.nu; f[2] = m._eHat; f[3] = m._a1; f[4] = m._a2; f[5] = m._b1; f[6] = m._b2; f[7] = m._b3;
+        f[8] = m._sqA1; f[9] = m._sqA2xIp; f[10] = m._sqB1; f[11] = m._sqB2xFMp; f[12] = m._sqB3xIp;
+        f[13] = m.epsilonFail; f[14] = m.linear ? 1.0f : 0.0f; f[15] = m.alphaCTE;
+    }
+    for (int i = 0; i < k->num_d_links; i++) lmat_of_link[i] = (int)(k->d_links[i].mat - k->d_linkMats);
+}
+
+// link transverse info frozen at init: area, strainSum
+void vx3ref_link_transverse(void *h, float *area, float *ssum) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_links; i++) {
+        area[i] = k->d_links[i].currentTransverseArea;
+        ssum[i] = k->d_links[i].currentTransverseStrainSum;
+    }
+}
+
+void vx3ref_surface(void *h, int *idx) {
+    RefSim *S = (RefSim *)h;
+    for (size_t i = 0; i < S->surface.size(); i++) idx[i] = vidx(S->k, S->surface[i]);
+}
+
+// contact force per voxel as accumulated by the last step's collision pass
+void vx3ref_last_contact(void *h, double *c3) {
+    RefSim *S = (RefSim *)h;
+    for (size_t i = 0; i < S->last_contact.size(); i++) c3[i] = S->last_contact[i];
+}
+
+void vx3ref_com(void *h, double *c3) { center_of_mass(((RefSim *)h)->k, c3); }
+
+// environment as imported: gravity multiplier of material 0, floor flag, temp settings
+void vx3ref_env(void *h, double *out8) {
+    RefSim *S = (RefSim *)h;
+    VX3_VoxelyzeKernel *k = S->k;
+    out8[0] = k->voxSize;
+    out8[1] = k->DtFrac;
+    out8[2] = k->VaryTempEnabled ? 1 : 0;
+    out8[3] = k->TempAmplitude;
+    out8[4] = k->TempPeriod;
+    out8[5] = k->num_d_voxels ? (k->d_voxels[0].isFloorEnabled() ? 1 : 0) : 0;
+    out8[6] = k->EnableCollision ? 1 : 0;
+    out8[7] = k->EnableExpansion;
+}
+
+// per voxel phase offset (cycles)
+void vx3ref_phase(void *h, double *ph) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_voxels; i++) ph[i] = k->d_voxels[i].phaseOffset;
+}
+
+} // extern "C"

@@ -1,0 +1,2 @@
+// Host-only stand-in (oracle reference build only).
+#pragma once

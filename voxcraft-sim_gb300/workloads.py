@@ -1,0 +1,186 @@
+"""Seeded synthetic robots in the reference's VXA format.
+
+The reference ships no benchmark suite or dataset; every workload here is
+generated from a seed.  A robot is a dense lattice of material ids
+(0 = empty, 1..K = palette entry) plus per-voxel actuation phase, written out
+as a VXA document that the reference's own reader accepts
+(src/VXA/VX_Object.cpp:1760-1884 for <Structure> with ASCII_READABLE layers
+and <PhaseOffset> rows; src/VXA/VX_Sim.cpp:185-294 for <Simulator>;
+src/old/VX_Environment.cpp:150-172 for <Environment>).
+
+Robot generators follow the workload descriptions:
+  * solid_block    -- n x n x n solid cube of one passive material
+  * bernoulli_body -- Bernoulli(p) fill, largest 6-connected component kept
+"""
+
+from __future__ import annotations
+
+import dataclasses
+from collections import deque
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Material:
+    E: float = 1e6
+    nu: float = 0.35
+    rho: float = 1e3
+    cte: float = 0.0
+    mu_static: float = 1.0
+    mu_kinetic: float = 0.5
+    fail_stress: float = 0.0   # 0 -> linear model without failure (MatModel 0)
+    fixed: int = 0
+    is_measured: int = 1
+    name: str = "mat"
+
+
+@dataclasses.dataclass
+class Robot:
+    """One simulation: lattice (z, y, x) of palette indices and its settings."""
+    grid: np.ndarray                      # int8/uint8 [Z, Y, X], 0 = empty
+    materials: List[Material]
+    phase: Optional[np.ndarray] = None    # float64 [Z, Y, X] in cycles (only occupied cells read)
+    vox_size: float = 0.01
+    z_offset: int = 0                     # lattice cells added below the body (drop height)
+    dt_frac: float = 0.9
+    bond_damping: float = 1.0
+    col_damping: float = 1.0
+    slow_damping: float = 0.0
+    gravity: bool = True
+    grav_acc: float = -9.81
+    floor: bool = True
+    temp_vary: bool = False
+    temp_amplitude: float = 0.0
+    temp_period: float = 0.2
+    temp_base: float = 25.0
+    enable_expansion: int = 0
+    enable_collision: bool = False
+    volume_effects: bool = True
+
+    def occupied(self) -> np.ndarray:
+        return self.grid > 0
+
+    def padded(self):
+        """Lattice with z_offset empty layers underneath, as written to the VXA."""
+        g = self.grid
+        if self.z_offset:
+            pad = np.zeros((self.z_offset,) + g.shape[1:], dtype=g.dtype)
+            g = np.concatenate([pad, g], axis=0)
+        ph = self.phase
+        if ph is not None and self.z_offset:
+            pad = np.zeros((self.z_offset,) + ph.shape[1:], dtype=ph.dtype)
+            ph = np.concatenate([pad, ph], axis=0)
+        return g, ph
+
+
+def largest_component(mask: np.ndarray) -> np.ndarray:
+    """Largest 6-connected component of a boolean [Z, Y, X] mask."""
+    Z, Y, X = mask.shape
+    label = np.zeros(mask.shape, dtype=np.int32)
+    best, best_n, cur = 0, 0, 0
+    for z, y, x in zip(*np.nonzero(mask)):
+        if label[z, y, x]:
+            continue
+        cur += 1
+        n = 0
+        q = deque([(z, y, x)])
+        label[z, y, x] = cur
+        while q:
+            a, b, c = q.popleft()
+            n += 1
+            for da, db, dc in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)):
+                na, nb, nc = a + da, b + db, c + dc
+                if 0 <= na < Z and 0 <= nb < Y and 0 <= nc < X and mask[na, nb, nc] and not label[na, nb, nc]:
+                    label[na, nb, nc] = cur
+                    q.append((na, nb, nc))
+        if n > best_n:
+            best, best_n = cur, n
+    return label == best if best else np.zeros_like(mask)
+
+
+def solid_block(n: int = 10, drop_cells: int = 2, material: Optional[Material] = None, **kw) -> Robot:
+    """n^3 solid block of one material, dropped from drop_cells lattice units."""
+    m = material or Material(E=1e6, nu=0.35, rho=1e3, cte=0.0, mu_static=1.0, mu_kinetic=0.5)
+    grid = np.ones((n, n, n), dtype=np.uint8)
+    return Robot(grid=grid, materials=[m], z_offset=drop_cells, **kw)
+
+
+def bernoulli_body(rng: np.random.Generator, dims: Sequence[int], p: float, materials: List[Material],
+                   random_phase: bool = False, **kw) -> Robot:
+    """Bernoulli(p) fill of a dims=(X, Y, Z) box, largest 6-connected component,
+    materials drawn uniformly per voxel, optional uniform phase in cycles [0,1)."""
+    X, Y, Z = dims
+    mask = rng.random((Z, Y, X)) < p
+    mask = largest_component(mask)
+    mats = rng.integers(1, len(materials) + 1, size=(Z, Y, X)).astype(np.uint8)
+    grid = np.where(mask, mats, 0).astype(np.uint8)
+    phase = None
+    if random_phase:
+        # phase offsets in cycles; 2*pi*phase is the phase angle in [0, 2*pi)
+        phase = rng.random((Z, Y, X))
+    return Robot(grid=grid, materials=materials, phase=phase, **kw)
+
+
+def _fmt(v: float) -> str:
+    return repr(float(v))
+
+
+def to_vxa(r: Robot) -> str:
+    """Serialise a Robot as a self-contained VXA document."""
+    g, ph = r.padded()
+    Z, Y, X = g.shape
+    if len(r.materials) > 9:
+        raise ValueError("ASCII_READABLE layers hold palette indices 0..9")
+    out = ['<VXA Version="1.1">', "<Simulator>",
+           f"<Integration><DtFrac>{_fmt(r.dt_frac)}</DtFrac></Integration>",
+           "<Damping>"
+           f"<BondDampingZ>{_fmt(r.bond_damping)}</BondDampingZ>"
+           f"<ColDampingZ>{_fmt(r.col_damping)}</ColDampingZ>"
+           f"<SlowDampingZ>{_fmt(r.slow_damping)}</SlowDampingZ>"
+           "</Damping>",
+           f"<Features><VolumeEffectsEnabled>{int(r.volume_effects)}</VolumeEffectsEnabled></Features>",
+           f"<AttachDetach><EnableCollision>{int(r.enable_collision)}</EnableCollision>"
+           "<EnableAttach>0</EnableAttach><EnableDetach>0</EnableDetach></AttachDetach>",
+           f"<EnableExpansion>{int(r.enable_expansion)}</EnableExpansion>",
+           "</Simulator>",
+           "<Environment>",
+           f"<Gravity><GravEnabled>{int(r.gravity)}</GravEnabled><GravAcc>{_fmt(r.grav_acc)}</GravAcc>"
+           f"<FloorEnabled>{int(r.floor)}</FloorEnabled></Gravity>",
+           "<Thermal><TempEnabled>0</TempEnabled>"
+           f"<TempAmplitude>{_fmt(r.temp_amplitude)}</TempAmplitude><TempBase>{_fmt(r.temp_base)}</TempBase>"
+           f"<VaryTempEnabled>{int(r.temp_vary)}</VaryTempEnabled><TempPeriod>{_fmt(r.temp_period)}</TempPeriod>"
+           "</Thermal>",
+           "</Environment>",
+           '<VXC Version="0.94">',
+           f"<Lattice><Lattice_Dim>{_fmt(r.vox_size)}</Lattice_Dim></Lattice>",
+           "<Palette>"]
+    for i, m in enumerate(r.materials):
+        out.append(
+            f'<Material ID="{i + 1}"><Name>{m.name}{i + 1}</Name>'
+            "<Display><Red>0.5</Red><Green>0.5</Green><Blue>0.5</Blue><Alpha>1</Alpha></Display>"
+            "<Mechanical>"
+            f"<MatModel>{0 if m.fail_stress == 0 else 1}</MatModel>"
+            f"<Elastic_Mod>{_fmt(m.E)}</Elastic_Mod><Fail_Stress>{_fmt(m.fail_stress)}</Fail_Stress>"
+            f"<Density>{_fmt(m.rho)}</Density><Poissons_Ratio>{_fmt(m.nu)}</Poissons_Ratio>"
+            f"<CTE>{_fmt(m.cte)}</CTE><MaterialTempPhase>0</MaterialTempPhase>"
+            f"<uStatic>{_fmt(m.mu_static)}</uStatic><uDynamic>{_fmt(m.mu_kinetic)}</uDynamic>"
+            f"<Fixed>{int(m.fixed)}</Fixed><isMeasured>{int(m.is_measured)}</isMeasured>"
+            "</Mechanical></Material>")
+    out.append("</Palette>")
+    out.append('<Structure Compression="ASCII_READABLE">')
+    out.append(f"<X_Voxels>{X}</X_Voxels><Y_Voxels>{Y}</Y_Voxels><Z_Voxels>{Z}</Z_Voxels>")
+    out.append("<Data>")
+    for z in range(Z):
+        out.append("<Layer><![CDATA[" + "".join(str(int(v)) for v in g[z].reshape(-1)) + "]]></Layer>")
+    out.append("</Data>")
+    if ph is not None:
+        out.append("<PhaseOffset>")
+        for z in range(Z):
+            out.append("<Layer><![CDATA[" + ",".join(repr(float(v)) for v in ph[z].reshape(-1)) + "]]></Layer>")
+        out.append("</PhaseOffset>")
+    out.append("</Structure>")
+    out.append("</VXC>")
+    out.append("</VXA>")
+    return "\n".join(out)
