@@ -1,0 +1,797 @@
+/* vx3_oracle.c -- CPU restatement of the reference VX3 time step (plain C).
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GB300 kernels, never linked
+ * into the shipped library.  Every function cites the reference file:line it
+ * restates (paths relative to the voxcraft-sim source tree).  Arithmetic is
+ * written so that C's usual conversions reproduce the reference's mix of
+ * float and double exactly (build with -ffp-contract=off).
+ *
+ * Scope: linear materials (MatModel 0/1), static lattice topology (no
+ * attach/detach/removal), no boundary-condition regions, no signals/cilia,
+ * force field = constant 0 (the reference default, VX3_ForceField.h:10-20).
+ */
+#include "vx3_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct { double x, y, z; } vec;
+typedef struct { double w, x, y, z; } quat;
+
+static vec V(double x, double y, double z) { vec r = {x, y, z}; return r; }
+static vec vadd(vec a, vec b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
+static vec vsub(vec a, vec b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
+static vec vneg(vec a) { return V(-a.x, -a.y, -a.z); }
+/* VX3_Vec3D operator*(f): (f*x, f*y, f*z)  (VX3_Vec3D.h:49,61) */
+static vec vscale(vec a, double f) { return V(f * a.x, f * a.y, f * a.z); }
+/* VX3_Vec3D operator/(f): Inv = 1/f; (Inv*x, ...)  (VX3_Vec3D.h:63) */
+static vec vdiv(vec a, double f) { double inv = 1.0 / f; return V(inv * a.x, inv * a.y, inv * a.z); }
+static double vlen(vec a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+static double vdot(vec a, vec b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+/* Normalized (VX3_Vec3D.h:94) */
+static vec vnormalized(vec a) { double l = sqrt(a.x * a.x + a.y * a.y + a.z * a.z); return l > 0 ? vdiv(a, l) : a; }
+
+static quat Q(double w, double x, double y, double z) { quat q = {w, x, y, z}; return q; }
+static quat qident(void) { return Q(1, 0, 0, 0); }
+static quat qconj(quat q) { return Q(q.w, -q.x, -q.y, -q.z); }
+/* VX3_Quat3D.h:217-222 */
+static quat qmul(quat a, quat f) {
+    return Q(a.w * f.w - a.x * f.x - a.y * f.y - a.z * f.z,
+             a.w * f.x + a.x * f.w + a.y * f.z - a.z * f.y,
+             a.w * f.y - a.x * f.z + a.y * f.w + a.z * f.x,
+             a.w * f.z + a.x * f.y - a.y * f.x + a.z * f.w);
+}
+/* VX3_Quat3D.h:439-447 */
+static vec qrot(quat q, vec f) {
+    double fx = f.x, fy = f.y, fz = f.z;
+    double tw = fx * q.x + fy * q.y + fz * q.z;
+    double tx = fx * q.w - fy * q.z + fz * q.y;
+    double ty = fx * q.z + fy * q.w - fz * q.x;
+    double tz = -fx * q.y + fy * q.x + fz * q.w;
+    return V(q.w * tx + q.x * tw + q.y * tz - q.z * ty,
+             q.w * ty - q.x * tz + q.y * tw + q.z * tx,
+             q.w * tz + q.x * ty - q.y * tx + q.z * tw);
+}
+/* VX3_Quat3D.h:465-473 */
+static vec qrotinv(quat q, vec f) {
+    double fx = f.x, fy = f.y, fz = f.z;
+    double tw = q.x * fx + q.y * fy + q.z * fz;
+    double tx = q.w * fx - q.y * fz + q.z * fy;
+    double ty = q.w * fy + q.x * fz - q.z * fx;
+    double tz = q.w * fz - q.x * fy + q.y * fx;
+    return V(tw * q.x + tx * q.w + ty * q.z - tz * q.y,
+             tw * q.y - tx * q.z + ty * q.w + tz * q.x,
+             tw * q.z + tx * q.y - ty * q.x + tz * q.w);
+}
+/* ToRotationVector (VX3_Quat3D.h:347-359) */
+static vec q_to_rotvec(quat q) {
+    if (q.w >= 1.0 || q.w <= -1.0) return V(0, 0, 0);
+    double sq = 1.0 - q.w * q.w;
+    vec v = V(q.x, q.y, q.z);
+    if (sq < 2.4e-3)
+        return vscale(vscale(v, 2.0), sqrt((2 - 2 * q.w) / sq));
+    return vdiv(vscale(vscale(v, 2.0), acos(q.w)), sqrt(sq));
+}
+/* FromRotationVector (VX3_Quat3D.h:363-377) */
+static quat q_from_rotvec(vec in) {
+    vec theta = vdiv(in, 2);
+    double s, m2 = theta.x * theta.x + theta.y * theta.y + theta.z * theta.z;
+    quat q;
+    if (m2 * m2 < 5.328e-15) {
+        q.w = 1.0 - 0.5 * m2;
+        s = 1.0 - m2 / 6.0;
+    } else {
+        double m = sqrt(m2);
+        q.w = cos(m);
+        s = sin(m) / m;
+    }
+    q.x = theta.x * s;
+    q.y = theta.y * s;
+    q.z = theta.z * s;
+    return q;
+}
+/* FromAngleToPosX (VX3_Quat3D.h:384-432); q is left unchanged for a zero vector */
+static quat q_from_angle_to_posx(quat q, vec r) {
+    if (r.x == 0 && r.y == 0 && r.z == 0) return q;
+    double yx = r.y / r.x, zx = r.z / r.x;
+    if (yx < 1.732e-2 && yx > -1.732e-2 && zx < 1.732e-2 && zx > -1.732e-2) {
+        q.x = 0;
+        q.y = 0.5 * zx;
+        q.z = -0.5 * yx;
+        q.w = 1 + 0.5 * (-q.y * q.y - q.z * q.z);
+        return q;
+    }
+    vec n = r; /* NormalizeFast (VX3_Vec3D.h:84) */
+    double l = sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+    if (l > 0) { double li = 1.0 / l; n.x *= li; n.y *= li; n.z *= li; }
+    double theta = acos(n.x);
+    if (theta > 3.14159265358979 - 1e-7) return Q(0, 0, 1, 0);
+    double axis_inv = 1.0 / sqrt(n.z * n.z + n.y * n.y);
+    double a = 0.5 * theta, s = sin(a);
+    return Q(cos(a), 0, n.z * axis_inv * s, -n.y * axis_inv * s);
+}
+
+/* VX3_Link.h:134-153 and :156-191 */
+static vec to_axis_x(int axis, vec v) {
+    if (axis == 1) return V(v.y, -v.x, v.z);
+    if (axis == 2) return V(v.z, v.y, -v.x);
+    return v;
+}
+static quat to_axis_xq(int axis, quat q) {
+    if (axis == 1) return Q(q.w, q.y, -q.x, q.z);
+    if (axis == 2) return Q(q.w, q.z, q.y, -q.x);
+    return q;
+}
+static vec to_axis_original(int axis, vec v) {
+    if (axis == 1) return V(-v.y, v.x, v.z);
+    if (axis == 2) return V(-v.z, v.y, v.x);
+    return v;
+}
+
+/* ------------------------------------------------------------- materials */
+typedef struct {
+    float E, nu, rho, cte, mu_s, mu_k, z_int, z_glob, z_col, eHat;
+    float sigma_fail, eps_fail;
+    double nom_size;
+    float grav_mult;
+    float mass, mass_inv, sqrt_mass, mom_inertia, mom_inertia_inv, c2xSqMxExS, c2xSqIxExSxSxS;
+    int fixed, is_measured;
+    double thermal_on_after;
+} vmat;
+
+typedef struct {
+    int m1, m2; /* vox1Mat, vox2Mat indices */
+    float E, nu, eHat, eps_fail, cte;
+    float a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp;
+} lmat;
+
+/* CVX_Material::updateDerived _eHat (src/old/VX_Material.cpp:542-549) */
+static float ehat(float E, float nu) { return E / ((1 - 2 * nu) * (1 + nu)); }
+
+/* CVX_MaterialVoxel::updateDerived (src/old/VX_MaterialVoxel.cpp:57-79) */
+static void vmat_derive(vmat *m) {
+    double volume = m->nom_size * m->nom_size * m->nom_size;
+    m->eHat = ehat(m->E, m->nu);
+    m->mass = (float)(volume * m->rho);
+    m->mom_inertia = (float)(m->mass * m->nom_size * m->nom_size / 6.0f);
+    if (volume == 0 || m->mass == 0 || m->mom_inertia == 0) {
+        m->mass_inv = m->sqrt_mass = m->mom_inertia_inv = m->c2xSqMxExS = m->c2xSqIxExSxSxS = 0.0f;
+        return;
+    }
+    m->mass_inv = 1.0f / m->mass;
+    m->sqrt_mass = sqrtf(m->mass);
+    m->mom_inertia_inv = 1.0f / m->mom_inertia;
+    m->c2xSqMxExS = (float)(2.0f * sqrt(m->mass * m->E * m->nom_size));
+    m->c2xSqIxExSxSxS = (float)(2.0f * sqrt(m->mom_inertia * m->E * m->nom_size * m->nom_size * m->nom_size));
+}
+
+/* Material import as CVX_Sim::Import + CopyMat do it (src/VXA/VX_Sim.cpp:73-86, 365-420,
+ * 145-148; setters src/old/VX_Material.cpp:372-532). */
+static void vmat_import(vmat *m, const vxo_material *in, const vxo_robot *r) {
+    memset(m, 0, sizeof(*m));
+    float E = (float)in->E;
+    float fail = in->model == 1 ? (float)in->fail_stress : -1.0f;
+    m->E = E;
+    m->sigma_fail = fail;
+    m->eps_fail = (fail == -1.0f) ? -1.0f : fail / E; /* setModelLinear (VX_Material.cpp:372-392) */
+    float nu = (float)in->nu;
+    if (nu < 0) nu = 0;
+    if (nu >= 0.5) nu = 0.5 - FLT_EPSILON * 2;
+    if (!r->volume_effects) nu = 0; /* EnableVolumeEffects(false) (VX_Sim.cpp:445-459) */
+    m->nu = nu;
+    float rho = (float)in->rho;
+    if (rho <= 0) rho = FLT_MIN;
+    m->rho = rho;
+    m->cte = (float)in->cte;
+    float ms = (float)in->mu_static, mk = (float)in->mu_kinetic;
+    m->mu_s = ms <= 0 ? 0 : ms;
+    m->mu_k = mk <= 0 ? 0 : mk;
+    float zi = (float)r->bond_damping, zg = (float)r->slow_damping, zc = (float)r->col_damping;
+    m->z_int = zi <= 0 ? 0 : zi;
+    m->z_glob = zg <= 0 ? 0 : zg;
+    m->z_col = zc <= 0 ? 0 : zc;
+    m->nom_size = r->vox_size;
+    /* CVX_Sim::SetGravityAccel (VX_Sim.cpp:485): gravity multiplier from GravAcc */
+    float ga = (float)r->grav_acc;
+    m->grav_mult = (float)(-ga / 9.80665);
+    m->fixed = in->fixed;
+    m->is_measured = in->is_measured;
+    m->thermal_on_after = in->thermal_on_after;
+    vmat_derive(m);
+}
+
+/* CVX_MaterialLink::updateAll + updateDerived (src/old/VX_MaterialLink.cpp:47-140) */
+static void lmat_make(lmat *l, const vmat *v1, const vmat *v2, int i1, int i2) {
+    l->m1 = i1;
+    l->m2 = i2;
+    float f1 = v1->sigma_fail, f2 = v2->sigma_fail, fail;
+    if (f1 == -1.0f) fail = f2;
+    else if (f2 == -1.0f) fail = f1;
+    else fail = f1 < f2 ? f1 : f2;
+    float E = 2.0f * v1->E * v2->E / (v1->E + v2->E);
+    l->E = E;
+    l->eps_fail = (fail == -1.0f) ? -1.0f : fail / E;
+    l->cte = 0.5f * (v1->cte + v2->cte);
+    float nu;
+    if (v1->nu == 0 && v2->nu == 0) nu = 0;
+    else {
+        float tmpEHat = 2 * v1->eHat * v2->eHat / (v1->eHat + v2->eHat);
+        float tmpE = E;
+        float c2 = (tmpEHat - tmpE) / (2 * tmpEHat) + 0.0625;
+        nu = sqrtf(c2) - 0.25;
+    }
+    l->nu = nu;
+    l->eHat = ehat(E, nu);
+    double nom = 0.5 * (v1->nom_size + v2->nom_size);
+    float L = (float)nom;
+    l->a1 = E * L;
+    l->a2 = E * L * L * L / (12.0f * (1 + nu));
+    l->b1 = E * L;
+    l->b2 = E * L * L / 2.0f;
+    l->b3 = E * L * L * L / 6.0f;
+    l->sqA1 = sqrtf(l->a1);
+    l->sqA2xIp = sqrtf(l->a2 * L * L / 6.0f);
+    l->sqB1 = sqrtf(l->b1);
+    l->sqB2xFMp = sqrtf(l->b2 * L / 2.0f);
+    l->sqB3xIp = sqrtf(l->b3 * L * L / 6.0f);
+}
+
+/* ---------------------------------------------------------------- state */
+enum { F_SURFACE = 1 << 1, F_FLOOR = 1 << 2, F_STATIC = 1 << 3 };
+enum { L_LVV = 1 };
+
+typedef struct {
+    int mat, ix, iy, iz, links[6];
+    vec pos, linMom, angMom, contact;
+    quat orient;
+    float tempe, prevDt;
+    int flags;
+    double phase;
+} voxel;
+
+typedef struct {
+    int neg, pos, axis, mat;
+    vec pos2, a1v, a2v;
+    vec fNeg, fPos, mNeg, mPos;
+    float strain, maxStrain, area, tss;
+    double rest;
+    int small, states;
+} link;
+
+typedef struct {
+    vxo_robot r;
+    int nv, nl, nvm, nlm, ns;
+    vmat *vm;
+    lmat *lm;
+    voxel *v;
+    link *l;
+    int *surf;
+    double *last_contact;
+    double t, optimal_dt;
+    float dt;
+    int surface_stale, diverged;
+} sim;
+
+/* VX3_Voxel::baseSize(axis) (VX3_Voxel.h:96-100); material size() = nomSize*extScale(1,1,1) */
+static double base_size(const sim *S, const voxel *v) {
+    const vmat *m = &S->vm[v->mat];
+    return m->nom_size * (1 + v->tempe * m->cte);
+}
+/* VX3_Voxel::baseSizeAverage (VX3_Voxel.h:102-105) */
+static double base_size_avg(const sim *S, const voxel *v) {
+    double b = base_size(S, v);
+    return (b + b + b) / 3.0f;
+}
+/* VX3_Voxel::floorPenetration (VX3_Voxel.h:185-188) */
+static float floor_pen(const sim *S, const voxel *v) {
+    return (float)(base_size_avg(S, v) / 2 - S->vm[v->mat].nom_size / 2 - v->pos.z);
+}
+/* VX3_Link::updateRestLength (VX3_Link.cu:80-83) */
+static void update_rest(sim *S, link *L) {
+    L->rest = 0.5 * (base_size(S, &S->v[L->neg]) + base_size(S, &S->v[L->pos]));
+}
+
+/* Lattice -> voxels and links, CVX_Sim::Import / CVoxelyze::addVoxel / addLink
+ * order (src/VXA/VX_Sim.cpp:88-107, src/old/Voxelyze.cpp:439-462, 508-539,
+ * src/old/VX_Link.cpp:21-54): voxels in x-fastest scan order; each new voxel
+ * links to already-present neighbours in direction order X_NEG, Y_NEG, Z_NEG
+ * (the only earlier ones), pVNeg being the lower lattice index. */
+void *vxo_create(const vxo_robot *r) {
+    sim *S = (sim *)calloc(1, sizeof(sim));
+    S->r = *r;
+    int nx = r->nx, ny = r->ny, nz = r->nz, ncell = nx * ny * nz;
+    S->nvm = r->n_materials;
+    S->vm = (vmat *)calloc(S->nvm ? S->nvm : 1, sizeof(vmat));
+    for (int i = 0; i < S->nvm; i++) vmat_import(&S->vm[i], &r->materials[i], r);
+
+    int *vid = (int *)malloc(sizeof(int) * (ncell ? ncell : 1));
+    S->nv = 0;
+    for (int c = 0; c < ncell; c++) vid[c] = r->lattice[c] > 0 ? S->nv++ : -1;
+    S->v = (voxel *)calloc(S->nv ? S->nv : 1, sizeof(voxel));
+    S->l = (link *)calloc(3 * (size_t)(S->nv ? S->nv : 1), sizeof(link));
+    S->lm = (lmat *)calloc((size_t)S->nvm * S->nvm + 1, sizeof(lmat));
+    S->nl = 0;
+    S->nlm = 0;
+    for (int c = 0; c < ncell; c++) {
+        if (vid[c] < 0) continue;
+        int x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);
+        voxel *v = &S->v[vid[c]];
+        v->mat = r->lattice[c] - 1;
+        v->ix = x; v->iy = y; v->iz = z;
+        /* CVoxelyze::addVoxel pos (Voxelyze.cpp:447); CVX_Voxel::reset (VX_Voxel.cpp:48-57) */
+        v->pos = V(x * r->vox_size, y * r->vox_size, z * r->vox_size);
+        v->orient = qident();
+        v->flags = F_STATIC | (r->floor_enabled ? F_FLOOR : 0);
+        v->tempe = 0.0f;
+        v->prevDt = 0.0f;
+        v->phase = r->phase ? r->phase[c] : 0.0;
+        for (int d = 0; d < 6; d++) v->links[d] = -1;
+        int nb[3] = {x > 0 ? vid[c - 1] : -1, y > 0 ? vid[c - nx] : -1, z > 0 ? vid[c - nx * ny] : -1};
+        for (int a = 0; a < 3; a++) {
+            if (nb[a] < 0) continue;
+            link *L = &S->l[S->nl];
+            L->neg = nb[a];
+            L->pos = vid[c];
+            L->axis = a;
+            /* CVoxelyze::combinedMaterial (Voxelyze.cpp:626-641): first use of a pair fixes
+             * (vox1Mat, vox2Mat) = (new voxel's material, neighbour's material) */
+            int m_new = v->mat, m_nb = S->v[nb[a]].mat, found = -1;
+            for (int k = 0; k < S->nlm; k++)
+                if ((S->lm[k].m1 == m_new && S->lm[k].m2 == m_nb) || (S->lm[k].m1 == m_nb && S->lm[k].m2 == m_new)) found = k;
+            if (found < 0) {
+                lmat_make(&S->lm[S->nlm], &S->vm[m_new], &S->vm[m_nb], m_new, m_nb);
+                found = S->nlm++;
+            }
+            L->mat = found;
+            L->small = 1;
+            L->states = 0;
+            /* CVX_Link::reset transverse info (VX_Link.cpp:56-71): voxels unstrained */
+            float sz = (float)S->vm[v->mat].nom_size, sz2 = (float)S->vm[m_nb].nom_size;
+            L->area = 0.5f * (sz2 * sz2 + sz * sz);
+            L->tss = 0.0f;
+            v->links[2 * a + 1] = S->nl;           /* new voxel: negative direction */
+            S->v[nb[a]].links[2 * a] = S->nl;      /* neighbour: positive direction */
+            S->nl++;
+        }
+    }
+    free(vid);
+    for (int i = 0; i < S->nl; i++) update_rest(S, &S->l[i]);
+    S->surf = (int *)malloc(sizeof(int) * (S->nv ? S->nv : 1));
+    S->last_contact = (double *)calloc(3 * (size_t)(S->nv ? S->nv : 1), sizeof(double));
+    S->surface_stale = 1;
+    return S;
+}
+
+void vxo_destroy(void *h) {
+    sim *S = (sim *)h;
+    if (!S) return;
+    free(S->vm); free(S->lm); free(S->v); free(S->l); free(S->surf); free(S->last_contact);
+    free(S);
+}
+
+/* VX3_Material::stress, linear branch (VX3_Material.cu:90-101) */
+static float mat_stress(const lmat *m, float strain, float tss) {
+    if (m->eps_fail != -1.0f && strain > m->eps_fail) return 0.0f;
+    if (m->nu == 0.0f) return m->E * strain;
+    return m->eHat * ((1 - m->nu) * strain + m->nu * tss);
+}
+
+/* VX3_Voxel::dampingMultiplier (VX3_Voxel.h:206-208) */
+static float damping_mult(const sim *S, const voxel *v) {
+    const vmat *m = &S->vm[v->mat];
+    return 2 * m->sqrt_mass * m->z_int / v->prevDt;
+}
+
+/* VX3_Link::orientLink + updateForces + updateStrain (VX3_Link.cu:90-260) */
+static void link_update(sim *S, link *L) {
+    voxel *vn = &S->v[L->neg], *vp = &S->v[L->pos];
+    const lmat *m = &S->lm[L->mat];
+    vec oldPos2 = L->pos2, oldA1 = L->a1v, oldA2 = L->a2v;
+
+    /* orientLink (:90-133) */
+    vec pos2 = to_axis_x(L->axis, vsub(vp->pos, vn->pos));
+    quat angle1 = to_axis_xq(L->axis, vn->orient);
+    quat angle2 = to_axis_xq(L->axis, vp->orient);
+    quat totalRot = qconj(angle1);
+    pos2 = qrot(totalRot, pos2);
+    angle2 = qmul(totalRot, angle2);
+    angle1 = qident();
+    float SmallTurn = (float)((fabs(pos2.z) + fabs(pos2.y)) / pos2.x);
+    float ExtendPerc = (float)(fabs(1 - pos2.x / L->rest));
+    const float HF = 1.2f, BEND = 0.05f, EXT = 0.50f;
+    if (!L->small && SmallTurn < BEND && ExtendPerc < EXT) {
+        L->small = 1;
+        L->states &= ~L_LVV;
+    } else if (L->small && (SmallTurn > HF * BEND || ExtendPerc > HF * EXT)) {
+        L->small = 0;
+        L->states &= ~L_LVV;
+    }
+    if (L->small) {
+        pos2.x -= L->rest;
+    } else {
+        angle1 = q_from_angle_to_posx(angle1, pos2);
+        angle2 = qmul(angle1, angle2);
+        pos2 = V(vlen(pos2) - L->rest, 0, 0);
+    }
+    vec a1v = q_to_rotvec(angle1), a2v = q_to_rotvec(angle2);
+    L->pos2 = pos2; L->a1v = a1v; L->a2v = a2v;
+
+    /* updateForces (:135-218) */
+    vec dPos2 = vscale(vsub(pos2, oldPos2), 0.5);
+    vec dA1 = vscale(vsub(a1v, oldA1), 0.5);
+    vec dA2 = vscale(vsub(a2v, oldA2), 0.5);
+    /* updateStrain (:220-260), linear materials */
+    float axialStrain = (float)(pos2.x / L->rest);
+    L->strain = axialStrain;
+    if (axialStrain > L->maxStrain) L->maxStrain = axialStrain;
+    float stress = mat_stress(m, axialStrain, L->tss);
+    if (m->eps_fail != -1.0f && L->maxStrain > m->eps_fail) { /* isFailed */
+        L->fNeg = L->fPos = L->mNeg = L->mPos = V(0, 0, 0);
+        return;
+    }
+    float b1 = m->b1, b2 = m->b2, b3 = m->b3, a2 = m->a2;
+    vec fNeg = V(stress * L->area, b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
+    vec fPos = vneg(fNeg);
+    vec mNeg = V(a2 * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (2 * a1v.y + a2v.y), b2 * pos2.y - b3 * (2 * a1v.z + a2v.z));
+    vec mPos = V(a2 * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z));
+    if (L->states & L_LVV) {
+        float sqA1 = m->sqA1, sqA2xIp = m->sqA2xIp, sqB1 = m->sqB1, sqB2xFMp = m->sqB2xFMp, sqB3xIp = m->sqB3xIp;
+        vec posCalc = V(sqA1 * dPos2.x, sqB1 * dPos2.y - sqB2xFMp * (dA1.z + dA2.z), sqB1 * dPos2.z + sqB2xFMp * (dA1.y + dA2.y));
+        float dmN = damping_mult(S, vn), dmP = damping_mult(S, vp);
+        fNeg = vadd(fNeg, vscale(posCalc, dmN));
+        fPos = vsub(fPos, vscale(posCalc, dmP));
+        mNeg = vsub(mNeg, vscale(V(-sqA2xIp * (dA2.x - dA1.x), sqB2xFMp * dPos2.z + sqB3xIp * (2 * dA1.y + dA2.y),
+                                   -sqB2xFMp * dPos2.y + sqB3xIp * (2 * dA1.z + dA2.z)), 0.5 * dmN));
+        mPos = vsub(mPos, vscale(V(sqA2xIp * (dA2.x - dA1.x), sqB2xFMp * dPos2.z + sqB3xIp * (dA1.y + 2 * dA2.y),
+                                   -sqB2xFMp * dPos2.y + sqB3xIp * (dA1.z + 2 * dA2.z)), 0.5 * dmP));
+    } else {
+        L->states |= L_LVV;
+    }
+    if (!L->small) {
+        fNeg = qrotinv(angle1, fNeg);
+        mNeg = qrotinv(angle1, mNeg);
+    }
+    fPos = qrotinv(angle2, fPos);
+    mPos = qrotinv(angle2, mPos);
+    L->fNeg = to_axis_original(L->axis, fNeg);
+    L->fPos = to_axis_original(L->axis, fPos);
+    L->mNeg = to_axis_original(L->axis, mNeg);
+    L->mPos = to_axis_original(L->axis, mPos);
+}
+
+/* VX3_Voxel::floorForce (VX3_Voxel.cu:399-426) */
+static void floor_force(const sim *S, voxel *v, vec *F) {
+    const vmat *m = &S->vm[v->mat];
+    float pen = floor_pen(S, v);
+    if (pen >= 0) {
+        vec vel = vscale(v->linMom, m->mass_inv);
+        vec hv = V(vel.x, vel.y, 0);
+        float pstiff = (float)(2 * m->E * m->nom_size);
+        float normal = pstiff * pen;
+        F->z += normal - (m->z_col * m->c2xSqMxExS) * vel.z;
+        if (v->flags & F_STATIC) {
+            float surf = (float)(F->x * F->x + F->y * F->y);
+            float fric = (m->mu_s * normal) * (m->mu_s * normal);
+            if (surf > fric) v->flags &= ~F_STATIC;
+        } else {
+            *F = vsub(*F, vscale(vnormalized(hv), m->mu_k * normal));
+        }
+    } else {
+        v->flags &= ~F_STATIC;
+    }
+}
+
+/* VX3_Voxel::timeStep with force()/moment() (VX3_Voxel.cu:162-277, 350-397) */
+static void voxel_update(sim *S, voxel *v, float dtf) {
+    const vmat *m = &S->vm[v->mat];
+    double dt = dtf;
+    v->prevDt = (float)dt;
+    if (dt == 0.0f) return;
+    /* force() */
+    vec F = V(0, 0, 0);
+    for (int i = 0; i < 6; i++) {
+        if (v->links[i] < 0) continue;
+        const link *L = &S->l[v->links[i]];
+        F = vadd(F, (i % 2 == 1) ? L->fPos : L->fNeg);
+    }
+    F = qrot(v->orient, F);
+    vec vel = vscale(v->linMom, m->mass_inv);
+    F = vsub(F, vscale(vel, m->z_glob * m->c2xSqMxExS));
+    F.z += -m->mass * 9.80665f * m->grav_mult;
+    F = vsub(F, v->contact);
+    v->contact = V(0, 0, 0);
+    F = vadd(F, V(0.0 * 0.0, 0.0 * 0.0, 0.0 * 0.0)); /* CiliaForce * Cilia, both zero */
+    /* force field, constant 0 (VX3_Voxel.cu:179-184) */
+    F.x += 0.0; F.y += 0.0; F.z += 0.0;
+    vec fric = F;
+    if (v->flags & F_FLOOR) floor_force(S, v, &F);
+    fric = vsub(F, fric);
+    v->linMom = vadd(v->linMom, vscale(F, dt));
+    vec translate = vscale(v->linMom, dt * m->mass_inv);
+    if ((v->flags & F_FLOOR) && floor_pen(S, v) >= 0) {
+        double work = fric.x * translate.x + fric.y * translate.y;
+        double hKe = 0.5 * m->mass_inv * (v->linMom.x * v->linMom.x + v->linMom.y * v->linMom.y);
+        if (hKe + work <= 0) v->flags |= F_STATIC;
+        if (v->flags & F_STATIC) {
+            v->linMom.x = v->linMom.y = 0;
+            translate.x = translate.y = 0;
+        }
+    } else {
+        v->flags &= ~F_STATIC;
+    }
+    v->pos = vadd(v->pos, translate);
+    /* moment() */
+    vec M = V(0, 0, 0);
+    for (int i = 0; i < 6; i++) {
+        if (v->links[i] < 0) continue;
+        const link *L = &S->l[v->links[i]];
+        M = vadd(M, (i % 2 == 1) ? L->mPos : L->mNeg);
+    }
+    M = qrot(v->orient, M);
+    vec angVel = vscale(v->angMom, m->mom_inertia_inv);
+    M = vsub(M, vscale(angVel, m->z_glob * m->c2xSqIxExSxSxS));
+    v->angMom = vadd(v->angMom, vscale(M, dt));
+    v->orient = qmul(q_from_rotvec(vscale(v->angMom, dt * m->mom_inertia_inv)), v->orient);
+    if ((v->flags & F_FLOOR) && floor_pen(S, v) >= 0) {
+        if (v->flags & F_STATIC) v->angMom = V(0, 0, 0);
+    }
+}
+
+/* recommendedTimeStep with axialStiffness (VX3_VoxelyzeKernel.cu:184-217, VX3_Link.cu:269-278) */
+double vxo_recommended_dt(void *h) {
+    sim *S = (sim *)h;
+    double MaxFreq2 = 0.0f;
+    for (int i = 0; i < S->nl; i++) {
+        link *L = &S->l[i];
+        const lmat *m = &S->lm[L->mat];
+        double m1 = S->vm[S->v[L->neg].mat].mass, m2 = S->vm[S->v[L->pos].mat].mass;
+        float k;
+        if (m->nu == 0.0f) k = m->a1;
+        else {
+            update_rest(S, L);
+            k = (float)(m->eHat * L->area / ((L->strain + 1) * L->rest));
+        }
+        double f2 = k / (m1 < m2 ? m1 : m2);
+        if (f2 > MaxFreq2) MaxFreq2 = f2;
+    }
+    if (MaxFreq2 <= 0.0f) {
+        for (int i = 0; i < S->nv; i++) {
+            const vmat *m = &S->vm[S->v[i].mat];
+            double f2 = m->E * m->nom_size / m->mass;
+            if (f2 > MaxFreq2) MaxFreq2 = f2;
+        }
+    }
+    if (MaxFreq2 <= 0.0f) return 0.0f;
+    return 1.0f / (6.283185f * sqrt(MaxFreq2));
+}
+
+static int is_linked(const sim *S, int a, int b) {
+    for (int d = 0; d < 6; d++) {
+        int li = S->v[a].links[d];
+        if (li < 0) continue;
+        int o = S->l[li].neg == a ? S->l[li].pos : S->l[li].neg;
+        if (o == b) return 1;
+    }
+    return 0;
+}
+
+/* handle_collision_attachment (collision half) + VX3_Collision
+ * (VX3_VoxelyzeKernel.cu:682-727, VX3_Collision.cu:3-31) */
+static void collide(sim *S, voxel *v1, voxel *v2, int i1, int i2) {
+    const vmat *m1 = &S->vm[v1->mat], *m2 = &S->vm[v2->mat];
+    if (m1->fixed && m2->fixed) return;
+    vec diff = vsub(v1->pos, v2->pos);
+    double bsa1 = base_size_avg(S, v1), bsa2 = base_size_avg(S, v2);
+    double wd = (bsa1 + bsa2) * 0.625;
+    if (diff.x > wd || diff.x < -wd) return;
+    if (diff.y > wd || diff.y < -wd) return;
+    if (diff.z > wd || diff.z < -wd) return;
+    if (vlen(diff) > wd) return;
+    if (is_linked(S, i1, i2)) return;
+    if (!S->r.enable_collision) return;
+    float k1 = (float)(2 * m1->E * m1->nom_size), k2 = (float)(2 * m2->E * m2->nom_size);
+    double pstiff = 2.0f / (1.0f / k1 + 1.0f / k2);
+    double dampC = 0.5f * (m1->z_col * m1->c2xSqMxExS + m2->z_col * m2->c2xSqMxExS);
+    vec offset = vsub(v2->pos, v1->pos);
+    double nom = (double)((bsa1 + bsa2) * 0.625);
+    double rel = nom - vlen(offset);
+    vec f = V(0, 0, 0);
+    if (rel > 0) {
+        vec u = vnormalized(offset);
+        double rv = vdot(vscale(v1->linMom, m1->mass_inv), u) - vdot(vscale(v2->linMom, m2->mass_inv), u);
+        f = vscale(u, pstiff * rel + dampC * rv);
+    }
+    v1->contact = vadd(v1->contact, f);
+    v2->contact = vadd(v2->contact, vneg(f));
+}
+
+/* doTimeStep (VX3_VoxelyzeKernel.cu:237-359) */
+static int do_step(sim *S) {
+    const vxo_robot *r = &S->r;
+    /* gpu_update_temperature (:625-650) + setTemperature (VX3_Voxel.cu:107-113) */
+    if (r->vary_temp && r->temp_period > 0) {
+        for (int i = 0; i < S->nv; i++) {
+            voxel *v = &S->v[i];
+            const vmat *m = &S->vm[v->mat];
+            if (m->thermal_on_after > S->t) continue;
+            if (m->fixed) continue;
+            double T = r->temp_amplitude * sin(2 * 3.1415926f * (S->t / r->temp_period + v->phase));
+            if (!r->enable_expansion && T > 0) T = 0;
+            v->tempe = (float)T;
+            for (int d = 0; d < 6; d++)
+                if (v->links[d] >= 0) update_rest(S, &S->l[v->links[d]]);
+        }
+    }
+    if (!S->optimal_dt) S->optimal_dt = vxo_recommended_dt(S);
+    if (S->optimal_dt < 1e-10) S->optimal_dt = 1e-10;
+    float dt = S->r.dt_frac * S->optimal_dt;
+    S->dt = dt;
+    /* gpu_update_links (:566-581), divergence over every link */
+    int div = 0;
+    for (int i = 0; i < S->nl; i++) {
+        link *L = &S->l[i];
+        if (S->vm[S->v[L->neg].mat].fixed && S->vm[S->v[L->pos].mat].fixed) continue;
+        link_update(S, L);
+        if (L->strain > 100) div = 1;
+    }
+    if (div) return 0;
+    /* regenerateSurfaceVoxels (:495-513, VX3_Voxel.cu:515-524) */
+    if (S->surface_stale) {
+        S->surface_stale = 0;
+        S->ns = 0;
+        for (int i = 0; i < S->nv; i++) {
+            int interior = 1;
+            for (int d = 0; d < 6; d++) if (S->v[i].links[d] < 0) interior = 0;
+            if (interior) S->v[i].flags |= F_SURFACE; else S->v[i].flags &= ~F_SURFACE;
+            if (!interior) S->surf[S->ns++] = i;
+        }
+    }
+    /* gpu_update_attach (:833-843): pairs first > second in surface order */
+    if (r->enable_collision) {
+        for (int a = 0; a < S->ns; a++)
+            for (int b = 0; b < a; b++) collide(S, &S->v[S->surf[a]], &S->v[S->surf[b]], S->surf[a], S->surf[b]);
+    }
+    for (int i = 0; i < S->nv; i++) {
+        S->last_contact[3 * i] = S->v[i].contact.x;
+        S->last_contact[3 * i + 1] = S->v[i].contact.y;
+        S->last_contact[3 * i + 2] = S->v[i].contact.z;
+    }
+    /* gpu_update_voxels (:582-623) */
+    for (int i = 0; i < S->nv; i++) {
+        if (S->vm[S->v[i].mat].fixed) continue;
+        voxel_update(S, &S->v[i], dt);
+    }
+    S->t += dt;
+    return 1;
+}
+
+int vxo_step(void *h, int n) {
+    sim *S = (sim *)h;
+    int done = 0;
+    for (int i = 0; i < n && !S->diverged; i++) {
+        if (!do_step(S)) { S->diverged = 1; break; }
+        done++;
+    }
+    return done;
+}
+
+void vxo_counts(void *h, int *nv, int *nl, int *ns) {
+    sim *S = (sim *)h;
+    *nv = S->nv; *nl = S->nl; *ns = S->ns;
+}
+double vxo_time(void *h) { return ((sim *)h)->t; }
+float vxo_dt(void *h) { return ((sim *)h)->dt; }
+
+void vxo_voxels(void *h, double *pos, double *orient, double *linmom, double *angmom, float *tempe, int *flags) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nv; i++) {
+        voxel *v = &S->v[i];
+        pos[3 * i] = v->pos.x; pos[3 * i + 1] = v->pos.y; pos[3 * i + 2] = v->pos.z;
+        orient[4 * i] = v->orient.w; orient[4 * i + 1] = v->orient.x; orient[4 * i + 2] = v->orient.y; orient[4 * i + 3] = v->orient.z;
+        linmom[3 * i] = v->linMom.x; linmom[3 * i + 1] = v->linMom.y; linmom[3 * i + 2] = v->linMom.z;
+        angmom[3 * i] = v->angMom.x; angmom[3 * i + 1] = v->angMom.y; angmom[3 * i + 2] = v->angMom.z;
+        tempe[i] = v->tempe;
+        flags[i] = v->flags;
+    }
+}
+
+void vxo_set_voxels(void *h, const double *pos, const double *orient, const double *linmom, const double *angmom) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nv; i++) {
+        voxel *v = &S->v[i];
+        v->pos = V(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        v->orient = Q(orient[4 * i], orient[4 * i + 1], orient[4 * i + 2], orient[4 * i + 3]);
+        v->linMom = V(linmom[3 * i], linmom[3 * i + 1], linmom[3 * i + 2]);
+        v->angMom = V(angmom[3 * i], angmom[3 * i + 1], angmom[3 * i + 2]);
+    }
+}
+
+void vxo_topology(void *h, int *mat, int *ijk, int *slots) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nv; i++) {
+        mat[i] = S->v[i].mat;
+        ijk[3 * i] = S->v[i].ix; ijk[3 * i + 1] = S->v[i].iy; ijk[3 * i + 2] = S->v[i].iz;
+        for (int d = 0; d < 6; d++) slots[6 * i + d] = S->v[i].links[d];
+    }
+}
+
+void vxo_link_topology(void *h, int *negpos, int *axis, int *small, int *states) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nl; i++) {
+        negpos[2 * i] = S->l[i].neg; negpos[2 * i + 1] = S->l[i].pos;
+        axis[i] = S->l[i].axis; small[i] = S->l[i].small; states[i] = S->l[i].states;
+    }
+}
+
+void vxo_links(void *h, float *strain, float *maxstrain, double *rest, double *local9, double *forces12) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nl; i++) {
+        link *L = &S->l[i];
+        strain[i] = L->strain; maxstrain[i] = L->maxStrain; rest[i] = L->rest;
+        double *p = local9 + 9 * i;
+        p[0] = L->pos2.x; p[1] = L->pos2.y; p[2] = L->pos2.z;
+        p[3] = L->a1v.x; p[4] = L->a1v.y; p[5] = L->a1v.z;
+        p[6] = L->a2v.x; p[7] = L->a2v.y; p[8] = L->a2v.z;
+        double *f = forces12 + 12 * i;
+        f[0] = L->fNeg.x; f[1] = L->fNeg.y; f[2] = L->fNeg.z;
+        f[3] = L->fPos.x; f[4] = L->fPos.y; f[5] = L->fPos.z;
+        f[6] = L->mNeg.x; f[7] = L->mNeg.y; f[8] = L->mNeg.z;
+        f[9] = L->mPos.x; f[10] = L->mPos.y; f[11] = L->mPos.z;
+    }
+}
+
+void vxo_voxel_mats(void *h, float *f16, double *nomsize, int *fm) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nvm; i++) {
+        vmat *m = &S->vm[i];
+        float *f = f16 + 16 * i;
+        f[0] = m->mass; f[1] = m->mass_inv; f[2] = m->sqrt_mass; f[3] = m->mom_inertia; f[4] = m->mom_inertia_inv;
+        f[5] = m->c2xSqMxExS; f[6] = m->c2xSqIxExSxSxS; f[7] = m->z_int; f[8] = m->z_glob; f[9] = m->z_col;
+        f[10] = m->mu_s; f[11] = m->mu_k; f[12] = m->E; f[13] = m->nu; f[14] = m->cte; f[15] = m->grav_mult;
+        nomsize[i] = m->nom_size;
+        fm[2 * i] = m->fixed; fm[2 * i + 1] = m->is_measured;
+    }
+}
+
+int vxo_num_link_mats(void *h) { return ((sim *)h)->nlm; }
+
+void vxo_link_mats(void *h, float *f16, int *lmat_of_link) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nlm; i++) {
+        lmat *m = &S->lm[i];
+        float *f = f16 + 16 * i;
+        f[0] = m->E; f[1] = m->nu; f[2] = m->eHat; f[3] = m->a1; f[4] = m->a2; f[5] = m->b1; f[6] = m->b2; f[7] = m->b3;
+        f[8] = m->sqA1; f[9] = m->sqA2xIp; f[10] = m->sqB1; f[11] = m->sqB2xFMp; f[12] = m->sqB3xIp;
+        f[13] = m->eps_fail; f[14] = 1.0f; f[15] = m->cte;
+    }
+    for (int i = 0; i < S->nl; i++) lmat_of_link[i] = S->l[i].mat;
+}
+
+void vxo_surface(void *h, int *idx) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->ns; i++) idx[i] = S->surf[i];
+}
+
+void vxo_last_contact(void *h, double *c3) {
+    sim *S = (sim *)h;
+    memcpy(c3, S->last_contact, sizeof(double) * 3 * (size_t)S->nv);
+}
+
+/* updateCurrentCenterOfMass (VX3_VoxelyzeKernel.cu:477-493) */
+void vxo_com(void *h, double *c3) {
+    sim *S = (sim *)h;
+    double total = 0;
+    vec sum = V(0, 0, 0);
+    for (int i = 0; i < S->nv; i++) {
+        const vmat *m = &S->vm[S->v[i].mat];
+        if (!m->is_measured) continue;
+        double mass = m->mass;
+        sum = vadd(sum, vscale(S->v[i].pos, mass));
+        total += mass;
+    }
+    vec c = V(0, 0, 0);
+    if (total != 0) c = vdiv(sum, total);
+    c3[0] = c.x; c3[1] = c.y; c3[2] = c.z;
+}

@@ -1,0 +1,64 @@
+/* vx3_oracle.h -- CPU restatement of the reference VX3 time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GB300
+ * kernels: tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+ * may load it; nothing in the shipped library links or calls it.
+ *
+ * Parity is pinned: tests/test_oracle_golden.py compares this restatement,
+ * bit for bit, against golden vectors produced by the reference's own
+ * sources compiled on the host (oracle/Makefile target `ref`,
+ * tests/golden/make_golden.py).
+ */
+#ifndef VX3_ORACLE_H
+#define VX3_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One palette entry, values as read from the VXA <Material> element. */
+typedef struct vxo_material {
+    double E, nu, rho, cte, mu_static, mu_kinetic;
+    double fail_stress;      /* used when model == 1 (MDL_LINEAR_FAIL) */
+    int model;               /* 0 = MDL_LINEAR, 1 = MDL_LINEAR_FAIL */
+    int fixed, is_measured;
+    double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
+} vxo_material;
+
+/* One simulation (one merged VXA). */
+typedef struct vxo_robot {
+    int nx, ny, nz;
+    const unsigned char *lattice; /* nx*ny*nz palette ids, x fastest, then y, then z */
+    const double *phase;          /* nx*ny*nz phase offsets (cycles) or NULL */
+    int n_materials;
+    const vxo_material *materials;
+    double vox_size, dt_frac, grav_acc;
+    int floor_enabled;
+    double temp_amplitude, temp_period, temp_base;
+    int temp_enabled, vary_temp, enable_expansion, enable_collision, volume_effects;
+    double bond_damping, col_damping, slow_damping;
+} vxo_robot;
+
+void *vxo_create(const vxo_robot *r);
+void vxo_destroy(void *h);
+void vxo_counts(void *h, int *nv, int *nl, int *nsurf);
+int vxo_step(void *h, int n);
+double vxo_time(void *h);
+float vxo_dt(void *h);
+void vxo_voxels(void *h, double *pos, double *orient, double *linmom, double *angmom, float *tempe, int *flags);
+void vxo_set_voxels(void *h, const double *pos, const double *orient, const double *linmom, const double *angmom);
+void vxo_topology(void *h, int *mat, int *ijk, int *slots);
+void vxo_link_topology(void *h, int *negpos, int *axis, int *small, int *states);
+void vxo_links(void *h, float *strain, float *maxstrain, double *rest, double *local9, double *forces12);
+void vxo_voxel_mats(void *h, float *f16, double *nomsize, int *fixed_measured);
+void vxo_link_mats(void *h, float *f16, int *lmat_of_link);
+int vxo_num_link_mats(void *h);
+void vxo_surface(void *h, int *idx);
+void vxo_last_contact(void *h, double *c3);
+void vxo_com(void *h, double *c3);
+double vxo_recommended_dt(void *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,113 @@
+"""Generate golden vectors from the reference's own VX3 physics (host build).
+
+Run where the reference tree is mounted:
+
+    make -C oracle ref            # compiles the reference sources into oracle/_ref/
+    python tests/golden/make_golden.py
+
+Each case is a small seeded robot.  The VXA document is fed to the
+reference's own reader (CXML_Rip + CVX_Sim::ReadVXA/Import) and stepped by the
+reference's VX3_Link/VX3_Voxel/VX3_Collision code; snapshots of the state are
+written to tests/golden/<case>.npz together with the inputs needed to rebuild
+the same robot without the reference (lattice, phase, palette, settings).
+The reference produces no golden vectors of its own for this path, so these
+files are what pins the oracle and, through it, the GB300 kernels.
+"""
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+import __graft_entry__  # noqa: E402
+
+__graft_entry__.load_package()
+import vx3g.workloads as wl  # noqa: E402
+import oracle_bridge as ob  # noqa: E402
+
+
+def cases():
+    """name -> (robot, steps, snapshot every)"""
+    out = {}
+    out["block3_drop"] = (wl.solid_block(3), 600, 200)
+    out["block10_drop"] = (wl.solid_block(10), 200, 100)
+    rng = np.random.default_rng(1)
+    mats = [wl.Material(E=1e6, nu=0.35, cte=0.0), wl.Material(E=1e6, nu=0.35, cte=0.01)]
+    out["bern6_thermal_collision"] = (
+        wl.bernoulli_body(rng, (6, 6, 6), 0.6, mats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                          temp_period=0.2, enable_collision=True, enable_expansion=1, z_offset=1), 400, 100)
+    rng = np.random.default_rng(2)
+    mats4 = [wl.Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]
+    out["bern8_4mat_phase"] = (
+        wl.bernoulli_body(rng, (8, 7, 5), 0.7, mats4, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                          temp_period=0.2, z_offset=0), 300, 100)
+    soft = [wl.Material(E=2e4, nu=0.0, rho=1e3, mu_static=0.2, mu_kinetic=0.1)]
+    grid = np.zeros((3, 2, 9), np.uint8)
+    grid[2, :, :] = 1        # a thin overhanging sheet ...
+    grid[:, :, 0:2] = 1      # ... on a short pillar: the free end sags into the large-angle branch
+    out["soft_cantilever_large_angle"] = (wl.Robot(grid=grid, materials=soft, volume_effects=False, z_offset=0),
+                                          1500, 500)
+    brittle = [wl.Material(E=2e4, nu=0.0, fail_stress=40.0, mu_static=0.2, mu_kinetic=0.1)]
+    out["brittle_failure"] = (wl.Robot(grid=grid.copy(), materials=brittle, volume_effects=False, z_offset=0),
+                              900, 300)
+    return out
+
+
+def snapshot(s):
+    v = s.voxels()
+    lk = s.links()
+    t = s.topology()
+    return dict(small=t["small"], states=t["states"], pos=v["pos"], orient=v["orient"], linmom=v["linmom"], angmom=v["angmom"], tempe=v["tempe"],
+                flags=v["flags"], strain=lk["strain"], maxstrain=lk["maxstrain"], rest=lk["rest"],
+                local9=lk["local9"], forces=lk["forces"], contact=s.last_contact(), com=s.com(),
+                time=np.array([s.time()]), dt=np.array([s.dt()], np.float32))
+
+
+def robot_record(r):
+    g, ph = r.padded()
+    mats = np.array([[m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress, m.fixed, m.is_measured]
+                     for m in r.materials], np.float64)
+    settings = dict(vox_size=r.vox_size, dt_frac=r.dt_frac, bond_damping=r.bond_damping, col_damping=r.col_damping,
+                    slow_damping=r.slow_damping, gravity=r.gravity, grav_acc=r.grav_acc, floor=r.floor,
+                    temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,
+                    temp_base=r.temp_base, enable_expansion=r.enable_expansion, enable_collision=r.enable_collision,
+                    volume_effects=r.volume_effects)
+    return dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
+                settings=np.array(json.dumps(settings)))
+
+
+def main():
+    if not ob.ref_available():
+        sys.exit("reference build missing: run `make -C oracle ref` first")
+    for name, (robot, steps, every) in cases().items():
+        s = ob.ref_sim(robot)
+        nv, nl, _ = s.counts()
+        rec = robot_record(robot)
+        topo = s.topology()
+        mats = s.materials(len(robot.materials))
+        rec.update({"topo_" + k: v for k, v in topo.items()})
+        rec.update({"mat_" + k: v for k, v in mats.items()})
+        rec["recommended_dt0"] = np.array([s.recommended_dt()])
+        done, snaps = 0, []
+        while done < steps:
+            n = s.step(every)
+            done += every
+            snaps.append(done)
+            for k, v in snapshot(s).items():
+                rec[f"s{done}_{k}"] = v
+            rec[f"s{done}_surface"] = s.surface()
+            if n < every:
+                break
+        rec["snap_steps"] = np.array(snaps)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **rec)
+        print(f"{name}: nv={nv} nl={nl} snaps={snaps} t={s.time():.6g} com={s.com()}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,25 @@
+"""Load the golden fixtures of tests/golden/ back into workloads.Robot objects."""
+
+import glob
+import json
+import os
+
+import numpy as np
+
+from vx3g import workloads as wl
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+
+
+def load(name):
+    d = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    s = json.loads(str(d["settings"]))
+    mats = [wl.Material(E=m[0], nu=m[1], rho=m[2], cte=m[3], mu_static=m[4], mu_kinetic=m[5], fail_stress=m[6],
+                        fixed=int(m[7]), is_measured=int(m[8])) for m in d["materials"]]
+    phase = d["phase"] if d["phase"].size else None
+    robot = wl.Robot(grid=d["lattice"], materials=mats, phase=phase, z_offset=0, **s)
+    return robot, d

@@ -1,0 +1,200 @@
+"""ctypes bridge to the two CPU checkers (test infrastructure).
+
+* the C restatement  oracle/_build/liboracle.so  (built from oracle/vx3_oracle.c)
+* the reference build oracle/_ref/libvx3ref.so   (built from the reference
+  sources; only present where the reference tree is mounted)
+
+Both expose the same getters, so a test can run the same synthetic robot
+through either and compare arrays.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+REF_SO = os.path.join(ROOT, "oracle", "_ref", "libvx3ref.so")
+
+
+class VxoMaterial(ctypes.Structure):
+    _fields_ = [("E", ctypes.c_double), ("nu", ctypes.c_double), ("rho", ctypes.c_double),
+                ("cte", ctypes.c_double), ("mu_static", ctypes.c_double), ("mu_kinetic", ctypes.c_double),
+                ("fail_stress", ctypes.c_double), ("model", ctypes.c_int), ("fixed", ctypes.c_int),
+                ("is_measured", ctypes.c_int), ("thermal_on_after", ctypes.c_double)]
+
+
+class VxoRobot(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("lattice", ctypes.c_void_p), ("phase", ctypes.c_void_p),
+                ("n_materials", ctypes.c_int), ("materials", ctypes.POINTER(VxoMaterial)),
+                ("vox_size", ctypes.c_double), ("dt_frac", ctypes.c_double), ("grav_acc", ctypes.c_double),
+                ("floor_enabled", ctypes.c_int),
+                ("temp_amplitude", ctypes.c_double), ("temp_period", ctypes.c_double), ("temp_base", ctypes.c_double),
+                ("temp_enabled", ctypes.c_int), ("vary_temp", ctypes.c_int), ("enable_expansion", ctypes.c_int),
+                ("enable_collision", ctypes.c_int), ("volume_effects", ctypes.c_int),
+                ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double)]
+
+
+def build_oracle():
+    if not os.path.exists(ORACLE_SO):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"])
+    return ORACLE_SO
+
+
+def _P(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _setup(lib, prefix):
+    h = ctypes.c_void_p
+    for name, res, args in [
+        ("destroy", None, [h]),
+        ("counts", None, [h, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+        ("step", ctypes.c_int, [h, ctypes.c_int]),
+        ("time", ctypes.c_double, [h]),
+        ("dt", ctypes.c_float, [h]),
+        ("voxels", None, [h] + [ctypes.c_void_p] * 6),
+        ("topology", None, [h] + [ctypes.c_void_p] * 3),
+        ("link_topology", None, [h] + [ctypes.c_void_p] * 4),
+        ("links", None, [h] + [ctypes.c_void_p] * 5),
+        ("voxel_mats", None, [h] + [ctypes.c_void_p] * 3),
+        ("link_mats", None, [h] + [ctypes.c_void_p] * 2),
+        ("num_link_mats", ctypes.c_int, [h]),
+        ("surface", None, [h, ctypes.c_void_p]),
+        ("last_contact", None, [h, ctypes.c_void_p]),
+        ("com", None, [h, ctypes.c_void_p]),
+        ("recommended_dt", ctypes.c_double, [h]),
+    ]:
+        f = getattr(lib, prefix + name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+class Sim:
+    """A robot running on one of the CPU checkers; same getters for both."""
+
+    def __init__(self, lib, prefix, handle, keep):
+        self.lib, self.p, self.h, self._keep = lib, prefix, ctypes.c_void_p(handle), keep
+
+    def _f(self, name):
+        return getattr(self.lib, self.p + name)
+
+    def counts(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._f("counts")(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def step(self, n):
+        return self._f("step")(self.h, n)
+
+    def time(self):
+        return self._f("time")(self.h)
+
+    def dt(self):
+        return self._f("dt")(self.h)
+
+    def recommended_dt(self):
+        return self._f("recommended_dt")(self.h)
+
+    def voxels(self):
+        nv = self.counts()[0]
+        pos, lm, am = np.zeros((nv, 3)), np.zeros((nv, 3)), np.zeros((nv, 3))
+        orient = np.zeros((nv, 4))
+        tempe = np.zeros(nv, np.float32)
+        flags = np.zeros(nv, np.int32)
+        self._f("voxels")(self.h, _P(pos), _P(orient), _P(lm), _P(am), _P(tempe), _P(flags))
+        return dict(pos=pos, orient=orient, linmom=lm, angmom=am, tempe=tempe, flags=flags)
+
+    def topology(self):
+        nv, nl, _ = self.counts()
+        mat = np.zeros(nv, np.int32)
+        ijk = np.zeros((nv, 3), np.int32)
+        slots = np.zeros((nv, 6), np.int32)
+        self._f("topology")(self.h, _P(mat), _P(ijk), _P(slots))
+        negpos = np.zeros((nl, 2), np.int32)
+        axis, small, states = (np.zeros(nl, np.int32) for _ in range(3))
+        self._f("link_topology")(self.h, _P(negpos), _P(axis), _P(small), _P(states))
+        return dict(mat=mat, ijk=ijk, slots=slots, negpos=negpos, axis=axis, small=small, states=states)
+
+    def links(self):
+        nl = self.counts()[1]
+        strain, maxstrain = np.zeros(nl, np.float32), np.zeros(nl, np.float32)
+        rest = np.zeros(nl)
+        local9 = np.zeros((nl, 9))
+        forces = np.zeros((nl, 12))
+        self._f("links")(self.h, _P(strain), _P(maxstrain), _P(rest), _P(local9), _P(forces))
+        return dict(strain=strain, maxstrain=maxstrain, rest=rest, local9=local9, forces=forces)
+
+    def materials(self, n_voxel_mats):
+        f = np.zeros((n_voxel_mats, 16), np.float32)
+        ns = np.zeros(n_voxel_mats)
+        fm = np.zeros((n_voxel_mats, 2), np.int32)
+        self._f("voxel_mats")(self.h, _P(f), _P(ns), _P(fm))
+        nlm = self._f("num_link_mats")(self.h)
+        lf = np.zeros((max(nlm, 1), 16), np.float32)
+        lol = np.zeros(max(self.counts()[1], 1), np.int32)
+        self._f("link_mats")(self.h, _P(lf), _P(lol))
+        return dict(vmat=f, nomsize=ns, fixed_measured=fm, lmat=lf[:nlm], lmat_of_link=lol[:self.counts()[1]])
+
+    def surface(self):
+        ns = self.counts()[2]
+        idx = np.zeros(max(ns, 1), np.int32)
+        self._f("surface")(self.h, _P(idx))
+        return idx[:ns]
+
+    def last_contact(self):
+        nv = self.counts()[0]
+        c = np.zeros((nv, 3))
+        self._f("last_contact")(self.h, _P(c))
+        return c
+
+    def com(self):
+        c = np.zeros(3)
+        self._f("com")(self.h, _P(c))
+        return c
+
+
+def robot_struct(robot):
+    """Pack a workloads.Robot into the oracle's vxo_robot (lattice with z_offset padding)."""
+    g, ph = robot.padded()
+    lattice = np.ascontiguousarray(g.reshape(-1).astype(np.uint8))
+    phase = None if ph is None else np.ascontiguousarray(ph.reshape(-1).astype(np.float64))
+    mats = (VxoMaterial * max(len(robot.materials), 1))()
+    for i, m in enumerate(robot.materials):
+        mats[i] = VxoMaterial(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic,
+                              m.fail_stress, 0 if m.fail_stress == 0 else 1, m.fixed, m.is_measured, 0.0)
+    Z, Y, X = g.shape
+    r = VxoRobot(X, Y, Z, _P(lattice), None if phase is None else _P(phase), len(robot.materials), mats,
+                 robot.vox_size, robot.dt_frac, robot.grav_acc, int(robot.floor),
+                 robot.temp_amplitude, robot.temp_period, robot.temp_base, 0, int(robot.temp_vary),
+                 int(robot.enable_expansion), int(robot.enable_collision), int(robot.volume_effects),
+                 robot.bond_damping, robot.col_damping, robot.slow_damping)
+    return r, (lattice, phase, mats)
+
+
+def oracle_sim(robot) -> Sim:
+    lib = _setup(ctypes.CDLL(build_oracle()), "vxo_")
+    lib.vxo_create.restype = ctypes.c_void_p
+    lib.vxo_create.argtypes = [ctypes.POINTER(VxoRobot)]
+    r, keep = robot_struct(robot)
+    h = lib.vxo_create(ctypes.byref(r))
+    return Sim(lib, "vxo_", h, (r, keep))
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref_sim(robot) -> Sim:
+    from vx3g.workloads import to_vxa
+    lib = _setup(ctypes.CDLL(REF_SO), "vx3ref_")
+    lib.vx3ref_create.restype = ctypes.c_void_p
+    lib.vx3ref_create.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+    h = lib.vx3ref_create(to_vxa(robot).encode(), int(robot.enable_collision), int(robot.enable_expansion))
+    return Sim(lib, "vx3ref_", h, None)
