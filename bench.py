@@ -1,0 +1,293 @@
+"""Benchmark of the GB300 VX3 step: voxel-steps/s, mixed precision vs FP64.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl vx3g|reference]
+                    [--workload c2|c1|c3|c5] [--precision mixed|fp64]
+
+A bench "step" is one CUDA-graph chunk of --chunk (default 100) physics time
+steps over the whole batch.  Timed steps are bracketed by CUDA events on the
+library's stream; the L2 cache is flushed (512 MB overwrite) before every timed
+chunk.  The default workload is the single large body (64^3 Bernoulli(0.6),
+collisions + floor, mixed precision).  Under torchrun each rank runs its own
+replica of the workload on its own GPU (robots are independent; no collective).
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+import __graft_entry__  # noqa: E402
+
+__graft_entry__.load_package()
+from vx3g import abi, workloads  # noqa: E402
+
+METRIC = "voxel-steps/s: mixed vs FP64 on GB300 at <=1e-5 rel COM err; bwd/fwd ratio"
+UNIT = "voxel-steps/s"
+
+WORKLOADS = {
+    "c1": ("10x10x10 solid block drop, 1 robot, floor+friction, no collisions", workloads.c1_block_drop),
+    "c2": ("64^3 Bernoulli(0.6) single body, 2 materials, 39C/5Hz actuation, self-collision + floor",
+           workloads.c2_single_body),
+    "c3": ("1024 robots [4,16]^3 Bernoulli(0.7), 4 materials, per-voxel phase, floor, no collisions",
+           workloads.c3_population),
+    "c5": ("256 robots [8,20]^3 Bernoulli(0.65), 4 materials, self-collision + floor", workloads.c5_population_collisions),
+}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(nv, nl, ns, actuated, contacts=0):
+    """Canonical bytes per physics step: link pass, voxel pass, collision."""
+    link = 164 * nl + 56 * nv + (4 * nl if actuated else 0)
+    voxel = 48 * nl + 240 * nv + (8 * nv if actuated else 0)
+    coll = 48 * ns + 24 * contacts
+    return dict(links=link, voxels=voxel, collision=coll)
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def barrier_and_max(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def init_dist(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return dist
+    return None
+
+
+def cpu_baseline_port(robots, threads, budget_s=20.0, max_steps=200):
+    """Time the oracle (the C restatement of the reference step, with the
+    reference's all-pairs surface collision loop) on the host, on a bounded
+    sample of the same workload: whole link+voxel steps of every robot for half
+    the budget, and leading rows of each robot's all-pairs collision loop for
+    the other half, scaled to the full S(S-1)/2 pairs.  Returns
+    (voxel-steps/s, sample description)."""
+    import oracle_bridge as ob
+    sims = [ob.oracle_sim(r) for r in robots]
+    for s in sims:
+        s.set_threads(threads)
+    nv = sum(s.counts()[0] for s in sims)
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps:
+        for s in sims:
+            s.step_no_collision(1)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s / 2:
+            break
+    t_lv = (time.perf_counter() - t0) / steps
+    t_coll, rows_note = 0.0, ""
+    coll = [(s, r) for s, r in zip(sims, robots) if r.enable_collision]
+    if coll:
+        per_robot_budget = budget_s / 2 / len(coll)
+        done_pairs = total_pairs = 0
+        for s, _ in coll:
+            ns = s.counts()[2]
+            pairs = ns * (ns - 1) / 2
+            k, spent = 0, 0.0
+            while k < ns and spent < per_robot_budget:
+                k2 = min(ns, max(k + 64, int(k * 1.5)))
+                spent += s.time_collision_rows(k, k2)
+                k = k2
+            done = k * (k - 1) / 2
+            t_coll += spent * (pairs / done) if done else 0.0
+            done_pairs += done
+            total_pairs += pairs
+        rows_note = f"; all-pairs collision timed on {done_pairs:.3g} of {total_pairs:.3g} surface pairs and scaled by pair count"
+    per_step = t_lv + t_coll
+    sample = (f"{steps} link+voxel step(s) of the full workload ({len(robots)} robot(s), {nv} voxels){rows_note}; "
+              f"{threads} thread(s)")
+    return nv / per_step, sample
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    builder = WORKLOADS[args.workload][1]
+    robots = builder()
+    cores = os.cpu_count() or 1
+    value, sample = cpu_baseline_port(robots, cores, budget_s=args.ref_budget)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "config": {"workload": WORKLOADS[args.workload][0], "robots": len(robots)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="vx3g", choices=["vx3g", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--chunk", type=int, default=100)
+    ap.add_argument("--ref-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank, world, local = dist_env()
+    dist = init_dist(world)
+    dev = local
+    desc, builder = WORKLOADS[args.workload]
+    robots = builder()
+    prec = abi.PRECISION_MIXED if args.precision == "mixed" else abi.PRECISION_FP64
+    b = abi.Batch(robots, prec, device=dev, graph_chunk=args.chunk)
+    actuated = any(r.temp_vary for r in robots)
+    surf = b.surface()
+    ns_coll = 0
+    for i, r in enumerate(robots):
+        if r.enable_collision:
+            ns_coll += int(np.count_nonzero((surf >= b.voxel_offset[i]) & (surf < b.voxel_offset[i + 1])))
+    W, K, C = args.warmup, args.steps, args.chunk
+    for _ in range(W):
+        b.step(C)
+    b.synchronize()
+    if dist:
+        dist.barrier()
+    per_chunk = []
+    with ClockSampler(dev) as clk:
+        for _ in range(K):
+            b.flush_l2()
+            per_chunk.append(b.time_steps(C))
+    b.synchronize()
+    if dist:
+        dist.barrier()
+    total_ms = barrier_and_max(float(np.sum(per_chunk)), world)
+    status = b.status()
+    vox_steps = b.nv * C * K * world
+    value = vox_steps / (total_ms / 1e3)
+
+    # e2e through the C ABI with host buffers: upload state, run a chunk, read COM back
+    st = b.state()
+    h2d = sum(a.nbytes for a in st.values())
+    t0 = time.perf_counter()
+    E = max(3, K // 5)
+    for _ in range(E):
+        b.set_state(**st)
+        b.step(C)
+        com = b.com()
+    e2e_s = time.perf_counter() - t0
+    d2h = com.nbytes
+    e2e_value = b.nv * C * E * world / e2e_s
+
+    # per-pass device times (after the measured run)
+    passes = b.time_passes(20)
+    ab = algorithmic_bytes(b.nv, b.nl, ns_coll, actuated)
+    shares = {k: passes[k] for k in passes}
+    dom = max(shares, key=shares.get)
+    peak, peak_kind = peaks()
+    achieved = ab[dom] / (passes[dom] / 1e3) / 1e9 if passes[dom] > 0 else 0.0
+    kernels_per_step = 2 + (5 if ns_coll else 0)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 link forces + f64 integration" if prec else "f64", "data": "synthetic (seeded generator)",
+        "config": {"workload": desc, "robots": len(robots), "voxels": b.nv, "links": b.nl,
+                   "collision_surface_voxels": ns_coll, "precision": args.precision,
+                   "physics_steps_per_bench_step": C,
+                   "l2": "512 MB overwrite before every timed chunk", "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "pass_ms": passes, "algorithmic_bytes_per_launch": ab},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": kernels_per_step * C * K,
+        "clocks": clk.summary(),
+        "robot_status_nonzero": int(np.count_nonzero(status)),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, sample = cpu_baseline_port(robots, 1, budget_s=15.0, max_steps=50)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

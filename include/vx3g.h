@@ -1,0 +1,159 @@
+/* vx3g.h -- C ABI of the GB300-native VX3 voxel-physics step.
+ *
+ * One context holds a batch of independent simulations ("robots"), each the
+ * equivalent of one VX3_VoxelyzeKernel built from one merged VXA document in
+ * the reference.  All state lives in GPU memory owned by the context; every
+ * call below takes and returns plain host pointers and sizes.  No call throws;
+ * every call returns VX3G_OK (0) or a negative error code, and
+ * vx3g_last_error() gives a one-line reason for the calling thread's last
+ * failure.  A context is not re-entrant: use one context per host thread.
+ *
+ * Reference interfaces each entry point replaces (voxcraft-sim source tree):
+ *   vx3g_create       VX3_VoxelyzeKernel::VX3_VoxelyzeKernel(CVX_Sim*)   src/VX3/VX3_VoxelyzeKernel.cu:27-105
+ *                     + the per-file setup of VX3_SimulationManager::readVXD  src/VX3/VX3_SimulationManager.cu:277-381
+ *   vx3g_step         VX3_VoxelyzeKernel::doTimeStep(float dt = -1), called in the
+ *                     CUDA_Simulation step loop                           src/VX3/VX3_VoxelyzeKernel.cu:237-359,
+ *                                                                         src/VX3/VX3_SimulationManager.cu:62-115
+ *   vx3g_dt           VX3_VoxelyzeKernel::recommendedTimeStep()*DtFrac    src/VX3/VX3_VoxelyzeKernel.cu:184-217,241-254
+ *   vx3g_com          VX3_VoxelyzeKernel::updateCurrentCenterOfMass()     src/VX3/VX3_VoxelyzeKernel.cu:477-493
+ *   vx3g_get_state    the device->host copy of voxel state in
+ *                     VX3_SimulationManager::collectResults               src/VX3/VX3_SimulationManager.cu:428-470
+ *   vx3g_status       doTimeStep's false return on divergence             src/VX3/VX3_VoxelyzeKernel.cu:271-281
+ *   vx3g_destroy      VX3_VoxelyzeKernel::cleanup()                       src/VX3/VX3_VoxelyzeKernel.cu:107-119
+ */
+#ifndef VX3G_H
+#define VX3G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ------------------------------------------------------ */
+#define VX3G_OK 0
+#define VX3G_ERR_INVALID (-1)      /* bad argument or descriptor */
+#define VX3G_ERR_UNSUPPORTED (-2)  /* input uses a feature outside the supported scope */
+#define VX3G_ERR_CUDA (-3)         /* CUDA runtime error (no device, launch failure, ...) */
+#define VX3G_ERR_NOMEM (-4)        /* device or host allocation failed */
+#define VX3G_ERR_DEVICE (-5)       /* a kernel reported an internal error (see vx3g_status) */
+
+/* ---- per-robot status words (vx3g_status) -------------------------------- */
+#define VX3G_ROBOT_OK 0
+#define VX3G_ROBOT_DIVERGED 1          /* a link strain exceeded 100; the robot stops stepping */
+#define VX3G_ROBOT_CONTACT_OVERFLOW 2  /* more contact candidates than one voxel can hold */
+
+/* ---- precision of the step ---------------------------------------------- */
+#define VX3G_PRECISION_FP64 0   /* the reference's arithmetic: FP64 vectors, FP32 scalars where it uses float */
+#define VX3G_PRECISION_MIXED 1  /* FP32 link forces/moments, FP64 position/orientation/momentum integration */
+
+/* One palette entry, with the values of the VXA <Material><Mechanical> element. */
+typedef struct vx3g_material {
+    double E;             /* Elastic_Mod (Pa) */
+    double nu;            /* Poissons_Ratio */
+    double rho;           /* Density (kg/m^3) */
+    double cte;           /* CTE (1/degC) */
+    double mu_static;     /* uStatic */
+    double mu_kinetic;    /* uDynamic */
+    double fail_stress;   /* Fail_Stress (Pa), used when model == 1 */
+    int model;            /* MatModel: 0 linear, 1 linear with failure; others -> VX3G_ERR_UNSUPPORTED */
+    int fixed;            /* Fixed */
+    int is_measured;      /* isMeasured (counts toward the centre of mass) */
+    double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
+} vx3g_material;
+
+/* One simulation: the content of a merged VXA document. */
+typedef struct vx3g_robot_desc {
+    int nx, ny, nz;                 /* X_Voxels, Y_Voxels, Z_Voxels */
+    const uint8_t *lattice;         /* nx*ny*nz palette ids, x fastest then y then z; 0 = empty */
+    const double *phase;            /* nx*ny*nz PhaseOffset values (cycles) or NULL for 0 */
+    int n_materials;                /* palette ids 1..n_materials, at most 16 */
+    const vx3g_material *materials;
+    double vox_size;                /* Lattice_Dim (m) */
+    double dt_frac;                 /* Integration/DtFrac */
+    double grav_acc;                /* Gravity/GravAcc (m/s^2); the reference applies it whatever GravEnabled says */
+    int floor_enabled;              /* Gravity/FloorEnabled */
+    double temp_amplitude, temp_period, temp_base; /* Thermal/TempAmplitude, TempPeriod, TempBase */
+    int temp_enabled;               /* Thermal/TempEnabled (only the initial temperature uses it) */
+    int vary_temp;                  /* Thermal/VaryTempEnabled */
+    int enable_expansion;           /* Simulator/EnableExpansion */
+    int enable_collision;           /* Simulator/AttachDetach/EnableCollision */
+    int volume_effects;             /* Simulator/Features/VolumeEffectsEnabled (0 forces Poisson's ratio to 0) */
+    double bond_damping, col_damping, slow_damping; /* Simulator/Damping/{Bond,Col,Slow}DampingZ */
+} vx3g_robot_desc;
+
+typedef struct vx3g_batch_desc {
+    int n_robots;
+    const vx3g_robot_desc *robots;
+    int precision;                  /* VX3G_PRECISION_* */
+    int device;                     /* CUDA device ordinal */
+    int graph_chunk;                /* steps captured per CUDA graph launch (0 -> 100) */
+} vx3g_batch_desc;
+
+typedef struct vx3g_ctx vx3g_ctx;
+
+/* Builds the lattice (voxel order, link order and Neg/Pos ends exactly as the
+ * reference's CVoxelyze), derives material constants, uploads the batch and
+ * computes each robot's time step.  Returns NULL on failure with *status set. */
+vx3g_ctx *vx3g_create(const vx3g_batch_desc *desc, int *status);
+void vx3g_destroy(vx3g_ctx *ctx);
+const char *vx3g_last_error(void);
+
+/* Advances every robot by n_steps time steps (asynchronous on the context's
+ * stream; robots that diverged stay frozen).  Full chunks run as CUDA graphs. */
+int vx3g_step(vx3g_ctx *ctx, int n_steps);
+int vx3g_synchronize(vx3g_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for event timing by the caller. */
+void *vx3g_stream(vx3g_ctx *ctx);
+
+/* Sizes: totals over the batch, and per-robot offsets into the packed arrays. */
+int vx3g_counts(vx3g_ctx *ctx, int *n_voxels, int *n_links, int *n_surface);
+int vx3g_offsets(vx3g_ctx *ctx, int *voxel_offset /* n_robots+1 */, int *link_offset /* n_robots+1 */);
+
+/* Host copies of the packed state (voxel order of each robot, robots
+ * back to back).  Any pointer may be NULL to skip that array.
+ *   pos, linmom, angmom: 3 doubles per voxel; orient: 4 doubles (w,x,y,z) per voxel. */
+int vx3g_get_state(vx3g_ctx *ctx, double *pos, double *orient, double *linmom, double *angmom);
+int vx3g_set_state(vx3g_ctx *ctx, const double *pos, const double *orient, const double *linmom,
+                   const double *angmom);
+/* tempe: float per voxel; flags: reference voxel bool-state bits (FLOOR_ENABLED 4,
+ * FLOOR_STATIC_FRICTION 8); contact: 3 doubles per voxel (last step's contact force). */
+int vx3g_get_voxel_aux(vx3g_ctx *ctx, float *tempe, int32_t *flags, double *contact);
+/* Link state in the reference's link order: strain, maxStrain (float),
+ * local9 = pos2, angle1v, angle2v (9 doubles), forces12 = forceNeg, forcePos,
+ * momentNeg, momentPos (12 doubles), small = small-angle flag. */
+int vx3g_get_links(vx3g_ctx *ctx, float *strain, float *max_strain, double *local9, double *forces12,
+                   int32_t *small);
+/* Topology: voxel lattice indices (3 ints), voxel palette index (0-based),
+ * link ends (neg, pos voxel indices, packed global), link axis (0 x, 1 y, 2 z). */
+int vx3g_get_topology(vx3g_ctx *ctx, int32_t *voxel_ijk, int32_t *voxel_mat, int32_t *link_ends,
+                      int32_t *link_axis);
+/* Surface voxels (fewer than six links), global voxel indices in voxel order. */
+int vx3g_get_surface(vx3g_ctx *ctx, int32_t *surface);
+
+int vx3g_com(vx3g_ctx *ctx, double *com /* 3 per robot */);
+int vx3g_dt(vx3g_ctx *ctx, double *dt /* per robot: the float step, widened */);
+int vx3g_time(vx3g_ctx *ctx, double *t /* per robot */);
+int vx3g_status(vx3g_ctx *ctx, int32_t *status /* per robot */);
+/* Steps taken so far by the context (every robot that has not diverged). */
+int64_t vx3g_steps_taken(vx3g_ctx *ctx);
+
+/* ---- measurement helpers (no counterpart in the reference) ---------------
+ * vx3g_time_steps: runs vx3g_step(ctx, n_steps) between two CUDA events on the
+ *   context's stream and returns the device time in milliseconds.
+ * vx3g_flush_l2: overwrites a context-owned buffer of `bytes` bytes on the
+ *   context's stream (evicts the L2 cache between timed iterations).
+ * vx3g_time_passes: launches each per-step pass `iters` times on its own
+ *   between CUDA events and returns the mean device time per launch in
+ *   milliseconds for: [0] link pass, [1] collision passes (all kernels of the
+ *   broad and narrow phase together), [2] voxel pass.  It advances the state
+ *   like extra steps would; use it after the measured run. */
+int vx3g_time_steps(vx3g_ctx *ctx, int n_steps, float *ms);
+int vx3g_flush_l2(vx3g_ctx *ctx, size_t bytes);
+int vx3g_time_passes(vx3g_ctx *ctx, int iters, float *ms3);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

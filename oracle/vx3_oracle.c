@@ -16,6 +16,10 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 typedef struct { double x, y, z; } vec;
 typedef struct { double w, x, y, z; } quat;
@@ -272,6 +276,7 @@ typedef struct {
     double t, optimal_dt;
     float dt;
     int surface_stale, diverged;
+    int threads; /* > 1: timing mode, loops run under OpenMP */
 } sim;
 
 /* VX3_Voxel::baseSize(axis) (VX3_Voxel.h:96-100); material size() = nomSize*extScale(1,1,1) */
@@ -361,6 +366,13 @@ void *vxo_create(const vxo_robot *r) {
     S->surf = (int *)malloc(sizeof(int) * (S->nv ? S->nv : 1));
     S->last_contact = (double *)calloc(3 * (size_t)(S->nv ? S->nv : 1), sizeof(double));
     S->surface_stale = 1;
+    S->threads = 1;
+    S->ns = 0;
+    for (int i = 0; i < S->nv; i++) {
+        int interior = 1;
+        for (int d = 0; d < 6; d++) if (S->v[i].links[d] < 0) interior = 0;
+        if (!interior) S->surf[S->ns++] = i;
+    }
     return S;
 }
 
@@ -607,11 +619,33 @@ static void collide(sim *S, voxel *v1, voxel *v2, int i1, int i2) {
     v2->contact = vadd(v2->contact, vneg(f));
 }
 
+/* The same all-pairs loop with rows spread over threads (timing mode only:
+ * contact sums then depend on thread interleaving). */
+static void collide_rows_threaded(sim *S, int row_begin, int row_end) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int a = row_begin; a < row_end; a++) {
+        for (int b = 0; b < a; b++) {
+            voxel *v1 = &S->v[S->surf[a]], *v2 = &S->v[S->surf[b]];
+            vec c1 = v1->contact, c2 = v2->contact;
+            collide(S, v1, v2, S->surf[a], S->surf[b]);
+            vec d1 = vsub(v1->contact, c1), d2 = vsub(v2->contact, c2);
+            if (d1.x != 0 || d1.y != 0 || d1.z != 0) {
+#pragma omp critical(vxo_contact)
+                {
+                    v1->contact = vadd(c1, d1);
+                    v2->contact = vadd(c2, d2);
+                }
+            }
+        }
+    }
+}
+
 /* doTimeStep (VX3_VoxelyzeKernel.cu:237-359) */
 static int do_step(sim *S) {
     const vxo_robot *r = &S->r;
     /* gpu_update_temperature (:625-650) + setTemperature (VX3_Voxel.cu:107-113) */
     if (r->vary_temp && r->temp_period > 0) {
+#pragma omp parallel for if (S->threads > 1) schedule(static)
         for (int i = 0; i < S->nv; i++) {
             voxel *v = &S->v[i];
             const vmat *m = &S->vm[v->mat];
@@ -630,6 +664,7 @@ static int do_step(sim *S) {
     S->dt = dt;
     /* gpu_update_links (:566-581), divergence over every link */
     int div = 0;
+#pragma omp parallel for if (S->threads > 1) schedule(static) reduction(| : div)
     for (int i = 0; i < S->nl; i++) {
         link *L = &S->l[i];
         if (S->vm[S->v[L->neg].mat].fixed && S->vm[S->v[L->pos].mat].fixed) continue;
@@ -650,8 +685,10 @@ static int do_step(sim *S) {
     }
     /* gpu_update_attach (:833-843): pairs first > second in surface order */
     if (r->enable_collision) {
-        for (int a = 0; a < S->ns; a++)
-            for (int b = 0; b < a; b++) collide(S, &S->v[S->surf[a]], &S->v[S->surf[b]], S->surf[a], S->surf[b]);
+        if (S->threads > 1) collide_rows_threaded(S, 0, S->ns);
+        else
+            for (int a = 0; a < S->ns; a++)
+                for (int b = 0; b < a; b++) collide(S, &S->v[S->surf[a]], &S->v[S->surf[b]], S->surf[a], S->surf[b]);
     }
     for (int i = 0; i < S->nv; i++) {
         S->last_contact[3 * i] = S->v[i].contact.x;
@@ -659,6 +696,7 @@ static int do_step(sim *S) {
         S->last_contact[3 * i + 2] = S->v[i].contact.z;
     }
     /* gpu_update_voxels (:582-623) */
+#pragma omp parallel for if (S->threads > 1) schedule(static)
     for (int i = 0; i < S->nv; i++) {
         if (S->vm[S->v[i].mat].fixed) continue;
         voxel_update(S, &S->v[i], dt);
@@ -674,6 +712,40 @@ int vxo_step(void *h, int n) {
         if (!do_step(S)) { S->diverged = 1; break; }
         done++;
     }
+    return done;
+}
+
+void vxo_set_threads(void *h, int n) {
+    sim *S = (sim *)h;
+    S->threads = n > 1 ? n : 1;
+#ifdef _OPENMP
+    if (n > 1) omp_set_num_threads(n);
+#endif
+}
+
+/* Seconds spent by the all-pairs collision loop over surface rows [begin, end)
+ * (each row tests all earlier surface voxels); used to time a bounded sample
+ * of the O(S^2) broad phase. Contact sums are cleared afterwards. */
+double vxo_time_collision_rows(void *h, int begin, int end) {
+    sim *S = (sim *)h;
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    if (S->threads > 1) collide_rows_threaded(S, begin, end);
+    else
+        for (int a = begin; a < end; a++)
+            for (int b = 0; b < a; b++) collide(S, &S->v[S->surf[a]], &S->v[S->surf[b]], S->surf[a], S->surf[b]);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    for (int i = 0; i < S->nv; i++) S->v[i].contact = V(0, 0, 0);
+    return (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+}
+
+/* Steps without the collision pass (to time the link and voxel passes alone). */
+int vxo_step_no_collision(void *h, int n) {
+    sim *S = (sim *)h;
+    int saved = S->r.enable_collision;
+    S->r.enable_collision = 0;
+    int done = vxo_step(h, n);
+    S->r.enable_collision = saved;
     return done;
 }
 

@@ -57,6 +57,10 @@ void vxo_surface(void *h, int *idx);
 void vxo_last_contact(void *h, double *c3);
 void vxo_com(void *h, double *c3);
 double vxo_recommended_dt(void *h);
+/* timing helpers for the CPU baseline (not used for parity) */
+void vxo_set_threads(void *h, int n);
+double vxo_time_collision_rows(void *h, int begin, int end);
+int vxo_step_no_collision(void *h, int n);
 
 #ifdef __cplusplus
 }

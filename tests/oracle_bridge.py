@@ -93,6 +93,22 @@ class Sim:
     def step(self, n):
         return self._f("step")(self.h, n)
 
+    # timing helpers of the C restatement (CPU baseline only)
+    def step_no_collision(self, n):
+        f = self.lib.vxo_step_no_collision
+        f.restype, f.argtypes = ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]
+        return f(self.h, n)
+
+    def set_threads(self, n):
+        f = self.lib.vxo_set_threads
+        f.restype, f.argtypes = None, [ctypes.c_void_p, ctypes.c_int]
+        f(self.h, n)
+
+    def time_collision_rows(self, begin, end):
+        f = self.lib.vxo_time_collision_rows
+        f.restype, f.argtypes = ctypes.c_double, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        return f(self.h, begin, end)
+
     def time(self):
         return self._f("time")(self.h)
 

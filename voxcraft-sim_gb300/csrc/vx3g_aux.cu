@@ -1,0 +1,285 @@
+// vx3g_aux.cu -- set-up and per-step passes other than the link/voxel passes:
+// initial temperature, stable time step, surface-voxel collision, centre of mass.
+// FP64 arithmetic throughout, compiled with --fmad=false.
+#include "vx3g_step.cuh"
+
+namespace vx3g {
+
+// ---------------------------------------------------------------- temperature at t = 0
+// The reference's first doTimeStep updates temperatures before anything else
+// (VX3_VoxelyzeKernel.cu:240, :625-650); the base size of every voxel for step 0
+// follows from that update (or from the initial temperature where it is skipped).
+template <bool EXACT> __global__ void k_init_temperature(Dev d) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= d.nv) return;
+    const uint2 vi = d.vinfo[v];
+    const VMat m = d.vmat[vi.y >> 8];
+    const RobotP &rp = d.rp[vi.x];
+    float te = d.tempe[v];
+    double bs = m.nom_size * (1 + te * m.cte);
+    bs = temperature_base_size<EXACT>(rp, m, d.phase[v], 0.0, bs, &te);
+    d.pos[v].w = bs;
+    d.tempe[v] = te;
+}
+
+void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s) {
+    if (!d.nv) return;
+    if (mixed) k_init_temperature<false><<<(d.nv + 255) / 256, 256, 0, s>>>(d);
+    else k_init_temperature<true><<<(d.nv + 255) / 256, 256, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------- stable time step
+// recommendedTimeStep (VX3_VoxelyzeKernel.cu:184-217) with VX3_Link::axialStiffness
+// (VX3_Link.cu:269-278): max over links of k/min(m1,m2), as a per-robot max of the
+// non-negative doubles' bit patterns (order independent, so deterministic).
+__global__ void k_dt_links(Dev d, unsigned long long *mx) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= d.nl) return;
+    const uint2 li = d.linfo[l];
+    const LMat &m = d.lmat[li.y >> 8];
+    const int2 e = d.ends[l];
+    const double m1 = d.vmat[d.vinfo[e.x].y >> 8].mass, m2 = d.vmat[d.vinfo[e.y].y >> 8].mass;
+    float k;
+    if (m.nu == 0.0f) {
+        k = m.a1;
+    } else {
+        const double rest = 0.5 * (d.pos[e.x].w + d.pos[e.y].w);
+        k = (float)(m.eHat * m.area / ((d.strain[l].x + 1) * rest));
+    }
+    const double f2 = k / (m1 < m2 ? m1 : m2);
+    if (f2 > 0) atomicMax(&mx[2 * li.x], (unsigned long long)__double_as_longlong(f2));
+}
+
+__global__ void k_dt_voxels(Dev d, unsigned long long *mx) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= d.nv) return;
+    const uint2 vi = d.vinfo[v];
+    const VMat &m = d.vmat[vi.y >> 8];
+    const double f2 = m.E * m.nom_size / m.mass;
+    if (f2 > 0) atomicMax(&mx[2 * vi.x + 1], (unsigned long long)__double_as_longlong(f2));
+}
+
+__global__ void k_dt_final(Dev d, const unsigned long long *mx) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= d.nr) return;
+    double f2 = __longlong_as_double((long long)mx[2 * r]);
+    if (f2 <= 0.0f) f2 = __longlong_as_double((long long)mx[2 * r + 1]);
+    double opt = (f2 <= 0.0f) ? 0.0f : 1.0f / (6.283185f * sqrt(f2));
+    if (opt < 1e-10) opt = 1e-10;  // doTimeStep (VX3_VoxelyzeKernel.cu:248-252)
+    d.dt[r] = (float)(d.rp[r].dt_frac * opt);
+}
+
+void launch_dt(const Dev &d, double *scratch, cudaStream_t s) {
+    unsigned long long *mx = (unsigned long long *)scratch;
+    cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * 2 * d.nr, s);
+    if (d.nl) k_dt_links<<<(d.nl + 255) / 256, 256, 0, s>>>(d, mx);
+    if (d.nv) k_dt_voxels<<<(d.nv + 255) / 256, 256, 0, s>>>(d, mx);
+    k_dt_final<<<(d.nr + 255) / 256, 256, 0, s>>>(d, mx);
+}
+
+// ---------------------------------------------------------------- collision
+// Broad phase: surface voxels of each collision-enabled robot are binned into a
+// uniform grid of cells of edge >= the largest possible envelope cutoff
+// (the cell of a voxel is floor(pos/cell)), stored in a hash table by counting
+// sort.  Narrow phase: each surface voxel gathers the surface voxels of its
+// robot in the 27 surrounding cells and applies the reference's exact test
+// (handle_collision_attachment, VX3_VoxelyzeKernel.cu:682-704), then sums the
+// contact forces of VX3_Collision (VX3_Collision.cu:3-31) in ascending partner
+// order -- the order in which the reference's serial pair loop (first > second
+// over the surface list, :833-843) accumulates them -- without atomics.
+__device__ __forceinline__ unsigned cell_hash(int cx, int cy, int cz, int r, int hmask) {
+    unsigned h = (unsigned)cx * 73856093u ^ (unsigned)cy * 19349663u ^ (unsigned)cz * 83492791u ^ (unsigned)r * 2654435761u;
+    h ^= h >> 15;
+    h *= 0x2c1b3c6du;
+    h ^= h >> 12;
+    return h & (unsigned)hmask;
+}
+
+__global__ void k_coll_bin(Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.ns) return;
+    const int v = d.csurf[s];
+    const int r = (int)d.vinfo[v].x;
+    const double cs = d.rp[r].cell_size;
+    const double4 p = d.pos[v];
+    const int4 c = make_int4((int)floor(p.x / cs), (int)floor(p.y / cs), (int)floor(p.z / cs), r);
+    d.ccell[s] = c;
+    atomicAdd(&d.hcount[cell_hash(c.x, c.y, c.z, c.w, d.hsize - 1)], 1);
+}
+
+// exclusive scan of hcount in blocks of 1024 (hsize is a multiple of 1024)
+__global__ void __launch_bounds__(1024) k_scan_blocks(Dev d) {
+    __shared__ int sh[1024];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    const int x = d.hcount[i];
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int y = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += y;
+        __syncthreads();
+    }
+    d.hstart[i] = sh[threadIdx.x] - x;
+    if (threadIdx.x == 1023) d.hblock[blockIdx.x] = sh[1023];
+}
+
+__global__ void __launch_bounds__(1024) k_scan_add(Dev d) {
+    __shared__ int base;
+    if (threadIdx.x < 32) {
+        int acc = 0;
+        for (int b = threadIdx.x; b < (int)blockIdx.x; b += 32) acc += d.hblock[b];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) base = acc;
+    }
+    __syncthreads();
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    const int v = d.hstart[i] + base;
+    d.hstart[i] = v;
+    d.hfill[i] = v;
+}
+
+__global__ void k_coll_scatter(Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.ns) return;
+    const int4 c = d.ccell[s];
+    const int slot = atomicAdd(&d.hfill[cell_hash(c.x, c.y, c.z, c.w, d.hsize - 1)], 1);
+    d.hsorted[slot] = s;
+}
+
+// force on voxel1 from the pair (voxel1, voxel2) as VX3_Collision computes it
+__device__ __forceinline__ V3<double> pair_force(const Dev &d, int v1, int v2, double bsa1, double bsa2) {
+    const VMat &m1 = d.vmat[d.vinfo[v1].y >> 8];
+    const VMat &m2 = d.vmat[d.vinfo[v2].y >> 8];
+    const double pstiff = 2.0f / (1.0f / m1.pstiff + 1.0f / m2.pstiff);
+    const double dampC = 0.5f * (m1.c_col + m2.c_col);
+    const double4 p1 = d.pos[v1], p2 = d.pos[v2];
+    const V3<double> offset{p2.x - p1.x, p2.y - p1.y, p2.z - p1.z};
+    const double nom = (bsa1 + bsa2) * 0.625;
+    const double rel = nom - len(offset);
+    if (!(rel > 0)) return V3<double>{0, 0, 0};
+    const V3<double> u = normalized(offset);
+    const double4 l1 = d.linmom[v1], l2 = d.linmom[v2];
+    const V3<double> w1 = scl(V3<double>{l1.x, l1.y, l1.z}, m1.mass_inv);
+    const V3<double> w2 = scl(V3<double>{l2.x, l2.y, l2.z}, m2.mass_inv);
+    const double rv = (w1.x * u.x + w1.y * u.y + w1.z * u.z) - (w2.x * u.x + w2.y * u.y + w2.z * u.z);
+    return scl(u, pstiff * rel + dampC * rv);
+}
+
+constexpr int kMaxContacts = 48;
+
+__global__ void k_coll_gather(Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.ns) return;
+    const int v = d.csurf[s];
+    const int r = (int)d.vinfo[v].x;
+    if (d.status[r] != 0) return;
+    const int4 c = d.ccell[s];
+    const double4 p = d.pos[v];
+    const double bsa = (p.w + p.w + p.w) / 3.0f;
+    const bool fixed = (d.vinfo[v].y & VF_FIXED) != 0;
+    const short4 ij = d.ijk[v];
+    int cand[kMaxContacts];
+    int nc = 0;
+    bool overflow = false;
+    for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+                const int cx = c.x + dx, cy = c.y + dy, cz = c.z + dz;
+                const unsigned h = cell_hash(cx, cy, cz, r, d.hsize - 1);
+                const int b = d.hstart[h], n = d.hcount[h];
+                for (int k = 0; k < n; k++) {
+                    const int t = d.hsorted[b + k];
+                    if (t == s) continue;
+                    const int4 ct = d.ccell[t];
+                    if (ct.x != cx || ct.y != cy || ct.z != cz || ct.w != r) continue;
+                    const int u = d.csurf[t];
+                    const bool ufixed = (d.vinfo[u].y & VF_FIXED) != 0;
+                    if (fixed && ufixed) continue;
+                    // exact envelope test with voxel1 = the later surface voxel
+                    const int a1 = t < s ? v : u, a2 = t < s ? u : v;
+                    const double4 pa = d.pos[a1], pb = d.pos[a2];
+                    const double ba = (pa.w + pa.w + pa.w) / 3.0f, bb = (pb.w + pb.w + pb.w) / 3.0f;
+                    const V3<double> diff{pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
+                    const double wd = (ba + bb) * 0.625;
+                    if (diff.x > wd || diff.x < -wd) continue;
+                    if (diff.y > wd || diff.y < -wd) continue;
+                    if (diff.z > wd || diff.z < -wd) continue;
+                    if (len(diff) > wd) continue;
+                    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): linked <=> face-adjacent in the lattice
+                    const short4 ik = d.ijk[u];
+                    const int man = abs(ik.x - ij.x) + abs(ik.y - ij.y) + abs(ik.z - ij.z);
+                    if (man == 1) continue;
+                    if (nc == kMaxContacts) { overflow = true; continue; }
+                    int j = nc++;
+                    while (j > 0 && cand[j - 1] > t) { cand[j] = cand[j - 1]; j--; }
+                    cand[j] = t;
+                }
+            }
+    if (overflow) atomicOr(&d.status[r], 2);
+    V3<double> acc{0, 0, 0};
+    for (int k = 0; k < nc; k++) {
+        const int t = cand[k];
+        const int u = d.csurf[t];
+        if (t < s) {  // pair (voxel1 = v, voxel2 = u): v.contactForce += force
+            const double4 pu = d.pos[u];
+            acc = add(acc, pair_force(d, v, u, bsa, (pu.w + pu.w + pu.w) / 3.0f));
+        } else {      // pair (voxel1 = u, voxel2 = v): v.contactForce += -force
+            const double4 pu = d.pos[u];
+            acc = add(acc, neg(pair_force(d, u, v, (pu.w + pu.w + pu.w) / 3.0f, bsa)));
+        }
+    }
+    d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
+}
+
+void launch_collision(const Dev &d, cudaStream_t s) {
+    if (!d.ns) return;
+    cudaMemsetAsync(d.hcount, 0, sizeof(int) * d.hsize, s);
+    const int g = (d.ns + 255) / 256;
+    k_coll_bin<<<g, 256, 0, s>>>(d);
+    k_scan_blocks<<<d.hsize / 1024, 1024, 0, s>>>(d);
+    k_scan_add<<<d.hsize / 1024, 1024, 0, s>>>(d);
+    k_coll_scatter<<<g, 256, 0, s>>>(d);
+    k_coll_gather<<<g, 256, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------- centre of mass
+// updateCurrentCenterOfMass (VX3_VoxelyzeKernel.cu:477-493): mass-weighted mean
+// of measured voxels, FP64, one block per robot with a fixed reduction order.
+__global__ void __launch_bounds__(256) k_com(Dev d, double *out) {
+    __shared__ double sh[4][256];
+    const int r = blockIdx.x;
+    const RobotP &rp = d.rp[r];
+    double sx = 0, sy = 0, sz = 0, sm = 0;
+    for (int i = threadIdx.x; i < rp.nv; i += 256) {
+        const int v = rp.voff + i;
+        const VMat &m = d.vmat[d.vinfo[v].y >> 8];
+        if (!m.is_measured) continue;
+        const double mass = m.mass;
+        const double4 p = d.pos[v];
+        sx += mass * p.x;
+        sy += mass * p.y;
+        sz += mass * p.z;
+        sm += mass;
+    }
+    sh[0][threadIdx.x] = sx; sh[1][threadIdx.x] = sy; sh[2][threadIdx.x] = sz; sh[3][threadIdx.x] = sm;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int k = 0; k < 4; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double tot = sh[3][0];
+        double inv = tot != 0 ? 1.0 / tot : 0.0;
+        out[3 * r] = tot != 0 ? inv * sh[0][0] : 0.0;
+        out[3 * r + 1] = tot != 0 ? inv * sh[1][0] : 0.0;
+        out[3 * r + 2] = tot != 0 ? inv * sh[2][0] : 0.0;
+    }
+}
+
+void launch_com(const Dev &d, double *out, cudaStream_t s) {
+    if (d.nr) k_com<<<d.nr, 256, 0, s>>>(d, out);
+}
+
+}  // namespace vx3g

@@ -1,0 +1,691 @@
+// vx3g_host.cpp -- host side of the C ABI: lattice building, material
+// constants, device memory, the step loop as CUDA graphs, and state access.
+//
+// Lattice building follows CVX_Sim::Import / CVoxelyze::addVoxel / addLink
+// (src/VXA/VX_Sim.cpp:88-107, src/old/Voxelyze.cpp:439-539, src/old/VX_Link.cpp:21-54):
+// voxels in x-fastest scan order; a new voxel links to the neighbours that
+// already exist, in direction order X_NEG, Y_NEG, Z_NEG, with the lower lattice
+// index as the link's negative end.  Material constants follow CVX_Material /
+// CVX_MaterialVoxel / CVX_MaterialLink (src/old/VX_Material*.cpp) in float, as the
+// reference computes them before copying them into its VX3 objects.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/vx3g.h"
+#include "vx3g_internal.h"
+
+using namespace vx3g;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CU(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(VX3G_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+    } while (0)
+
+struct HostVMat {
+    float E, nu, rho, cte, mu_s, mu_k, z_int, z_glob, z_col, eHat, sigma_fail, grav_mult;
+    float mass, mass_inv, sqrt_mass, mom, mom_inv, c2m, c2i;
+    double nom;
+};
+
+float ehat(float E, float nu) { return E / ((1 - 2 * nu) * (1 + nu)); }
+
+// CVX_Sim::CopyMat + Import damping + EnableVolumeEffects + CVX_MaterialVoxel::updateDerived
+HostVMat import_material(const vx3g_material &in, const vx3g_robot_desc &r) {
+    HostVMat m{};
+    m.E = (float)in.E;
+    m.sigma_fail = in.model == 1 ? (float)in.fail_stress : -1.0f;
+    float nu = (float)in.nu;
+    if (nu < 0) nu = 0;
+    if (nu >= 0.5) nu = 0.5 - FLT_EPSILON * 2;
+    if (!r.volume_effects) nu = 0;
+    m.nu = nu;
+    float rho = (float)in.rho;
+    if (rho <= 0) rho = FLT_MIN;
+    m.rho = rho;
+    m.cte = (float)in.cte;
+    float ms = (float)in.mu_static, mk = (float)in.mu_kinetic;
+    m.mu_s = ms <= 0 ? 0 : ms;
+    m.mu_k = mk <= 0 ? 0 : mk;
+    float zi = (float)r.bond_damping, zg = (float)r.slow_damping, zc = (float)r.col_damping;
+    m.z_int = zi <= 0 ? 0 : zi;
+    m.z_glob = zg <= 0 ? 0 : zg;
+    m.z_col = zc <= 0 ? 0 : zc;
+    m.nom = r.vox_size;
+    float ga = (float)r.grav_acc;
+    m.grav_mult = (float)(-ga / 9.80665);  // CVX_Sim::SetGravityAccel (VX_Sim.cpp:485)
+    m.eHat = ehat(m.E, m.nu);
+    double volume = m.nom * m.nom * m.nom;
+    m.mass = (float)(volume * m.rho);
+    m.mom = (float)(m.mass * m.nom * m.nom / 6.0f);
+    if (volume == 0 || m.mass == 0 || m.mom == 0) return m;
+    m.mass_inv = 1.0f / m.mass;
+    m.sqrt_mass = sqrtf(m.mass);
+    m.mom_inv = 1.0f / m.mom;
+    m.c2m = (float)(2.0f * std::sqrt((double)(m.mass * m.E) * m.nom));
+    m.c2i = (float)(2.0f * std::sqrt((double)(m.mom * m.E) * m.nom * m.nom * m.nom));
+    return m;
+}
+
+// CVX_MaterialLink::updateAll + updateDerived (src/old/VX_MaterialLink.cpp:47-140);
+// vox1 is the material of the voxel being added, vox2 its existing neighbour's.
+LMat combine(const HostVMat &v1, const HostVMat &v2) {
+    LMat l{};
+    float f1 = v1.sigma_fail, f2 = v2.sigma_fail, failS;
+    if (f1 == -1.0f) failS = f2;
+    else if (f2 == -1.0f) failS = f1;
+    else failS = f1 < f2 ? f1 : f2;
+    float E = 2.0f * v1.E * v2.E / (v1.E + v2.E);
+    l.E = E;
+    l.eps_fail = (failS == -1.0f) ? -1.0f : failS / E;
+    float nu;
+    if (v1.nu == 0 && v2.nu == 0) {
+        nu = 0;
+    } else {
+        float tmpEHat = 2 * v1.eHat * v2.eHat / (v1.eHat + v2.eHat);
+        float c2 = (float)((tmpEHat - E) / (2 * tmpEHat) + 0.0625);
+        nu = (float)(sqrtf(c2) - 0.25);
+    }
+    l.nu = nu;
+    l.eHat = ehat(E, nu);
+    float L = (float)(0.5 * (v1.nom + v2.nom));
+    l.a1 = E * L;
+    l.a2 = E * L * L * L / (12.0f * (1 + nu));
+    l.b1 = E * L;
+    l.b2 = E * L * L / 2.0f;
+    l.b3 = E * L * L * L / 6.0f;
+    l.sqA1 = sqrtf(l.a1);
+    l.sqA2xIp = sqrtf(l.a2 * L * L / 6.0f);
+    l.sqB1 = sqrtf(l.b1);
+    l.sqB2xFMp = sqrtf(l.b2 * L / 2.0f);
+    l.sqB3xIp = sqrtf(l.b3 * L * L / 6.0f);
+    // transverse area/strain sum at creation (CVX_Link::updateTransverseInfo, unstrained voxels)
+    float s1 = (float)v1.nom, s2 = (float)v2.nom;
+    l.area = 0.5f * (s2 * s2 + s1 * s1);
+    l.tss = 0.0f;
+    return l;
+}
+
+}  // namespace
+
+struct vx3g_ctx {
+    int precision = 0, chunk = 100, device = 0, nr = 0;
+    cudaStream_t stream = nullptr;
+    Dev d{};
+    std::vector<void *> allocs;
+    double *scratch = nullptr;  // dt reduction / com output
+    // host copies of static topology
+    std::vector<int> voff, loff;
+    std::vector<int2> ends;
+    std::vector<uint32_t> laxis;
+    std::vector<short4> ijk;
+    std::vector<int> vmat_local, surface;
+    std::vector<unsigned char> vfixed;
+    int64_t steps = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    void *flush = nullptr;
+    size_t flush_bytes = 0;
+
+    template <class T> int alloc(T **p, size_t n) {
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, n ? n * sizeof(T) : 16);
+        if (e != cudaSuccess) return fail(VX3G_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(q);
+        *p = (T *)q;
+        return cudaMemsetAsync(q, 0, n ? n * sizeof(T) : 16, stream) == cudaSuccess ? VX3G_OK : fail(VX3G_ERR_CUDA, "memset");
+    }
+    template <class T> int upload(T **p, const std::vector<T> &h) {
+        int rc = alloc(p, h.size());
+        if (rc) return rc;
+        if (!h.empty()) CU(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+        return VX3G_OK;
+    }
+    ~vx3g_ctx() {
+        for (auto &g : graph)
+            if (g) cudaGraphExecDestroy(g);
+        if (stream) cudaStreamSynchronize(stream);
+        for (void *p : allocs) cudaFree(p);
+        if (flush) cudaFree(flush);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
+    if (!desc || desc->n_robots <= 0 || !desc->robots) return fail(VX3G_ERR_INVALID, "empty batch descriptor");
+    if (desc->precision != VX3G_PRECISION_FP64 && desc->precision != VX3G_PRECISION_MIXED)
+        return fail(VX3G_ERR_INVALID, "unknown precision");
+    c->precision = desc->precision;
+    c->chunk = desc->graph_chunk > 0 ? desc->graph_chunk : 100;
+    if (c->chunk & 1) c->chunk++;  // even chunks keep the time-buffer parity aligned
+    c->device = desc->device;
+    c->nr = desc->n_robots;
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+
+    std::vector<VMat> vmats;
+    std::vector<LMat> lmats;
+    std::vector<RobotP> rps(c->nr);
+    std::vector<double4> pos, quat;
+    std::vector<float> tempe;
+    std::vector<double> phase;
+    std::vector<uint2> vinfo, linfo;
+    std::vector<int> csurf;
+    c->voff.assign(c->nr + 1, 0);
+    c->loff.assign(c->nr + 1, 0);
+
+    for (int r = 0; r < c->nr; r++) {
+        const vx3g_robot_desc &R = desc->robots[r];
+        if (R.nx <= 0 || R.ny <= 0 || R.nz <= 0 || !R.lattice)
+            return fail(VX3G_ERR_INVALID, "robot " + std::to_string(r) + ": empty lattice");
+        if (R.nx > 32767 || R.ny > 32767 || R.nz > 32767) return fail(VX3G_ERR_INVALID, "lattice too large");
+        if (R.n_materials < 1 || R.n_materials > 16 || !R.materials)
+            return fail(VX3G_ERR_INVALID, "robot " + std::to_string(r) + ": palette must hold 1..16 materials");
+        if (!(R.vox_size > 0)) return fail(VX3G_ERR_INVALID, "vox_size must be positive");
+        std::vector<HostVMat> hm(R.n_materials);
+        const int vbase = (int)vmats.size(), lbase = (int)lmats.size();
+        double cte_max = 0;
+        for (int i = 0; i < R.n_materials; i++) {
+            const vx3g_material &in = R.materials[i];
+            if (in.model != 0 && in.model != 1)
+                return fail(VX3G_ERR_UNSUPPORTED, "only linear material models (MatModel 0/1) are supported");
+            if (in.model == 1 && !(in.fail_stress > 0)) return fail(VX3G_ERR_INVALID, "fail_stress must be positive");
+            if (!(in.E > 0)) return fail(VX3G_ERR_INVALID, "Young's modulus must be positive");
+            hm[i] = import_material(in, R);
+            const HostVMat &m = hm[i];
+            VMat v{};
+            v.mass = m.mass; v.mass_inv = m.mass_inv; v.mom_inv = m.mom_inv;
+            v.c_glob = m.z_glob * m.c2m;
+            v.c_glob_rot = m.z_glob * m.c2i;
+            v.c_col = m.z_col * m.c2m;
+            v.grav_force = -m.mass * 9.80665f * m.grav_mult;
+            v.pstiff = (float)(2 * m.E * m.nom);
+            v.mu_s = m.mu_s; v.mu_k = m.mu_k; v.cte = m.cte;
+            v.dmc = 2 * m.sqrt_mass * m.z_int;
+            v.E = m.E; v.nu = m.nu;
+            v.fixed = in.fixed ? 1 : 0;
+            v.is_measured = in.is_measured ? 1 : 0;
+            v.nom_size = m.nom;
+            v.thermal_on_after = in.thermal_on_after;
+            vmats.push_back(v);
+            cte_max = std::fmax(cte_max, std::fabs((double)m.cte));
+        }
+        const int nx = R.nx, ny = R.ny, nz = R.nz;
+        const long long ncell = (long long)nx * ny * nz;
+        std::vector<int> vid(ncell, -1);
+        const int v0 = (int)pos.size();
+        c->voff[r] = v0;
+        c->loff[r] = (int)c->ends.size();
+        int nvr = 0;
+        for (long long i = 0; i < ncell; i++) {
+            int p = R.lattice[i];
+            if (p > R.n_materials) return fail(VX3G_ERR_INVALID, "lattice names a missing palette entry");
+            if (p > 0) vid[i] = v0 + nvr++;
+        }
+        std::vector<int> pair_lmat(R.n_materials * R.n_materials, -1);
+        // initial temperature: UpdateMatTemps at import (VX_Sim.cpp:462-478, VX_Environment.cpp:326-345)
+        float temp0 = 0.0f;
+        if (R.temp_enabled) {
+            double cur = R.vary_temp ? (R.temp_period == 0 ? 0.0 : R.temp_base + R.temp_amplitude * std::sin(0.0))
+                                     : R.temp_base + R.temp_amplitude;
+            temp0 = (float)((float)cur - R.temp_base);
+        }
+        for (long long i = 0; i < ncell; i++) {
+            if (vid[i] < 0) continue;
+            const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long long)nx * ny));
+            const int mi = R.lattice[i] - 1;
+            pos.push_back(make_double4(x * R.vox_size, y * R.vox_size, z * R.vox_size, 0.0));
+            quat.push_back(make_double4(1, 0, 0, 0));
+            tempe.push_back(temp0);
+            phase.push_back(R.phase ? R.phase[i] : 0.0);
+            c->ijk.push_back(make_short4((short)x, (short)y, (short)z, 0));
+            c->vmat_local.push_back(mi);
+            uint32_t fl = VF_STATIC | (R.materials[mi].fixed ? VF_FIXED : 0u);
+            vinfo.push_back(make_uint2((unsigned)r, fl | ((uint32_t)(vbase + mi) << 8)));
+            c->vfixed.push_back(R.materials[mi].fixed ? 1 : 0);
+            const long long nb[3] = {x > 0 ? i - 1 : -1, y > 0 ? i - nx : -1, z > 0 ? i - (long long)nx * ny : -1};
+            for (int a = 0; a < 3; a++) {
+                if (nb[a] < 0 || vid[nb[a]] < 0) continue;
+                const int vn = vid[nb[a]], vp = vid[i];
+                const int mn = c->vmat_local[vn], mp = mi;
+                int &lm = pair_lmat[mp * R.n_materials + mn];
+                if (lm < 0) {
+                    lm = (int)lmats.size() - lbase;
+                    pair_lmat[mn * R.n_materials + mp] = lm;
+                    lmats.push_back(combine(hm[mp], hm[mn]));
+                }
+                const int l = (int)c->ends.size();
+                c->ends.push_back(make_int2(vn, vp));
+                c->laxis.push_back((uint32_t)a);
+                const bool bothFixed = R.materials[mn].fixed && R.materials[mp].fixed;
+                linfo.push_back(make_uint2((unsigned)r, (uint32_t)a | LF_SMALL | (bothFixed ? LF_BOTH_FIXED : 0u) |
+                                                            ((uint32_t)(lbase + lm) << 8)));
+                vinfo[vn].y |= 1u << (2 * a);       // neighbour: link in its positive direction
+                vinfo[vp].y |= 1u << (2 * a + 1);   // new voxel: link in its negative direction
+                (void)l;
+            }
+        }
+        RobotP &rp = rps[r];
+        rp.vox_size = R.vox_size;
+        rp.temp_amp = R.temp_amplitude;
+        rp.temp_period = R.temp_period;
+        rp.dt_frac = R.dt_frac;
+        rp.voff = v0;
+        rp.nv = nvr;
+        rp.loff = c->loff[r];
+        rp.nl = (int)c->ends.size() - rp.loff;
+        rp.floor = R.floor_enabled ? 1 : 0;
+        rp.vary_temp = R.vary_temp ? 1 : 0;
+        rp.expansion = R.enable_expansion ? 1 : 0;
+        rp.collision = R.enable_collision ? 1 : 0;
+        // largest base size over the run bounds the envelope cutoff 1.25*bs
+        double tmax = std::fmax(std::fabs(R.temp_amplitude), std::fabs((double)temp0));
+        rp.cell_size = 1.25 * R.vox_size * (1.0 + tmax * cte_max) * (1.0 + 1e-6);
+        rp.soff = (int)csurf.size();
+        for (int k = 0; k < nvr; k++) {
+            const int v = v0 + k;
+            const bool interior = (vinfo[v].y & VF_LINKMASK) == VF_LINKMASK;
+            if (!interior) c->surface.push_back(v);
+            if (!interior && R.enable_collision) csurf.push_back(v);
+        }
+        rp.ns = (int)csurf.size() - rp.soff;
+    }
+    c->voff[c->nr] = (int)pos.size();
+    c->loff[c->nr] = (int)c->ends.size();
+    if (pos.size() > (size_t)INT32_MAX / 8) return fail(VX3G_ERR_INVALID, "batch too large");
+
+    Dev &d = c->d;
+    d.nv = (int)pos.size();
+    d.nl = (int)c->ends.size();
+    d.nr = c->nr;
+    d.ns = (int)csurf.size();
+    int rc;
+    if ((rc = c->upload(&d.pos, pos)) || (rc = c->upload(&d.quat, quat)) || (rc = c->alloc(&d.linmom, d.nv)) ||
+        (rc = c->alloc(&d.angmom, d.nv)) || (rc = c->alloc(&d.contact, d.nv)) || (rc = c->upload(&d.tempe, tempe)) ||
+        (rc = c->upload(&d.phase, phase)) || (rc = c->upload(&d.vinfo, vinfo)) || (rc = c->upload(&d.ijk, c->ijk)) ||
+        (rc = c->upload(&d.ends, c->ends)) || (rc = c->upload(&d.linfo, linfo)) || (rc = c->alloc(&d.strain, d.nl)))
+        return rc;
+    const size_t rsz = c->precision == VX3G_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    char *ls = nullptr, *sl = nullptr;
+    if ((rc = c->alloc(&ls, 9 * (size_t)d.nl * rsz)) || (rc = c->alloc(&sl, 6 * (size_t)d.nv * 6 * rsz))) return rc;
+    d.lstate = ls;
+    d.slots = sl;
+    RobotP *drp;
+    VMat *dvm;
+    LMat *dlm;
+    if ((rc = c->upload(&drp, rps)) || (rc = c->upload(&dvm, vmats)) || (rc = c->upload(&dlm, lmats))) return rc;
+    d.rp = drp;
+    d.vmat = dvm;
+    d.lmat = dlm;
+    if ((rc = c->alloc(&d.dt, d.nr)) || (rc = c->alloc(&d.T, 2 * (size_t)d.nr)) || (rc = c->alloc(&d.status, d.nr)) ||
+        (rc = c->alloc(&d.err, 1)) || (rc = c->alloc(&c->scratch, 4 * (size_t)d.nr + 4)))
+        return rc;
+    // collision tables
+    int hs = 1024;
+    while (hs < 2 * d.ns) hs <<= 1;
+    d.hsize = hs;
+    if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.hcount, hs)) ||
+        (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.hsorted, d.ns)) ||
+        (rc = c->alloc(&d.hblock, hs / 1024)))
+        return rc;
+
+    launch_init_temperature(d, c->precision == VX3G_PRECISION_MIXED, c->stream);
+    launch_dt(d, c->scratch, c->stream);
+    CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(c->stream));
+    return VX3G_OK;
+}
+
+void enqueue_step(vx3g_ctx *c, int parity) {
+    const Dev &d = c->d;
+    if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(d, c->stream);
+    else launch_links_mixed(d, c->stream);
+    launch_collision(d, c->stream);
+    if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(d, parity, c->stream);
+    else launch_voxels_mixed(d, parity, c->stream);
+}
+
+int get_graph(vx3g_ctx *c, int parity, cudaGraphExec_t *out) {
+    if (!c->graph[parity]) {
+        cudaGraph_t g;
+        CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < c->chunk; i++) enqueue_step(c, (parity + i) & 1);
+        CU(cudaStreamEndCapture(c->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&c->graph[parity], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(VX3G_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    }
+    *out = c->graph[parity];
+    return VX3G_OK;
+}
+
+template <class T> int download(vx3g_ctx *c, std::vector<T> &h, const T *dptr, size_t n) {
+    h.resize(n);
+    if (n) CU(cudaMemcpyAsync(h.data(), dptr, n * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+    return VX3G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *vx3g_last_error(void) { return g_err.c_str(); }
+
+vx3g_ctx *vx3g_create(const vx3g_batch_desc *desc, int *status) {
+    vx3g_ctx *c = new (std::nothrow) vx3g_ctx();
+    if (!c) {
+        if (status) *status = fail(VX3G_ERR_NOMEM, "host allocation failed");
+        return nullptr;
+    }
+    int rc = build(c, desc);
+    if (status) *status = rc;
+    if (rc != VX3G_OK) {
+        delete c;
+        return nullptr;
+    }
+    return c;
+}
+
+void vx3g_destroy(vx3g_ctx *c) { delete c; }
+
+int vx3g_step(vx3g_ctx *c, int n) {
+    if (!c || n < 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_step");
+    CU(cudaSetDevice(c->device));
+    while (n > 0) {
+        const int parity = (int)(c->steps & 1);
+        if (n >= c->chunk) {
+            cudaGraphExec_t g;
+            int rc = get_graph(c, parity, &g);
+            if (rc) return rc;
+            CU(cudaGraphLaunch(g, c->stream));
+            n -= c->chunk;
+            c->steps += c->chunk;
+        } else {
+            enqueue_step(c, parity);
+            n -= 1;
+            c->steps += 1;
+        }
+    }
+    CU(cudaGetLastError());
+    return VX3G_OK;
+}
+
+int vx3g_synchronize(vx3g_ctx *c) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    CU(cudaStreamSynchronize(c->stream));
+    return VX3G_OK;
+}
+
+void *vx3g_stream(vx3g_ctx *c) { return c ? (void *)c->stream : nullptr; }
+int64_t vx3g_steps_taken(vx3g_ctx *c) { return c ? c->steps : -1; }
+
+int vx3g_counts(vx3g_ctx *c, int *nv, int *nl, int *ns) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    if (nv) *nv = c->d.nv;
+    if (nl) *nl = c->d.nl;
+    if (ns) *ns = (int)c->surface.size();
+    return VX3G_OK;
+}
+
+int vx3g_offsets(vx3g_ctx *c, int *vo, int *lo) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    for (int r = 0; r <= c->nr; r++) {
+        if (vo) vo[r] = c->voff[r];
+        if (lo) lo[r] = c->loff[r];
+    }
+    return VX3G_OK;
+}
+
+int vx3g_get_state(vx3g_ctx *c, double *pos, double *orient, double *linmom, double *angmom) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    const size_t n = c->d.nv;
+    std::vector<double4> a, b, l, m;
+    int rc;
+    if (pos && (rc = download(c, a, c->d.pos, n))) return rc;
+    if (orient && (rc = download(c, b, c->d.quat, n))) return rc;
+    if (linmom && (rc = download(c, l, c->d.linmom, n))) return rc;
+    if (angmom && (rc = download(c, m, c->d.angmom, n))) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; i++) {
+        if (pos) { pos[3 * i] = a[i].x; pos[3 * i + 1] = a[i].y; pos[3 * i + 2] = a[i].z; }
+        if (orient) { orient[4 * i] = b[i].x; orient[4 * i + 1] = b[i].y; orient[4 * i + 2] = b[i].z; orient[4 * i + 3] = b[i].w; }
+        if (linmom) { linmom[3 * i] = l[i].x; linmom[3 * i + 1] = l[i].y; linmom[3 * i + 2] = l[i].z; }
+        if (angmom) { angmom[3 * i] = m[i].x; angmom[3 * i + 1] = m[i].y; angmom[3 * i + 2] = m[i].z; }
+    }
+    return VX3G_OK;
+}
+
+int vx3g_set_state(vx3g_ctx *c, const double *pos, const double *orient, const double *linmom, const double *angmom) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    const size_t n = c->d.nv;
+    std::vector<double4> a;
+    int rc;
+    if (pos) {  // keep the base size in .w
+        if ((rc = download(c, a, c->d.pos, n))) return rc;
+        CU(cudaStreamSynchronize(c->stream));
+        for (size_t i = 0; i < n; i++) { a[i].x = pos[3 * i]; a[i].y = pos[3 * i + 1]; a[i].z = pos[3 * i + 2]; }
+        CU(cudaMemcpyAsync(c->d.pos, a.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
+    }
+    std::vector<double4> b(n);
+    if (orient) {
+        for (size_t i = 0; i < n; i++) b[i] = make_double4(orient[4 * i], orient[4 * i + 1], orient[4 * i + 2], orient[4 * i + 3]);
+        CU(cudaMemcpyAsync(c->d.quat, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+    }
+    if (linmom) {
+        for (size_t i = 0; i < n; i++) b[i] = make_double4(linmom[3 * i], linmom[3 * i + 1], linmom[3 * i + 2], 0);
+        CU(cudaMemcpyAsync(c->d.linmom, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+    }
+    if (angmom) {
+        for (size_t i = 0; i < n; i++) b[i] = make_double4(angmom[3 * i], angmom[3 * i + 1], angmom[3 * i + 2], 0);
+        CU(cudaMemcpyAsync(c->d.angmom, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    return VX3G_OK;
+}
+
+int vx3g_get_voxel_aux(vx3g_ctx *c, float *tempe, int32_t *flags, double *contact) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    const size_t n = c->d.nv;
+    std::vector<float> t;
+    std::vector<uint2> vi;
+    std::vector<double4> ct;
+    std::vector<RobotP> rps;
+    int rc;
+    if (tempe && (rc = download(c, t, c->d.tempe, n))) return rc;
+    if (flags && ((rc = download(c, vi, c->d.vinfo, n)) || (rc = download(c, rps, c->d.rp, (size_t)c->nr)))) return rc;
+    if (contact && (rc = download(c, ct, c->d.contact, n))) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; i++) {
+        if (tempe) tempe[i] = t[i];
+        if (flags) {
+            const uint32_t f = vi[i].y;
+            // reference voxState bits: SURFACE(2, set for interior voxels), FLOOR_ENABLED(4), FLOOR_STATIC_FRICTION(8)
+            flags[i] = (((f & VF_LINKMASK) == VF_LINKMASK) ? 2 : 0) | (rps[vi[i].x].floor ? 4 : 0) | ((f & VF_STATIC) ? 8 : 0);
+        }
+        if (contact) { contact[3 * i] = ct[i].x; contact[3 * i + 1] = ct[i].y; contact[3 * i + 2] = ct[i].z; }
+    }
+    return VX3G_OK;
+}
+
+int vx3g_get_links(vx3g_ctx *c, float *strain, float *max_strain, double *local9, double *forces12, int32_t *small) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    const size_t nl = c->d.nl, nv = c->d.nv;
+    const bool fp64 = c->precision == VX3G_PRECISION_FP64;
+    const size_t rsz = fp64 ? 8 : 4;
+    std::vector<float2> sm;
+    std::vector<uint2> li;
+    std::vector<char> ls, sl;
+    int rc;
+    if ((strain || max_strain) && (rc = download(c, sm, c->d.strain, nl))) return rc;
+    if (small && (rc = download(c, li, c->d.linfo, nl))) return rc;
+    if (local9 && (rc = download(c, ls, (const char *)c->d.lstate, 9 * nl * rsz))) return rc;
+    if (forces12 && (rc = download(c, sl, (const char *)c->d.slots, 36 * nv * rsz))) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    auto rd = [&](const std::vector<char> &buf, size_t idx) -> double {
+        if (fp64) return ((const double *)buf.data())[idx];
+        return (double)((const float *)buf.data())[idx];
+    };
+    for (size_t l = 0; l < nl; l++) {
+        if (strain) strain[l] = sm[l].x;
+        if (max_strain) max_strain[l] = sm[l].y;
+        if (small) small[l] = (li[l].y & LF_SMALL) ? 1 : 0;
+        if (local9)
+            for (int k = 0; k < 9; k++) local9[9 * l + k] = rd(ls, (size_t)k * nl + l);
+        if (forces12) {
+            const int a = (int)c->laxis[l];
+            const size_t sn = ((size_t)(2 * a) * nv + c->ends[l].x) * 6, sp = ((size_t)(2 * a + 1) * nv + c->ends[l].y) * 6;
+            for (int k = 0; k < 3; k++) {
+                forces12[12 * l + k] = rd(sl, sn + k);         // forceNeg
+                forces12[12 * l + 3 + k] = rd(sl, sp + k);     // forcePos
+                forces12[12 * l + 6 + k] = rd(sl, sn + 3 + k); // momentNeg
+                forces12[12 * l + 9 + k] = rd(sl, sp + 3 + k); // momentPos
+            }
+        }
+    }
+    return VX3G_OK;
+}
+
+int vx3g_get_topology(vx3g_ctx *c, int32_t *ijk, int32_t *vmat, int32_t *ends, int32_t *axis) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    for (size_t i = 0; i < (size_t)c->d.nv; i++) {
+        if (ijk) { ijk[3 * i] = c->ijk[i].x; ijk[3 * i + 1] = c->ijk[i].y; ijk[3 * i + 2] = c->ijk[i].z; }
+        if (vmat) vmat[i] = c->vmat_local[i];
+    }
+    for (size_t l = 0; l < (size_t)c->d.nl; l++) {
+        if (ends) { ends[2 * l] = c->ends[l].x; ends[2 * l + 1] = c->ends[l].y; }
+        if (axis) axis[l] = (int32_t)c->laxis[l];
+    }
+    return VX3G_OK;
+}
+
+int vx3g_get_surface(vx3g_ctx *c, int32_t *surface) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    for (size_t i = 0; i < c->surface.size(); i++) surface[i] = c->surface[i];
+    return VX3G_OK;
+}
+
+int vx3g_com(vx3g_ctx *c, double *com) {
+    if (!c || !com) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_com");
+    std::vector<double> out;
+    double *dout = c->scratch;  // 4*nr doubles
+    launch_com(c->d, dout, c->stream);
+    CU(cudaGetLastError());
+    int rc = download(c, out, (const double *)dout, 3 * (size_t)c->nr);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    memcpy(com, out.data(), 3 * c->nr * sizeof(double));
+    return VX3G_OK;
+}
+
+int vx3g_dt(vx3g_ctx *c, double *dt) {
+    if (!c || !dt) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_dt");
+    std::vector<float> h;
+    int rc = download(c, h, c->d.dt, (size_t)c->nr);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    for (int r = 0; r < c->nr; r++) dt[r] = h[r];
+    return VX3G_OK;
+}
+
+int vx3g_time(vx3g_ctx *c, double *t) {
+    if (!c || !t) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_time");
+    std::vector<double> h;
+    int rc = download(c, h, c->d.T + (size_t)(c->steps & 1) * c->nr, (size_t)c->nr);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    memcpy(t, h.data(), c->nr * sizeof(double));
+    return VX3G_OK;
+}
+
+int vx3g_status(vx3g_ctx *c, int32_t *st) {
+    if (!c || !st) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_status");
+    std::vector<int> h;
+    int rc = download(c, h, c->d.status, (size_t)c->nr);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    memcpy(st, h.data(), c->nr * sizeof(int));
+    return VX3G_OK;
+}
+
+int vx3g_time_steps(vx3g_ctx *c, int n, float *ms) {
+    if (!c || !ms || n < 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_time_steps");
+    cudaEvent_t a, b;
+    CU(cudaEventCreate(&a));
+    CU(cudaEventCreate(&b));
+    CU(cudaEventRecord(a, c->stream));
+    int rc = vx3g_step(c, n);
+    CU(cudaEventRecord(b, c->stream));
+    CU(cudaEventSynchronize(b));
+    CU(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return rc;
+}
+
+int vx3g_flush_l2(vx3g_ctx *c, size_t bytes) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    if (bytes > c->flush_bytes) {
+        if (c->flush) cudaFree(c->flush);
+        c->flush = nullptr;
+        c->flush_bytes = 0;
+        CU(cudaMalloc(&c->flush, bytes));
+        c->flush_bytes = bytes;
+    }
+    static unsigned char v = 0;
+    CU(cudaMemsetAsync(c->flush, ++v, bytes, c->stream));
+    return VX3G_OK;
+}
+
+int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms3) {
+    if (!c || !ms3 || iters <= 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_time_passes");
+    cudaEvent_t a, b;
+    CU(cudaEventCreate(&a));
+    CU(cudaEventCreate(&b));
+    const Dev &d = c->d;
+    for (int pass = 0; pass < 3; pass++) {
+        CU(cudaEventRecord(a, c->stream));
+        for (int i = 0; i < iters; i++) {
+            if (pass == 0) {
+                if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(d, c->stream);
+                else launch_links_mixed(d, c->stream);
+            } else if (pass == 1) {
+                launch_collision(d, c->stream);
+            } else {
+                const int parity = (int)(c->steps & 1);
+                if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(d, parity, c->stream);
+                else launch_voxels_mixed(d, parity, c->stream);
+                c->steps++;
+            }
+        }
+        CU(cudaEventRecord(b, c->stream));
+        CU(cudaEventSynchronize(b));
+        float ms = 0;
+        CU(cudaEventElapsedTime(&ms, a, b));
+        ms3[pass] = ms / iters;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    CU(cudaGetLastError());
+    return VX3G_OK;
+}
+
+}  // extern "C"

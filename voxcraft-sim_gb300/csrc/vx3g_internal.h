@@ -1,0 +1,108 @@
+// vx3g_internal.h -- device data layout shared by the host code and kernels.
+//
+// HBM layout (all arrays packed over the whole batch; robots back to back in
+// the reference's voxel order, x fastest):
+//   voxel v : pos[v]    double4 {x, y, z, baseSize}   baseSize = nomSize*(1+tempe*cte) of the
+//                                                      current step (VX3_Voxel::baseSize, VX3_Voxel.h:96-100)
+//             quat[v]   double4 {w, x, y, z}
+//             linmom[v] double4 {x, y, z, -}, angmom[v] double4 {x, y, z, -}
+//             vinfo[v]  uint2 {robot, flags | vmat<<8}
+//             contact[v] double4, tempe[v] float, phase[v] double, ijk[v] short4
+//   link l  : ends[l] int2 {neg, pos}, linfo[l] uint2 {robot, flags | lmat<<8},
+//             local state (pos2, angle1v, angle2v): 9 component-major arrays of R,
+//             strain[l] float2 {strain, maxStrain}
+//   slots   : slot[dir*NV + v] = {force, moment} of the link attached to voxel v in
+//             direction dir (X_POS..Z_NEG), written by the link pass, read in order 0..5 by
+//             the voxel pass (the summation order of VX3_Voxel::force/moment).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vx3g {
+
+// voxel flag bits (low 8 bits of vinfo.y)
+enum : uint32_t {
+    VF_LINKMASK = 0x3F,   // bit d set: a link exists in direction d
+    VF_STATIC = 1u << 6,  // FLOOR_STATIC_FRICTION
+    VF_FIXED = 1u << 7,   // material Fixed (voxel never steps)
+};
+// link flag bits (low 8 bits of linfo.y)
+enum : uint32_t {
+    LF_AXIS = 0x3,
+    LF_SMALL = 1u << 2,       // smallAngle
+    LF_LVV = 1u << 3,         // LOCAL_VELOCITY_VALID
+    LF_BOTH_FIXED = 1u << 4,  // both ends fixed: gpu_update_links skips the link
+};
+
+struct VMat {  // one voxel material (global index), constants as the reference derives them
+    float mass, mass_inv, mom_inv;
+    float c_glob;      // zetaGlobal*_2xSqMxExS          globalDampingTranslateC
+    float c_glob_rot;  // zetaGlobal*_2xSqIxExSxSxS      globalDampingRotateC
+    float c_col;       // zetaCollision*_2xSqMxExS       collisionDampingTranslateC
+    float grav_force;  // -_mass*9.80665f*gravMult       gravityForce
+    float pstiff;      // (float)(2*E*nomSize)           penetrationStiffness
+    float mu_s, mu_k, cte;
+    float dmc;         // 2*_sqrtMass*zetaInternal       dampingMultiplier numerator
+    float E, nu;
+    int fixed, is_measured;
+    double nom_size;
+    double thermal_on_after;
+};
+
+struct LMat {  // one link material (global index)
+    float E, nu, eHat, eps_fail;
+    float a1, a2, b1, b2, b3;
+    float sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp;
+    float area, tss;  // transverse area / strain sum frozen at link creation
+};
+
+struct RobotP {
+    double vox_size, temp_amp, temp_period, dt_frac, cell_size;
+    int voff, nv, loff, nl, soff, ns;
+    int floor, vary_temp, expansion, collision;
+};
+
+template <class R> struct Slot { R f[3]; R m[3]; };
+
+struct Dev {
+    // voxels
+    double4 *pos, *quat, *linmom, *angmom, *contact;
+    float *tempe;
+    double *phase;
+    uint2 *vinfo;
+    short4 *ijk;
+    // links
+    int2 *ends;
+    uint2 *linfo;
+    void *lstate;   // 9*NL of R, component-major
+    float2 *strain;
+    void *slots;    // 6*NV Slot<R>
+    // robots
+    const RobotP *rp;
+    float *dt;
+    double *T;      // [2][NR] time, double-buffered by step parity
+    int *status;
+    // materials
+    const VMat *vmat;
+    const LMat *lmat;
+    // collision
+    int *csurf;     // collision surface list (global voxel index), NS entries
+    int4 *ccell;    // cell coords + robot per collision-surface voxel
+    int *hcount, *hstart, *hfill, *hsorted, *hblock;
+    int hsize;      // power of two
+    int *err;       // device error word
+    int nv, nl, nr, ns;
+};
+
+// launchers (defined in the .cu files)
+void launch_links_fp64(const Dev &d, cudaStream_t s);
+void launch_voxels_fp64(const Dev &d, int parity, cudaStream_t s);
+void launch_links_mixed(const Dev &d, cudaStream_t s);
+void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s);
+void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
+void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
+void launch_collision(const Dev &d, cudaStream_t s);
+void launch_com(const Dev &d, double *out4, cudaStream_t s);
+
+}  // namespace vx3g

@@ -184,3 +184,50 @@ def to_vxa(r: Robot) -> str:
     out.append("</VXC>")
     out.append("</VXA>")
     return "\n".join(out)
+
+
+# ------------------------------------------------------------------ named workloads
+def c1_block_drop() -> List[Robot]:
+    """Plain FP64 reference method: 10x10x10 solid block (E=1e6 Pa, Poisson 0.35,
+    1e3 kg/m^3, 0.01 m voxels, bond damping 1.0) dropped from 0.02 m onto a
+    floor with mu_s=1, mu_k=0.5; gravity on, collisions off."""
+    m = Material(E=1e6, nu=0.35, rho=1e3, mu_static=1.0, mu_kinetic=0.5)
+    return [solid_block(10, drop_cells=2, material=m, bond_damping=1.0, col_damping=1.0, slow_damping=0.0)]
+
+
+def c2_single_body(seed: int = 0, n: int = 64) -> List[Robot]:
+    """Single large body: n^3 Bernoulli(0.6) fill, largest 6-connected component,
+    two materials per voxel (passive E=1e6; active E=1e6 with CTE=0.01), +-39 C
+    at 5 Hz with expansion off, self-collision and floor on."""
+    rng = np.random.default_rng(seed)
+    mats = [Material(E=1e6, nu=0.35, cte=0.0, name="passive"), Material(E=1e6, nu=0.35, cte=0.01, name="active")]
+    return [bernoulli_body(rng, (n, n, n), 0.6, mats, temp_vary=True, temp_amplitude=39.0, temp_period=0.2,
+                           enable_collision=True)]
+
+
+def c3_population(seed: int = 0, n_robots: int = 1024, lo: int = 4, hi: int = 16) -> List[Robot]:
+    """Batched population: robots with dims uniform in [lo,hi]^3, Bernoulli(0.7),
+    largest component, 4 materials with E log-uniform in [1e5,1e7] and CTE 0.01,
+    per-voxel actuation phase uniform in [0, 2*pi) (stored in cycles), +-39 C at
+    5 Hz, floor on, collisions off."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_robots):
+        dims = tuple(int(x) for x in rng.integers(lo, hi + 1, size=3))
+        mats = [Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]
+        out.append(bernoulli_body(rng, dims, 0.7, mats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                                  temp_period=0.2))
+    return out
+
+
+def c5_population_collisions(seed: int = 0, n_robots: int = 256) -> List[Robot]:
+    """Collision-heavy population: 256 robots with dims uniform in [8,20]^3,
+    Bernoulli(0.65), 4 materials, per-voxel phase, self-collision and floor on."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_robots):
+        dims = tuple(int(x) for x in rng.integers(8, 21, size=3))
+        mats = [Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]
+        out.append(bernoulli_body(rng, dims, 0.65, mats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                                  temp_period=0.2, enable_collision=True))
+    return out
