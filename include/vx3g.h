@@ -43,6 +43,7 @@ extern "C" {
 #define VX3G_ROBOT_OK 0
 #define VX3G_ROBOT_DIVERGED 1          /* a link strain exceeded 100; the robot stops stepping */
 #define VX3G_ROBOT_CONTACT_OVERFLOW 2  /* more contact candidates than one voxel can hold */
+#define VX3G_ROBOT_STOPPED 4           /* stopped by the caller (vx3g_stop_robot) */
 
 /* ---- precision of the step ---------------------------------------------- */
 #define VX3G_PRECISION_FP64 0   /* the reference's arithmetic: FP64 vectors, FP32 scalars where it uses float */
@@ -136,6 +137,9 @@ int vx3g_com(vx3g_ctx *ctx, double *com /* 3 per robot */);
 int vx3g_dt(vx3g_ctx *ctx, double *dt /* per robot: the float step, widened */);
 int vx3g_time(vx3g_ctx *ctx, double *t /* per robot */);
 int vx3g_status(vx3g_ctx *ctx, int32_t *status /* per robot */);
+/* Stops one robot: it no longer steps (CUDA_Simulation's per-simulation loop
+ * exit when StopConditionMet(), src/VX3/VX3_SimulationManager.cu:63-64). */
+int vx3g_stop_robot(vx3g_ctx *ctx, int robot);
 /* Steps taken so far by the context (every robot that has not diverged). */
 int64_t vx3g_steps_taken(vx3g_ctx *ctx);
 

@@ -18,13 +18,13 @@ LIB_PATH = os.path.join(HERE, "_build", "libvx3g.so")
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
-ROBOT_OK, ROBOT_DIVERGED, ROBOT_CONTACT_OVERFLOW = 0, 1, 2
+ROBOT_OK, ROBOT_DIVERGED, ROBOT_CONTACT_OVERFLOW, ROBOT_STOPPED = 0, 1, 2, 4
 
 EXPORTS = [
     "vx3g_create", "vx3g_destroy", "vx3g_last_error", "vx3g_step", "vx3g_synchronize", "vx3g_stream",
     "vx3g_counts", "vx3g_offsets", "vx3g_get_state", "vx3g_set_state", "vx3g_get_voxel_aux", "vx3g_get_links",
     "vx3g_get_topology", "vx3g_get_surface", "vx3g_com", "vx3g_dt", "vx3g_time", "vx3g_status",
-    "vx3g_steps_taken", "vx3g_time_steps", "vx3g_flush_l2", "vx3g_time_passes",
+    "vx3g_steps_taken", "vx3g_time_steps", "vx3g_flush_l2", "vx3g_time_passes", "vx3g_stop_robot",
 ]
 
 
@@ -89,6 +89,7 @@ def load(path: str = LIB_PATH):
     lib.vx3g_time_steps.argtypes = [vp, ip, dp]
     lib.vx3g_flush_l2.argtypes = [vp, ctypes.c_size_t]
     lib.vx3g_time_passes.argtypes = [vp, ip, dp]
+    lib.vx3g_stop_robot.argtypes = [vp, ip]
     _lib = lib
     return lib
 
@@ -240,6 +241,9 @@ class Batch:
         ms = np.zeros(3, np.float32)
         _check(self.lib.vx3g_time_passes(self.h, int(iters), _P(ms)), "vx3g_time_passes")
         return dict(links=float(ms[0]), collision=float(ms[1]), voxels=float(ms[2]))
+
+    def stop_robot(self, r: int):
+        _check(self.lib.vx3g_stop_robot(self.h, int(r)), "vx3g_stop_robot")
 
     def status(self):
         s = np.zeros(self.n_robots, np.int32)

@@ -26,7 +26,11 @@ UNITS = [
     ("vx3g_aux.cu", ["--fmad=false"]),
     ("vx3g_mixed.cu", []),
     ("vx3g_host.cpp", []),
+    ("vx3g_xml.cpp", []),
+    ("vx3g_manager.cpp", []),
 ]
+MAIN = "vx3g_sim_main.cpp"
+EXE = os.path.join(OUT, "vx3g_sim")
 
 
 def nvcc():
@@ -50,14 +54,18 @@ def _compile(unit, extra, verbose):
 
 def build(verbose=False, force=False):
     os.makedirs(OUT, exist_ok=True)
-    srcs = [os.path.join(CSRC, u) for u, _ in UNITS] + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+    srcs = [os.path.join(CSRC, u) for u, _ in UNITS + [(MAIN, [])]] + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
                                                         if f.endswith((".h", ".cuh"))]
     srcs.append(os.path.join(os.path.dirname(HERE), "include", "vx3g.h"))
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in srcs):
+    srcs.append(os.path.join(os.path.dirname(HERE), "include", "vx3_simulation_manager.h"))
+    newest = max(os.path.getmtime(s) for s in srcs)
+    if not force and all(os.path.exists(p) and os.path.getmtime(p) >= newest for p in (LIB, EXE)):
         return LIB
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        results = list(ex.map(lambda u: _compile(u[0], u[1], verbose), UNITS))
-    objs = [o for o, _ in results]
+    units = UNITS + [(MAIN, [])]
+    with ThreadPoolExecutor(max_workers=len(units)) as ex:
+        results = list(ex.map(lambda u: _compile(u[0], u[1], verbose), units))
+    objs = [o for o, _ in results[:len(UNITS)]]
+    main_obj = results[len(UNITS)][0]
     if verbose:
         for _, log in results:
             sys.stderr.write(log)
@@ -65,6 +73,10 @@ def build(verbose=False, force=False):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
+    cmd = [nvcc()] + ARCH + ["-cudart", "static", "-o", EXE, main_obj] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link of vx3g_sim failed:\n{r.stderr}")
     return LIB
 
 

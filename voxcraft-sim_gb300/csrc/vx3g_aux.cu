@@ -19,7 +19,8 @@ template <bool EXACT> __global__ void k_init_temperature(Dev d) {
     double bs = m.nom_size * (1 + te * m.cte);
     bs = temperature_base_size<EXACT>(rp, m, d.phase[v], 0.0, bs, &te);
     d.pos[v].w = bs;
-    d.tempe[v] = te;
+    d.tempe[v] = te;              // parity-0 buffer: the temperature step 0 uses
+    d.tempe[d.nv + v] = te;       // parity-1 buffer: unchanged for robots without actuation
 }
 
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s) {
@@ -281,5 +282,9 @@ __global__ void __launch_bounds__(256) k_com(Dev d, double *out) {
 void launch_com(const Dev &d, double *out, cudaStream_t s) {
     if (d.nr) k_com<<<d.nr, 256, 0, s>>>(d, out);
 }
+
+__global__ void k_or_status(Dev d, int r, int bits) { d.status[r] |= bits; }
+
+void launch_or_status(const Dev &d, int robot, int bits, cudaStream_t s) { k_or_status<<<1, 1, 0, s>>>(d, robot, bits); }
 
 }  // namespace vx3g

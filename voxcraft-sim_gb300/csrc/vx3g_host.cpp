@@ -312,13 +312,15 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     if (pos.size() > (size_t)INT32_MAX / 8) return fail(VX3G_ERR_INVALID, "batch too large");
 
     Dev &d = c->d;
+    std::vector<float> tempe2(tempe);  // two parity buffers of the per-voxel temperature
+    tempe2.insert(tempe2.end(), tempe.begin(), tempe.end());
     d.nv = (int)pos.size();
     d.nl = (int)c->ends.size();
     d.nr = c->nr;
     d.ns = (int)csurf.size();
     int rc;
     if ((rc = c->upload(&d.pos, pos)) || (rc = c->upload(&d.quat, quat)) || (rc = c->alloc(&d.linmom, d.nv)) ||
-        (rc = c->alloc(&d.angmom, d.nv)) || (rc = c->alloc(&d.contact, d.nv)) || (rc = c->upload(&d.tempe, tempe)) ||
+        (rc = c->alloc(&d.angmom, d.nv)) || (rc = c->alloc(&d.contact, d.nv)) || (rc = c->upload(&d.tempe, tempe2)) ||
         (rc = c->upload(&d.phase, phase)) || (rc = c->upload(&d.vinfo, vinfo)) || (rc = c->upload(&d.ijk, c->ijk)) ||
         (rc = c->upload(&d.ends, c->ends)) || (rc = c->upload(&d.linfo, linfo)) || (rc = c->alloc(&d.strain, d.nl)))
         return rc;
@@ -510,7 +512,9 @@ int vx3g_get_voxel_aux(vx3g_ctx *c, float *tempe, int32_t *flags, double *contac
     std::vector<double4> ct;
     std::vector<RobotP> rps;
     int rc;
-    if (tempe && (rc = download(c, t, c->d.tempe, n))) return rc;
+    // the buffer of the last step taken holds the temperature that step used
+    const size_t tb = c->steps > 0 ? (size_t)((c->steps - 1) & 1) : 0;
+    if (tempe && (rc = download(c, t, c->d.tempe + tb * n, n))) return rc;
     if (flags && ((rc = download(c, vi, c->d.vinfo, n)) || (rc = download(c, rps, c->d.rp, (size_t)c->nr)))) return rc;
     if (contact && (rc = download(c, ct, c->d.contact, n))) return rc;
     CU(cudaStreamSynchronize(c->stream));
@@ -623,6 +627,13 @@ int vx3g_status(vx3g_ctx *c, int32_t *st) {
     if (rc) return rc;
     CU(cudaStreamSynchronize(c->stream));
     memcpy(st, h.data(), c->nr * sizeof(int));
+    return VX3G_OK;
+}
+
+int vx3g_stop_robot(vx3g_ctx *c, int robot) {
+    if (!c || robot < 0 || robot >= c->nr) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_stop_robot");
+    launch_or_status(c->d, robot, VX3G_ROBOT_STOPPED, c->stream);
+    CU(cudaGetLastError());
     return VX3G_OK;
 }
 

@@ -104,5 +104,6 @@ void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
 void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 void launch_collision(const Dev &d, cudaStream_t s);
 void launch_com(const Dev &d, double *out4, cudaStream_t s);
+void launch_or_status(const Dev &d, int robot, int bits, cudaStream_t s);
 
 }  // namespace vx3g

@@ -318,12 +318,15 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
     const double4 am = d.angmom[v];
     const double tn = Tcur + dt;
 
+    const bool actuated = rp.vary_temp && rp.temp_period > 0;
+    float *tcur = d.tempe + (size_t)parity * d.nv, *tnext = d.tempe + (size_t)(parity ^ 1) * d.nv;
     if (dt == 0.0f) {  // VX3_Voxel::timeStep returns before moving; temperature still follows time
-        float te = d.tempe[v];
-        double bs = temperature_base_size<EXACT>(rp, m, d.phase[v], tn, p.w, &te);
-        p.w = bs;
-        d.pos[v] = p;
-        d.tempe[v] = te;
+        if (actuated) {
+            float te = tcur[v];
+            p.w = temperature_base_size<EXACT>(rp, m, d.phase[v], tn, p.w, &te);
+            d.pos[v] = p;
+            tnext[v] = te;
+        }
         return;
     }
 
@@ -448,11 +451,14 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
     // static friction freezes rotation (VX3_Voxel.cu:259-264), penetration after the move
     if (floorOn && (float)(bsa / 2 - m.nom_size / 2 - p.z) >= 0 && stat) amv = V3<double>{0, 0, 0};
 
-    // next step's temperature
-    float te = d.tempe[v];
-    p.w = temperature_base_size<EXACT>(rp, m, d.phase[v], tn, bs, &te);
+    // next step's temperature; tempe is double-buffered by step parity so that the
+    // buffer of the step just taken keeps the value that step used (the reference's tempe)
+    if (actuated) {
+        float te = tcur[v];
+        p.w = temperature_base_size<EXACT>(rp, m, d.phase[v], tn, bs, &te);
+        tnext[v] = te;
+    }
     d.pos[v] = p;
-    d.tempe[v] = te;
     d.linmom[v] = make_double4(lmv.x, lmv.y, lmv.z, 0.0);
     d.angmom[v] = make_double4(amv.x, amv.y, amv.z, 0.0);
     const uint32_t nfl = stat ? (fl | VF_STATIC) : (fl & ~VF_STATIC);

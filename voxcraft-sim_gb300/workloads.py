@@ -58,6 +58,9 @@ class Robot:
     enable_expansion: int = 0
     enable_collision: bool = False
     volume_effects: bool = True
+    stop_time: Optional[float] = None     # StopConditionFormula "t - stop_time" (> 0 stops)
+    fitness_x: bool = False               # FitnessFunction "x" (COM displacement along x)
+    record_step: int = 0                  # RecordHistory/RecordStepSize
 
     def occupied(self) -> np.ndarray:
         return self.grid > 0
@@ -127,6 +130,31 @@ def _fmt(v: float) -> str:
     return repr(float(v))
 
 
+def structure_xml(r: Robot, replace: Optional[str] = None) -> str:
+    """The <Structure> element (ASCII_READABLE layers, optional PhaseOffset rows);
+    with replace="VXA.VXC.Structure" it is a VXD override of a base VXA."""
+    g, ph = r.padded()
+    Z, Y, X = g.shape
+    attr = f' replace="{replace}"' if replace else ""
+    out = [f'<Structure{attr} Compression="ASCII_READABLE">',
+           f"<X_Voxels>{X}</X_Voxels><Y_Voxels>{Y}</Y_Voxels><Z_Voxels>{Z}</Z_Voxels>", "<Data>"]
+    for z in range(Z):
+        out.append("<Layer><![CDATA[" + "".join(str(int(v)) for v in g[z].reshape(-1)) + "]]></Layer>")
+    out.append("</Data>")
+    if ph is not None:
+        out.append("<PhaseOffset>")
+        for z in range(Z):
+            out.append("<Layer><![CDATA[" + ",".join(repr(float(v)) for v in ph[z].reshape(-1)) + "]]></Layer>")
+        out.append("</PhaseOffset>")
+    out.append("</Structure>")
+    return "\n".join(out)
+
+
+def to_vxd(r: Robot) -> str:
+    """A VXD document that replaces the base VXA's structure with this robot's."""
+    return "<VXD>\n" + structure_xml(r, replace="VXA.VXC.Structure") + "\n</VXD>\n"
+
+
 def to_vxa(r: Robot) -> str:
     """Serialise a Robot as a self-contained VXA document."""
     g, ph = r.padded()
@@ -144,6 +172,11 @@ def to_vxa(r: Robot) -> str:
            f"<AttachDetach><EnableCollision>{int(r.enable_collision)}</EnableCollision>"
            "<EnableAttach>0</EnableAttach><EnableDetach>0</EnableDetach></AttachDetach>",
            f"<EnableExpansion>{int(r.enable_expansion)}</EnableExpansion>",
+           *([f"<StopCondition><StopConditionFormula><mtSUB><mtVAR>t</mtVAR><mtCONST>{_fmt(r.stop_time)}</mtCONST>"
+              "</mtSUB></StopConditionFormula></StopCondition>"] if r.stop_time is not None else []),
+           *(["<FitnessFunction><mtVAR>x</mtVAR></FitnessFunction>"] if r.fitness_x else []),
+           *([f"<RecordHistory><RecordStepSize>{int(r.record_step)}</RecordStepSize><RecordVoxel>1</RecordVoxel>"
+              "<RecordLink>0</RecordLink></RecordHistory>"] if r.record_step else []),
            "</Simulator>",
            "<Environment>",
            f"<Gravity><GravEnabled>{int(r.gravity)}</GravEnabled><GravAcc>{_fmt(r.grav_acc)}</GravAcc>"
@@ -169,18 +202,7 @@ def to_vxa(r: Robot) -> str:
             f"<Fixed>{int(m.fixed)}</Fixed><isMeasured>{int(m.is_measured)}</isMeasured>"
             "</Mechanical></Material>")
     out.append("</Palette>")
-    out.append('<Structure Compression="ASCII_READABLE">')
-    out.append(f"<X_Voxels>{X}</X_Voxels><Y_Voxels>{Y}</Y_Voxels><Z_Voxels>{Z}</Z_Voxels>")
-    out.append("<Data>")
-    for z in range(Z):
-        out.append("<Layer><![CDATA[" + "".join(str(int(v)) for v in g[z].reshape(-1)) + "]]></Layer>")
-    out.append("</Data>")
-    if ph is not None:
-        out.append("<PhaseOffset>")
-        for z in range(Z):
-            out.append("<Layer><![CDATA[" + ",".join(repr(float(v)) for v in ph[z].reshape(-1)) + "]]></Layer>")
-        out.append("</PhaseOffset>")
-    out.append("</Structure>")
+    out.append(structure_xml(r))
     out.append("</VXC>")
     out.append("</VXA>")
     return "\n".join(out)
