@@ -25,7 +25,7 @@ template <bool EXACT> __global__ void k_init_temperature(Dev d) {
 
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s) {
     if (!d.nv) return;
-    if (mixed) k_init_temperature<false><<<(d.nv + 255) / 256, 256, 0, s>>>(d);
+    if (mixed) launch_init_temperature_mixed(d, s);
     else k_init_temperature<true><<<(d.nv + 255) / 256, 256, 0, s>>>(d);
 }
 
@@ -44,7 +44,7 @@ __global__ void k_dt_links(Dev d, unsigned long long *mx) {
     if (m.nu == 0.0f) {
         k = m.a1;
     } else {
-        const double rest = 0.5 * (d.pos[e.x].w + d.pos[e.y].w);
+        const double rest = 0.5 * (load_state(d, d.pos, e.x).w + load_state(d, d.pos, e.y).w);
         k = (float)(m.eHat * m.area / ((d.strain[l].x + 1) * rest));
     }
     const double f2 = k / (m1 < m2 ? m1 : m2);
@@ -101,10 +101,11 @@ __global__ void k_coll_bin(Dev d) {
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
-    const double cs = d.rp[r].cell_size;
-    const double4 p = d.pos[v];
-    const int4 c = make_int4((int)floor(p.x / cs), (int)floor(p.y / cs), (int)floor(p.z / cs), r);
+    const double ic = d.rp[r].inv_cell;
+    const double4 p = load_state(d, d.pos, v);
+    const int4 c = make_int4((int)floor(p.x * ic), (int)floor(p.y * ic), (int)floor(p.z * ic), r);
     d.ccell[s] = c;
+    d.cposf[s] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.0f);
     atomicAdd(&d.hcount[cell_hash(c.x, c.y, c.z, c.w, d.hsize - 1)], 1);
 }
 
@@ -154,13 +155,13 @@ __device__ __forceinline__ V3<double> pair_force(const Dev &d, int v1, int v2, d
     const VMat &m2 = d.vmat[d.vinfo[v2].y >> 8];
     const double pstiff = 2.0f / (1.0f / m1.pstiff + 1.0f / m2.pstiff);
     const double dampC = 0.5f * (m1.c_col + m2.c_col);
-    const double4 p1 = d.pos[v1], p2 = d.pos[v2];
+    const double4 p1 = load_state(d, d.pos, v1), p2 = load_state(d, d.pos, v2);
     const V3<double> offset{p2.x - p1.x, p2.y - p1.y, p2.z - p1.z};
     const double nom = (bsa1 + bsa2) * 0.625;
     const double rel = nom - len(offset);
     if (!(rel > 0)) return V3<double>{0, 0, 0};
     const V3<double> u = normalized(offset);
-    const double4 l1 = d.linmom[v1], l2 = d.linmom[v2];
+    const double4 l1 = load_state(d, d.linmom, v1), l2 = load_state(d, d.linmom, v2);
     const V3<double> w1 = scl(V3<double>{l1.x, l1.y, l1.z}, m1.mass_inv);
     const V3<double> w2 = scl(V3<double>{l2.x, l2.y, l2.z}, m2.mass_inv);
     const double rv = (w1.x * u.x + w1.y * u.y + w1.z * u.z) - (w2.x * u.x + w2.y * u.y + w2.z * u.z);
@@ -176,8 +177,10 @@ __global__ void k_coll_gather(Dev d) {
     const int r = (int)d.vinfo[v].x;
     if (d.status[r] != 0) return;
     const int4 c = d.ccell[s];
-    const double4 p = d.pos[v];
-    const double bsa = (p.w + p.w + p.w) / 3.0f;
+    const float4 pf = d.cposf[s];
+    // FP32 prefilter radius: the cell edge bounds every cutoff; the 1e-3 margin covers
+    // FP32 rounding of positions up to ~100 m from the origin, so no true pair is lost
+    const float cut = (float)d.rp[r].cell_size * 1.001f, cut2 = cut * cut;
     const bool fixed = (d.vinfo[v].y & VF_FIXED) != 0;
     const short4 ij = d.ijk[v];
     int cand[kMaxContacts];
@@ -194,12 +197,17 @@ __global__ void k_coll_gather(Dev d) {
                     if (t == s) continue;
                     const int4 ct = d.ccell[t];
                     if (ct.x != cx || ct.y != cy || ct.z != cz || ct.w != r) continue;
+                    const float4 tf = d.cposf[t];
+                    const float ex = tf.x - pf.x, ey = tf.y - pf.y, ez = tf.z - pf.z;
+                    if (ex * ex + ey * ey + ez * ez > cut2) continue;
                     const int u = d.csurf[t];
-                    const bool ufixed = (d.vinfo[u].y & VF_FIXED) != 0;
-                    if (fixed && ufixed) continue;
-                    // exact envelope test with voxel1 = the later surface voxel
+                    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): linked <=> face-adjacent in the lattice
+                    const short4 ik = d.ijk[u];
+                    if (abs(ik.x - ij.x) + abs(ik.y - ij.y) + abs(ik.z - ij.z) == 1) continue;
+                    if (fixed && (d.vinfo[u].y & VF_FIXED)) continue;
+                    // exact envelope test of the reference, voxel1 = the later surface voxel
                     const int a1 = t < s ? v : u, a2 = t < s ? u : v;
-                    const double4 pa = d.pos[a1], pb = d.pos[a2];
+                    const double4 pa = load_state(d, d.pos, a1), pb = load_state(d, d.pos, a2);
                     const double ba = (pa.w + pa.w + pa.w) / 3.0f, bb = (pb.w + pb.w + pb.w) / 3.0f;
                     const V3<double> diff{pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
                     const double wd = (ba + bb) * 0.625;
@@ -207,27 +215,30 @@ __global__ void k_coll_gather(Dev d) {
                     if (diff.y > wd || diff.y < -wd) continue;
                     if (diff.z > wd || diff.z < -wd) continue;
                     if (len(diff) > wd) continue;
-                    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): linked <=> face-adjacent in the lattice
-                    const short4 ik = d.ijk[u];
-                    const int man = abs(ik.x - ij.x) + abs(ik.y - ij.y) + abs(ik.z - ij.z);
-                    if (man == 1) continue;
-                    if (nc == kMaxContacts) { overflow = true; continue; }
+                    if (nc == kMaxContacts) {
+                        overflow = true;
+                        continue;
+                    }
                     int j = nc++;
-                    while (j > 0 && cand[j - 1] > t) { cand[j] = cand[j - 1]; j--; }
+                    while (j > 0 && cand[j - 1] > t) {
+                        cand[j] = cand[j - 1];
+                        j--;
+                    }
                     cand[j] = t;
                 }
             }
     if (overflow) atomicOr(&d.status[r], 2);
     V3<double> acc{0, 0, 0};
-    for (int k = 0; k < nc; k++) {
-        const int t = cand[k];
-        const int u = d.csurf[t];
-        if (t < s) {  // pair (voxel1 = v, voxel2 = u): v.contactForce += force
-            const double4 pu = d.pos[u];
-            acc = add(acc, pair_force(d, v, u, bsa, (pu.w + pu.w + pu.w) / 3.0f));
-        } else {      // pair (voxel1 = u, voxel2 = v): v.contactForce += -force
-            const double4 pu = d.pos[u];
-            acc = add(acc, neg(pair_force(d, u, v, (pu.w + pu.w + pu.w) / 3.0f, bsa)));
+    if (nc) {
+        const double4 pv = load_state(d, d.pos, v);
+        const double bsa = (pv.w + pv.w + pv.w) / 3.0f;
+        for (int k = 0; k < nc; k++) {
+            const int t = cand[k];
+            const int u = d.csurf[t];
+            const double4 pu = load_state(d, d.pos, u);
+            const double bu = (pu.w + pu.w + pu.w) / 3.0f;
+            if (t < s) acc = add(acc, pair_force(d, v, u, bsa, bu));        // v.contactForce += force
+            else acc = add(acc, neg(pair_force(d, u, v, bu, bsa)));          // v.contactForce += -force
         }
     }
     d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
@@ -257,7 +268,7 @@ __global__ void __launch_bounds__(256) k_com(Dev d, double *out) {
         const VMat &m = d.vmat[d.vinfo[v].y >> 8];
         if (!m.is_measured) continue;
         const double mass = m.mass;
-        const double4 p = d.pos[v];
+        const double4 p = load_state(d, d.pos, v);
         sx += mass * p.x;
         sy += mass * p.y;
         sz += mass * p.z;

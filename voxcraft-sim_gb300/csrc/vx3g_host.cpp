@@ -122,6 +122,31 @@ LMat combine(const HostVMat &v1, const HostVMat &v2) {
     return l;
 }
 
+// A 32-byte voxel-state slot: four doubles, or (mixed precision) a float4 hi
+// followed by a float4 lo whose sum is the value.
+double4 to_slot(double a, double b, double c, double w, bool mixed) {
+    if (!mixed) return make_double4(a, b, c, w);
+    const double v[4] = {a, b, c, w};
+    float f[8];
+    for (int k = 0; k < 4; k++) {
+        f[k] = (float)v[k];
+        f[4 + k] = (float)(v[k] - (double)f[k]);
+    }
+    double4 out;
+    memcpy(&out, f, sizeof out);
+    return out;
+}
+
+void from_slot(const double4 &s, bool mixed, double out[4]) {
+    if (!mixed) {
+        out[0] = s.x; out[1] = s.y; out[2] = s.z; out[3] = s.w;
+        return;
+    }
+    float f[8];
+    memcpy(f, &s, sizeof f);
+    for (int k = 0; k < 4; k++) out[k] = (double)f[k] + (double)f[4 + k];
+}
+
 }  // namespace
 
 struct vx3g_ctx {
@@ -220,6 +245,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             v.mu_s = m.mu_s; v.mu_k = m.mu_k; v.cte = m.cte;
             v.dmc = 2 * m.sqrt_mass * m.z_int;
             v.E = m.E; v.nu = m.nu;
+            v.nom_hi = (float)m.nom;
+            v.nom_lo = (float)(m.nom - (double)v.nom_hi);
             v.fixed = in.fixed ? 1 : 0;
             v.is_measured = in.is_measured ? 1 : 0;
             v.nom_size = m.nom;
@@ -251,8 +278,9 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             if (vid[i] < 0) continue;
             const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long long)nx * ny));
             const int mi = R.lattice[i] - 1;
-            pos.push_back(make_double4(x * R.vox_size, y * R.vox_size, z * R.vox_size, 0.0));
-            quat.push_back(make_double4(1, 0, 0, 0));
+            const bool mx = c->precision == VX3G_PRECISION_MIXED;
+            pos.push_back(to_slot(x * R.vox_size, y * R.vox_size, z * R.vox_size, 0.0, mx));
+            quat.push_back(to_slot(1, 0, 0, 0, mx));
             tempe.push_back(temp0);
             phase.push_back(R.phase ? R.phase[i] : 0.0);
             c->ijk.push_back(make_short4((short)x, (short)y, (short)z, 0));
@@ -286,6 +314,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         rp.vox_size = R.vox_size;
         rp.temp_amp = R.temp_amplitude;
         rp.temp_period = R.temp_period;
+        rp.inv_period = R.temp_period > 0 ? 1.0 / R.temp_period : 0.0;
         rp.dt_frac = R.dt_frac;
         rp.voff = v0;
         rp.nv = nvr;
@@ -296,8 +325,20 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         rp.expansion = R.enable_expansion ? 1 : 0;
         rp.collision = R.enable_collision ? 1 : 0;
         // largest base size over the run bounds the envelope cutoff 1.25*bs
-        double tmax = std::fmax(std::fabs(R.temp_amplitude), std::fabs((double)temp0));
-        rp.cell_size = 1.25 * R.vox_size * (1.0 + tmax * cte_max) * (1.0 + 1e-6);
+        // the envelope cutoff (bsa1+bsa2)*0.625 is at most 1.25*vox_size*fmax, fmax the largest
+        // base-size factor 1+T*cte any voxel can reach: T spans the initial temperature and,
+        // with actuation, [-|A|, 0] (or [-|A|, |A|] with expansion enabled)
+        double tlo = temp0, thi = temp0;
+        if (R.vary_temp && R.temp_period > 0) {
+            tlo = std::fmin(tlo, -std::fabs(R.temp_amplitude));
+            thi = std::fmax(thi, R.enable_expansion ? std::fabs(R.temp_amplitude) : 0.0);
+        }
+        double fmax = 0.0;
+        for (int i = 0; i < R.n_materials; i++)
+            fmax = std::fmax(fmax, std::fmax(1.0 + tlo * hm[i].cte, 1.0 + thi * hm[i].cte));
+        rp.cell_size = 1.25 * R.vox_size * fmax * (1.0 + 1e-6);
+        rp.inv_cell = 1.0 / rp.cell_size;
+        (void)cte_max;
         rp.soff = (int)csurf.size();
         for (int k = 0; k < nvr; k++) {
             const int v = v0 + k;
@@ -315,6 +356,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     std::vector<float> tempe2(tempe);  // two parity buffers of the per-voxel temperature
     tempe2.insert(tempe2.end(), tempe.begin(), tempe.end());
     d.nv = (int)pos.size();
+    d.mixed = c->precision == VX3G_PRECISION_MIXED ? 1 : 0;
     d.nl = (int)c->ends.size();
     d.nr = c->nr;
     d.ns = (int)csurf.size();
@@ -343,7 +385,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     int hs = 1024;
     while (hs < 2 * d.ns) hs <<= 1;
     d.hsize = hs;
-    if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.hcount, hs)) ||
+    if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.cposf, d.ns)) ||
+        (rc = c->alloc(&d.hcount, hs)) ||
         (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.hsorted, d.ns)) ||
         (rc = c->alloc(&d.hblock, hs / 1024)))
         return rc;
@@ -465,11 +508,13 @@ int vx3g_get_state(vx3g_ctx *c, double *pos, double *orient, double *linmom, dou
     if (linmom && (rc = download(c, l, c->d.linmom, n))) return rc;
     if (angmom && (rc = download(c, m, c->d.angmom, n))) return rc;
     CU(cudaStreamSynchronize(c->stream));
+    const bool mx = c->d.mixed != 0;
+    double t4[4];
     for (size_t i = 0; i < n; i++) {
-        if (pos) { pos[3 * i] = a[i].x; pos[3 * i + 1] = a[i].y; pos[3 * i + 2] = a[i].z; }
-        if (orient) { orient[4 * i] = b[i].x; orient[4 * i + 1] = b[i].y; orient[4 * i + 2] = b[i].z; orient[4 * i + 3] = b[i].w; }
-        if (linmom) { linmom[3 * i] = l[i].x; linmom[3 * i + 1] = l[i].y; linmom[3 * i + 2] = l[i].z; }
-        if (angmom) { angmom[3 * i] = m[i].x; angmom[3 * i + 1] = m[i].y; angmom[3 * i + 2] = m[i].z; }
+        if (pos) { from_slot(a[i], mx, t4); pos[3 * i] = t4[0]; pos[3 * i + 1] = t4[1]; pos[3 * i + 2] = t4[2]; }
+        if (orient) { from_slot(b[i], mx, t4); for (int k = 0; k < 4; k++) orient[4 * i + k] = t4[k]; }
+        if (linmom) { from_slot(l[i], mx, t4); linmom[3 * i] = t4[0]; linmom[3 * i + 1] = t4[1]; linmom[3 * i + 2] = t4[2]; }
+        if (angmom) { from_slot(m[i], mx, t4); angmom[3 * i] = t4[0]; angmom[3 * i + 1] = t4[1]; angmom[3 * i + 2] = t4[2]; }
     }
     return VX3G_OK;
 }
@@ -477,27 +522,33 @@ int vx3g_get_state(vx3g_ctx *c, double *pos, double *orient, double *linmom, dou
 int vx3g_set_state(vx3g_ctx *c, const double *pos, const double *orient, const double *linmom, const double *angmom) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
     const size_t n = c->d.nv;
+    const bool mx = c->d.mixed != 0;
     std::vector<double4> a;
     int rc;
+    double t4[4];
     if (pos) {  // keep the base size in .w
         if ((rc = download(c, a, c->d.pos, n))) return rc;
         CU(cudaStreamSynchronize(c->stream));
-        for (size_t i = 0; i < n; i++) { a[i].x = pos[3 * i]; a[i].y = pos[3 * i + 1]; a[i].z = pos[3 * i + 2]; }
+        for (size_t i = 0; i < n; i++) {
+            from_slot(a[i], mx, t4);
+            a[i] = to_slot(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], t4[3], mx);
+        }
         CU(cudaMemcpyAsync(c->d.pos, a.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
     }
     std::vector<double4> b(n);
     if (orient) {
-        for (size_t i = 0; i < n; i++) b[i] = make_double4(orient[4 * i], orient[4 * i + 1], orient[4 * i + 2], orient[4 * i + 3]);
+        for (size_t i = 0; i < n; i++) b[i] = to_slot(orient[4 * i], orient[4 * i + 1], orient[4 * i + 2], orient[4 * i + 3], mx);
         CU(cudaMemcpyAsync(c->d.quat, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
         CU(cudaStreamSynchronize(c->stream));
     }
     if (linmom) {
-        for (size_t i = 0; i < n; i++) b[i] = make_double4(linmom[3 * i], linmom[3 * i + 1], linmom[3 * i + 2], 0);
+        for (size_t i = 0; i < n; i++) b[i] = to_slot(linmom[3 * i], linmom[3 * i + 1], linmom[3 * i + 2], 0, mx);
         CU(cudaMemcpyAsync(c->d.linmom, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
         CU(cudaStreamSynchronize(c->stream));
     }
     if (angmom) {
-        for (size_t i = 0; i < n; i++) b[i] = make_double4(angmom[3 * i], angmom[3 * i + 1], angmom[3 * i + 2], 0);
+        for (size_t i = 0; i < n; i++) b[i] = to_slot(angmom[3 * i], angmom[3 * i + 1], angmom[3 * i + 2], 0, mx);
         CU(cudaMemcpyAsync(c->d.angmom, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
     }
     CU(cudaStreamSynchronize(c->stream));

@@ -45,6 +45,7 @@ struct VMat {  // one voxel material (global index), constants as the reference 
     float mu_s, mu_k, cte;
     float dmc;         // 2*_sqrtMass*zetaInternal       dampingMultiplier numerator
     float E, nu;
+    float nom_hi, nom_lo;  // nomSize as an FP32 hi/lo pair (mixed precision)
     int fixed, is_measured;
     double nom_size;
     double thermal_on_after;
@@ -58,7 +59,7 @@ struct LMat {  // one link material (global index)
 };
 
 struct RobotP {
-    double vox_size, temp_amp, temp_period, dt_frac, cell_size;
+    double vox_size, temp_amp, temp_period, inv_period, dt_frac, cell_size, inv_cell;
     int voff, nv, loff, nl, soff, ns;
     int floor, vary_temp, expansion, collision;
 };
@@ -89,11 +90,25 @@ struct Dev {
     // collision
     int *csurf;     // collision surface list (global voxel index), NS entries
     int4 *ccell;    // cell coords + robot per collision-surface voxel
+    float4 *cposf;  // FP32 copy of the position (prefilter) per collision-surface voxel
     int *hcount, *hstart, *hfill, *hsorted, *hblock;
     int hsize;      // power of two
     int *err;       // device error word
     int nv, nl, nr, ns;
+    int mixed;      // 1: voxel state is compensated FP32 (see below)
 };
+
+// In the mixed-precision layout each 32-byte double4 slot of pos/quat/linmom/angmom
+// holds two float4 {hi, lo}: the value is hi + lo (an unevaluated sum of two
+// floats, ~48 significant bits), advanced with two-sum arithmetic.
+#ifdef __CUDACC__
+__device__ __forceinline__ double4 load_state(const Dev &d, const double4 *a, int v) {
+    if (!d.mixed) return a[v];
+    const float4 *f = reinterpret_cast<const float4 *>(a) + 2 * (size_t)v;
+    const float4 h = f[0], l = f[1];
+    return make_double4((double)h.x + l.x, (double)h.y + l.y, (double)h.z + l.z, (double)h.w + l.w);
+}
+#endif
 
 // launchers (defined in the .cu files)
 void launch_links_fp64(const Dev &d, cudaStream_t s);
@@ -101,6 +116,7 @@ void launch_voxels_fp64(const Dev &d, int parity, cudaStream_t s);
 void launch_links_mixed(const Dev &d, cudaStream_t s);
 void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s);
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
+void launch_init_temperature_mixed(const Dev &d, cudaStream_t s);
 void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 void launch_collision(const Dev &d, cudaStream_t s);
 void launch_com(const Dev &d, double *out4, cudaStream_t s);

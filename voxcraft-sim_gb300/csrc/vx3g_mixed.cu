@@ -1,14 +1,370 @@
-// Mixed-precision instantiation of the step passes: FP32 link math and force
-// sums, FP64 position/orientation/momentum accumulation.
+// vx3g_mixed.cu -- the mixed-precision step: FP32 link forces and moments,
+// compensated FP32 (hi + lo float pairs, two-sum arithmetic) for positions,
+// orientations and momenta.  No FP64 arithmetic runs per link; per voxel only the
+// actuation phase is reduced in FP64.
+//
+// The link pass restates VX3_Link::orientLink/updateForces (src/VX3/VX3_Link.cu:90-218)
+// without the cancellations FP32 would suffer:
+//  * pos2 = R(conj(q1)) * toAxisX(pPos - pNeg) is formed as
+//      L*R(conj(q1))e_x + R(conj(q1)) * toAxisX(delta),  delta = (pPos - pNeg) - L*e_axis,
+//    with delta taken from the hi/lo pairs (exact differences of nearby values) and
+//    R(q)e_x - e_x = (-2(y^2+z^2), 2(xy-wz), 2(xz+wy)) evaluated directly, so the axial
+//    deviation pos2.x - L never subtracts two nearly equal FP32 numbers;
+//  * angle2 = conj(q1)*q2 = |q1|^2 + conj(q1)*(q2 - q1), the difference again from the
+//    hi/lo pairs; the rotation vector uses 2*atan2(|v|, w)/|v|.
+// The voxel pass restates VX3_Voxel::timeStep (src/VX3/VX3_Voxel.cu:162-277) with the
+// same sums in FP32 and every accumulation (p += F dt, x += p dt/m, L += M dt,
+// q += (dq - 1) q) done as a two-sum into the hi/lo pair.
 #include "vx3g_step.cuh"
 
 namespace vx3g {
 
+__device__ __forceinline__ void quick_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    e = b - (s - a);
+}
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+// (hi, lo) += x
+__device__ __forceinline__ void df_add(float &hi, float &lo, float x) {
+    float s, e;
+    two_sum(hi, x, s, e);
+    e += lo;
+    quick_two_sum(s, e, hi, lo);
+}
+// (ah + al) - (bh + bl) rounded once, for nearby values
+__device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl) {
+    float s, e;
+    two_sum(ah, -bh, s, e);
+    return s + (e + (al - bl));
+}
+// (ah + al) - (bh + bl) - (ch + cl): the axial deviation of a link (a-b ~= c)
+__device__ __forceinline__ float df_diff3(float ah, float al, float bh, float bl, float ch, float cl) {
+    float s, e;
+    two_sum(ah, -bh, s, e);
+    float s2, e2;
+    two_sum(s, -ch, s2, e2);
+    return s2 + (e2 + (e + ((al - bl) - cl)));
+}
+
+__device__ __forceinline__ V3<float> rotvec_f(float w, V3<float> v) {
+    const float s2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    if (!(s2 > 0.0f)) return V3<float>{0, 0, 0};
+    const float s = sqrtf(s2);
+    return scl(v, 2.0f * atan2f(s, w) / s);
+}
+
+// ------------------------------------------------------------- link pass
+__global__ void __launch_bounds__(256) k_links_mixed(Dev d) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= d.nl) return;
+    const uint2 li = d.linfo[l];
+    const int r = (int)li.x;
+    if (d.status[r] != 0) return;
+    const uint32_t fl = li.y;
+    if (fl & LF_BOTH_FIXED) return;
+    const int axis = fl & LF_AXIS;
+    const int2 e = d.ends[l];
+    const float4 *P = reinterpret_cast<const float4 *>(d.pos);
+    const float4 *Q = reinterpret_cast<const float4 *>(d.quat);
+    const float4 pnH = P[2 * e.x], pnL = P[2 * e.x + 1], ppH = P[2 * e.y], ppL = P[2 * e.y + 1];
+    const float4 qnH = Q[2 * e.x], qnL = Q[2 * e.x + 1], qpH = Q[2 * e.y], qpL = Q[2 * e.y + 1];
+    const LMat &m = d.lmat[fl >> 8];
+    float *ls = (float *)d.lstate;
+    const size_t NL = (size_t)d.nl;
+    const V3<float> oldPos2{ls[l], ls[NL + l], ls[2 * NL + l]};
+    const V3<float> oldA1{ls[3 * NL + l], ls[4 * NL + l], ls[5 * NL + l]};
+    const V3<float> oldA2{ls[6 * NL + l], ls[7 * NL + l], ls[8 * NL + l]};
+
+    // rest length L = 0.5*(bsNeg + bsPos) as a hi/lo pair (VX3_Link::updateRestLength)
+    float Lh, Ll;
+    two_sum(pnH.w, ppH.w, Lh, Ll);
+    Ll += pnL.w + ppL.w;
+    quick_two_sum(0.5f * Lh, 0.5f * Ll, Lh, Ll);
+    // delta = (pPos - pNeg) - L*e_axis in the global frame
+    const float ax = axis == 0 ? Lh : 0.0f, ay = axis == 1 ? Lh : 0.0f, az = axis == 2 ? Lh : 0.0f;
+    const float axl = axis == 0 ? Ll : 0.0f, ayl = axis == 1 ? Ll : 0.0f, azl = axis == 2 ? Ll : 0.0f;
+    const V3<float> delta{df_diff3(ppH.x, ppL.x, pnH.x, pnL.x, ax, axl), df_diff3(ppH.y, ppL.y, pnH.y, pnL.y, ay, ayl),
+                          df_diff3(ppH.z, ppL.z, pnH.z, pnL.z, az, azl)};
+    const Q4<float> a1 = to_axis_xq(axis, Q4<float>{qnH.x, qnH.y, qnH.z, qnH.w});
+    const Q4<float> dq = to_axis_xq(axis, Q4<float>{df_diff(qpH.x, qpL.x, qnH.x, qnL.x), df_diff(qpH.y, qpL.y, qnH.y, qnL.y),
+                                                   df_diff(qpH.z, qpL.z, qnH.z, qnL.z), df_diff(qpH.w, qpL.w, qnH.w, qnL.w)});
+    const Q4<float> c = qconj(a1);
+    const Q4<float> cd = qmul(c, dq);  // angle2 = conj(q1)*q2 = |q1|^2 + conj(q1)*(q2-q1), |q1| = 1
+    const V3<float> rd = qrot(c, to_axis_x(axis, delta));
+    const float L = Lh;
+    float pxm = -2.0f * L * (a1.y * a1.y + a1.z * a1.z) + rd.x;  // pos2.x - L
+    float py = 2.0f * L * (a1.x * a1.y - a1.w * a1.z) + rd.y;
+    float pz = 2.0f * L * (a1.x * a1.z + a1.w * a1.y) + rd.z;
+    const float px = L + pxm;
+    const float SmallTurn = (fabsf(pz) + fabsf(py)) / px;
+    const float ExtendPerc = fabsf(pxm / L);
+    const float HF = 1.2f, BEND = 0.05f, EXT = 0.50f;
+    bool small = (fl & LF_SMALL) != 0, lvv = (fl & LF_LVV) != 0;
+    if (!small && SmallTurn < BEND && ExtendPerc < EXT) {
+        small = true;
+        lvv = false;
+    } else if (small && (SmallTurn > HF * BEND || ExtendPerc > HF * EXT)) {
+        small = false;
+        lvv = false;
+    }
+    Q4<float> angle1{1, 0, 0, 0};
+    float w2 = 1.0f + cd.w;
+    V3<float> v2{cd.x, cd.y, cd.z};
+    V3<float> pos2;
+    if (small) {
+        pos2 = V3<float>{pxm, py, pz};
+    } else {
+        angle1 = from_angle_to_posx(angle1, V3<float>{px, py, pz});
+        const Q4<float> a2 = qmul(angle1, Q4<float>{w2, v2.x, v2.y, v2.z});
+        w2 = a2.w;
+        v2 = V3<float>{a2.x, a2.y, a2.z};
+        const float len2 = sqrtf(px * px + py * py + pz * pz);
+        pos2 = V3<float>{(pxm * (px + L) + py * py + pz * pz) / (len2 + L), 0, 0};  // |pos2| - L
+    }
+    const V3<float> a1v = small ? V3<float>{0, 0, 0} : rotvec_f(angle1.w, V3<float>{angle1.x, angle1.y, angle1.z});
+    const V3<float> a2v = rotvec_f(w2, v2);
+    ls[l] = pos2.x; ls[NL + l] = pos2.y; ls[2 * NL + l] = pos2.z;
+    ls[3 * NL + l] = a1v.x; ls[4 * NL + l] = a1v.y; ls[5 * NL + l] = a1v.z;
+    ls[6 * NL + l] = a2v.x; ls[7 * NL + l] = a2v.y; ls[8 * NL + l] = a2v.z;
+
+    const V3<float> dPos2 = scl(sub(pos2, oldPos2), 0.5f);
+    const V3<float> dA1 = scl(sub(a1v, oldA1), 0.5f);
+    const V3<float> dA2 = scl(sub(a2v, oldA2), 0.5f);
+    const float axialStrain = pos2.x / L;
+    float2 sm = d.strain[l];
+    sm.x = axialStrain;
+    if (axialStrain > sm.y) sm.y = axialStrain;
+    d.strain[l] = sm;
+    if (axialStrain > 100) atomicOr(&d.status[r], 1);
+
+    Slot<float> *S = (Slot<float> *)d.slots;
+    Slot<float> *sNeg = &S[(size_t)(2 * axis) * d.nv + e.x];
+    Slot<float> *sPos = &S[(size_t)(2 * axis + 1) * d.nv + e.y];
+    float stress;
+    if (m.eps_fail != -1.0f && axialStrain > m.eps_fail) stress = 0.0f;
+    else if (m.nu == 0.0f) stress = m.E * axialStrain;
+    else stress = m.eHat * ((1 - m.nu) * axialStrain + m.nu * m.tss);
+    uint32_t nfl = (fl & ~(LF_SMALL | LF_LVV)) | (small ? LF_SMALL : 0u);
+    if (m.eps_fail != -1.0f && sm.y > m.eps_fail) {
+        const V3<float> z{0, 0, 0};
+        store_slot(sNeg, z, z);
+        store_slot(sPos, z, z);
+        nfl |= lvv ? LF_LVV : 0u;
+        if (nfl != fl) d.linfo[l].y = nfl;
+        return;
+    }
+    const float b1 = m.b1, b2 = m.b2, b3 = m.b3, a2 = m.a2;
+    V3<float> fNeg{stress * m.area, b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y)};
+    V3<float> fPos = neg(fNeg);
+    V3<float> mNeg{a2 * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (2 * a1v.y + a2v.y), b2 * pos2.y - b3 * (2 * a1v.z + a2v.z)};
+    V3<float> mPos{a2 * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z)};
+    if (lvv) {
+        const V3<float> posCalc{m.sqA1 * dPos2.x, m.sqB1 * dPos2.y - m.sqB2xFMp * (dA1.z + dA2.z),
+                                m.sqB1 * dPos2.z + m.sqB2xFMp * (dA1.y + dA2.y)};
+        const float dtf = d.dt[r];
+        const uint32_t fnv = d.vinfo[e.x].y, fpv = d.vinfo[e.y].y;
+        const float dmN = d.vmat[fnv >> 8].dmc / ((fnv & VF_FIXED) ? 0.0f : dtf);
+        const float dmP = d.vmat[fpv >> 8].dmc / ((fpv & VF_FIXED) ? 0.0f : dtf);
+        fNeg = add(fNeg, scl(posCalc, dmN));
+        fPos = sub(fPos, scl(posCalc, dmP));
+        mNeg = sub(mNeg, scl(V3<float>{-m.sqA2xIp * (dA2.x - dA1.x), m.sqB2xFMp * dPos2.z + m.sqB3xIp * (2 * dA1.y + dA2.y),
+                                       -m.sqB2xFMp * dPos2.y + m.sqB3xIp * (2 * dA1.z + dA2.z)},
+                             0.5f * dmN));
+        mPos = sub(mPos, scl(V3<float>{m.sqA2xIp * (dA2.x - dA1.x), m.sqB2xFMp * dPos2.z + m.sqB3xIp * (dA1.y + 2 * dA2.y),
+                                       -m.sqB2xFMp * dPos2.y + m.sqB3xIp * (dA1.z + 2 * dA2.z)},
+                             0.5f * dmP));
+    } else {
+        lvv = true;
+    }
+    nfl |= lvv ? LF_LVV : 0u;
+    if (!small) {
+        fNeg = qrotinv(angle1, fNeg);
+        mNeg = qrotinv(angle1, mNeg);
+    }
+    const Q4<float> angle2{w2, v2.x, v2.y, v2.z};
+    fPos = qrotinv(angle2, fPos);
+    mPos = qrotinv(angle2, mPos);
+    store_slot(sNeg, to_axis_original(axis, fNeg), to_axis_original(axis, mNeg));
+    store_slot(sPos, to_axis_original(axis, fPos), to_axis_original(axis, mPos));
+    if (nfl != fl) d.linfo[l].y = nfl;
+}
+
+// base size nomSize*(1 + T*cte) as a hi/lo pair
+__device__ __forceinline__ void base_size_df(const VMat &m, float te, float &hi, float &lo) {
+    const float f = 1 + te * m.cte;
+    const float p = m.nom_hi * f;
+    const float err = fmaf(m.nom_hi, f, -p) + m.nom_lo * f;
+    quick_two_sum(p, err, hi, lo);
+}
+
+// temperature at time t (gpu_update_temperature, VX3_VoxelyzeKernel.cu:625-650): the phase
+// 2*3.1415926f*(t/P + phase) reduced to cycles in FP64, the sine in FP32
+__device__ __forceinline__ float temperature_f(const RobotP &rp, double phase, double t) {
+    double c = (t * rp.inv_period + phase) * ((double)(2 * 3.1415926f) * (1.0 / 6.283185307179586));
+    c -= floor(c);
+    float T = (float)rp.temp_amp * sinpif(2.0f * (float)c);
+    if (!rp.expansion && T > 0) T = 0;
+    return T;
+}
+
+__global__ void k_init_temperature_mixed(Dev d) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= d.nv) return;
+    const uint2 vi = d.vinfo[v];
+    const VMat m = d.vmat[vi.y >> 8];
+    const RobotP &rp = d.rp[vi.x];
+    float te = d.tempe[v];
+    if (rp.vary_temp && rp.temp_period > 0 && !(m.thermal_on_after > 0.0) && !m.fixed) te = temperature_f(rp, d.phase[v], 0.0);
+    float4 *P = reinterpret_cast<float4 *>(d.pos);
+    base_size_df(m, te, P[2 * v].w, P[2 * v + 1].w);
+    d.tempe[v] = te;
+    d.tempe[d.nv + v] = te;
+}
+
+// ------------------------------------------------------------ voxel pass
+__global__ void __launch_bounds__(256) k_voxels_mixed(Dev d, int parity) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= d.nv) return;
+    const uint2 vi = d.vinfo[v];
+    const int r = (int)vi.x;
+    const RobotP &rp = d.rp[r];
+    const double Tcur = d.T[(size_t)parity * d.nr + r];
+    const int st = d.status[r];
+    const float dtf = d.dt[r];
+    if (v == rp.voff) d.T[(size_t)(parity ^ 1) * d.nr + r] = (st == 0) ? Tcur + dtf : Tcur;
+    if (st != 0) return;
+    uint32_t fl = vi.y;
+    if (fl & VF_FIXED) return;
+    const VMat m = d.vmat[fl >> 8];
+    float4 *P = reinterpret_cast<float4 *>(d.pos);
+    float4 *Qa = reinterpret_cast<float4 *>(d.quat);
+    float4 *LM = reinterpret_cast<float4 *>(d.linmom);
+    float4 *AM = reinterpret_cast<float4 *>(d.angmom);
+    float4 pH = P[2 * v], pL = P[2 * v + 1];
+    float4 qH = Qa[2 * v], qL = Qa[2 * v + 1];
+    float4 lH = LM[2 * v], lL = LM[2 * v + 1];
+    float4 aH = AM[2 * v], aL = AM[2 * v + 1];
+    const bool actuated = rp.vary_temp && rp.temp_period > 0;
+    float *tcur = d.tempe + (size_t)parity * d.nv, *tnext = d.tempe + (size_t)(parity ^ 1) * d.nv;
+    const double tn = Tcur + dtf;
+    if (dtf != 0.0f) {
+        V3<float> Fs{0, 0, 0}, Ms{0, 0, 0};
+        const Slot<float> *S = (const Slot<float> *)d.slots;
+#pragma unroll
+        for (int dir = 0; dir < 6; dir++) {
+            if (fl & (1u << dir)) {
+                const Slot<float> s = S[(size_t)dir * d.nv + v];
+                Fs = add(Fs, V3<float>{s.f[0], s.f[1], s.f[2]});
+                Ms = add(Ms, V3<float>{s.m[0], s.m[1], s.m[2]});
+            }
+        }
+        bool stat = (fl & VF_STATIC) != 0;
+        const bool floorOn = rp.floor != 0;
+        const Q4<float> o{qH.x, qH.y, qH.z, qH.w};
+        V3<float> F = qrot(o, Fs);
+        const V3<float> vel{(lH.x + lL.x) * m.mass_inv, (lH.y + lL.y) * m.mass_inv, (lH.z + lL.z) * m.mass_inv};
+        F = sub(F, scl(vel, m.c_glob));
+        F.z += m.grav_force;
+        if (rp.collision) {
+            const double4 c = d.contact[v];
+            F = sub(F, V3<float>{(float)c.x, (float)c.y, (float)c.z});
+        }
+        // floor penetration bsa/2 - nom/2 - z with bsa = base size (VX3_Voxel.h:185-188)
+        const float pen = 0.5f * ((pH.w - m.nom_hi) + (pL.w - m.nom_lo)) - (pH.z + pL.z);
+        V3<float> fric = F;
+        if (floorOn) {
+            if (pen >= 0) {
+                const float normal = m.pstiff * pen;
+                F.z += normal - m.c_col * vel.z;
+                if (stat) {
+                    if (F.x * F.x + F.y * F.y > (m.mu_s * normal) * (m.mu_s * normal)) stat = false;
+                } else {
+                    F = sub(F, scl(normalized(V3<float>{vel.x, vel.y, 0}), m.mu_k * normal));
+                }
+            } else {
+                stat = false;
+            }
+        }
+        fric = sub(F, fric);
+        df_add(lH.x, lL.x, F.x * dtf);
+        df_add(lH.y, lL.y, F.y * dtf);
+        df_add(lH.z, lL.z, F.z * dtf);
+        const float km = dtf * m.mass_inv;
+        V3<float> tr{(lH.x + lL.x) * km, (lH.y + lL.y) * km, (lH.z + lL.z) * km};
+        if (floorOn && pen >= 0) {
+            const float lx = lH.x + lL.x, ly = lH.y + lL.y;
+            const float work = fric.x * tr.x + fric.y * tr.y;
+            const float hKe = 0.5f * m.mass_inv * (lx * lx + ly * ly);
+            if (hKe + work <= 0) stat = true;
+            if (stat) {
+                lH.x = lL.x = lH.y = lL.y = 0;
+                tr.x = tr.y = 0;
+            }
+        } else {
+            stat = false;
+        }
+        df_add(pH.x, pL.x, tr.x);
+        df_add(pH.y, pL.y, tr.y);
+        df_add(pH.z, pL.z, tr.z);
+        V3<float> M = qrot(o, Ms);
+        const V3<float> avel{(aH.x + aL.x) * m.mom_inv, (aH.y + aL.y) * m.mom_inv, (aH.z + aL.z) * m.mom_inv};
+        M = sub(M, scl(avel, m.c_glob_rot));
+        df_add(aH.x, aL.x, M.x * dtf);
+        df_add(aH.y, aL.y, M.y * dtf);
+        df_add(aH.z, aL.z, M.z * dtf);
+        // q' = Quat(angMom*dt/I)*q = q + (dq - 1)*q (FromRotationVector, VX3_Quat3D.h:363-377)
+        const float ki = dtf * m.mom_inv;
+        const V3<float> th{0.5f * (aH.x + aL.x) * ki, 0.5f * (aH.y + aL.y) * ki, 0.5f * (aH.z + aL.z) * ki};
+        const float m2 = th.x * th.x + th.y * th.y + th.z * th.z;
+        float dw, sfac;
+        if (m2 * m2 < 5.328e-15f) {
+            dw = -0.5f * m2;
+            sfac = 1.0f - m2 / 6.0f;
+        } else {
+            const float mm = sqrtf(m2);
+            float sn, cs;
+            sincosf(0.5f * mm, &sn, &cs);
+            dw = -2.0f * sn * sn;
+            sfac = 2.0f * sn * cs / mm;
+        }
+        const Q4<float> delta = qmul(Q4<float>{dw, th.x * sfac, th.y * sfac, th.z * sfac}, o);
+        df_add(qH.x, qL.x, delta.w);
+        df_add(qH.y, qL.y, delta.x);
+        df_add(qH.z, qL.z, delta.y);
+        df_add(qH.w, qL.w, delta.z);
+        const float pen2 = 0.5f * ((pH.w - m.nom_hi) + (pL.w - m.nom_lo)) - (pH.z + pL.z);
+        if (floorOn && pen2 >= 0 && stat) aH.x = aH.y = aH.z = aL.x = aL.y = aL.z = 0;
+        const uint32_t nfl = stat ? (fl | VF_STATIC) : (fl & ~VF_STATIC);
+        if (nfl != fl) d.vinfo[v].y = nfl;
+        Qa[2 * v] = qH;
+        Qa[2 * v + 1] = qL;
+        LM[2 * v] = lH;
+        LM[2 * v + 1] = lL;
+        AM[2 * v] = aH;
+        AM[2 * v + 1] = aL;
+    }
+    if (actuated) {  // next step's temperature and base size
+        float te = tcur[v];
+        if (!(m.thermal_on_after > tn)) te = temperature_f(rp, d.phase[v], tn);
+        base_size_df(m, te, pH.w, pL.w);
+        tnext[v] = te;
+    }
+    P[2 * v] = pH;
+    P[2 * v + 1] = pL;
+}
+
 void launch_links_mixed(const Dev &d, cudaStream_t s) {
-    if (d.nl) k_links<float><<<(d.nl + 255) / 256, 256, 0, s>>>(d);
+    if (d.nl) k_links_mixed<<<(d.nl + 255) / 256, 256, 0, s>>>(d);
 }
 void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s) {
-    if (d.nv) k_voxels<float><<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity);
+    if (d.nv) k_voxels_mixed<<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity);
+}
+void launch_init_temperature_mixed(const Dev &d, cudaStream_t s) {
+    if (d.nv) k_init_temperature_mixed<<<(d.nv + 255) / 256, 256, 0, s>>>(d);
 }
 
 }  // namespace vx3g
