@@ -79,15 +79,17 @@ void launch_dt(const Dev &d, double *scratch, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------- collision
-// Broad phase: surface voxels of each collision-enabled robot are binned into a
-// uniform grid of cells of edge >= the largest possible envelope cutoff
-// (the cell of a voxel is floor(pos/cell)), stored in a hash table by counting
-// sort.  Narrow phase: each surface voxel gathers the surface voxels of its
-// robot in the 27 surrounding cells and applies the reference's exact test
-// (handle_collision_attachment, VX3_VoxelyzeKernel.cu:682-704), then sums the
-// contact forces of VX3_Collision (VX3_Collision.cu:3-31) in ascending partner
-// order -- the order in which the reference's serial pair loop (first > second
-// over the surface list, :833-843) accumulates them -- without atomics.
+// The reference tests every pair of surface voxels each step (gpu_update_attach,
+// VX3_VoxelyzeKernel.cu:833-843).  Here each surface voxel keeps a list of the
+// surface voxels of its robot that were within cutoff + skin when the list was
+// built (a Verlet list: uniform grid of cell edge cutoff + skin, hashed, counting
+// sort).  The lists are rebuilt in a step where any voxel has moved more than
+// half the skin since the last build, so every pair within the cutoff is in the
+// lists; each step the reference's exact test (handle_collision_attachment,
+// :682-704) runs on the listed pairs and the contact forces of VX3_Collision
+// (VX3_Collision.cu:3-31) are summed in ascending partner order -- the order in
+// which the reference's serial pair loop accumulates them -- without atomics.
+// The candidate set is therefore the reference's, pair for pair.
 __device__ __forceinline__ unsigned cell_hash(int cx, int cy, int cz, int r, int hmask) {
     unsigned h = (unsigned)cx * 73856093u ^ (unsigned)cy * 19349663u ^ (unsigned)cz * 83492791u ^ (unsigned)r * 2654435761u;
     h ^= h >> 15;
@@ -96,12 +98,40 @@ __device__ __forceinline__ unsigned cell_hash(int cx, int cy, int cz, int r, int
     return h & (unsigned)hmask;
 }
 
+__device__ __forceinline__ float4 pos_f(const Dev &d, int v) {
+    if (d.mixed) {
+        const float4 *f = reinterpret_cast<const float4 *>(d.pos) + 2 * (size_t)v;
+        const float4 h = f[0], l = f[1];
+        return make_float4(h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w);
+    }
+    const double4 p = d.pos[v];
+    return make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
+}
+
+// 1. has any voxel moved more than half the skin since the last build?
+__global__ void k_coll_check(Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.ns) return;
+    const int v = d.csurf[s];
+    const RobotP &rp = d.rp[d.vinfo[v].x];
+    const float4 p = pos_f(d, v), q = d.cref[s];
+    const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
+    const float lim = 0.49f * (float)rp.skin;
+    if (ex * ex + ey * ey + ez * ez > lim * lim) atomicOr(d.cflag, 1);
+}
+
+__global__ void k_coll_clear(Dev d) {
+    if (!*d.cflag) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.hsize; i += gridDim.x * blockDim.x) d.hcount[i] = 0;
+}
+
 __global__ void k_coll_bin(Dev d) {
+    if (!*d.cflag) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
-    const double ic = d.rp[r].inv_cell;
+    const double ic = d.rp[r].inv_list_cell;
     const double4 p = load_state(d, d.pos, v);
     const int4 c = make_int4((int)floor(p.x * ic), (int)floor(p.y * ic), (int)floor(p.z * ic), r);
     d.ccell[s] = c;
@@ -111,6 +141,7 @@ __global__ void k_coll_bin(Dev d) {
 
 // exclusive scan of hcount in blocks of 1024 (hsize is a multiple of 1024)
 __global__ void __launch_bounds__(1024) k_scan_blocks(Dev d) {
+    if (!*d.cflag) return;
     __shared__ int sh[1024];
     const int i = blockIdx.x * 1024 + threadIdx.x;
     const int x = d.hcount[i];
@@ -127,6 +158,7 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(Dev d) {
 }
 
 __global__ void __launch_bounds__(1024) k_scan_add(Dev d) {
+    if (!*d.cflag) return;
     __shared__ int base;
     if (threadIdx.x < 32) {
         int acc = 0;
@@ -142,6 +174,7 @@ __global__ void __launch_bounds__(1024) k_scan_add(Dev d) {
 }
 
 __global__ void k_coll_scatter(Dev d) {
+    if (!*d.cflag) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.ns) return;
     const int4 c = d.ccell[s];
@@ -149,41 +182,21 @@ __global__ void k_coll_scatter(Dev d) {
     d.hsorted[slot] = s;
 }
 
-// force on voxel1 from the pair (voxel1, voxel2) as VX3_Collision computes it
-__device__ __forceinline__ V3<double> pair_force(const Dev &d, int v1, int v2, double bsa1, double bsa2) {
-    const VMat &m1 = d.vmat[d.vinfo[v1].y >> 8];
-    const VMat &m2 = d.vmat[d.vinfo[v2].y >> 8];
-    const double pstiff = 2.0f / (1.0f / m1.pstiff + 1.0f / m2.pstiff);
-    const double dampC = 0.5f * (m1.c_col + m2.c_col);
-    const double4 p1 = load_state(d, d.pos, v1), p2 = load_state(d, d.pos, v2);
-    const V3<double> offset{p2.x - p1.x, p2.y - p1.y, p2.z - p1.z};
-    const double nom = (bsa1 + bsa2) * 0.625;
-    const double rel = nom - len(offset);
-    if (!(rel > 0)) return V3<double>{0, 0, 0};
-    const V3<double> u = normalized(offset);
-    const double4 l1 = load_state(d, d.linmom, v1), l2 = load_state(d, d.linmom, v2);
-    const V3<double> w1 = scl(V3<double>{l1.x, l1.y, l1.z}, m1.mass_inv);
-    const V3<double> w2 = scl(V3<double>{l2.x, l2.y, l2.z}, m2.mass_inv);
-    const double rv = (w1.x * u.x + w1.y * u.y + w1.z * u.z) - (w2.x * u.x + w2.y * u.y + w2.z * u.z);
-    return scl(u, pstiff * rel + dampC * rv);
-}
-
-constexpr int kMaxContacts = 48;
-
-__global__ void k_coll_gather(Dev d) {
+// 2. list every unlinked surface voxel of the same robot within cutoff + skin, ascending
+__global__ void k_coll_list(Dev d) {
+    if (!*d.cflag) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
-    if (d.status[r] != 0) return;
     const int4 c = d.ccell[s];
     const float4 pf = d.cposf[s];
-    // FP32 prefilter radius: the cell edge bounds every cutoff; the 1e-3 margin covers
-    // FP32 rounding of positions up to ~100 m from the origin, so no true pair is lost
-    const float cut = (float)d.rp[r].cell_size * 1.001f, cut2 = cut * cut;
+    const RobotP &rp = d.rp[r];
+    // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
+    const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
     const bool fixed = (d.vinfo[v].y & VF_FIXED) != 0;
     const short4 ij = d.ijk[v];
-    int cand[kMaxContacts];
+    int *out = d.nbr + (size_t)s * kNbrCap;
     int nc = 0;
     bool overflow = false;
     for (int dz = -1; dz <= 1; dz++)
@@ -205,40 +218,82 @@ __global__ void k_coll_gather(Dev d) {
                     const short4 ik = d.ijk[u];
                     if (abs(ik.x - ij.x) + abs(ik.y - ij.y) + abs(ik.z - ij.z) == 1) continue;
                     if (fixed && (d.vinfo[u].y & VF_FIXED)) continue;
-                    // exact envelope test of the reference, voxel1 = the later surface voxel
-                    const int a1 = t < s ? v : u, a2 = t < s ? u : v;
-                    const double4 pa = load_state(d, d.pos, a1), pb = load_state(d, d.pos, a2);
-                    const double ba = (pa.w + pa.w + pa.w) / 3.0f, bb = (pb.w + pb.w + pb.w) / 3.0f;
-                    const V3<double> diff{pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
-                    const double wd = (ba + bb) * 0.625;
-                    if (diff.x > wd || diff.x < -wd) continue;
-                    if (diff.y > wd || diff.y < -wd) continue;
-                    if (diff.z > wd || diff.z < -wd) continue;
-                    if (len(diff) > wd) continue;
-                    if (nc == kMaxContacts) {
+                    if (nc == kNbrCap) {
                         overflow = true;
                         continue;
                     }
                     int j = nc++;
-                    while (j > 0 && cand[j - 1] > t) {
-                        cand[j] = cand[j - 1];
+                    while (j > 0 && out[j - 1] > t) {
+                        out[j] = out[j - 1];
                         j--;
                     }
-                    cand[j] = t;
+                    out[j] = t;
                 }
             }
     if (overflow) atomicOr(&d.status[r], 2);
+    d.nnb[s] = nc;
+    d.cref[s] = pf;
+}
+
+// force on voxel1 from the pair (voxel1, voxel2) as VX3_Collision computes it
+__device__ __forceinline__ V3<double> pair_force(const Dev &d, int v1, int v2, double bsa1, double bsa2) {
+    const VMat &m1 = d.vmat[d.vinfo[v1].y >> 8];
+    const VMat &m2 = d.vmat[d.vinfo[v2].y >> 8];
+    const double pstiff = 2.0f / (1.0f / m1.pstiff + 1.0f / m2.pstiff);
+    const double dampC = 0.5f * (m1.c_col + m2.c_col);
+    const double4 p1 = load_state(d, d.pos, v1), p2 = load_state(d, d.pos, v2);
+    const V3<double> offset{p2.x - p1.x, p2.y - p1.y, p2.z - p1.z};
+    const double nom = (bsa1 + bsa2) * 0.625;
+    const double rel = nom - len(offset);
+    if (!(rel > 0)) return V3<double>{0, 0, 0};
+    const V3<double> u = normalized(offset);
+    const double4 l1 = load_state(d, d.linmom, v1), l2 = load_state(d, d.linmom, v2);
+    const V3<double> w1 = scl(V3<double>{l1.x, l1.y, l1.z}, m1.mass_inv);
+    const V3<double> w2 = scl(V3<double>{l2.x, l2.y, l2.z}, m2.mass_inv);
+    const double rv = (w1.x * u.x + w1.y * u.y + w1.z * u.z) - (w2.x * u.x + w2.y * u.y + w2.z * u.z);
+    return scl(u, pstiff * rel + dampC * rv);
+}
+
+// 3. exact test and contact forces on the listed pairs, ascending partner order
+__global__ void k_coll_eval(Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.ns) return;
+    const int v = d.csurf[s];
+    const int r = (int)d.vinfo[v].x;
+    if (d.status[r] != 0) return;
+    const int n = d.nnb[s];
+    const int *lst = d.nbr + (size_t)s * kNbrCap;
     V3<double> acc{0, 0, 0};
-    if (nc) {
+    if (n) {
+        const float4 pf = pos_f(d, v);
         const double4 pv = load_state(d, d.pos, v);
-        const double bsa = (pv.w + pv.w + pv.w) / 3.0f;
-        for (int k = 0; k < nc; k++) {
-            const int t = cand[k];
+        double bsa = 0;
+        bool have_bsa = false;
+        for (int k = 0; k < n; k++) {
+            const int t = lst[k];
             const int u = d.csurf[t];
+            // FP32 prefilter against the current cutoff: only pairs within 0.1% of it reach FP64
+            const float4 tf = pos_f(d, u);
+            const float ex = tf.x - pf.x, ey = tf.y - pf.y, ez = tf.z - pf.z;
+            const float cw = (pf.w + tf.w) * 0.625f * 1.001f;
+            if (ex * ex + ey * ey + ez * ez > cw * cw) continue;
+            if (!have_bsa) {
+                bsa = (pv.w + pv.w + pv.w) / 3.0f;  // baseSizeAverage (VX3_Voxel.h:102-105)
+                have_bsa = true;
+            }
             const double4 pu = load_state(d, d.pos, u);
             const double bu = (pu.w + pu.w + pu.w) / 3.0f;
-            if (t < s) acc = add(acc, pair_force(d, v, u, bsa, bu));        // v.contactForce += force
-            else acc = add(acc, neg(pair_force(d, u, v, bu, bsa)));          // v.contactForce += -force
+            // exact envelope test, voxel1 = the later surface voxel
+            const double4 &pa = t < s ? pv : pu, &pb = t < s ? pu : pv;
+            const double ba = t < s ? bsa : bu, bb = t < s ? bu : bsa;
+            const V3<double> diff{pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
+            const double wd = (ba + bb) * 0.625;
+            if (diff.x > wd || diff.x < -wd) continue;
+            if (diff.y > wd || diff.y < -wd) continue;
+            if (diff.z > wd || diff.z < -wd) continue;
+            if (len(diff) > wd) continue;
+            if (t < s) acc = add(acc, pair_force(d, v, u, bsa, bu));    // v.contactForce += force
+            else acc = add(acc, neg(pair_force(d, u, v, bu, bsa)));      // v.contactForce += -force
         }
     }
     d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
@@ -246,13 +301,16 @@ __global__ void k_coll_gather(Dev d) {
 
 void launch_collision(const Dev &d, cudaStream_t s) {
     if (!d.ns) return;
-    cudaMemsetAsync(d.hcount, 0, sizeof(int) * d.hsize, s);
     const int g = (d.ns + 255) / 256;
+    cudaMemsetAsync(d.cflag, 0, sizeof(int), s);
+    k_coll_check<<<g, 256, 0, s>>>(d);
+    k_coll_clear<<<152 * 4, 256, 0, s>>>(d);
     k_coll_bin<<<g, 256, 0, s>>>(d);
     k_scan_blocks<<<d.hsize / 1024, 1024, 0, s>>>(d);
     k_scan_add<<<d.hsize / 1024, 1024, 0, s>>>(d);
     k_coll_scatter<<<g, 256, 0, s>>>(d);
-    k_coll_gather<<<g, 256, 0, s>>>(d);
+    k_coll_list<<<g, 256, 0, s>>>(d);
+    k_coll_eval<<<g, 256, 0, s>>>(d);
 }
 
 // ---------------------------------------------------------------- centre of mass

@@ -337,7 +337,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         for (int i = 0; i < R.n_materials; i++)
             fmax = std::fmax(fmax, std::fmax(1.0 + tlo * hm[i].cte, 1.0 + thi * hm[i].cte));
         rp.cell_size = 1.25 * R.vox_size * fmax * (1.0 + 1e-6);
-        rp.inv_cell = 1.0 / rp.cell_size;
+        rp.skin = 0.3 * R.vox_size;
+        rp.inv_list_cell = 1.0 / (rp.cell_size + rp.skin);
         (void)cte_max;
         rp.soff = (int)csurf.size();
         for (int k = 0; k < nvr; k++) {
@@ -383,9 +384,11 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         return rc;
     // collision tables
     int hs = 1024;
-    while (hs < 2 * d.ns) hs <<= 1;
+    while (hs < d.ns) hs <<= 1;
     d.hsize = hs;
     if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.cposf, d.ns)) ||
+        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1)) ||
+        (rc = c->upload(&d.cref, std::vector<float4>((size_t)d.ns, make_float4(1e30f, 1e30f, 1e30f, 0.0f)))) ||
         (rc = c->alloc(&d.hcount, hs)) ||
         (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.hsorted, d.ns)) ||
         (rc = c->alloc(&d.hblock, hs / 1024)))

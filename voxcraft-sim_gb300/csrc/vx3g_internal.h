@@ -59,12 +59,17 @@ struct LMat {  // one link material (global index)
 };
 
 struct RobotP {
-    double vox_size, temp_amp, temp_period, inv_period, dt_frac, cell_size, inv_cell;
+    double vox_size, temp_amp, temp_period, inv_period, dt_frac;
+    double cell_size;      // upper bound of the envelope cutoff (bsa1+bsa2)*0.625
+    double skin;           // Verlet skin of the contact-candidate lists
+    double inv_list_cell;  // 1 / (cell_size + skin): grid used to build the lists
     int voff, nv, loff, nl, soff, ns;
     int floor, vary_temp, expansion, collision;
 };
 
 template <class R> struct Slot { R f[3]; R m[3]; };
+
+constexpr int kNbrCap = 64;  // contact candidates kept per collision-surface voxel
 
 struct Dev {
     // voxels
@@ -91,6 +96,10 @@ struct Dev {
     int *csurf;     // collision surface list (global voxel index), NS entries
     int4 *ccell;    // cell coords + robot per collision-surface voxel
     float4 *cposf;  // FP32 copy of the position (prefilter) per collision-surface voxel
+    float4 *cref;   // position at the last list build, per collision-surface voxel
+    int *nbr;       // candidate list: kNbrCap surface indices per collision-surface voxel, ascending
+    int *nnb;       // candidate count per collision-surface voxel
+    int *cflag;     // 1: rebuild the candidate lists this step
     int *hcount, *hstart, *hfill, *hsorted, *hblock;
     int hsize;      // power of two
     int *err;       // device error word
