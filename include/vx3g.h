@@ -82,6 +82,8 @@ typedef struct vx3g_robot_desc {
     int enable_collision;           /* Simulator/AttachDetach/EnableCollision */
     int volume_effects;             /* Simulator/Features/VolumeEffectsEnabled (0 forces Poisson's ratio to 0) */
     double bond_damping, col_damping, slow_damping; /* Simulator/Damping/{Bond,Col,Slow}DampingZ */
+    const double *log10E;           /* nx*ny*nz per-voxel log10 Young's modulus overriding the palette's,
+                                       or NULL (per-voxel stiffness is not expressible in a VXA palette) */
 } vx3g_robot_desc;
 
 typedef struct vx3g_batch_desc {
@@ -143,14 +145,31 @@ int vx3g_stop_robot(vx3g_ctx *ctx, int robot);
 /* Steps taken so far by the context (every robot that has not diverged). */
 int64_t vx3g_steps_taken(vx3g_ctx *ctx);
 
+/* ---- differentiation (no counterpart in the reference) ---------------------
+ * vx3g_record: advances n_steps (exactly like vx3g_step) and keeps the state
+ *   every `checkpoint_every` steps, as the forward pass of a gradient.  FP64
+ *   contexts without collisions only (VX3G_ERR_UNSUPPORTED otherwise).
+ * vx3g_backward: gradient of L = sum_r w_r . (COM_r(end) - COM_r(start)) over the
+ *   recorded run with respect to every voxel's actuation phase (in cycles, the
+ *   unit of vx3g_robot_desc.phase) and log10 of its Young's modulus, by the
+ *   hand-written adjoint of the step run backwards over the recorded steps; each
+ *   checkpoint interval is recomputed from its checkpoint.  dL_dcom: w, 3 per
+ *   robot; dL_dphase, dL_dlog10E: one per voxel (either may be NULL).  The
+ *   discrete events of the run (friction stick/slip, contact, the small/large
+ *   angle switch of each link, the temperature clamp) are held as the run took
+ *   them, and the time step is held fixed.  The context keeps the recorded end
+ *   state; backward may be called again with other weights. */
+int vx3g_record(vx3g_ctx *ctx, int n_steps, int checkpoint_every);
+int vx3g_backward(vx3g_ctx *ctx, const double *dL_dcom, double *dL_dphase, double *dL_dlog10E);
+
 /* ---- measurement helpers (no counterpart in the reference) ---------------
  * vx3g_time_steps: runs vx3g_step(ctx, n_steps) between two CUDA events on the
  *   context's stream and returns the device time in milliseconds.
  * vx3g_flush_l2: overwrites a context-owned buffer of `bytes` bytes on the
  *   context's stream (evicts the L2 cache between timed iterations).
- * vx3g_time_passes: launches each per-step pass `iters` times on its own
- *   between CUDA events and returns the mean device time per launch in
- *   milliseconds for: [0] link pass, [1] collision passes (all kernels of the
+ * vx3g_time_passes: runs each per-step pass `iters` times on its own, captured
+ *   in one CUDA graph as the step graphs run it, between CUDA events, and
+ *   returns the mean device time per pass in milliseconds for: [0] link pass, [1] collision passes (all kernels of the
  *   broad and narrow phase together), [2] voxel pass.  It advances the state
  *   like extra steps would; use it after the measured run. */
 int vx3g_time_steps(vx3g_ctx *ctx, int n_steps, float *ms);

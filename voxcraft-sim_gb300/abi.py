@@ -25,6 +25,7 @@ EXPORTS = [
     "vx3g_counts", "vx3g_offsets", "vx3g_get_state", "vx3g_set_state", "vx3g_get_voxel_aux", "vx3g_get_links",
     "vx3g_get_topology", "vx3g_get_surface", "vx3g_com", "vx3g_dt", "vx3g_time", "vx3g_status",
     "vx3g_steps_taken", "vx3g_time_steps", "vx3g_flush_l2", "vx3g_time_passes", "vx3g_stop_robot",
+    "vx3g_record", "vx3g_backward",
 ]
 
 
@@ -44,7 +45,8 @@ class RobotDesc(ctypes.Structure):
                 ("temp_amplitude", ctypes.c_double), ("temp_period", ctypes.c_double), ("temp_base", ctypes.c_double),
                 ("temp_enabled", ctypes.c_int), ("vary_temp", ctypes.c_int), ("enable_expansion", ctypes.c_int),
                 ("enable_collision", ctypes.c_int), ("volume_effects", ctypes.c_int),
-                ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double)]
+                ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
+                ("log10E", ctypes.c_void_p)]
 
 
 class BatchDesc(ctypes.Structure):
@@ -90,6 +92,8 @@ def load(path: str = LIB_PATH):
     lib.vx3g_flush_l2.argtypes = [vp, ctypes.c_size_t]
     lib.vx3g_time_passes.argtypes = [vp, ip, dp]
     lib.vx3g_stop_robot.argtypes = [vp, ip]
+    lib.vx3g_record.argtypes = [vp, ip, ip]
+    lib.vx3g_backward.argtypes = [vp, dp, dp, dp]
     _lib = lib
     return lib
 
@@ -117,11 +121,18 @@ def robot_desc(robot):
         mats[i] = Material(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress,
                            0 if m.fail_stress == 0 else 1, int(m.fixed), int(m.is_measured), 0.0)
     Z, Y, X = g.shape
+    log10E = getattr(robot, "log10E", None)
+    if log10E is not None:
+        le = log10E
+        if robot.z_offset:
+            le = np.concatenate([np.zeros((robot.z_offset,) + le.shape[1:]), le], axis=0)
+        log10E = np.ascontiguousarray(le.reshape(-1).astype(np.float64))
     d = RobotDesc(X, Y, Z, _P(lattice), _P(phase), len(robot.materials), mats, robot.vox_size, robot.dt_frac,
                   robot.grav_acc, int(robot.floor), robot.temp_amplitude, robot.temp_period, robot.temp_base, 0,
                   int(robot.temp_vary), int(robot.enable_expansion), int(robot.enable_collision),
-                  int(robot.volume_effects), robot.bond_damping, robot.col_damping, robot.slow_damping)
-    return d, (lattice, phase, mats)
+                  int(robot.volume_effects), robot.bond_damping, robot.col_damping, robot.slow_damping,
+                  _P(log10E))
+    return d, (lattice, phase, mats, log10E)
 
 
 class Batch:
@@ -241,6 +252,16 @@ class Batch:
         ms = np.zeros(3, np.float32)
         _check(self.lib.vx3g_time_passes(self.h, int(iters), _P(ms)), "vx3g_time_passes")
         return dict(links=float(ms[0]), collision=float(ms[1]), voxels=float(ms[2]))
+
+    def record(self, n: int, checkpoint_every: int = 100):
+        _check(self.lib.vx3g_record(self.h, int(n), int(checkpoint_every)), "vx3g_record")
+
+    def backward(self, dL_dcom):
+        w = np.ascontiguousarray(np.asarray(dL_dcom, np.float64).reshape(self.n_robots, 3))
+        gp = np.zeros(self.nv)
+        ge = np.zeros(self.nv)
+        _check(self.lib.vx3g_backward(self.h, _P(w), _P(gp), _P(ge)), "vx3g_backward")
+        return gp, ge
 
     def stop_robot(self, r: int):
         _check(self.lib.vx3g_stop_robot(self.h, int(r)), "vx3g_stop_robot")

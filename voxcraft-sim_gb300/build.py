@@ -25,6 +25,7 @@ UNITS = [
     ("vx3g_fp64.cu", ["--fmad=false"]),
     ("vx3g_aux.cu", ["--fmad=false"]),
     ("vx3g_mixed.cu", []),
+    ("vx3g_adjoint.cu", ["--fmad=false"]),
     ("vx3g_host.cpp", []),
     ("vx3g_xml.cpp", []),
     ("vx3g_manager.cpp", []),

@@ -10,6 +10,7 @@
 // reference computes them before copying them into its VX3 objects.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -18,6 +19,7 @@
 #include <vector>
 
 #include "../../include/vx3g.h"
+#include "vx3g_adjoint.h"
 #include "vx3g_internal.h"
 
 using namespace vx3g;
@@ -85,6 +87,26 @@ HostVMat import_material(const vx3g_material &in, const vx3g_robot_desc &r) {
 
 // CVX_MaterialLink::updateAll + updateDerived (src/old/VX_MaterialLink.cpp:47-140);
 // vox1 is the material of the voxel being added, vox2 its existing neighbour's.
+VMat to_vmat(const HostVMat &m, const vx3g_material &in) {
+    VMat v{};
+    v.mass = m.mass; v.mass_inv = m.mass_inv; v.mom_inv = m.mom_inv;
+    v.c_glob = m.z_glob * m.c2m;
+    v.c_glob_rot = m.z_glob * m.c2i;
+    v.c_col = m.z_col * m.c2m;
+    v.grav_force = -m.mass * 9.80665f * m.grav_mult;
+    v.pstiff = (float)(2 * m.E * m.nom);
+    v.mu_s = m.mu_s; v.mu_k = m.mu_k; v.cte = m.cte;
+    v.dmc = 2 * m.sqrt_mass * m.z_int;
+    v.E = m.E; v.nu = m.nu;
+    v.nom_hi = (float)m.nom;
+    v.nom_lo = (float)(m.nom - (double)v.nom_hi);
+    v.fixed = in.fixed ? 1 : 0;
+    v.is_measured = in.is_measured ? 1 : 0;
+    v.nom_size = m.nom;
+    v.thermal_on_after = in.thermal_on_after;
+    return v;
+}
+
 LMat combine(const HostVMat &v1, const HostVMat &v2) {
     LMat l{};
     float f1 = v1.sigma_fail, f2 = v2.sigma_fail, failS;
@@ -163,6 +185,18 @@ struct vx3g_ctx {
     std::vector<int> vmat_local, surface;
     std::vector<unsigned char> vfixed;
     int64_t steps = 0;
+    std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
+    bool any_collision = false;
+    // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
+    std::vector<void *> rec_mem;
+    std::vector<Snap> rec_ck, rec_store;
+    Snap rec_end{};
+    void *rec_slots = nullptr;
+    int64_t rec_start = -1;
+    int rec_n = 0, rec_k = 0;
+    void *adj_mem = nullptr;
+    AdjBufs ab{};
+    std::vector<std::pair<long, cudaGraphExec_t>> adj_graphs;  // backward intervals, by (len, parity)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     void *flush = nullptr;
     size_t flush_bytes = 0;
@@ -181,10 +215,23 @@ struct vx3g_ctx {
         if (!h.empty()) CU(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
         return VX3G_OK;
     }
+    void free_record() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto &g : adj_graphs) cudaGraphExecDestroy(g.second);
+        adj_graphs.clear();
+        for (void *p : rec_mem) cudaFree(p);
+        rec_mem.clear();
+        rec_ck.clear();
+        rec_store.clear();
+        rec_slots = nullptr;
+        rec_start = -1;
+    }
     ~vx3g_ctx() {
         for (auto &g : graph)
             if (g) cudaGraphExecDestroy(g);
         if (stream) cudaStreamSynchronize(stream);
+        free_record();
+        if (adj_mem) cudaFree(adj_mem);
         for (void *p : allocs) cudaFree(p);
         if (flush) cudaFree(flush);
         if (stream) cudaStreamDestroy(stream);
@@ -234,25 +281,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             if (in.model == 1 && !(in.fail_stress > 0)) return fail(VX3G_ERR_INVALID, "fail_stress must be positive");
             if (!(in.E > 0)) return fail(VX3G_ERR_INVALID, "Young's modulus must be positive");
             hm[i] = import_material(in, R);
-            const HostVMat &m = hm[i];
-            VMat v{};
-            v.mass = m.mass; v.mass_inv = m.mass_inv; v.mom_inv = m.mom_inv;
-            v.c_glob = m.z_glob * m.c2m;
-            v.c_glob_rot = m.z_glob * m.c2i;
-            v.c_col = m.z_col * m.c2m;
-            v.grav_force = -m.mass * 9.80665f * m.grav_mult;
-            v.pstiff = (float)(2 * m.E * m.nom);
-            v.mu_s = m.mu_s; v.mu_k = m.mu_k; v.cte = m.cte;
-            v.dmc = 2 * m.sqrt_mass * m.z_int;
-            v.E = m.E; v.nu = m.nu;
-            v.nom_hi = (float)m.nom;
-            v.nom_lo = (float)(m.nom - (double)v.nom_hi);
-            v.fixed = in.fixed ? 1 : 0;
-            v.is_measured = in.is_measured ? 1 : 0;
-            v.nom_size = m.nom;
-            v.thermal_on_after = in.thermal_on_after;
-            vmats.push_back(v);
-            cte_max = std::fmax(cte_max, std::fabs((double)m.cte));
+            if (!R.log10E) vmats.push_back(to_vmat(hm[i], in));
+            cte_max = std::fmax(cte_max, std::fabs((double)hm[i].cte));
         }
         const int nx = R.nx, ny = R.ny, nz = R.nz;
         const long long ncell = (long long)nx * ny * nz;
@@ -267,6 +297,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             if (p > 0) vid[i] = v0 + nvr++;
         }
         std::vector<int> pair_lmat(R.n_materials * R.n_materials, -1);
+        std::vector<HostVMat> hv;  // per voxel when the robot carries per-voxel moduli
+        if (R.log10E) hv.resize(nvr);
         // initial temperature: UpdateMatTemps at import (VX_Sim.cpp:462-478, VX_Environment.cpp:326-345)
         float temp0 = 0.0f;
         if (R.temp_enabled) {
@@ -286,18 +318,34 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             c->ijk.push_back(make_short4((short)x, (short)y, (short)z, 0));
             c->vmat_local.push_back(mi);
             uint32_t fl = VF_STATIC | (R.materials[mi].fixed ? VF_FIXED : 0u);
-            vinfo.push_back(make_uint2((unsigned)r, fl | ((uint32_t)(vbase + mi) << 8)));
+            int vm = vbase + mi;
+            if (R.log10E) {  // this voxel's own material: the palette entry with E = 10^log10E
+                if (!std::isfinite(R.log10E[i])) return fail(VX3G_ERR_INVALID, "log10E must be finite");
+                vx3g_material mm = R.materials[mi];
+                mm.E = std::pow(10.0, R.log10E[i]);
+                hv[vid[i] - v0] = import_material(mm, R);
+                vm = (int)vmats.size();
+                vmats.push_back(to_vmat(hv[vid[i] - v0], mm));
+            }
+            vinfo.push_back(make_uint2((unsigned)r, fl | ((uint32_t)vm << 8)));
             c->vfixed.push_back(R.materials[mi].fixed ? 1 : 0);
             const long long nb[3] = {x > 0 ? i - 1 : -1, y > 0 ? i - nx : -1, z > 0 ? i - (long long)nx * ny : -1};
             for (int a = 0; a < 3; a++) {
                 if (nb[a] < 0 || vid[nb[a]] < 0) continue;
                 const int vn = vid[nb[a]], vp = vid[i];
                 const int mn = c->vmat_local[vn], mp = mi;
-                int &lm = pair_lmat[mp * R.n_materials + mn];
-                if (lm < 0) {
+                int lm;
+                if (R.log10E) {  // one link material per link
                     lm = (int)lmats.size() - lbase;
-                    pair_lmat[mn * R.n_materials + mp] = lm;
-                    lmats.push_back(combine(hm[mp], hm[mn]));
+                    lmats.push_back(combine(hv[vp - v0], hv[vn - v0]));
+                } else {
+                    int &plm = pair_lmat[mp * R.n_materials + mn];
+                    if (plm < 0) {
+                        plm = (int)lmats.size() - lbase;
+                        pair_lmat[mn * R.n_materials + mp] = plm;
+                        lmats.push_back(combine(hm[mp], hm[mn]));
+                    }
+                    lm = plm;
                 }
                 const int l = (int)c->ends.size();
                 c->ends.push_back(make_int2(vn, vp));
@@ -351,6 +399,14 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     }
     c->voff[c->nr] = (int)pos.size();
     c->loff[c->nr] = (int)c->ends.size();
+    if (vmats.size() >= (1u << 24) || lmats.size() >= (1u << 24))
+        return fail(VX3G_ERR_INVALID, "more than 2^24 materials (per-voxel moduli on a very large batch)");
+    c->mass_tot.assign(c->nr, 0.0);
+    for (size_t v = 0; v < vinfo.size(); v++) {
+        const VMat &m = vmats[vinfo[v].y >> 8];
+        if (m.is_measured) c->mass_tot[vinfo[v].x] += (double)m.mass;
+    }
+    c->any_collision = !csurf.empty();
     if (pos.size() > (size_t)INT32_MAX / 8) return fail(VX3G_ERR_INVALID, "batch too large");
 
     Dev &d = c->d;
@@ -722,12 +778,16 @@ int vx3g_flush_l2(vx3g_ctx *c, size_t bytes) {
 
 int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms3) {
     if (!c || !ms3 || iters <= 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_time_passes");
+    CU(cudaSetDevice(c->device));
     cudaEvent_t a, b;
     CU(cudaEventCreate(&a));
     CU(cudaEventCreate(&b));
     const Dev &d = c->d;
     for (int pass = 0; pass < 3; pass++) {
-        CU(cudaEventRecord(a, c->stream));
+        // each pass repeated `iters` times inside one CUDA graph, as the step graphs run it
+        const int p0 = (int)(c->steps & 1);
+        cudaGraph_t g;
+        CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < iters; i++) {
             if (pass == 0) {
                 if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(d, c->stream);
@@ -735,20 +795,235 @@ int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms3) {
             } else if (pass == 1) {
                 launch_collision(d, c->stream);
             } else {
-                const int parity = (int)(c->steps & 1);
-                if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(d, parity, c->stream);
-                else launch_voxels_mixed(d, parity, c->stream);
-                c->steps++;
+                if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(d, (p0 + i) & 1, c->stream);
+                else launch_voxels_mixed(d, (p0 + i) & 1, c->stream);
             }
         }
+        CU(cudaStreamEndCapture(c->stream, &g));
+        cudaGraphExec_t ex = nullptr;
+        cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(VX3G_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        CU(cudaEventRecord(a, c->stream));
+        CU(cudaGraphLaunch(ex, c->stream));
         CU(cudaEventRecord(b, c->stream));
         CU(cudaEventSynchronize(b));
+        cudaGraphExecDestroy(ex);
+        if (pass == 2) c->steps += iters;
         float ms = 0;
         CU(cudaEventElapsedTime(&ms, a, b));
         ms3[pass] = ms / iters;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    CU(cudaGetLastError());
+    return VX3G_OK;
+}
+
+// ---- differentiation: recorded run with checkpoints, adjoint run backwards
+
+}  // extern "C"
+
+namespace {
+
+size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t snap_bytes(const Dev &d) {
+    const size_t nv = d.nv, nl = d.nl, nr = d.nr;
+    return 4 * al256(nv * sizeof(double4)) + al256(nv * sizeof(uint2)) + al256(2 * nv * sizeof(float)) +
+           al256(9 * nl * sizeof(double)) + al256(nl * sizeof(float2)) + al256(nl * sizeof(uint2)) +
+           al256(2 * nr * sizeof(double)) + al256(nr * sizeof(int));
+}
+
+Snap carve(const Dev &d, char *p) {
+    const size_t nv = d.nv, nl = d.nl, nr = d.nr;
+    auto take = [&p](size_t n) {
+        char *q = p;
+        p += al256(n);
+        return q;
+    };
+    Snap s;
+    s.pos = (double4 *)take(nv * sizeof(double4));
+    s.quat = (double4 *)take(nv * sizeof(double4));
+    s.linmom = (double4 *)take(nv * sizeof(double4));
+    s.angmom = (double4 *)take(nv * sizeof(double4));
+    s.vinfo = (uint2 *)take(nv * sizeof(uint2));
+    s.tempe = (float *)take(2 * nv * sizeof(float));
+    s.lstate = (double *)take(9 * nl * sizeof(double));
+    s.strain = (float2 *)take(nl * sizeof(float2));
+    s.linfo = (uint2 *)take(nl * sizeof(uint2));
+    s.T = (double *)take(2 * nr * sizeof(double));
+    s.status = (int *)take(nr * sizeof(int));
+    return s;
+}
+
+Snap live_snap(const Dev &d) {
+    Snap s;
+    s.pos = d.pos; s.quat = d.quat; s.linmom = d.linmom; s.angmom = d.angmom;
+    s.vinfo = d.vinfo; s.tempe = d.tempe;
+    s.lstate = (double *)d.lstate; s.strain = d.strain; s.linfo = d.linfo;
+    s.T = d.T; s.status = d.status;
+    return s;
+}
+
+int alloc_snaps(vx3g_ctx *c, std::vector<Snap> &out, int n) {
+    const size_t sb = snap_bytes(c->d);
+    for (int i = 0; i < n; i++) {
+        void *m = nullptr;
+        cudaError_t e = cudaMalloc(&m, sb);
+        if (e != cudaSuccess) return fail(VX3G_ERR_NOMEM, std::string("cudaMalloc (state snapshots): ") + cudaGetErrorString(e));
+        c->rec_mem.push_back(m);
+        out.push_back(carve(c->d, (char *)m));
+    }
+    return VX3G_OK;
+}
+
+// One checkpoint interval of the backward pass as a CUDA graph: recompute the
+// interval's len states from the live state (the checkpoint, copied in just before),
+// then run the reverse steps over them.  Cached per (len, parity of the first step).
+void enqueue_adj_segment(vx3g_ctx *c, const AdjBufs &a0, int len, int p0) {
+    const Dev &d = c->d;
+    const Snap live = live_snap(d);
+    for (int i = 0; i < len; i++) {
+        launch_snap_copy(c->rec_store[i], live, d.nv, d.nl, d.nr, c->stream);
+        enqueue_step(c, (p0 + i) & 1);
+    }
+    AdjBufs a = a0;
+    launch_adj_slots(d, c->rec_store[len - 1], a, c->stream);
+    for (int i = len - 1; i >= 0; i--) {
+        a.parity = (p0 + i) & 1;
+        launch_adj_voxel_link(d, c->rec_store[i], a, c->stream);
+        launch_adj_gather_slots(d, c->rec_store[i], i > 0 ? &c->rec_store[i - 1] : nullptr, a, c->stream);
+    }
+}
+
+int adj_segment_graph(vx3g_ctx *c, const AdjBufs &a, int len, int p0, cudaGraphExec_t *out) {
+    const long key = 2L * len + p0;
+    for (auto &e : c->adj_graphs)
+        if (e.first == key) {
+            *out = e.second;
+            return VX3G_OK;
+        }
+    cudaGraph_t g;
+    CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_adj_segment(c, a, len, p0);
+    CU(cudaStreamEndCapture(c->stream, &g));
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(VX3G_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    c->adj_graphs.push_back({key, ex});
+    *out = ex;
+    return VX3G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vx3g_record(vx3g_ctx *c, int n, int k) {
+    if (!c || n < 0 || k <= 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_record");
+    if (c->precision != VX3G_PRECISION_FP64) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint runs on FP64 contexts");
+    if (c->any_collision) return fail(VX3G_ERR_UNSUPPORTED, "collisions are not differentiated");
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    c->free_record();
+    const int nck = (n + k - 1) / k;
+    int rc = alloc_snaps(c, c->rec_ck, nck);
+    if (rc) {
+        c->free_record();
+        return rc;
+    }
+    const Dev &d = c->d;
+    const Snap live = live_snap(d);
+    c->rec_start = c->steps;
+    c->rec_n = n;
+    c->rec_k = k;
+    for (int j = 0; j < nck; j++) {
+        launch_snap_copy(c->rec_ck[j], live, d.nv, d.nl, d.nr, c->stream);
+        rc = vx3g_step(c, std::min(k, n - j * k));
+        if (rc) {
+            c->free_record();
+            return rc;
+        }
+    }
+    CU(cudaGetLastError());
+    return VX3G_OK;
+}
+
+int vx3g_backward(vx3g_ctx *c, const double *dL_dcom, double *dL_dphase, double *dL_dlog10E) {
+    if (!c || !dL_dcom) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_backward");
+    if (c->rec_start < 0 || c->steps != c->rec_start + c->rec_n)
+        return fail(VX3G_ERR_INVALID, "no recorded run ends at the current state (call vx3g_record first)");
+    CU(cudaSetDevice(c->device));
+    const Dev &d = c->d;
+    const size_t nv = d.nv, nl = d.nl, nr = d.nr;
+    int rc;
+    if (!c->adj_mem) {  // adjoint buffers, kept for later calls
+        const size_t bytes = al256(13 * nv * 8) * 2 + al256(6 * nv * 8) + al256(nv * 8) * 4 + al256(9 * nl * 8) +
+                             al256(54 * nv * 8) + al256(3 * nr * 8) + al256(nr * 8);
+        cudaError_t e = cudaMalloc(&c->adj_mem, bytes);
+        if (e != cudaSuccess) {
+            c->adj_mem = nullptr;
+            return fail(VX3G_ERR_NOMEM, std::string("cudaMalloc (adjoint buffers): ") + cudaGetErrorString(e));
+        }
+        char *p = (char *)c->adj_mem;
+        auto take = [&p](size_t n) {
+            char *q = p;
+            p += al256(n);
+            return (double *)q;
+        };
+        AdjBufs &a = c->ab;
+        a.lv = take(13 * nv * 8);
+        a.lown = take(13 * nv * 8);
+        a.lF = take(6 * nv * 8);
+        a.lbs = take(nv * 8);
+        a.lE = take(nv * 8);
+        a.gphase = take(nv * 8);
+        a.glogE = take(nv * 8);
+        a.lloc = take(9 * nl * 8);
+        a.aslot = take(54 * nv * 8);
+        a.w = take(3 * nr * 8);
+        a.mass_tot = take(nr * 8);
+        CU(cudaMemcpyAsync((void *)a.mass_tot, c->mass_tot.data(), nr * 8, cudaMemcpyHostToDevice, c->stream));
+    }
+    const int n = c->rec_n, k = c->rec_k;
+    const int store = std::min(n, k);
+    if ((int)c->rec_store.size() < store || !c->rec_slots) {  // recompute store + the end state
+        for (auto &g : c->adj_graphs) cudaGraphExecDestroy(g.second);
+        c->adj_graphs.clear();
+        c->rec_store.clear();
+        std::vector<Snap> end;
+        if ((rc = alloc_snaps(c, c->rec_store, store)) || (rc = alloc_snaps(c, end, 1))) return rc;
+        c->rec_end = end[0];
+        void *m = nullptr;
+        cudaError_t e = cudaMalloc(&m, 36 * nv * sizeof(double));
+        if (e != cudaSuccess) return fail(VX3G_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        c->rec_mem.push_back(m);
+        c->rec_slots = m;
+    }
+    AdjBufs a = c->ab;
+    CU(cudaMemcpyAsync((void *)a.w, dL_dcom, 3 * nr * 8, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemsetAsync(a.gphase, 0, nv * 8, c->stream));
+    CU(cudaMemsetAsync(a.glogE, 0, nv * 8, c->stream));
+    const Snap live = live_snap(d);
+    launch_snap_copy(c->rec_end, live, d.nv, d.nl, d.nr, c->stream);
+    CU(cudaMemcpyAsync(c->rec_slots, d.slots, 36 * nv * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    launch_adj_seed(d, a, c->stream);
+    const int nck = (n + k - 1) / k;
+    for (int j = nck - 1; j >= 0; j--) {
+        const int len = std::min(k, n - j * k);
+        const int p0 = (int)((c->rec_start + (int64_t)j * k) & 1);
+        launch_snap_copy(live, c->rec_ck[j], d.nv, d.nl, d.nr, c->stream);
+        cudaGraphExec_t g = nullptr;
+        if ((rc = adj_segment_graph(c, a, len, p0, &g))) return rc;
+        CU(cudaGraphLaunch(g, c->stream));
+    }
+    launch_snap_copy(live, c->rec_end, d.nv, d.nl, d.nr, c->stream);
+    CU(cudaMemcpyAsync(d.slots, c->rec_slots, 36 * nv * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    if (dL_dphase) CU(cudaMemcpyAsync(dL_dphase, a.gphase, nv * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (dL_dlog10E) CU(cudaMemcpyAsync(dL_dlog10E, a.glogE, nv * 8, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
     CU(cudaGetLastError());
     return VX3G_OK;
 }

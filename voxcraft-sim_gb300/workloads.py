@@ -58,6 +58,7 @@ class Robot:
     enable_expansion: int = 0
     enable_collision: bool = False
     volume_effects: bool = True
+    log10E: Optional[np.ndarray] = None   # float64 [Z, Y, X] per-voxel log10 E (C ABI only; not in VXA)
     stop_time: Optional[float] = None     # StopConditionFormula "t - stop_time" (> 0 stops)
     fitness_x: bool = False               # FitnessFunction "x" (COM displacement along x)
     record_step: int = 0                  # RecordHistory/RecordStepSize
@@ -240,6 +241,19 @@ def c3_population(seed: int = 0, n_robots: int = 1024, lo: int = 4, hi: int = 16
         out.append(bernoulli_body(rng, dims, 0.7, mats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
                                   temp_period=0.2))
     return out
+
+
+def c4_differentiable(seed: int = 0) -> List[Robot]:
+    """Differentiable single robot: 12x12x6 fully filled body, per-voxel actuation
+    phase uniform in [0, 2*pi) (stored in cycles) and per-voxel log10 E uniform in
+    [5, 7], 5 Hz actuation, floor friction on, no collisions."""
+    rng = np.random.default_rng(seed)
+    grid = np.ones((6, 12, 12), np.uint8)
+    phase = rng.random((6, 12, 12)).astype(np.float32).astype(np.float64)
+    log10E = rng.uniform(5, 7, size=(6, 12, 12)).astype(np.float32).astype(np.float64)
+    m = Material(E=1e6, nu=0.35, rho=1e3, cte=0.01, mu_static=1.0, mu_kinetic=0.5)
+    return [Robot(grid=grid, materials=[m], phase=phase, log10E=log10E, temp_vary=True, temp_amplitude=39.0,
+                  temp_period=0.2)]
 
 
 def c5_population_collisions(seed: int = 0, n_robots: int = 256) -> List[Robot]:
