@@ -162,6 +162,26 @@ int64_t vx3g_steps_taken(vx3g_ctx *ctx);
 int vx3g_record(vx3g_ctx *ctx, int n_steps, int checkpoint_every);
 int vx3g_backward(vx3g_ctx *ctx, const double *dL_dcom, double *dL_dphase, double *dL_dlog10E);
 
+/* ---- stable time step without allocation (no counterpart in the reference as
+ * an entry point; the reference evaluates recommendedTimeStep inside its first
+ * doTimeStep, VX3_VoxelyzeKernel.cu:184-217, 248-253) ----------------------------
+ * vx3g_recommended_dt_noalloc: rdt[r] = recommendedTimeStep of robot r in its
+ *   current state (seconds, before DtFrac and the 1e-10 floor; vx3g_create sets
+ *   the context's dt to (float)(DtFrac * max(rdt, 1e-10))).  With Poisson's ratio
+ *   on, the stiffness term follows the links' current strain, so the value
+ *   changes as the robot deforms.
+ *   For callers that must not allocate device memory at this point: a control
+ *   loop re-checking the stable step between chunks in a process whose device
+ *   memory budget is fixed, or code that runs while the device is in use by work
+ *   that an allocation (which can synchronise the device) would disturb.  Its
+ *   reduction scratch is a fixed 96 KB array in the library's device image; the
+ *   call allocates nothing and frees nothing.  At most 4096 robots per context
+ *   (VX3G_ERR_INVALID beyond).  The first call on a device looks the scratch up
+ *   (once per device); make that first call before any stream capture.  Calls
+ *   that overlap in time on the same device share the one scratch array and race
+ *   (wrong results): serialise them.  Blocking: returns when rdt is filled. */
+int vx3g_recommended_dt_noalloc(vx3g_ctx *ctx, double *rdt);
+
 /* ---- measurement helpers (no counterpart in the reference) ---------------
  * vx3g_time_steps: runs vx3g_step(ctx, n_steps) between two CUDA events on the
  *   context's stream and returns the device time in milliseconds.

@@ -25,7 +25,7 @@ EXPORTS = [
     "vx3g_counts", "vx3g_offsets", "vx3g_get_state", "vx3g_set_state", "vx3g_get_voxel_aux", "vx3g_get_links",
     "vx3g_get_topology", "vx3g_get_surface", "vx3g_com", "vx3g_dt", "vx3g_time", "vx3g_status",
     "vx3g_steps_taken", "vx3g_time_steps", "vx3g_flush_l2", "vx3g_time_passes", "vx3g_stop_robot",
-    "vx3g_record", "vx3g_backward",
+    "vx3g_record", "vx3g_backward", "vx3g_recommended_dt_noalloc",
 ]
 
 
@@ -93,6 +93,7 @@ def load(path: str = LIB_PATH):
     lib.vx3g_time_passes.argtypes = [vp, ip, dp]
     lib.vx3g_stop_robot.argtypes = [vp, ip]
     lib.vx3g_record.argtypes = [vp, ip, ip]
+    lib.vx3g_recommended_dt_noalloc.argtypes = [vp, dp]
     lib.vx3g_backward.argtypes = [vp, dp, dp, dp]
     _lib = lib
     return lib
@@ -262,6 +263,11 @@ class Batch:
         ge = np.zeros(self.nv)
         _check(self.lib.vx3g_backward(self.h, _P(w), _P(gp), _P(ge)), "vx3g_backward")
         return gp, ge
+
+    def recommended_dt_noalloc(self):
+        out = np.zeros(self.n_robots)
+        _check(self.lib.vx3g_recommended_dt_noalloc(self.h, _P(out)), "vx3g_recommended_dt_noalloc")
+        return out
 
     def stop_robot(self, r: int):
         _check(self.lib.vx3g_stop_robot(self.h, int(r)), "vx3g_stop_robot")

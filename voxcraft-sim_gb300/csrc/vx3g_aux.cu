@@ -1,6 +1,8 @@
 // vx3g_aux.cu -- set-up and per-step passes other than the link/voxel passes:
 // initial temperature, stable time step, surface-voxel collision, centre of mass.
 // FP64 arithmetic throughout, compiled with --fmad=false.
+#include <mutex>
+
 #include "vx3g_step.cuh"
 
 namespace vx3g {
@@ -76,6 +78,65 @@ void launch_dt(const Dev &d, double *scratch, cudaStream_t s) {
     if (d.nl) k_dt_links<<<(d.nl + 255) / 256, 256, 0, s>>>(d, mx);
     if (d.nv) k_dt_voxels<<<(d.nv + 255) / 256, 256, 0, s>>>(d, mx);
     k_dt_final<<<(d.nr + 255) / 256, 256, 0, s>>>(d, mx);
+}
+
+// ---------------------------------------------------------------- stable time step, no allocation
+// vx3g_recommended_dt_noalloc computes recommendedTimeStep for every robot with its
+// reduction scratch in device memory reserved when the module loads, not in memory
+// the context or the call allocates: 2 per-robot maxima (link and voxel terms) and
+// the per-robot result, for at most kNoAllocMaxRobots robots (96 KB).
+constexpr int kNoAllocMaxRobots = 4096;
+static __device__ __align__(256) unsigned long long g_dt_noalloc[3 * kNoAllocMaxRobots];
+
+// recommendedTimeStep from the maxima (VX3_VoxelyzeKernel.cu:184-217), without DtFrac
+__global__ void k_dt_recommended(int nr, const unsigned long long *mx, double *out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nr) return;
+    double f2 = __longlong_as_double((long long)mx[2 * r]);
+    if (f2 <= 0.0f) f2 = __longlong_as_double((long long)mx[2 * r + 1]);
+    out[r] = (f2 <= 0.0f) ? 0.0f : 1.0f / (6.283185f * sqrt(f2));
+}
+
+int recommended_dt_noalloc(const Dev &d, int device, double *out_host, cudaStream_t s, const char **why) {
+    if (d.nr > kNoAllocMaxRobots) {
+        *why = "vx3g_recommended_dt_noalloc: at most 4096 robots per context";
+        return -1;
+    }
+    // the scratch address, looked up once per device (with that device current)
+    static std::mutex lock;
+    static void *addr[64] = {};
+    if (device < 0 || device >= 64) {
+        *why = "vx3g_recommended_dt_noalloc: device ordinal out of range";
+        return -1;
+    }
+    void *base;
+    {
+        std::lock_guard<std::mutex> g(lock);
+        if (!addr[device]) {
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_dt_noalloc) != cudaSuccess) {
+                *why = "vx3g_recommended_dt_noalloc: cudaGetSymbolAddress failed";
+                return -3;
+            }
+            addr[device] = p;
+        }
+        base = addr[device];
+    }
+    unsigned long long *mx = (unsigned long long *)base;  // 2*nr maxima: must start at zero
+    double *res = (double *)(mx + 2 * kNoAllocMaxRobots);
+    if (cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * 2 * d.nr, s) != cudaSuccess) {
+        *why = "vx3g_recommended_dt_noalloc: cudaMemsetAsync failed";
+        return -3;
+    }
+    if (d.nl) k_dt_links<<<(d.nl + 255) / 256, 256, 0, s>>>(d, mx);
+    if (d.nv) k_dt_voxels<<<(d.nv + 255) / 256, 256, 0, s>>>(d, mx);
+    if (d.nr) k_dt_recommended<<<(d.nr + 255) / 256, 256, 0, s>>>(d.nr, mx, res);
+    if (cudaMemcpyAsync(out_host, res, sizeof(double) * d.nr, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        *why = "vx3g_recommended_dt_noalloc: CUDA error";
+        return -3;
+    }
+    return 0;
 }
 
 // ---------------------------------------------------------------- collision

@@ -820,6 +820,16 @@ int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms3) {
     return VX3G_OK;
 }
 
+int vx3g_recommended_dt_noalloc(vx3g_ctx *c, double *rdt) {
+    if (!c || !rdt) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_recommended_dt_noalloc");
+    CU(cudaSetDevice(c->device));
+    const char *why = "";
+    const int rc = recommended_dt_noalloc(c->d, c->device, rdt, c->stream, &why);
+    if (rc == -1) return fail(VX3G_ERR_INVALID, why);
+    if (rc != 0) return fail(VX3G_ERR_CUDA, why);
+    return VX3G_OK;
+}
+
 // ---- differentiation: recorded run with checkpoints, adjoint run backwards
 
 }  // extern "C"

@@ -130,5 +130,8 @@ void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 void launch_collision(const Dev &d, cudaStream_t s);
 void launch_com(const Dev &d, double *out4, cudaStream_t s);
 void launch_or_status(const Dev &d, int robot, int bits, cudaStream_t s);
+// stable time step of every robot with module-static scratch (vx3g_recommended_dt_noalloc);
+// returns 0, -1 (invalid) or -3 (CUDA error, message in *why)
+int recommended_dt_noalloc(const Dev &d, int device, double *out_host, cudaStream_t s, const char **why);
 
 }  // namespace vx3g
