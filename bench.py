@@ -3,6 +3,9 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl vx3g|reference]
                     [--workload c2|c1|c3|c5] [--precision mixed|fp64]
 
+The default line also carries the adjoint's backward/forward time ratio on the
+differentiable 12x12x6 robot ("adjoint"; --no-adjoint leaves it out).
+
 A bench "step" is one CUDA-graph chunk of --chunk (default 100) physics time
 steps over the whole batch.  Timed steps are bracketed by CUDA events on the
 library's stream; the L2 cache is flushed (512 MB overwrite) before every timed
@@ -179,6 +182,38 @@ def cpu_baseline_port(robots, threads, budget_s=20.0, max_steps=200):
     return nv / per_step, sample
 
 
+def measure_adjoint(dev, n=2000, k=100, reps=3):
+    """Backward/forward time ratio on the differentiable 12x12x6 robot: FP64 forward
+    of n steps (CUDA-graph chunks) vs vx3g_record (forward with checkpoints) and
+    vx3g_backward (checkpoint recompute + reverse sweep), host wall clock around
+    synchronised calls, best of `reps`."""
+    robot = workloads.c4_differentiable(0)[0]
+    fwd, rec, bwd = [], [], []
+    for _ in range(reps):
+        b = abi.Batch([robot], abi.PRECISION_FP64, device=dev)
+        b.synchronize()
+        t0 = time.perf_counter()
+        b.step(n)
+        b.synchronize()
+        fwd.append(time.perf_counter() - t0)
+        b.close()
+        b = abi.Batch([robot], abi.PRECISION_FP64, device=dev)
+        b.synchronize()
+        t0 = time.perf_counter()
+        b.record(n, k)
+        b.synchronize()
+        rec.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        b.backward(np.array([[-1.0, 0.0, 0.0]]))
+        bwd.append(time.perf_counter() - t0)
+        b.close()
+    f, r, w = min(fwd), min(rec), min(bwd)
+    return {"workload": "12x12x6 differentiable robot (864 voxels, per-voxel phase and log10 E), "
+                        f"{n} FP64 steps, checkpoint every {k}",
+            "fwd_fp64_ms": f * 1e3, "record_ms": r * 1e3, "backward_ms": w * 1e3,
+            "bwd_over_fwd": w / f, "record_plus_bwd_over_fwd": (r + w) / f}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -206,6 +241,11 @@ def main():
     ap.add_argument("--chunk", type=int, default=100)
     ap.add_argument("--ref-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch every step's kernels one by one instead of replaying CUDA graphs "
+                         "(what a per-kernel profiler can attribute; the list rebuild kernels then run "
+                         "every step and return at once unless a rebuild is due)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -216,7 +256,7 @@ def main():
     desc, builder = WORKLOADS[args.workload]
     robots = builder()
     prec = abi.PRECISION_MIXED if args.precision == "mixed" else abi.PRECISION_FP64
-    b = abi.Batch(robots, prec, device=dev, graph_chunk=args.chunk)
+    b = abi.Batch(robots, prec, device=dev, graph_chunk=-1 if args.no_graphs else args.chunk)
     actuated = any(r.temp_vary for r in robots)
     surf = b.surface()
     ns_coll = 0
@@ -262,7 +302,9 @@ def main():
     dom = max(shares, key=shares.get)
     peak, peak_kind = peaks()
     achieved = ab[dom] / (passes[dom] / 1e3) / 1e9 if passes[dom] > 0 else 0.0
-    kernels_per_step = 2 + (5 if ns_coll else 0)
+    # link pass + voxel pass; collision: displacement check, 6 list-rebuild kernels
+    # (they return at once unless a rebuild is due) and the contact evaluation
+    kernels_per_step = 2 + (8 if ns_coll else 0)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -270,7 +312,7 @@ def main():
         "dtype": "f32 link forces + f64 integration" if prec else "f64", "data": "synthetic (seeded generator)",
         "config": {"workload": desc, "robots": len(robots), "voxels": b.nv, "links": b.nl,
                    "collision_surface_voxels": ns_coll, "precision": args.precision,
-                   "physics_steps_per_bench_step": C,
+                   "physics_steps_per_bench_step": C, "cuda_graphs": not args.no_graphs,
                    "l2": "512 MB overwrite before every timed chunk", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
@@ -280,6 +322,8 @@ def main():
         "clocks": clk.summary(),
         "robot_status_nonzero": int(np.count_nonzero(status)),
     }
+    if rank == 0 and args.workload == "c2" and not args.no_adjoint:
+        line["adjoint"] = measure_adjoint(dev)
     if rank == 0 and not args.no_cpu_baseline:
         v, sample = cpu_baseline_port(robots, 1, budget_s=15.0, max_steps=50)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}

@@ -91,7 +91,9 @@ typedef struct vx3g_batch_desc {
     const vx3g_robot_desc *robots;
     int precision;                  /* VX3G_PRECISION_* */
     int device;                     /* CUDA device ordinal */
-    int graph_chunk;                /* steps captured per CUDA graph launch (0 -> 100) */
+    int graph_chunk;                /* steps captured per CUDA graph launch (0 -> 100; < 0: no
+                                       graphs, every step's kernels launched one by one, e.g.
+                                       for a per-kernel profiler) */
 } vx3g_batch_desc;
 
 typedef struct vx3g_ctx vx3g_ctx;

@@ -318,6 +318,7 @@ __device__ __forceinline__ V3<double> pair_force(const Dev &d, int v1, int v2, d
 // 3. exact test and contact forces on the listed pairs, ascending partner order
 __global__ void k_coll_eval(Dev d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) *d.cflag = 0;  // the rebuild (if any) is done; the next check starts clear
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
@@ -360,18 +361,80 @@ __global__ void k_coll_eval(Dev d) {
     d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
 }
 
-void launch_collision(const Dev &d, cudaStream_t s) {
-    if (!d.ns) return;
-    const int g = (d.ns + 255) / 256;
-    cudaMemsetAsync(d.cflag, 0, sizeof(int), s);
-    k_coll_check<<<g, 256, 0, s>>>(d);
+// 1'. the displacement check inside a CUDA graph: the last block to finish sets the
+// conditional node that runs the list rebuild (threadfence-reduction pattern, no wait)
+__global__ void k_coll_check_cond(Dev d, cudaGraphConditionalHandle h) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < d.ns) {
+        const int v = d.csurf[s];
+        const RobotP &rp = d.rp[d.vinfo[v].x];
+        const float4 p = pos_f(d, v), q = d.cref[s];
+        const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
+        const float lim = 0.49f * (float)rp.skin;
+        if (ex * ex + ey * ey + ez * ez > lim * lim) atomicOr(d.cflag, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(d.ccount, 1u);
+        if (prev == gridDim.x - 1) {
+            __threadfence();
+            cudaGraphSetConditional(h, atomicOr(d.cflag, 0) ? 1u : 0u);
+            *d.ccount = 0;
+        }
+    }
+}
+
+static void enqueue_rebuild(const Dev &d, int g, cudaStream_t s) {
     k_coll_clear<<<152 * 4, 256, 0, s>>>(d);
     k_coll_bin<<<g, 256, 0, s>>>(d);
     k_scan_blocks<<<d.hsize / 1024, 1024, 0, s>>>(d);
     k_scan_add<<<d.hsize / 1024, 1024, 0, s>>>(d);
     k_coll_scatter<<<g, 256, 0, s>>>(d);
     k_coll_list<<<g, 256, 0, s>>>(d);
-    k_coll_eval<<<g, 256, 0, s>>>(d);
+}
+
+cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side) {
+    if (!d.ns) return cudaSuccess;
+    const int g = (d.ns + 255) / 256;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(s, &cs);
+    if (e != cudaSuccess) return e;
+    if (cs == cudaStreamCaptureStatusActive && side) {
+        // in a graph: check, then IF(rebuild due) { rebuild }, then the narrow phase
+        cudaGraph_t graph;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t nd = 0;
+        if ((e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, nullptr, nullptr, nullptr)) != cudaSuccess) return e;
+        cudaGraphConditionalHandle h;
+        if ((e = cudaGraphConditionalHandleCreate(&h, graph, 0, 0)) != cudaSuccess) return e;
+        k_coll_check_cond<<<g, 256, 0, s>>>(d, h);
+        if ((e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &nd)) != cudaSuccess) return e;
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeIf;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        if ((e = cudaGraphAddNode(&node, graph, deps, nullptr, nd, &p)) != cudaSuccess) return e;
+        cudaGraph_t body = p.conditional.phGraph_out[0];
+        if ((e = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
+            cudaSuccess)
+            return e;
+        enqueue_rebuild(d, g, side);
+        if ((e = cudaStreamEndCapture(side, &body)) != cudaSuccess) return e;
+        if ((e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+            cudaSuccess)
+            return e;
+    } else {
+        // outside a graph: every rebuild kernel runs and returns at once unless the flag is set
+        cudaMemsetAsync(d.cflag, 0, sizeof(int), s);
+        k_coll_check<<<g, 256, 0, s>>>(d);
+        enqueue_rebuild(d, g, s);
+    }
+    if (d.mixed) launch_coll_eval_mixed(d, s);
+    else k_coll_eval<<<g, 256, 0, s>>>(d);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- centre of mass

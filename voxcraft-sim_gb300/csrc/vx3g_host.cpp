@@ -174,6 +174,7 @@ void from_slot(const double4 &s, bool mixed, double out[4]) {
 struct vx3g_ctx {
     int precision = 0, chunk = 100, device = 0, nr = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;  // helper stream for capturing conditional graph bodies
     Dev d{};
     std::vector<void *> allocs;
     double *scratch = nullptr;  // dt reduction / com output
@@ -234,6 +235,7 @@ struct vx3g_ctx {
         if (adj_mem) cudaFree(adj_mem);
         for (void *p : allocs) cudaFree(p);
         if (flush) cudaFree(flush);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -247,10 +249,12 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     c->precision = desc->precision;
     c->chunk = desc->graph_chunk > 0 ? desc->graph_chunk : 100;
     if (c->chunk & 1) c->chunk++;  // even chunks keep the time-buffer parity aligned
+    if (desc->graph_chunk < 0) c->chunk = INT32_MAX;  // no graphs: single steps only
     c->device = desc->device;
     c->nr = desc->n_robots;
     CU(cudaSetDevice(c->device));
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
 
     std::vector<VMat> vmats;
     std::vector<LMat> lmats;
@@ -443,7 +447,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     while (hs < d.ns) hs <<= 1;
     d.hsize = hs;
     if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.cposf, d.ns)) ||
-        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1)) ||
+        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1)) || (rc = c->alloc(&d.ccount, 1)) ||
         (rc = c->upload(&d.cref, std::vector<float4>((size_t)d.ns, make_float4(1e30f, 1e30f, 1e30f, 0.0f)))) ||
         (rc = c->alloc(&d.hcount, hs)) ||
         (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.hsorted, d.ns)) ||
@@ -457,21 +461,28 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     return VX3G_OK;
 }
 
-void enqueue_step(vx3g_ctx *c, int parity) {
+cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
     const Dev &d = c->d;
     if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(d, c->stream);
     else launch_links_mixed(d, c->stream);
-    launch_collision(d, c->stream);
+    const cudaError_t e = launch_collision(d, c->stream, c->side);
     if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(d, parity, c->stream);
     else launch_voxels_mixed(d, parity, c->stream);
+    return e;
 }
 
 int get_graph(vx3g_ctx *c, int parity, cudaGraphExec_t *out) {
     if (!c->graph[parity]) {
         cudaGraph_t g;
         CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        for (int i = 0; i < c->chunk; i++) enqueue_step(c, (parity + i) & 1);
-        CU(cudaStreamEndCapture(c->stream, &g));
+        cudaError_t ce = cudaSuccess;
+        for (int i = 0; i < c->chunk && ce == cudaSuccess; i++) ce = enqueue_step(c, (parity + i) & 1);
+        cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+        if (ce != cudaSuccess) {
+            if (ee == cudaSuccess) cudaGraphDestroy(g);
+            return fail(VX3G_ERR_CUDA, std::string("step graph capture: ") + cudaGetErrorString(ce));
+        }
+        CU(ee);
         cudaError_t e = cudaGraphInstantiate(&c->graph[parity], g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return fail(VX3G_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
@@ -522,7 +533,7 @@ int vx3g_step(vx3g_ctx *c, int n) {
             n -= c->chunk;
             c->steps += c->chunk;
         } else {
-            enqueue_step(c, parity);
+            CU(enqueue_step(c, parity));
             n -= 1;
             c->steps += 1;
         }
@@ -793,7 +804,7 @@ int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms3) {
                 if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(d, c->stream);
                 else launch_links_mixed(d, c->stream);
             } else if (pass == 1) {
-                launch_collision(d, c->stream);
+                launch_collision(d, c->stream, c->side);
             } else {
                 if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(d, (p0 + i) & 1, c->stream);
                 else launch_voxels_mixed(d, (p0 + i) & 1, c->stream);
@@ -896,7 +907,7 @@ void enqueue_adj_segment(vx3g_ctx *c, const AdjBufs &a0, int len, int p0) {
     const Snap live = live_snap(d);
     for (int i = 0; i < len; i++) {
         launch_snap_copy(c->rec_store[i], live, d.nv, d.nl, d.nr, c->stream);
-        enqueue_step(c, (p0 + i) & 1);
+        (void)enqueue_step(c, (p0 + i) & 1);  // no collision in recorded runs
     }
     AdjBufs a = a0;
     launch_adj_slots(d, c->rec_store[len - 1], a, c->stream);

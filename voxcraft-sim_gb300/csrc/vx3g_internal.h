@@ -100,6 +100,7 @@ struct Dev {
     int *nbr;       // candidate list: kNbrCap surface indices per collision-surface voxel, ascending
     int *nnb;       // candidate count per collision-surface voxel
     int *cflag;     // 1: rebuild the candidate lists this step
+    unsigned *ccount;  // blocks of the displacement check that have finished (graph path)
     int *hcount, *hstart, *hfill, *hsorted, *hblock;
     int hsize;      // power of two
     int *err;       // device error word
@@ -127,7 +128,10 @@ void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s);
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s);
 void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
-void launch_collision(const Dev &d, cudaStream_t s);
+// surface-voxel collision of one step; `side` (optional) is a helper stream used when
+// `s` is being captured into a CUDA graph (the list rebuild becomes a conditional node)
+cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side);
+void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);
 void launch_com(const Dev &d, double *out4, cudaStream_t s);
 void launch_or_status(const Dev &d, int robot, int bits, cudaStream_t s);
 // stable time step of every robot with module-static scratch (vx3g_recommended_dt_noalloc);

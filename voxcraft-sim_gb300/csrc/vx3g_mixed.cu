@@ -57,6 +57,68 @@ __device__ __forceinline__ V3<float> rotvec_f(float w, V3<float> v) {
     return scl(v, 2.0f * atan2f(s, w) / s);
 }
 
+// ------------------------------------------------------------- collision narrow phase
+// handle_collision_attachment + VX3_Collision::updateContactForce
+// (src/VX3/VX3_VoxelyzeKernel.cu:682-727, src/VX3/VX3_Collision.cu:3-31) on the
+// listed pairs, in FP32: the pair offset is taken from the hi/lo pairs (one rounding
+// of an exact difference), the envelope test and the force in FP32, contacts summed
+// in ascending partner order as the FP64 pass does.
+__global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) *d.cflag = 0;  // the rebuild (if any) is done; the next check starts clear
+    if (s >= d.ns) return;
+    const int v = d.csurf[s];
+    const uint2 vi = d.vinfo[v];
+    const int r = (int)vi.x;
+    if (d.status[r] != 0) return;
+    const int n = d.nnb[s];
+    const int *lst = d.nbr + (size_t)s * kNbrCap;
+    const float4 *P = reinterpret_cast<const float4 *>(d.pos);
+    const float4 *LM = reinterpret_cast<const float4 *>(d.linmom);
+    V3<float> acc{0, 0, 0};
+    if (n) {
+        const float4 pvH = P[2 * v], pvL = P[2 * v + 1];
+        const float bv = pvH.w + pvL.w;  // baseSizeAverage = baseSize (isotropic)
+        const VMat &mv = d.vmat[vi.y >> 8];
+        for (int k = 0; k < n; k++) {
+            const int t = lst[k];
+            const int u = d.csurf[t];
+            const float4 puH = P[2 * u], puL = P[2 * u + 1];
+            // offset from the later surface voxel (voxel1) to the earlier one (voxel2)
+            const float sg = t < s ? 1.0f : -1.0f;
+            const float ox = sg * df_diff(puH.x, puL.x, pvH.x, pvL.x);
+            const float oy = sg * df_diff(puH.y, puL.y, pvH.y, pvL.y);
+            const float oz = sg * df_diff(puH.z, puL.z, pvH.z, pvL.z);
+            const float bu = puH.w + puL.w;
+            const float wd = (bv + bu) * 0.625f;
+            const float dist = sqrtf(ox * ox + oy * oy + oz * oz);
+            if (!(dist <= wd)) continue;
+            const float rel = wd - dist;
+            if (!(rel > 0)) continue;
+            const VMat &mu = d.vmat[d.vinfo[u].y >> 8];
+            const float pstiff = 2.0f / (1.0f / mv.pstiff + 1.0f / mu.pstiff);
+            const float dampC = 0.5f * (mv.c_col + mu.c_col);
+            const float inv = 1.0f / dist;
+            const float ux = ox * inv, uy = oy * inv, uz = oz * inv;
+            const float4 lvH = LM[2 * v], luH = LM[2 * u];
+            const float w1x = lvH.x * mv.mass_inv, w1y = lvH.y * mv.mass_inv, w1z = lvH.z * mv.mass_inv;
+            const float w2x = luH.x * mu.mass_inv, w2y = luH.y * mu.mass_inv, w2z = luH.z * mu.mass_inv;
+            // voxel1 = the later one: rv = w1.u - w2.u with (1, 2) = (v, u) when t < s, else (u, v)
+            const float rv = sg * ((w1x * ux + w1y * uy + w1z * uz) - (w2x * ux + w2y * uy + w2z * uz));
+            const float f = pstiff * rel + dampC * rv;
+            // v.contactForce += force (v is voxel1) or -= force (v is voxel2); force along u
+            acc.x += sg * ux * f;
+            acc.y += sg * uy * f;
+            acc.z += sg * uz * f;
+        }
+    }
+    d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
+}
+
+void launch_coll_eval_mixed(const Dev &d, cudaStream_t s) {
+    if (d.ns) k_coll_eval_mixed<<<(d.ns + 255) / 256, 256, 0, s>>>(d);
+}
+
 // ------------------------------------------------------------- link pass
 __global__ void __launch_bounds__(256) k_links_mixed(Dev d) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
