@@ -182,6 +182,30 @@ def cpu_baseline_port(robots, threads, budget_s=20.0, max_steps=200):
     return nv / per_step, sample
 
 
+def ncu_traffic(workload, precision, kernel):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu summary
+    of this workload (profiles/ncu_traffic.json), or None."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        return json.load(open(p))[f"{workload}/{precision}"][kernel]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def pinned_copy(arrays):
+    """Copies of the arrays in page-locked host memory (torch's pinned allocator)."""
+    try:
+        import torch
+        out = {}
+        for k, a in arrays.items():
+            t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+            t[...] = a
+            out[k] = t
+        return out
+    except (ImportError, RuntimeError):
+        return arrays
+
+
 def measure_adjoint(dev, n=2000, k=100, reps=3):
     """Backward/forward time ratio on the differentiable 12x12x6 robot: FP64 forward
     of n steps (CUDA-graph chunks) vs vx3g_record (forward with checkpoints) and
@@ -242,6 +266,7 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--tune-cache", default=None, help="JSON cache of tuned launch shapes (read and appended)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every step's kernels one by one instead of replaying CUDA graphs "
                          "(what a per-kernel profiler can attribute; the list rebuild kernels then run "
@@ -264,8 +289,10 @@ def main():
         if r.enable_collision:
             ns_coll += int(np.count_nonzero((surf >= b.voxel_offset[i]) & (surf < b.voxel_offset[i + 1])))
     W, K, C = args.warmup, args.steps, args.chunk
-    for _ in range(W):
-        b.step(C)
+    # warm-up: W-1 chunks of real steps while the launch shapes are tuned, then one
+    # chunk through the (re)built step graph
+    b.autotune(max(16, (W - 1) * C), args.tune_cache)
+    b.step(C)
     b.synchronize()
     if dist:
         dist.barrier()
@@ -282,8 +309,9 @@ def main():
     vox_steps = b.nv * C * K * world
     value = vox_steps / (total_ms / 1e3)
 
-    # e2e through the C ABI with host buffers: upload state, run a chunk, read COM back
-    st = b.state()
+    # e2e through the C ABI with host buffers: upload state from pinned host memory,
+    # run a chunk, read COM back
+    st = pinned_copy(b.state())
     h2d = sum(a.nbytes for a in st.values())
     t0 = time.perf_counter()
     E = max(3, K // 5)
@@ -295,13 +323,21 @@ def main():
     d2h = com.nbytes
     e2e_value = b.nv * C * E * world / e2e_s
 
-    # per-pass device times (after the measured run)
+    # per-pass device times (after the measured run); the dominant kernel is the
+    # single kernel with the largest time: the link pass, the voxel pass or the
+    # contact evaluation (the collision pass's other kernels are the small check and
+    # the rebuild, which runs only in some steps)
     passes = b.time_passes(20)
     ab = algorithmic_bytes(b.nv, b.nl, ns_coll, actuated)
-    shares = {k: passes[k] for k in passes}
-    dom = max(shares, key=shares.get)
+    kernel_ms = {"k_links_mixed" if prec else "k_links": passes["links"],
+                 "k_voxels_mixed" if prec else "k_voxels": passes["voxels"]}
+    if ns_coll:
+        kernel_ms["k_coll_eval_mixed" if prec else "k_coll_eval"] = passes["contact_eval"]
+    kernel_bytes = dict(zip(kernel_ms, [ab["links"], ab["voxels"], ab["collision"]]))
+    dom = max(kernel_ms, key=kernel_ms.get)
     peak, peak_kind = peaks()
-    achieved = ab[dom] / (passes[dom] / 1e3) / 1e9 if passes[dom] > 0 else 0.0
+    achieved = kernel_bytes[dom] / (kernel_ms[dom] / 1e3) / 1e9 if kernel_ms[dom] > 0 else 0.0
+    traffic = ncu_traffic(args.workload, args.precision, dom)
     # link pass + voxel pass; collision: displacement check, 6 list-rebuild kernels
     # (they return at once unless a rebuild is due) and the contact evaluation
     kernels_per_step = 2 + (8 if ns_coll else 0)
@@ -313,10 +349,14 @@ def main():
         "config": {"workload": desc, "robots": len(robots), "voxels": b.nv, "links": b.nl,
                    "collision_surface_voxels": ns_coll, "precision": args.precision,
                    "physics_steps_per_bench_step": C, "cuda_graphs": not args.no_graphs,
+                   "launch_shapes": {"links": [int(x) for x in b.launch_shapes()[:2]],
+                                     "voxels": [int(x) for x in b.launch_shapes()[2:]]},
                    "l2": "512 MB overwrite before every timed chunk", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-                     "pass_ms": passes, "algorithmic_bytes_per_launch": ab},
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "kernel_ms": kernel_ms, "pass_ms": passes, "algorithmic_bytes_per_launch": ab,
+                     "whole_step_algorithmic_gbs": (ab["links"] + ab["voxels"] + ab["collision"]) * C * K * world
+                     / (total_ms / 1e3) / 1e9},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": kernels_per_step * C * K,
         "clocks": clk.summary(),

@@ -184,6 +184,18 @@ int vx3g_backward(vx3g_ctx *ctx, const double *dL_dcom, double *dL_dphase, doubl
  *   (wrong results): serialise them.  Blocking: returns when rdt is filled. */
 int vx3g_recommended_dt_noalloc(vx3g_ctx *ctx, double *rdt);
 
+/* ---- launch-shape autotuning (no counterpart in the reference) ---------------
+ * vx3g_autotune: advances n_steps exactly like vx3g_step (results identical),
+ *   timing the link and voxel passes of a mixed-precision context under each of
+ *   their compiled launch shapes (threads per block x minimum resident blocks),
+ *   and keeps the fastest.  With cache_json (a path, or NULL) the choice is read
+ *   from / appended to a flat JSON object keyed by GPU name and batch size; a
+ *   cached choice is applied without timing.  FP64 contexts just step.
+ * vx3g_launch_shapes: the shapes in use: {link threads, link min blocks, voxel
+ *   threads, voxel min blocks}. */
+int vx3g_autotune(vx3g_ctx *ctx, int n_steps, const char *cache_json);
+int vx3g_launch_shapes(vx3g_ctx *ctx, int32_t *shapes4);
+
 /* ---- measurement helpers (no counterpart in the reference) ---------------
  * vx3g_time_steps: runs vx3g_step(ctx, n_steps) between two CUDA events on the
  *   context's stream and returns the device time in milliseconds.
@@ -191,12 +203,13 @@ int vx3g_recommended_dt_noalloc(vx3g_ctx *ctx, double *rdt);
  *   context's stream (evicts the L2 cache between timed iterations).
  * vx3g_time_passes: runs each per-step pass `iters` times on its own, captured
  *   in one CUDA graph as the step graphs run it, between CUDA events, and
- *   returns the mean device time per pass in milliseconds for: [0] link pass, [1] collision passes (all kernels of the
- *   broad and narrow phase together), [2] voxel pass.  It advances the state
- *   like extra steps would; use it after the measured run. */
+ *   returns the mean device time per pass in milliseconds (ms4[4]) for: [0] link pass, [1] collision passes (all kernels of the
+ *   broad and narrow phase together), [2] voxel pass, [3] the contact evaluation
+ *   kernel alone.  It advances the state like extra steps would; use it after
+ *   the measured run. */
 int vx3g_time_steps(vx3g_ctx *ctx, int n_steps, float *ms);
 int vx3g_flush_l2(vx3g_ctx *ctx, size_t bytes);
-int vx3g_time_passes(vx3g_ctx *ctx, int iters, float *ms3);
+int vx3g_time_passes(vx3g_ctx *ctx, int iters, float *ms4);
 
 #ifdef __cplusplus
 }

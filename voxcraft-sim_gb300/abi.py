@@ -25,7 +25,7 @@ EXPORTS = [
     "vx3g_counts", "vx3g_offsets", "vx3g_get_state", "vx3g_set_state", "vx3g_get_voxel_aux", "vx3g_get_links",
     "vx3g_get_topology", "vx3g_get_surface", "vx3g_com", "vx3g_dt", "vx3g_time", "vx3g_status",
     "vx3g_steps_taken", "vx3g_time_steps", "vx3g_flush_l2", "vx3g_time_passes", "vx3g_stop_robot",
-    "vx3g_record", "vx3g_backward", "vx3g_recommended_dt_noalloc",
+    "vx3g_record", "vx3g_backward", "vx3g_recommended_dt_noalloc", "vx3g_autotune", "vx3g_launch_shapes",
 ]
 
 
@@ -94,6 +94,8 @@ def load(path: str = LIB_PATH):
     lib.vx3g_stop_robot.argtypes = [vp, ip]
     lib.vx3g_record.argtypes = [vp, ip, ip]
     lib.vx3g_recommended_dt_noalloc.argtypes = [vp, dp]
+    lib.vx3g_autotune.argtypes = [vp, ip, ctypes.c_char_p]
+    lib.vx3g_launch_shapes.argtypes = [vp, vp]
     lib.vx3g_backward.argtypes = [vp, dp, dp, dp]
     _lib = lib
     return lib
@@ -250,9 +252,9 @@ class Batch:
         _check(self.lib.vx3g_flush_l2(self.h, int(nbytes)), "vx3g_flush_l2")
 
     def time_passes(self, iters: int = 50):
-        ms = np.zeros(3, np.float32)
+        ms = np.zeros(4, np.float32)
         _check(self.lib.vx3g_time_passes(self.h, int(iters), _P(ms)), "vx3g_time_passes")
-        return dict(links=float(ms[0]), collision=float(ms[1]), voxels=float(ms[2]))
+        return dict(links=float(ms[0]), collision=float(ms[1]), voxels=float(ms[2]), contact_eval=float(ms[3]))
 
     def record(self, n: int, checkpoint_every: int = 100):
         _check(self.lib.vx3g_record(self.h, int(n), int(checkpoint_every)), "vx3g_record")
@@ -263,6 +265,15 @@ class Batch:
         ge = np.zeros(self.nv)
         _check(self.lib.vx3g_backward(self.h, _P(w), _P(gp), _P(ge)), "vx3g_backward")
         return gp, ge
+
+    def autotune(self, n_steps: int, cache_json=None):
+        c = None if cache_json is None else str(cache_json).encode()
+        _check(self.lib.vx3g_autotune(self.h, int(n_steps), c), "vx3g_autotune")
+
+    def launch_shapes(self):
+        out = np.zeros(4, np.int32)
+        _check(self.lib.vx3g_launch_shapes(self.h, _P(out)), "vx3g_launch_shapes")
+        return out
 
     def recommended_dt_noalloc(self):
         out = np.zeros(self.n_robots)

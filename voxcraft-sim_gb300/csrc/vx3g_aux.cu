@@ -174,11 +174,9 @@ __global__ void k_coll_check(Dev d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.ns) return;
     const int v = d.csurf[s];
-    const RobotP &rp = d.rp[d.vinfo[v].x];
-    const float4 p = pos_f(d, v), q = d.cref[s];
+    const float4 p = pos_f(d, v), q = d.cref[s];  // q.w: squared displacement limit
     const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
-    const float lim = 0.49f * (float)rp.skin;
-    if (ex * ex + ey * ey + ez * ez > lim * lim) atomicOr(d.cflag, 1);
+    if (ex * ex + ey * ey + ez * ez > q.w) atomicOr(d.cflag, 1);
 }
 
 __global__ void k_coll_clear(Dev d) {
@@ -283,17 +281,20 @@ __global__ void k_coll_list(Dev d) {
                         overflow = true;
                         continue;
                     }
+                    // the list holds voxel indices in ascending order: csurf is ascending, so
+                    // this is the ascending surface-index order of the reference's pair loop
                     int j = nc++;
-                    while (j > 0 && out[j - 1] > t) {
+                    while (j > 0 && out[j - 1] > u) {
                         out[j] = out[j - 1];
                         j--;
                     }
-                    out[j] = t;
+                    out[j] = u;
                 }
             }
     if (overflow) atomicOr(&d.status[r], 2);
     d.nnb[s] = nc;
-    d.cref[s] = pf;
+    const float lim = 0.49f * (float)rp.skin;  // rebuild when a voxel has moved farther than this
+    d.cref[s] = make_float4(pf.x, pf.y, pf.z, lim * lim);
 }
 
 // force on voxel1 from the pair (voxel1, voxel2) as VX3_Collision computes it
@@ -332,8 +333,7 @@ __global__ void k_coll_eval(Dev d) {
         double bsa = 0;
         bool have_bsa = false;
         for (int k = 0; k < n; k++) {
-            const int t = lst[k];
-            const int u = d.csurf[t];
+            const int u = lst[k];  // partner voxel, ascending
             // FP32 prefilter against the current cutoff: only pairs within 0.1% of it reach FP64
             const float4 tf = pos_f(d, u);
             const float ex = tf.x - pf.x, ey = tf.y - pf.y, ez = tf.z - pf.z;
@@ -346,15 +346,15 @@ __global__ void k_coll_eval(Dev d) {
             const double4 pu = load_state(d, d.pos, u);
             const double bu = (pu.w + pu.w + pu.w) / 3.0f;
             // exact envelope test, voxel1 = the later surface voxel
-            const double4 &pa = t < s ? pv : pu, &pb = t < s ? pu : pv;
-            const double ba = t < s ? bsa : bu, bb = t < s ? bu : bsa;
+            const double4 &pa = u < v ? pv : pu, &pb = u < v ? pu : pv;
+            const double ba = u < v ? bsa : bu, bb = u < v ? bu : bsa;
             const V3<double> diff{pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
             const double wd = (ba + bb) * 0.625;
             if (diff.x > wd || diff.x < -wd) continue;
             if (diff.y > wd || diff.y < -wd) continue;
             if (diff.z > wd || diff.z < -wd) continue;
             if (len(diff) > wd) continue;
-            if (t < s) acc = add(acc, pair_force(d, v, u, bsa, bu));    // v.contactForce += force
+            if (u < v) acc = add(acc, pair_force(d, v, u, bsa, bu));    // v.contactForce += force
             else acc = add(acc, neg(pair_force(d, u, v, bu, bsa)));      // v.contactForce += -force
         }
     }
@@ -367,11 +367,9 @@ __global__ void k_coll_check_cond(Dev d, cudaGraphConditionalHandle h) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < d.ns) {
         const int v = d.csurf[s];
-        const RobotP &rp = d.rp[d.vinfo[v].x];
-        const float4 p = pos_f(d, v), q = d.cref[s];
+        const float4 p = pos_f(d, v), q = d.cref[s];  // q.w: squared displacement limit
         const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
-        const float lim = 0.49f * (float)rp.skin;
-        if (ex * ex + ey * ey + ez * ez > lim * lim) atomicOr(d.cflag, 1);
+        if (ex * ex + ey * ey + ez * ez > q.w) atomicOr(d.cflag, 1);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -432,9 +430,55 @@ cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side) {
         k_coll_check<<<g, 256, 0, s>>>(d);
         enqueue_rebuild(d, g, s);
     }
-    if (d.mixed) launch_coll_eval_mixed(d, s);
-    else k_coll_eval<<<g, 256, 0, s>>>(d);
+    launch_coll_eval(d, s);
     return cudaGetLastError();
+}
+
+void launch_coll_eval(const Dev &d, cudaStream_t s) {
+    if (!d.ns) return;
+    if (d.mixed) launch_coll_eval_mixed(d, s);
+    else k_coll_eval<<<(d.ns + 255) / 256, 256, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------- host state exchange
+// vx3g_set_state / vx3g_get_state convert between plain doubles (comps per voxel)
+// and the 32-byte state slots on the device: double4, or float4 hi + float4 lo
+// (mixed).  keep_w keeps the slot's 4th component (the base size of pos).
+__device__ __forceinline__ void put_slot(double4 *dst, size_t i, int mixed, double a, double b, double c, double w) {
+    if (!mixed) {
+        dst[i] = make_double4(a, b, c, w);
+        return;
+    }
+    float4 *f = reinterpret_cast<float4 *>(dst) + 2 * i;
+    const float ha = (float)a, hb = (float)b, hc = (float)c, hw = (float)w;
+    f[0] = make_float4(ha, hb, hc, hw);
+    f[1] = make_float4((float)(a - (double)ha), (float)(b - (double)hb), (float)(c - (double)hc), (float)(w - (double)hw));
+}
+
+__global__ void k_pack_state(Dev d, double4 *dst, const double *src, int comps, int keep_w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nv) return;
+    const double *x = src + (size_t)comps * i;
+    const double w = comps == 4 ? x[3] : (keep_w ? load_state(d, dst, i).w : 0.0);
+    put_slot(dst, i, d.mixed, x[0], x[1], x[2], w);
+}
+
+__global__ void k_unpack_state(Dev d, double *dst, const double4 *src, int comps) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nv) return;
+    const double4 v = load_state(d, src, i);
+    double *x = dst + (size_t)comps * i;
+    x[0] = v.x;
+    x[1] = v.y;
+    x[2] = v.z;
+    if (comps == 4) x[3] = v.w;
+}
+
+void launch_pack_state(const Dev &d, double4 *dst, const double *staged, int comps, int keep_w, cudaStream_t s) {
+    if (d.nv) k_pack_state<<<(d.nv + 255) / 256, 256, 0, s>>>(d, dst, staged, comps, keep_w);
+}
+void launch_unpack_state(const Dev &d, double *staged, const double4 *src, int comps, cudaStream_t s) {
+    if (d.nv) k_unpack_state<<<(d.nv + 255) / 256, 256, 0, s>>>(d, staged, src, comps);
 }
 
 // ---------------------------------------------------------------- centre of mass

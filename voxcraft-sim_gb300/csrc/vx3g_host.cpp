@@ -186,6 +186,7 @@ struct vx3g_ctx {
     std::vector<int> vmat_local, surface;
     std::vector<unsigned char> vfixed;
     int64_t steps = 0;
+    int shape_links = 0, shape_voxels = 0;  // launch shapes of the mixed passes (vx3g_autotune)
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -201,6 +202,7 @@ struct vx3g_ctx {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     void *flush = nullptr;
     size_t flush_bytes = 0;
+    double *stage = nullptr;  // 4 doubles per voxel: host state exchange
 
     template <class T> int alloc(T **p, size_t n) {
         void *q = nullptr;
@@ -235,6 +237,7 @@ struct vx3g_ctx {
         if (adj_mem) cudaFree(adj_mem);
         for (void *p : allocs) cudaFree(p);
         if (flush) cudaFree(flush);
+        if (stage) cudaFree(stage);
         if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -461,13 +464,19 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     return VX3G_OK;
 }
 
+void enqueue_links(vx3g_ctx *c) {
+    if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(c->d, c->stream);
+    else launch_links_mixed(c->d, c->stream, c->shape_links);
+}
+void enqueue_voxels(vx3g_ctx *c, int parity) {
+    if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(c->d, parity, c->stream);
+    else launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels);
+}
+
 cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
-    const Dev &d = c->d;
-    if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(d, c->stream);
-    else launch_links_mixed(d, c->stream);
-    const cudaError_t e = launch_collision(d, c->stream, c->side);
-    if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(d, parity, c->stream);
-    else launch_voxels_mixed(d, parity, c->stream);
+    enqueue_links(c);
+    const cudaError_t e = launch_collision(c->d, c->stream, c->side);
+    enqueue_voxels(c, parity);
     return e;
 }
 
@@ -568,60 +577,51 @@ int vx3g_offsets(vx3g_ctx *c, int *vo, int *lo) {
     return VX3G_OK;
 }
 
+static int ensure_stage(vx3g_ctx *c) {
+    if (c->stage) return VX3G_OK;
+    cudaError_t e = cudaMalloc(&c->stage, 4 * sizeof(double) * (size_t)(c->d.nv ? c->d.nv : 1));
+    if (e != cudaSuccess) {
+        c->stage = nullptr;
+        return fail(VX3G_ERR_NOMEM, std::string("cudaMalloc (state staging): ") + cudaGetErrorString(e));
+    }
+    return VX3G_OK;
+}
+
 int vx3g_get_state(vx3g_ctx *c, double *pos, double *orient, double *linmom, double *angmom) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    CU(cudaSetDevice(c->device));
+    int rc = ensure_stage(c);
+    if (rc) return rc;
     const size_t n = c->d.nv;
-    std::vector<double4> a, b, l, m;
-    int rc;
-    if (pos && (rc = download(c, a, c->d.pos, n))) return rc;
-    if (orient && (rc = download(c, b, c->d.quat, n))) return rc;
-    if (linmom && (rc = download(c, l, c->d.linmom, n))) return rc;
-    if (angmom && (rc = download(c, m, c->d.angmom, n))) return rc;
-    CU(cudaStreamSynchronize(c->stream));
-    const bool mx = c->d.mixed != 0;
-    double t4[4];
-    for (size_t i = 0; i < n; i++) {
-        if (pos) { from_slot(a[i], mx, t4); pos[3 * i] = t4[0]; pos[3 * i + 1] = t4[1]; pos[3 * i + 2] = t4[2]; }
-        if (orient) { from_slot(b[i], mx, t4); for (int k = 0; k < 4; k++) orient[4 * i + k] = t4[k]; }
-        if (linmom) { from_slot(l[i], mx, t4); linmom[3 * i] = t4[0]; linmom[3 * i + 1] = t4[1]; linmom[3 * i + 2] = t4[2]; }
-        if (angmom) { from_slot(m[i], mx, t4); angmom[3 * i] = t4[0]; angmom[3 * i + 1] = t4[1]; angmom[3 * i + 2] = t4[2]; }
+    double *out[4] = {pos, orient, linmom, angmom};
+    const double4 *src[4] = {c->d.pos, c->d.quat, c->d.linmom, c->d.angmom};
+    for (int k = 0; k < 4; k++) {
+        if (!out[k]) continue;
+        const int comps = k == 1 ? 4 : 3;
+        launch_unpack_state(c->d, c->stage, src[k], comps, c->stream);
+        CU(cudaMemcpyAsync(out[k], c->stage, comps * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     }
+    CU(cudaStreamSynchronize(c->stream));
+    CU(cudaGetLastError());
     return VX3G_OK;
 }
 
 int vx3g_set_state(vx3g_ctx *c, const double *pos, const double *orient, const double *linmom, const double *angmom) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    CU(cudaSetDevice(c->device));
+    int rc = ensure_stage(c);
+    if (rc) return rc;
     const size_t n = c->d.nv;
-    const bool mx = c->d.mixed != 0;
-    std::vector<double4> a;
-    int rc;
-    double t4[4];
-    if (pos) {  // keep the base size in .w
-        if ((rc = download(c, a, c->d.pos, n))) return rc;
-        CU(cudaStreamSynchronize(c->stream));
-        for (size_t i = 0; i < n; i++) {
-            from_slot(a[i], mx, t4);
-            a[i] = to_slot(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], t4[3], mx);
-        }
-        CU(cudaMemcpyAsync(c->d.pos, a.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
-        CU(cudaStreamSynchronize(c->stream));
-    }
-    std::vector<double4> b(n);
-    if (orient) {
-        for (size_t i = 0; i < n; i++) b[i] = to_slot(orient[4 * i], orient[4 * i + 1], orient[4 * i + 2], orient[4 * i + 3], mx);
-        CU(cudaMemcpyAsync(c->d.quat, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
-        CU(cudaStreamSynchronize(c->stream));
-    }
-    if (linmom) {
-        for (size_t i = 0; i < n; i++) b[i] = to_slot(linmom[3 * i], linmom[3 * i + 1], linmom[3 * i + 2], 0, mx);
-        CU(cudaMemcpyAsync(c->d.linmom, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
-        CU(cudaStreamSynchronize(c->stream));
-    }
-    if (angmom) {
-        for (size_t i = 0; i < n; i++) b[i] = to_slot(angmom[3 * i], angmom[3 * i + 1], angmom[3 * i + 2], 0, mx);
-        CU(cudaMemcpyAsync(c->d.angmom, b.data(), n * sizeof(double4), cudaMemcpyHostToDevice, c->stream));
+    const double *in[4] = {pos, orient, linmom, angmom};
+    double4 *dst[4] = {c->d.pos, c->d.quat, c->d.linmom, c->d.angmom};
+    for (int k = 0; k < 4; k++) {
+        if (!in[k]) continue;
+        const int comps = k == 1 ? 4 : 3;
+        CU(cudaMemcpyAsync(c->stage, in[k], comps * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        launch_pack_state(c->d, dst[k], c->stage, comps, k == 0, c->stream);  // pos keeps its base size
     }
     CU(cudaStreamSynchronize(c->stream));
+    CU(cudaGetLastError());
     return VX3G_OK;
 }
 
@@ -787,28 +787,23 @@ int vx3g_flush_l2(vx3g_ctx *c, size_t bytes) {
     return VX3G_OK;
 }
 
-int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms3) {
-    if (!c || !ms3 || iters <= 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_time_passes");
+int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms4) {
+    if (!c || !ms4 || iters <= 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_time_passes");
     CU(cudaSetDevice(c->device));
     cudaEvent_t a, b;
     CU(cudaEventCreate(&a));
     CU(cudaEventCreate(&b));
     const Dev &d = c->d;
-    for (int pass = 0; pass < 3; pass++) {
+    for (int pass = 0; pass < 4; pass++) {
         // each pass repeated `iters` times inside one CUDA graph, as the step graphs run it
         const int p0 = (int)(c->steps & 1);
         cudaGraph_t g;
         CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < iters; i++) {
-            if (pass == 0) {
-                if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(d, c->stream);
-                else launch_links_mixed(d, c->stream);
-            } else if (pass == 1) {
-                launch_collision(d, c->stream, c->side);
-            } else {
-                if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(d, (p0 + i) & 1, c->stream);
-                else launch_voxels_mixed(d, (p0 + i) & 1, c->stream);
-            }
+            if (pass == 0) enqueue_links(c);
+            else if (pass == 1) launch_collision(d, c->stream, c->side);
+            else if (pass == 2) enqueue_voxels(c, (p0 + i) & 1);
+            else launch_coll_eval(d, c->stream);
         }
         CU(cudaStreamEndCapture(c->stream, &g));
         cudaGraphExec_t ex = nullptr;
@@ -823,11 +818,106 @@ int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms3) {
         if (pass == 2) c->steps += iters;
         float ms = 0;
         CU(cudaEventElapsedTime(&ms, a, b));
-        ms3[pass] = ms / iters;
+        ms4[pass] = ms / iters;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     CU(cudaGetLastError());
+    return VX3G_OK;
+}
+
+int vx3g_autotune(vx3g_ctx *c, int n_steps, const char *cache_json) {
+    if (!c || n_steps < 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_autotune");
+    if (c->precision != VX3G_PRECISION_MIXED) return vx3g_step(c, n_steps);  // one shape per FP64 pass
+    CU(cudaSetDevice(c->device));
+    cudaDeviceProp prop;
+    CU(cudaGetDeviceProperties(&prop, c->device));
+    const std::string key = std::string(prop.name) + "|mixed|" + std::to_string(c->d.nv) + "|" +
+                            std::to_string(c->d.nl) + "|" + std::to_string(c->d.ns);
+    std::string cache;
+    if (cache_json) {
+        if (FILE *f = fopen(cache_json, "rb")) {
+            char buf[4096];
+            size_t k;
+            while ((k = fread(buf, 1, sizeof buf, f)) > 0) cache.append(buf, k);
+            fclose(f);
+        }
+        const size_t at = cache.find("\"" + key + "\": [");
+        int a = -1, b = -1;
+        if (at != std::string::npos &&
+            sscanf(cache.c_str() + at + key.size() + 5, "%d, %d", &a, &b) == 2 && a >= 0 && a < kMixedShapes &&
+            b >= 0 && b < kMixedShapes) {
+            if (a != c->shape_links || b != c->shape_voxels) {
+                for (auto &g : c->graph)
+                    if (g) cudaGraphExecDestroy(g), g = nullptr;
+            }
+            c->shape_links = a;
+            c->shape_voxels = b;
+            return vx3g_step(c, n_steps);
+        }
+    }
+    // time the passes of real steps, cycling through the shapes (results do not depend on them)
+    const int warm = 2 * kMixedShapes;
+    if (n_steps < warm + 2 * kMixedShapes) return vx3g_step(c, n_steps);
+    std::vector<cudaEvent_t> ev(4 * (size_t)n_steps);
+    for (auto &e : ev) CU(cudaEventCreate(&e));
+    for (int i = 0; i < n_steps; i++) {
+        const int parity = (int)(c->steps & 1);
+        c->shape_links = c->shape_voxels = i % kMixedShapes;
+        CU(cudaEventRecord(ev[4 * i], c->stream));
+        enqueue_links(c);
+        CU(cudaEventRecord(ev[4 * i + 1], c->stream));
+        CU(launch_collision(c->d, c->stream, nullptr));
+        CU(cudaEventRecord(ev[4 * i + 2], c->stream));
+        enqueue_voxels(c, parity);
+        CU(cudaEventRecord(ev[4 * i + 3], c->stream));
+        c->steps++;
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    double tl[kMixedShapes] = {}, tv[kMixedShapes] = {};
+    for (int i = warm; i < n_steps; i++) {
+        float a = 0, b = 0;
+        CU(cudaEventElapsedTime(&a, ev[4 * i], ev[4 * i + 1]));
+        CU(cudaEventElapsedTime(&b, ev[4 * i + 2], ev[4 * i + 3]));
+        tl[i % kMixedShapes] += a;
+        tv[i % kMixedShapes] += b;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    int bl = 0, bv = 0;
+    for (int k = 1; k < kMixedShapes; k++) {
+        if (tl[k] < tl[bl]) bl = k;
+        if (tv[k] < tv[bv]) bv = k;
+    }
+    c->shape_links = bl;
+    c->shape_voxels = bv;
+    for (auto &g : c->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
+    if (cache_json) {  // flat JSON object {"<gpu>|mixed|nv|nl|ns": [link shape, voxel shape], ...}
+        std::string body = cache;
+        const size_t close = body.rfind('}');
+        const std::string entry = "\"" + key + "\": [" + std::to_string(bl) + ", " + std::to_string(bv) + "]";
+        if (close == std::string::npos || body.find('"') == std::string::npos) {
+            body = "{\n  " + entry + "\n}\n";
+        } else {
+            body = body.substr(0, close);
+            while (!body.empty() && (body.back() == '\n' || body.back() == ' ')) body.pop_back();
+            body += ",\n  " + entry + "\n}\n";
+        }
+        if (FILE *f = fopen(cache_json, "wb")) {
+            fwrite(body.data(), 1, body.size(), f);
+            fclose(f);
+        }
+    }
+    return VX3G_OK;
+}
+
+int vx3g_launch_shapes(vx3g_ctx *c, int32_t *shapes4) {
+    if (!c || !shapes4) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_launch_shapes");
+    const bool mx = c->precision == VX3G_PRECISION_MIXED;
+    shapes4[0] = mx ? kLinkShapes[c->shape_links].threads : 256;
+    shapes4[1] = mx ? kLinkShapes[c->shape_links].min_blocks : 1;
+    shapes4[2] = mx ? kVoxelShapes[c->shape_voxels].threads : 256;
+    shapes4[3] = mx ? kVoxelShapes[c->shape_voxels].min_blocks : 1;
     return VX3G_OK;
 }
 

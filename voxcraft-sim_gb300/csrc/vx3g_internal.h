@@ -96,8 +96,8 @@ struct Dev {
     int *csurf;     // collision surface list (global voxel index), NS entries
     int4 *ccell;    // cell coords + robot per collision-surface voxel
     float4 *cposf;  // FP32 copy of the position (prefilter) per collision-surface voxel
-    float4 *cref;   // position at the last list build, per collision-surface voxel
-    int *nbr;       // candidate list: kNbrCap surface indices per collision-surface voxel, ascending
+    float4 *cref;   // position at the last list build (w: squared displacement that forces a rebuild)
+    int *nbr;       // candidate list: kNbrCap partner voxel indices per collision-surface voxel, ascending
     int *nnb;       // candidate count per collision-surface voxel
     int *cflag;     // 1: rebuild the candidate lists this step
     unsigned *ccount;  // blocks of the displacement check that have finished (graph path)
@@ -123,8 +123,12 @@ __device__ __forceinline__ double4 load_state(const Dev &d, const double4 *a, in
 // launchers (defined in the .cu files)
 void launch_links_fp64(const Dev &d, cudaStream_t s);
 void launch_voxels_fp64(const Dev &d, int parity, cudaStream_t s);
-void launch_links_mixed(const Dev &d, cudaStream_t s);
-void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s);
+// launch shapes of the mixed-precision passes (vx3g_mixed.cu), chosen by vx3g_autotune
+struct LaunchShape { int threads, min_blocks; };
+constexpr int kMixedShapes = 4;
+extern const LaunchShape kLinkShapes[kMixedShapes], kVoxelShapes[kMixedShapes];
+void launch_links_mixed(const Dev &d, cudaStream_t s, int shape = 0);
+void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape = 0);
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s);
 void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
@@ -132,7 +136,11 @@ void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 // `s` is being captured into a CUDA graph (the list rebuild becomes a conditional node)
 cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);
+void launch_coll_eval(const Dev &d, cudaStream_t s);  // the contact evaluation alone
 void launch_com(const Dev &d, double *out4, cudaStream_t s);
+// state exchange with plain doubles (comps = 3 or 4 per voxel) staged in device memory
+void launch_pack_state(const Dev &d, double4 *dst, const double *staged, int comps, int keep_w, cudaStream_t s);
+void launch_unpack_state(const Dev &d, double *staged, const double4 *src, int comps, cudaStream_t s);
 void launch_or_status(const Dev &d, int robot, int bits, cudaStream_t s);
 // stable time step of every robot with module-static scratch (vx3g_recommended_dt_noalloc);
 // returns 0, -1 (invalid) or -3 (CUDA error, message in *why)

@@ -81,11 +81,10 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
         const float bv = pvH.w + pvL.w;  // baseSizeAverage = baseSize (isotropic)
         const VMat &mv = d.vmat[vi.y >> 8];
         for (int k = 0; k < n; k++) {
-            const int t = lst[k];
-            const int u = d.csurf[t];
+            const int u = lst[k];  // partner voxel, ascending
             const float4 puH = P[2 * u], puL = P[2 * u + 1];
             // offset from the later surface voxel (voxel1) to the earlier one (voxel2)
-            const float sg = t < s ? 1.0f : -1.0f;
+            const float sg = u < v ? 1.0f : -1.0f;
             const float ox = sg * df_diff(puH.x, puL.x, pvH.x, pvL.x);
             const float oy = sg * df_diff(puH.y, puL.y, pvH.y, pvL.y);
             const float oz = sg * df_diff(puH.z, puL.z, pvH.z, pvL.z);
@@ -103,7 +102,7 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
             const float4 lvH = LM[2 * v], luH = LM[2 * u];
             const float w1x = lvH.x * mv.mass_inv, w1y = lvH.y * mv.mass_inv, w1z = lvH.z * mv.mass_inv;
             const float w2x = luH.x * mu.mass_inv, w2y = luH.y * mu.mass_inv, w2z = luH.z * mu.mass_inv;
-            // voxel1 = the later one: rv = w1.u - w2.u with (1, 2) = (v, u) when t < s, else (u, v)
+            // voxel1 = the later one: rv = w1.u - w2.u with (1, 2) = (v, u) when u < v, else (u, v)
             const float rv = sg * ((w1x * ux + w1y * uy + w1z * uz) - (w2x * ux + w2y * uy + w2z * uz));
             const float f = pstiff * rel + dampC * rv;
             // v.contactForce += force (v is voxel1) or -= force (v is voxel2); force along u
@@ -120,26 +119,32 @@ void launch_coll_eval_mixed(const Dev &d, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------- link pass
-__global__ void __launch_bounds__(256) k_links_mixed(Dev d) {
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= d.nl) return;
+__device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
+    // every load that depends only on l is issued before the first branch, then the
+    // endpoint state: two dependent load levels instead of four (latency-bound kernel)
     const uint2 li = d.linfo[l];
+    const int2 e = d.ends[l];
+    float *ls = (float *)d.lstate;
+    const size_t NL = (size_t)d.nl;
+    const V3<float> oldPos2{ls[l], ls[NL + l], ls[2 * NL + l]};
+    // angle1v is zero while a link is in the small-angle branch (the flag it entered
+    // this step with says so); it is read and written only for large-angle links and
+    // zeroed once when a link returns to the small branch
+    const bool wasSmall = (li.y & LF_SMALL) != 0;
+    V3<float> oldA1{0, 0, 0};
+    if (!wasSmall) oldA1 = V3<float>{ls[3 * NL + l], ls[4 * NL + l], ls[5 * NL + l]};
+    const V3<float> oldA2{ls[6 * NL + l], ls[7 * NL + l], ls[8 * NL + l]};
+    float2 sm = d.strain[l];
+    const float4 *P = reinterpret_cast<const float4 *>(d.pos);
+    const float4 *Q = reinterpret_cast<const float4 *>(d.quat);
+    const float4 pnH = P[2 * e.x], pnL = P[2 * e.x + 1], ppH = P[2 * e.y], ppL = P[2 * e.y + 1];
+    const float4 qnH = Q[2 * e.x], qnL = Q[2 * e.x + 1], qpH = Q[2 * e.y], qpL = Q[2 * e.y + 1];
     const int r = (int)li.x;
     if (d.status[r] != 0) return;
     const uint32_t fl = li.y;
     if (fl & LF_BOTH_FIXED) return;
     const int axis = fl & LF_AXIS;
-    const int2 e = d.ends[l];
-    const float4 *P = reinterpret_cast<const float4 *>(d.pos);
-    const float4 *Q = reinterpret_cast<const float4 *>(d.quat);
-    const float4 pnH = P[2 * e.x], pnL = P[2 * e.x + 1], ppH = P[2 * e.y], ppL = P[2 * e.y + 1];
-    const float4 qnH = Q[2 * e.x], qnL = Q[2 * e.x + 1], qpH = Q[2 * e.y], qpL = Q[2 * e.y + 1];
     const LMat &m = d.lmat[fl >> 8];
-    float *ls = (float *)d.lstate;
-    const size_t NL = (size_t)d.nl;
-    const V3<float> oldPos2{ls[l], ls[NL + l], ls[2 * NL + l]};
-    const V3<float> oldA1{ls[3 * NL + l], ls[4 * NL + l], ls[5 * NL + l]};
-    const V3<float> oldA2{ls[6 * NL + l], ls[7 * NL + l], ls[8 * NL + l]};
 
     // rest length L = 0.5*(bsNeg + bsPos) as a hi/lo pair (VX3_Link::updateRestLength)
     float Lh, Ll;
@@ -190,14 +195,15 @@ __global__ void __launch_bounds__(256) k_links_mixed(Dev d) {
     const V3<float> a1v = small ? V3<float>{0, 0, 0} : rotvec_f(angle1.w, V3<float>{angle1.x, angle1.y, angle1.z});
     const V3<float> a2v = rotvec_f(w2, v2);
     ls[l] = pos2.x; ls[NL + l] = pos2.y; ls[2 * NL + l] = pos2.z;
-    ls[3 * NL + l] = a1v.x; ls[4 * NL + l] = a1v.y; ls[5 * NL + l] = a1v.z;
+    if (!(small && wasSmall)) {
+        ls[3 * NL + l] = a1v.x; ls[4 * NL + l] = a1v.y; ls[5 * NL + l] = a1v.z;
+    }
     ls[6 * NL + l] = a2v.x; ls[7 * NL + l] = a2v.y; ls[8 * NL + l] = a2v.z;
 
     const V3<float> dPos2 = scl(sub(pos2, oldPos2), 0.5f);
     const V3<float> dA1 = scl(sub(a1v, oldA1), 0.5f);
     const V3<float> dA2 = scl(sub(a2v, oldA2), 0.5f);
     const float axialStrain = pos2.x / L;
-    float2 sm = d.strain[l];
     sm.x = axialStrain;
     if (axialStrain > sm.y) sm.y = axialStrain;
     d.strain[l] = sm;
@@ -288,10 +294,18 @@ __global__ void k_init_temperature_mixed(Dev d) {
 }
 
 // ------------------------------------------------------------ voxel pass
-__global__ void __launch_bounds__(256) k_voxels_mixed(Dev d, int parity) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= d.nv) return;
+__device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parity) {
+    // the voxel's own state is loaded together with its info word, before any branch
+    // (latency-bound kernel: one dependent level fewer)
     const uint2 vi = d.vinfo[v];
+    float4 *P = reinterpret_cast<float4 *>(d.pos);
+    float4 *Qa = reinterpret_cast<float4 *>(d.quat);
+    float4 *LM = reinterpret_cast<float4 *>(d.linmom);
+    float4 *AM = reinterpret_cast<float4 *>(d.angmom);
+    float4 pH = P[2 * v], pL = P[2 * v + 1];
+    float4 qH = Qa[2 * v], qL = Qa[2 * v + 1];
+    float4 lH = LM[2 * v], lL = LM[2 * v + 1];
+    float4 aH = AM[2 * v], aL = AM[2 * v + 1];
     const int r = (int)vi.x;
     const RobotP &rp = d.rp[r];
     const double Tcur = d.T[(size_t)parity * d.nr + r];
@@ -302,14 +316,6 @@ __global__ void __launch_bounds__(256) k_voxels_mixed(Dev d, int parity) {
     uint32_t fl = vi.y;
     if (fl & VF_FIXED) return;
     const VMat m = d.vmat[fl >> 8];
-    float4 *P = reinterpret_cast<float4 *>(d.pos);
-    float4 *Qa = reinterpret_cast<float4 *>(d.quat);
-    float4 *LM = reinterpret_cast<float4 *>(d.linmom);
-    float4 *AM = reinterpret_cast<float4 *>(d.angmom);
-    float4 pH = P[2 * v], pL = P[2 * v + 1];
-    float4 qH = Qa[2 * v], qL = Qa[2 * v + 1];
-    float4 lH = LM[2 * v], lL = LM[2 * v + 1];
-    float4 aH = AM[2 * v], aL = AM[2 * v + 1];
     const bool actuated = rp.vary_temp && rp.temp_period > 0;
     float *tcur = d.tempe + (size_t)parity * d.nv, *tnext = d.tempe + (size_t)(parity ^ 1) * d.nv;
     const double tn = Tcur + dtf;
@@ -419,11 +425,39 @@ __global__ void __launch_bounds__(256) k_voxels_mixed(Dev d, int parity) {
     P[2 * v + 1] = pL;
 }
 
-void launch_links_mixed(const Dev &d, cudaStream_t s) {
-    if (d.nl) k_links_mixed<<<(d.nl + 255) / 256, 256, 0, s>>>(d);
+// Launch-shape variants (threads per block, minimum resident blocks): the same body,
+// so every variant computes bit-identical results; they trade registers for
+// occupancy (both passes are latency-bound gathers).  vx3g_autotune picks one per
+// context by timing real steps.
+template <int TPB, int MINB> __global__ void __launch_bounds__(TPB, MINB) k_links_mixed(Dev d) {
+    const int l = blockIdx.x * TPB + threadIdx.x;
+    if (l < d.nl) links_mixed_body(d, l);
 }
-void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s) {
-    if (d.nv) k_voxels_mixed<<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity);
+template <int TPB, int MINB> __global__ void __launch_bounds__(TPB, MINB) k_voxels_mixed(Dev d, int parity) {
+    const int v = blockIdx.x * TPB + threadIdx.x;
+    if (v < d.nv) voxels_mixed_body(d, v, parity);
+}
+
+const LaunchShape kLinkShapes[kMixedShapes] = {{256, 1}, {256, 4}, {128, 9}, {128, 10}};
+const LaunchShape kVoxelShapes[kMixedShapes] = {{256, 1}, {256, 3}, {128, 7}, {128, 8}};
+
+void launch_links_mixed(const Dev &d, cudaStream_t s, int shape) {
+    if (!d.nl) return;
+    switch (shape) {
+        case 1: k_links_mixed<256, 4><<<(d.nl + 255) / 256, 256, 0, s>>>(d); break;
+        case 2: k_links_mixed<128, 9><<<(d.nl + 127) / 128, 128, 0, s>>>(d); break;
+        case 3: k_links_mixed<128, 10><<<(d.nl + 127) / 128, 128, 0, s>>>(d); break;
+        default: k_links_mixed<256, 1><<<(d.nl + 255) / 256, 256, 0, s>>>(d); break;
+    }
+}
+void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape) {
+    if (!d.nv) return;
+    switch (shape) {
+        case 1: k_voxels_mixed<256, 3><<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity); break;
+        case 2: k_voxels_mixed<128, 7><<<(d.nv + 127) / 128, 128, 0, s>>>(d, parity); break;
+        case 3: k_voxels_mixed<128, 8><<<(d.nv + 127) / 128, 128, 0, s>>>(d, parity); break;
+        default: k_voxels_mixed<256, 1><<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity); break;
+    }
 }
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s) {
     if (d.nv) k_init_temperature_mixed<<<(d.nv + 255) / 256, 256, 0, s>>>(d);
