@@ -150,16 +150,16 @@ int64_t vx3g_steps_taken(vx3g_ctx *ctx);
 /* ---- differentiation (no counterpart in the reference) ---------------------
  * vx3g_record: advances n_steps (exactly like vx3g_step) and keeps the state
  *   every `checkpoint_every` steps, as the forward pass of a gradient.  FP64
- *   contexts without collisions only (VX3G_ERR_UNSUPPORTED otherwise).
+ *   contexts only (VX3G_ERR_UNSUPPORTED otherwise); self-collision included.
  * vx3g_backward: gradient of L = sum_r w_r . (COM_r(end) - COM_r(start)) over the
  *   recorded run with respect to every voxel's actuation phase (in cycles, the
  *   unit of vx3g_robot_desc.phase) and log10 of its Young's modulus, by the
  *   hand-written adjoint of the step run backwards over the recorded steps; each
  *   checkpoint interval is recomputed from its checkpoint.  dL_dcom: w, 3 per
  *   robot; dL_dphase, dL_dlog10E: one per voxel (either may be NULL).  The
- *   discrete events of the run (friction stick/slip, contact, the small/large
- *   angle switch of each link, the temperature clamp) are held as the run took
- *   them, and the time step is held fixed.  The context keeps the recorded end
+ *   discrete events of the run (friction stick/slip, floor and voxel-voxel
+ *   contact, the small/large angle switch of each link, the temperature clamp)
+ *   are held as the run took them, and the time step is held fixed.  The context keeps the recorded end
  *   state; backward may be called again with other weights. */
 int vx3g_record(vx3g_ctx *ctx, int n_steps, int checkpoint_every);
 int vx3g_backward(vx3g_ctx *ctx, const double *dL_dcom, double *dL_dphase, double *dL_dlog10E);

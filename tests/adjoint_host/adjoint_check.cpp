@@ -184,12 +184,14 @@ struct Stored {
 };
 
 struct Adj {
-    std::vector<double> lv, lown, lF, lbs, lE, lloc, aslot, gph, gle, w, mt;
+    std::vector<double> lv, lown, lF, lbs, lE, lloc, aslot, gph, gle, lcon, lcc, w, mt;
     AdjBufs a{};
     Adj(int nv, int nl) : lv(13 * nv), lown(13 * nv), lF(6 * nv), lbs(nv), lE(nv), lloc(9 * nl), aslot(54 * nv),
-                          gph(nv), gle(nv), w{1, 0, 0}, mt{0} {
-        a = AdjBufs{lv.data(), lown.data(), lF.data(), lbs.data(), lE.data(), lloc.data(), aslot.data(),
-                    gph.data(), gle.data(), w.data(), mt.data(), 0};
+                          gph(nv), gle(nv), lcon(3 * nv), lcc(8 * nv), w{1, 0, 0}, mt{0} {
+        a = AdjBufs{};
+        a.lv = lv.data(); a.lown = lown.data(); a.lF = lF.data(); a.lbs = lbs.data(); a.lE = lE.data();
+        a.lloc = lloc.data(); a.aslot = aslot.data(); a.gphase = gph.data(); a.glogE = gle.data();
+        a.lcon = lcon.data(); a.lcc = lcc.data(); a.w = w.data(); a.mass_tot = mt.data(); a.parity = 0;
     }
     void reverse_step(const World &w, const Snap &s, int parity) {
         a.parity = parity;

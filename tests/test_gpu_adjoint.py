@@ -139,7 +139,7 @@ def test_record_advances_like_step():
     assert a.steps_taken() == 250
 
 
-def test_backward_needs_a_record_and_fp64_without_collisions():
+def test_backward_needs_a_record_and_fp64():
     base = _c4()
     b = abi.Batch([base], abi.PRECISION_FP64)
     with pytest.raises(abi.Vx3gError, match="record"):
@@ -151,11 +151,69 @@ def test_backward_needs_a_record_and_fp64_without_collisions():
     m = abi.Batch([base], abi.PRECISION_MIXED)
     with pytest.raises(abi.Vx3gError, match="FP64"):
         m.record(10, 5)
-    rng = np.random.default_rng(0)
-    col = wl.bernoulli_body(rng, (5, 4, 3), 0.9, [wl.Material()], enable_collision=True)
-    c = abi.Batch([col], abi.PRECISION_FP64)
-    with pytest.raises(abi.Vx3gError, match="collision"):
-        c.record(10, 5)
+
+
+def _contact_robot():
+    """A self-colliding body with contacts from the first steps on: thermal expansion
+    (EnableExpansion, 39 C, CTE 0.01) grows voxels to 1.39 voxel sizes, so diagonal
+    neighbours (1.41 apart) fall inside the 1.25 x base-size contact envelope."""
+    rng = np.random.default_rng(4)
+    mats = [wl.Material(E=2e5, nu=0.35, cte=0.01), wl.Material(E=1e6, nu=0.35, cte=0.01)]
+    r = wl.bernoulli_body(rng, (6, 5, 4), 0.85, mats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                          enable_collision=True, enable_expansion=1)
+    log10E = np.where(r.grid > 0, rng.uniform(5.3, 6.0, size=r.grid.shape), 0.0).astype(np.float32).astype(np.float64)
+    return wl.Robot(**{**r.__dict__, "log10E": log10E})
+
+
+def test_collision_adjoint_matches_central_fd():
+    """With voxel-voxel contact forces in the loop: 16 seeded parameters (8 phases,
+    8 moduli) against central differences at eps = 1e-5 and 1e-6 over 150 steps;
+    at least 12 of 16 within 3% at one of them."""
+    base = _contact_robot()
+    n = 150
+    b = abi.Batch([base], abi.PRECISION_FP64)
+    b.record(n, 50)
+    assert np.count_nonzero(np.abs(b.voxel_aux()["contact"]).sum(1)) > 0  # contacts in play
+    gp, ge = b.backward(np.array([[-1.0, 0.0, 0.0]]))
+    gp = gp / (2 * np.pi)
+    dt0 = b.dt()[0]
+    b.close()
+    grid = base.grid.reshape(-1) > 0
+    ph = base.phase.reshape(-1)
+    le = base.log10E.reshape(-1)
+    idx = np.flatnonzero(grid)  # voxel order = lattice order of the filled cells
+    rng = np.random.default_rng(2)
+    pick = rng.choice(len(idx), 16, replace=False)
+    lemax = np.sort(le[idx])[-4:].min()
+    adj, fds = [], []
+    for j, k in enumerate(pick):
+        cell = idx[k]
+        row = []
+        for eps in (1e-5, 1e-6):
+            if j < 8:
+                d = eps / (2 * np.pi)
+                p1, p2 = ph.copy(), ph.copy()
+                p1[cell] += d
+                p2[cell] -= d
+                f1, d1 = _loss(_with(base, phase=p1.reshape(base.phase.shape)), n)
+                f2, d2 = _loss(_with(base, phase=p2.reshape(base.phase.shape)), n)
+            else:
+                if le[cell] >= lemax:
+                    break
+                e1, e2 = le.copy(), le.copy()
+                e1[cell] += eps
+                e2[cell] -= eps
+                f1, d1 = _loss(_with(base, log10E=e1.reshape(base.log10E.shape)), n)
+                f2, d2 = _loss(_with(base, log10E=e2.reshape(base.log10E.shape)), n)
+            assert d1 == dt0 and d2 == dt0
+            row.append((f1 - f2) / (2 * eps))
+        if len(row) < 2:
+            continue
+        adj.append(gp[k] if j < 8 else ge[k])
+        fds.append(row)
+    adj, fds = np.array(adj), np.array(fds).T
+    rel = rel_errors(adj, fds)
+    assert np.sum(rel.min(axis=0) <= 0.03) >= 0.75 * len(adj), (adj, fds, rel)
 
 
 def test_torch_autograd_wrapper():

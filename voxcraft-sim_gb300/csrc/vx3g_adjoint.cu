@@ -79,6 +79,15 @@ void launch_adj_gather_slots(const Dev &d, const Snap &sg, const Snap *ss, const
     }
 }
 
+__global__ void __launch_bounds__(128) k_adj_contact(Dev d, Snap s, AdjBufs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.ns) adj::adj_contact(d, s, a, i);
+}
+
+void launch_adj_contact(const Dev &d, const Snap &s, const AdjBufs &a, cudaStream_t st) {
+    if (d.ns) k_adj_contact<<<(d.ns + 127) / 128, 128, 0, st>>>(d, s, a);
+}
+
 void launch_adj_seed(const Dev &d, const AdjBufs &a, cudaStream_t st) {
     const int n = d.nv > d.nl ? d.nv : d.nl;
     if (n) k_adj_seed<<<(n + 127) / 128, 128, 0, st>>>(d, a);

@@ -339,6 +339,7 @@ __device__ __forceinline__ void adj_voxel(const Dev &d, const Snap &s, const Adj
     for (int i = 0; i < 6; i++) lF[i] = 0.0;
     a.lbs[v] = 0.0;
     a.lE[v] = 0.0;
+    a.lcon[3 * (size_t)v] = a.lcon[3 * (size_t)v + 1] = a.lcon[3 * (size_t)v + 2] = 0.0;
     const uint2 vi = s.vinfo[v];
     const int r = (int)vi.x;
     const uint32_t fl = vi.y;
@@ -371,6 +372,10 @@ __device__ __forceinline__ void adj_voxel(const Dev &d, const Snap &s, const Adj
     const V vel = scl(lm, m.mass_inv);
     F = sub(F, scl(vel, m.c_glob));
     F.z += m.grav_force;
+    if (rp.collision) {  // this step's contact force (recomputed into d.contact for this state)
+        const double4 c = d.contact[v];
+        F = sub(F, V{c.x, c.y, c.z});
+    }
     F = add(F, V{0.0, 0.0, 0.0});
     V fric = F;
     bool contact = false, kinetic = false;
@@ -442,6 +447,11 @@ __device__ __forceinline__ void adj_voxel(const Dev &d, const Snap &s, const Adj
     if (zero_xy) llm1.x = llm1.y = 0;
     llm = add(llm, llm1);
     const V lFt = scl(llm1, dt);  // dL/dF (total force)
+    if (rp.collision) {  // F = ... - contact
+        a.lcon[3 * (size_t)v] = -lFt.x;
+        a.lcon[3 * (size_t)v + 1] = -lFt.y;
+        a.lcon[3 * (size_t)v + 2] = -lFt.z;
+    }
     V lvel{0, 0, 0};
     double lbs = 0;
     if (contact) {
@@ -622,6 +632,13 @@ __device__ __forceinline__ void adj_gather(const Dev &d, const Snap &s, const Ad
             lbs += o[7];
             lE += o[8];
         }
+    if (d.rp[r].collision) {  // contact forces (zero for voxels off the collision surface)
+        const double *c = a.lcc + 8 * (size_t)v;
+        acc[0] += c[0]; acc[1] += c[1]; acc[2] += c[2];
+        acc[7] += c[3]; acc[8] += c[4]; acc[9] += c[5];
+        lbs += c[6];
+        lE += c[7];
+    }
     double *lv = a.lv + 13 * (size_t)v;
     for (int i = 0; i < 13; i++) lv[i] = acc[i];
     if (s.status[r] != 0) return;
@@ -636,6 +653,77 @@ __device__ __forceinline__ void adj_gather(const Dev &d, const Snap &s, const Ad
             a.gphase[v] += lbs * m.nom_size * (double)m.cte * rp.temp_amp * cos(arg) * (double)(2 * 3.1415926f);
     }
     a.glogE[v] += lE * (double)m.E * 2.302585092994046;  // dE/dlog10(E) = E ln 10
+}
+
+// ------------------------------------------------------------ contact forces
+// The force on surface voxel v from a listed partner u in contact
+// (handle_collision_attachment + VX3_Collision::updateContactForce,
+// src/VX3/VX3_VoxelyzeKernel.cu:682-727, src/VX3/VX3_Collision.cu:3-31) is, whichever
+// is voxel1, G = uh*s with D = p_u - p_v, d = |D|, uh = D/d, s = k*rel + c*rv,
+// rel = 0.625*(bs_v + bs_u) - d, rv = (w_v - w_u).uh, w = linMom/m,
+// k = 2/(1/k_v + 1/k_u), k_i = 2*E_i*L_i, c = (c_v + c_u)/2, c_i ~ sqrt(E_i); and
+// -G on u.  With mu = dL/dcontact_v - dL/dcontact_u and a = mu.uh:
+//   dL/dD  = (s*(mu - a*uh) + a*c*((w_v - w_u) - rv*uh))/d - a*k*uh   (p_u: +, p_v: -)
+//   dL/dw_v = a*c*uh,  dL/dbs_v = 0.625*a*k,
+//   dL/dE_v = a*rel * 2*k_u^2/(k_v + k_u)^2 * 2*L_v + a*rv * c_v/(4*E_v).
+// Each surface voxel gathers its own share from its partners in ascending order, with
+// the reference's exact test deciding contact as in the forward pass.
+__device__ __forceinline__ void adj_contact(const Dev &d, const Snap &s, const AdjBufs &a, int si) {
+    const int v = d.csurf[si];
+    double *out = a.lcc + 8 * (size_t)v;
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const uint2 vi = s.vinfo[v];
+    const int n = d.nnb[si];
+    if (s.status[vi.x] == 0 && n > 0) {
+        const int *lst = d.nbr + (size_t)si * kNbrCap;
+        const double4 pv = s.pos[v], lmv4 = s.linmom[v];
+        const double bsa = (pv.w + pv.w + pv.w) / 3.0f;
+        const VMat &mv = d.vmat[vi.y >> 8];
+        const V lcv{a.lcon[3 * (size_t)v], a.lcon[3 * (size_t)v + 1], a.lcon[3 * (size_t)v + 2]};
+        const V wv = scl(V{lmv4.x, lmv4.y, lmv4.z}, mv.mass_inv);
+        for (int k = 0; k < n; k++) {
+            const int u = lst[k];
+            const double4 pu = s.pos[u];
+            const double bu = (pu.w + pu.w + pu.w) / 3.0f;
+            // the forward pass's exact test, voxel1 = the later surface voxel
+            const double4 &p1 = u < v ? pv : pu, &p2 = u < v ? pu : pv;
+            const double b1 = u < v ? bsa : bu, b2 = u < v ? bu : bsa;
+            const V diff{p1.x - p2.x, p1.y - p2.y, p1.z - p2.z};
+            const double wd = (b1 + b2) * 0.625;
+            if (diff.x > wd || diff.x < -wd || diff.y > wd || diff.y < -wd || diff.z > wd || diff.z < -wd) continue;
+            if (len(diff) > wd) continue;
+            const V off{p2.x - p1.x, p2.y - p1.y, p2.z - p1.z};
+            const double relf = (b1 + b2) * 0.625 - len(off);
+            if (!(relf > 0)) continue;
+            // the pair's force on v and its derivatives
+            const uint2 ui = s.vinfo[u];
+            const VMat &mu_ = d.vmat[ui.y >> 8];
+            const double kk = 2.0f / (1.0f / mv.pstiff + 1.0f / mu_.pstiff);
+            const double cc = 0.5f * (mv.c_col + mu_.c_col);
+            const V D{pu.x - pv.x, pu.y - pv.y, pu.z - pv.z};
+            const double dd = len(D);
+            const V uh = scl(D, 1.0 / dd);
+            const double rel = (bsa + bu) * 0.625 - dd;
+            const double4 lmu4 = s.linmom[u];
+            const V wu = scl(V{lmu4.x, lmu4.y, lmu4.z}, mu_.mass_inv);
+            const V wvu = sub(wv, wu);
+            const double rv = dot(wvu, uh);
+            const double sf = kk * rel + cc * rv;
+            const V mu{lcv.x - a.lcon[3 * (size_t)u], lcv.y - a.lcon[3 * (size_t)u + 1],
+                       lcv.z - a.lcon[3 * (size_t)u + 2]};
+            const double am = dot(mu, uh);
+            const V gD = sub(scl(add(scl(sub(mu, scl(uh, am)), sf), scl(sub(wvu, scl(uh, rv)), am * cc)), 1.0 / dd),
+                             scl(uh, am * kk));
+            acc[0] -= gD.x; acc[1] -= gD.y; acc[2] -= gD.z;  // D = p_u - p_v
+            const double lw = am * cc * (double)mv.mass_inv;
+            acc[3] += lw * uh.x; acc[4] += lw * uh.y; acc[5] += lw * uh.z;
+            acc[6] += 0.625 * am * kk;
+            const double kv = mv.pstiff, ku = mu_.pstiff;
+            acc[7] += am * rel * 2.0 * ku * ku / ((kv + ku) * (kv + ku)) * 2.0 * mv.nom_size +
+                      am * rv * (double)mv.c_col / (4.0 * (double)mv.E);
+        }
+    }
+    for (int i = 0; i < 8; i++) out[i] = acc[i];
 }
 
 // dL/d(final state) for L = sum_r w_r . COM_r(end): m_v/M_r * w_r on each measured voxel (k_com)

@@ -29,6 +29,8 @@ struct AdjBufs {
     double *aslot;  // 9 per voxel-direction: a link's dL/d(pos3, quat4), dL/d(base size), dL/dE for that end
     double *gphase; // per voxel: accumulated dL/d(phase)
     double *glogE;  // per voxel: accumulated dL/d(log10 E)
+    double *lcon;   // 3 per voxel: dL/d(contact force) of this step (the voxel pass consumes it)
+    double *lcc;    // 8 per voxel: the contact adjoint's dL/d(pos3, linMom3, base size, E) for that voxel
     const double *w;         // 3 per robot: dL/dCOM
     const double *mass_tot;  // per robot: total mass of the measured voxels
     int parity;     // step parity of the step being reversed (time buffer)
@@ -42,6 +44,9 @@ void launch_snap_copy(const Snap &dst, const Snap &src, int nv, int nl, int nr, 
 void launch_adj_slots(const Dev &d, const Snap &s, const AdjBufs &a, cudaStream_t st);
 void launch_adj_voxel_link(const Dev &d, const Snap &s, const AdjBufs &a, cudaStream_t st);
 void launch_adj_gather_slots(const Dev &d, const Snap &sg, const Snap *ss, const AdjBufs &a, cudaStream_t st);
+// with collisions: the contact forces of the step must be in d.contact (and the candidate
+// lists valid) for the voxel adjoint; then the contact adjoint, then the gather
+void launch_adj_contact(const Dev &d, const Snap &s, const AdjBufs &a, cudaStream_t st);
 // dL/d(final state) for L = sum_r w_r . COM_r(end); also zeroes the link-state adjoint
 void launch_adj_seed(const Dev &d, const AdjBufs &a, cudaStream_t st);
 

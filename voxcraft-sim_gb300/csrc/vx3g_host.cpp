@@ -992,20 +992,43 @@ int alloc_snaps(vx3g_ctx *c, std::vector<Snap> &out, int n) {
 // One checkpoint interval of the backward pass as a CUDA graph: recompute the
 // interval's len states from the live state (the checkpoint, copied in just before),
 // then run the reverse steps over them.  Cached per (len, parity of the first step).
-void enqueue_adj_segment(vx3g_ctx *c, const AdjBufs &a0, int len, int p0) {
+cudaError_t enqueue_adj_segment(vx3g_ctx *c, const AdjBufs &a0, int len, int p0) {
     const Dev &d = c->d;
     const Snap live = live_snap(d);
-    for (int i = 0; i < len; i++) {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < len && e == cudaSuccess; i++) {
         launch_snap_copy(c->rec_store[i], live, d.nv, d.nl, d.nr, c->stream);
-        (void)enqueue_step(c, (p0 + i) & 1);  // no collision in recorded runs
+        e = enqueue_step(c, (p0 + i) & 1);
     }
     AdjBufs a = a0;
-    launch_adj_slots(d, c->rec_store[len - 1], a, c->stream);
-    for (int i = len - 1; i >= 0; i--) {
-        a.parity = (p0 + i) & 1;
-        launch_adj_voxel_link(d, c->rec_store[i], a, c->stream);
-        launch_adj_gather_slots(d, c->rec_store[i], i > 0 ? &c->rec_store[i - 1] : nullptr, a, c->stream);
+    if (!c->any_collision) {
+        launch_adj_slots(d, c->rec_store[len - 1], a, c->stream);
+        for (int i = len - 1; i >= 0; i--) {
+            a.parity = (p0 + i) & 1;
+            launch_adj_voxel_link(d, c->rec_store[i], a, c->stream);
+            launch_adj_gather_slots(d, c->rec_store[i], i > 0 ? &c->rec_store[i - 1] : nullptr, a, c->stream);
+        }
+        return e;
     }
+    // with collisions, per reverse step: the step's contact forces from its stored state
+    // (the candidate lists checked and rebuilt against that state as the forward pass
+    // does), then the link-force recompute, the voxel and link adjoints, the contact
+    // adjoint and the gather
+    for (int i = len - 1; i >= 0 && e == cudaSuccess; i--) {
+        const Snap &st = c->rec_store[i];
+        Dev ds = d;
+        ds.pos = st.pos;
+        ds.linmom = st.linmom;
+        ds.vinfo = st.vinfo;
+        ds.status = st.status;
+        e = launch_collision(ds, c->stream, c->side);
+        a.parity = (p0 + i) & 1;
+        launch_adj_slots(d, st, a, c->stream);
+        launch_adj_voxel_link(d, st, a, c->stream);
+        launch_adj_contact(d, st, a, c->stream);
+        launch_adj_gather_slots(d, st, nullptr, a, c->stream);
+    }
+    return e;
 }
 
 int adj_segment_graph(vx3g_ctx *c, const AdjBufs &a, int len, int p0, cudaGraphExec_t *out) {
@@ -1017,8 +1040,13 @@ int adj_segment_graph(vx3g_ctx *c, const AdjBufs &a, int len, int p0, cudaGraphE
         }
     cudaGraph_t g;
     CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_adj_segment(c, a, len, p0);
-    CU(cudaStreamEndCapture(c->stream, &g));
+    const cudaError_t ce = enqueue_adj_segment(c, a, len, p0);
+    const cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+    if (ce != cudaSuccess) {
+        if (ee == cudaSuccess) cudaGraphDestroy(g);
+        return fail(VX3G_ERR_CUDA, std::string("backward graph capture: ") + cudaGetErrorString(ce));
+    }
+    CU(ee);
     cudaGraphExec_t ex = nullptr;
     cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
     cudaGraphDestroy(g);
@@ -1035,7 +1063,6 @@ extern "C" {
 int vx3g_record(vx3g_ctx *c, int n, int k) {
     if (!c || n < 0 || k <= 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_record");
     if (c->precision != VX3G_PRECISION_FP64) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint runs on FP64 contexts");
-    if (c->any_collision) return fail(VX3G_ERR_UNSUPPORTED, "collisions are not differentiated");
     CU(cudaSetDevice(c->device));
     CU(cudaStreamSynchronize(c->stream));
     c->free_record();
@@ -1072,7 +1099,8 @@ int vx3g_backward(vx3g_ctx *c, const double *dL_dcom, double *dL_dphase, double 
     int rc;
     if (!c->adj_mem) {  // adjoint buffers, kept for later calls
         const size_t bytes = al256(13 * nv * 8) * 2 + al256(6 * nv * 8) + al256(nv * 8) * 4 + al256(9 * nl * 8) +
-                             al256(54 * nv * 8) + al256(3 * nr * 8) + al256(nr * 8);
+                             al256(54 * nv * 8) + al256(3 * nr * 8) + al256(nr * 8) + al256(3 * nv * 8) +
+                             al256(8 * nv * 8);
         cudaError_t e = cudaMalloc(&c->adj_mem, bytes);
         if (e != cudaSuccess) {
             c->adj_mem = nullptr;
@@ -1096,6 +1124,10 @@ int vx3g_backward(vx3g_ctx *c, const double *dL_dcom, double *dL_dphase, double 
         a.aslot = take(54 * nv * 8);
         a.w = take(3 * nr * 8);
         a.mass_tot = take(nr * 8);
+        a.lcon = take(3 * nv * 8);
+        a.lcc = take(8 * nv * 8);
+        CU(cudaMemsetAsync(a.lcon, 0, 3 * nv * 8, c->stream));
+        CU(cudaMemsetAsync(a.lcc, 0, 8 * nv * 8, c->stream));  // stays zero off the collision surface
         CU(cudaMemcpyAsync((void *)a.mass_tot, c->mass_tot.data(), nr * 8, cudaMemcpyHostToDevice, c->stream));
     }
     const int n = c->rec_n, k = c->rec_k;
@@ -1108,7 +1140,7 @@ int vx3g_backward(vx3g_ctx *c, const double *dL_dcom, double *dL_dphase, double 
         if ((rc = alloc_snaps(c, c->rec_store, store)) || (rc = alloc_snaps(c, end, 1))) return rc;
         c->rec_end = end[0];
         void *m = nullptr;
-        cudaError_t e = cudaMalloc(&m, 36 * nv * sizeof(double));
+        cudaError_t e = cudaMalloc(&m, (36 + 4) * nv * sizeof(double));  // slots + contact forces
         if (e != cudaSuccess) return fail(VX3G_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         c->rec_mem.push_back(m);
         c->rec_slots = m;
@@ -1120,6 +1152,8 @@ int vx3g_backward(vx3g_ctx *c, const double *dL_dcom, double *dL_dphase, double 
     const Snap live = live_snap(d);
     launch_snap_copy(c->rec_end, live, d.nv, d.nl, d.nr, c->stream);
     CU(cudaMemcpyAsync(c->rec_slots, d.slots, 36 * nv * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync((double *)c->rec_slots + 36 * nv, d.contact, nv * sizeof(double4), cudaMemcpyDeviceToDevice,
+                       c->stream));
     launch_adj_seed(d, a, c->stream);
     const int nck = (n + k - 1) / k;
     for (int j = nck - 1; j >= 0; j--) {
@@ -1132,6 +1166,8 @@ int vx3g_backward(vx3g_ctx *c, const double *dL_dcom, double *dL_dphase, double 
     }
     launch_snap_copy(live, c->rec_end, d.nv, d.nl, d.nr, c->stream);
     CU(cudaMemcpyAsync(d.slots, c->rec_slots, 36 * nv * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(d.contact, (double *)c->rec_slots + 36 * nv, nv * sizeof(double4), cudaMemcpyDeviceToDevice,
+                       c->stream));
     if (dL_dphase) CU(cudaMemcpyAsync(dL_dphase, a.gphase, nv * 8, cudaMemcpyDeviceToHost, c->stream));
     if (dL_dlog10E) CU(cudaMemcpyAsync(dL_dlog10E, a.glogE, nv * 8, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
