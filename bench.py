@@ -192,6 +192,23 @@ def ncu_traffic(workload, precision, kernel):
         return None
 
 
+def host_description():
+    """CPU model and logical core count of the host the CPU baseline ran on."""
+    model = ""
+    try:
+        for ln in open("/proc/cpuinfo"):
+            k = ln.split(":")[0].strip().lower()
+            if k in ("model name", "cpu model", "hardware") and ":" in ln:
+                model = ln.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    if not model:
+        import platform
+        model = platform.processor() or platform.machine()
+    return {"cpu": model, "nproc": os.cpu_count()}
+
+
 def pinned_copy(arrays):
     """Copies of the arrays in page-locked host memory (torch's pinned allocator)."""
     try:
@@ -285,7 +302,8 @@ def run_reference(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "config": {"workload": WORKLOADS[args.workload][0], "robots": len(robots)},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                             "host": host_description()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -403,8 +421,18 @@ def main():
     if rank == 0 and args.workload == "c5" and not args.no_adjoint:
         line["adjoint"] = measure_adjoint_population(dev)
     if rank == 0 and not args.no_cpu_baseline:
-        v, sample = cpu_baseline_port(robots, 1, budget_s=15.0, max_steps=50)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+        # single-threaded, pinned to one core for the measurement
+        pinned = None
+        if hasattr(os, "sched_getaffinity"):
+            pinned = os.sched_getaffinity(0)
+            os.sched_setaffinity(0, {min(pinned)})
+        try:
+            v, sample = cpu_baseline_port(robots, 1, budget_s=15.0, max_steps=50)
+        finally:
+            if pinned is not None:
+                os.sched_setaffinity(0, pinned)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
+                                "host": host_description()}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -118,6 +118,18 @@ void launch_coll_eval_mixed(const Dev &d, cudaStream_t s) {
     if (d.ns) k_coll_eval_mixed<<<(d.ns + 255) / 256, 256, 0, s>>>(d);
 }
 
+// ------------------------------------------------------------- programmatic dependent launch
+// The link and voxel kernels are launched with programmatic stream serialization:
+// a kernel may start while the previous one finishes.  Each first issues the loads
+// that do not depend on the previous kernel, then waits for it to complete
+// (griddepcontrol.wait: a no-op when launched without the attribute), and only then
+// lets the next kernel launch, so a kernel never starts before the one two places
+// earlier has finished.  Every store comes after the wait.
+__device__ __forceinline__ void pdl_wait_then_release() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ------------------------------------------------------------- link pass
 __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     // every load that depends only on l is issued before the first branch, then the
@@ -135,6 +147,7 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     if (!wasSmall) oldA1 = V3<float>{ls[3 * NL + l], ls[4 * NL + l], ls[5 * NL + l]};
     const V3<float> oldA2{ls[6 * NL + l], ls[7 * NL + l], ls[8 * NL + l]};
     float2 sm = d.strain[l];
+    pdl_wait_then_release();  // the previous voxel pass has moved the endpoints
     const float4 *P = reinterpret_cast<const float4 *>(d.pos);
     const float4 *Q = reinterpret_cast<const float4 *>(d.quat);
     const float4 pnH = P[2 * e.x], pnL = P[2 * e.x + 1], ppH = P[2 * e.y], ppL = P[2 * e.y + 1];
@@ -306,6 +319,7 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
     float4 qH = Qa[2 * v], qL = Qa[2 * v + 1];
     float4 lH = LM[2 * v], lL = LM[2 * v + 1];
     float4 aH = AM[2 * v], aL = AM[2 * v + 1];
+    pdl_wait_then_release();  // the link pass (or the contact evaluation) of this step is done
     const int r = (int)vi.x;
     const RobotP &rp = d.rp[r];
     const double Tcur = d.T[(size_t)parity * d.nr + r];
@@ -441,22 +455,37 @@ template <int TPB, int MINB> __global__ void __launch_bounds__(TPB, MINB) k_voxe
 const LaunchShape kLinkShapes[kMixedShapes] = {{256, 1}, {256, 4}, {128, 9}, {128, 10}};
 const LaunchShape kVoxelShapes[kMixedShapes] = {{256, 1}, {256, 3}, {128, 7}, {128, 8}};
 
+// launch with programmatic stream serialization (see pdl_wait_then_release)
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), int n, int threads, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((n + threads - 1) / threads));
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 void launch_links_mixed(const Dev &d, cudaStream_t s, int shape) {
     if (!d.nl) return;
     switch (shape) {
-        case 1: k_links_mixed<256, 4><<<(d.nl + 255) / 256, 256, 0, s>>>(d); break;
-        case 2: k_links_mixed<128, 9><<<(d.nl + 127) / 128, 128, 0, s>>>(d); break;
-        case 3: k_links_mixed<128, 10><<<(d.nl + 127) / 128, 128, 0, s>>>(d); break;
-        default: k_links_mixed<256, 1><<<(d.nl + 255) / 256, 256, 0, s>>>(d); break;
+        case 1: launch_pdl(k_links_mixed<256, 4>, d.nl, 256, s, d); break;
+        case 2: launch_pdl(k_links_mixed<128, 9>, d.nl, 128, s, d); break;
+        case 3: launch_pdl(k_links_mixed<128, 10>, d.nl, 128, s, d); break;
+        default: launch_pdl(k_links_mixed<256, 1>, d.nl, 256, s, d); break;
     }
 }
 void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape) {
     if (!d.nv) return;
     switch (shape) {
-        case 1: k_voxels_mixed<256, 3><<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity); break;
-        case 2: k_voxels_mixed<128, 7><<<(d.nv + 127) / 128, 128, 0, s>>>(d, parity); break;
-        case 3: k_voxels_mixed<128, 8><<<(d.nv + 127) / 128, 128, 0, s>>>(d, parity); break;
-        default: k_voxels_mixed<256, 1><<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity); break;
+        case 1: launch_pdl(k_voxels_mixed<256, 3>, d.nv, 256, s, d, parity); break;
+        case 2: launch_pdl(k_voxels_mixed<128, 7>, d.nv, 128, s, d, parity); break;
+        case 3: launch_pdl(k_voxels_mixed<128, 8>, d.nv, 128, s, d, parity); break;
+        default: launch_pdl(k_voxels_mixed<256, 1>, d.nv, 256, s, d, parity); break;
     }
 }
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s) {
