@@ -303,7 +303,9 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             if (p > R.n_materials) return fail(VX3G_ERR_INVALID, "lattice names a missing palette entry");
             if (p > 0) vid[i] = v0 + nvr++;
         }
-        std::vector<int> pair_lmat(R.n_materials * R.n_materials, -1);
+        std::vector<int> pair_lmat(R.n_materials * R.n_materials, -1);  // unordered pair -> combined values
+        std::vector<int> ori_lmat(R.n_materials * R.n_materials, -1);   // (neg, pos) -> oriented material
+        std::vector<LMat> pair_vals;
         std::vector<HostVMat> hv;  // per voxel when the robot carries per-voxel moduli
         if (R.log10E) hv.resize(nvr);
         // initial temperature: UpdateMatTemps at import (VX_Sim.cpp:462-478, VX_Environment.cpp:326-345)
@@ -341,18 +343,36 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
                 if (nb[a] < 0 || vid[nb[a]] < 0) continue;
                 const int vn = vid[nb[a]], vp = vid[i];
                 const int mn = c->vmat_local[vn], mp = mi;
+                // each ends' damping numerator and Fixed flag ride with the link material, so the
+                // link pass needs no per-voxel material lookups
+                auto orient = [&](LMat l, const HostVMat &neg, const HostVMat &pos, bool fneg, bool fpos) {
+                    l.dmcN = 2 * neg.sqrt_mass * neg.z_int;
+                    l.dmcP = 2 * pos.sqrt_mass * pos.z_int;
+                    l.fixN = fneg ? 1 : 0;
+                    l.fixP = fpos ? 1 : 0;
+                    return l;
+                };
                 int lm;
                 if (R.log10E) {  // one link material per link
                     lm = (int)lmats.size() - lbase;
-                    lmats.push_back(combine(hv[vp - v0], hv[vn - v0]));
+                    lmats.push_back(orient(combine(hv[vp - v0], hv[vn - v0]), hv[vn - v0], hv[vp - v0],
+                                           R.materials[mn].fixed, R.materials[mp].fixed));
                 } else {
-                    int &plm = pair_lmat[mp * R.n_materials + mn];
-                    if (plm < 0) {
-                        plm = (int)lmats.size() - lbase;
-                        pair_lmat[mn * R.n_materials + mp] = plm;
-                        lmats.push_back(combine(hm[mp], hm[mn]));
+                    // the combined constants come from the pair's first use (vox1 = the new voxel);
+                    // oriented entries (negative end's material first) share them
+                    int &base = pair_lmat[mp * R.n_materials + mn];
+                    if (base < 0) {
+                        base = (int)pair_vals.size();
+                        pair_lmat[mn * R.n_materials + mp] = base;
+                        pair_vals.push_back(combine(hm[mp], hm[mn]));
                     }
-                    lm = plm;
+                    int &ori = ori_lmat[mn * R.n_materials + mp];
+                    if (ori < 0) {
+                        ori = (int)lmats.size() - lbase;
+                        lmats.push_back(orient(pair_vals[base], hm[mn], hm[mp], R.materials[mn].fixed,
+                                               R.materials[mp].fixed));
+                    }
+                    lm = ori;
                 }
                 const int l = (int)c->ends.size();
                 c->ends.push_back(make_int2(vn, vp));

@@ -51,11 +51,13 @@ struct VMat {  // one voxel material (global index), constants as the reference 
     double thermal_on_after;
 };
 
-struct LMat {  // one link material (global index)
+struct LMat {  // one link material (global index), oriented: (negative end, positive end) materials
     float E, nu, eHat, eps_fail;
     float a1, a2, b1, b2, b3;
     float sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp;
     float area, tss;  // transverse area / strain sum frozen at link creation
+    float dmcN, dmcP; // the ends' dampingMultiplier numerators 2*sqrt(m)*zetaInternal (VMat.dmc)
+    int fixN, fixP;   // the ends' materials are Fixed
 };
 
 struct RobotP {

@@ -50,9 +50,19 @@ __device__ __forceinline__ float df_diff3(float ah, float al, float bh, float bl
     return s2 + (e2 + (e + ((al - bl) - cl)));
 }
 
+// Rotation vector of a unit quaternion, v * 2*atan2(|v|, w)/|v|.  For the small
+// rotations most links carry (|v|/w < 0.01) the factor is (2/w) * atan(x)/x with
+// x = |v|/w, taken from the Maclaurin series of arctan, atan(x)/x = 1 - x^2/3 + x^4/5
+// - ..., whose first omitted term (x^6/7 < 1.5e-13) is far below FP32 rounding; this
+// needs neither the square root nor the arctangent.
 __device__ __forceinline__ V3<float> rotvec_f(float w, V3<float> v) {
     const float s2 = v.x * v.x + v.y * v.y + v.z * v.z;
     if (!(s2 > 0.0f)) return V3<float>{0, 0, 0};
+    if (w > 0.0f && s2 < 1e-4f * (w * w)) {
+        const float iw = 1.0f / w;
+        const float x2 = s2 * (iw * iw);
+        return scl(v, 2.0f * iw * (1.0f - x2 * (1.0f / 3.0f - x2 * 0.2f)));
+    }
     const float s = sqrtf(s2);
     return scl(v, 2.0f * atan2f(s, w) / s);
 }
@@ -247,9 +257,8 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
         const V3<float> posCalc{m.sqA1 * dPos2.x, m.sqB1 * dPos2.y - m.sqB2xFMp * (dA1.z + dA2.z),
                                 m.sqB1 * dPos2.z + m.sqB2xFMp * (dA1.y + dA2.y)};
         const float dtf = d.dt[r];
-        const uint32_t fnv = d.vinfo[e.x].y, fpv = d.vinfo[e.y].y;
-        const float dmN = d.vmat[fnv >> 8].dmc / ((fnv & VF_FIXED) ? 0.0f : dtf);
-        const float dmP = d.vmat[fpv >> 8].dmc / ((fpv & VF_FIXED) ? 0.0f : dtf);
+        const float dmN = m.dmcN / (m.fixN ? 0.0f : dtf);
+        const float dmP = m.dmcP / (m.fixP ? 0.0f : dtf);
         fNeg = add(fNeg, scl(posCalc, dmN));
         fPos = sub(fPos, scl(posCalc, dmP));
         mNeg = sub(mNeg, scl(V3<float>{-m.sqA2xIp * (dA2.x - dA1.x), m.sqB2xFMp * dPos2.z + m.sqB3xIp * (2 * dA1.y + dA2.y),
