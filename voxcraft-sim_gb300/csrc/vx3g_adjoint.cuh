@@ -675,14 +675,15 @@ __device__ __forceinline__ void adj_contact(const Dev &d, const Snap &s, const A
     const uint2 vi = s.vinfo[v];
     const int n = d.nnb[si];
     if (s.status[vi.x] == 0 && n > 0) {
-        const int *lst = d.nbr + (size_t)si * kNbrCap;
+        const int *lst = d.nbr + si;  // slot-major: entry k at lst[k*ns]
+        const size_t ns = (size_t)d.ns;
         const double4 pv = s.pos[v], lmv4 = s.linmom[v];
         const double bsa = (pv.w + pv.w + pv.w) / 3.0f;
         const VMat &mv = d.vmat[vi.y >> 8];
         const V lcv{a.lcon[3 * (size_t)v], a.lcon[3 * (size_t)v + 1], a.lcon[3 * (size_t)v + 2]};
         const V wv = scl(V{lmv4.x, lmv4.y, lmv4.z}, mv.mass_inv);
         for (int k = 0; k < n; k++) {
-            const int u = lst[k];
+            const int u = lst[k * ns];
             const double4 pu = s.pos[u];
             const double bu = (pu.w + pu.w + pu.w) / 3.0f;
             // the forward pass's exact test, voxel1 = the later surface voxel

@@ -255,7 +255,8 @@ __global__ void k_coll_list(Dev d) {
     const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
     const bool fixed = (d.vinfo[v].y & VF_FIXED) != 0;
     const short4 ij = d.ijk[v];
-    int *out = d.nbr + (size_t)s * kNbrCap;
+    int *out = d.nbr + s;  // entry j at out[j*ns]: slot-major, so list reads coalesce across a warp
+    const size_t ns = (size_t)d.ns;
     int nc = 0;
     bool overflow = false;
     for (int dz = -1; dz <= 1; dz++)
@@ -284,11 +285,11 @@ __global__ void k_coll_list(Dev d) {
                     // the list holds voxel indices in ascending order: csurf is ascending, so
                     // this is the ascending surface-index order of the reference's pair loop
                     int j = nc++;
-                    while (j > 0 && out[j - 1] > u) {
-                        out[j] = out[j - 1];
+                    while (j > 0 && out[(j - 1) * ns] > u) {
+                        out[j * ns] = out[(j - 1) * ns];
                         j--;
                     }
-                    out[j] = u;
+                    out[j * ns] = u;
                 }
             }
     if (overflow) atomicOr(&d.status[r], 2);
@@ -325,7 +326,8 @@ __global__ void k_coll_eval(Dev d) {
     const int r = (int)d.vinfo[v].x;
     if (d.status[r] != 0) return;
     const int n = d.nnb[s];
-    const int *lst = d.nbr + (size_t)s * kNbrCap;
+    const int *lst = d.nbr + s;  // slot-major: entry k at lst[k*ns]
+    const size_t ns = (size_t)d.ns;
     V3<double> acc{0, 0, 0};
     if (n) {
         const float4 pf = pos_f(d, v);
@@ -333,7 +335,7 @@ __global__ void k_coll_eval(Dev d) {
         double bsa = 0;
         bool have_bsa = false;
         for (int k = 0; k < n; k++) {
-            const int u = lst[k];  // partner voxel, ascending
+            const int u = lst[k * ns];  // partner voxel, ascending
             // FP32 prefilter against the current cutoff: only pairs within 0.1% of it reach FP64
             const float4 tf = pos_f(d, u);
             const float ex = tf.x - pf.x, ey = tf.y - pf.y, ez = tf.z - pf.z;

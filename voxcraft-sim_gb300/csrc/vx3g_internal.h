@@ -99,7 +99,7 @@ struct Dev {
     int4 *ccell;    // cell coords + robot per collision-surface voxel
     float4 *cposf;  // FP32 copy of the position (prefilter) per collision-surface voxel
     float4 *cref;   // position at the last list build (w: squared displacement that forces a rebuild)
-    int *nbr;       // candidate list: kNbrCap partner voxel indices per collision-surface voxel, ascending
+    int *nbr;       // candidate lists, slot-major [kNbrCap][NS]: partner voxel indices, ascending
     int *nnb;       // candidate count per collision-surface voxel
     int *cflag;     // 1: rebuild the candidate lists this step
     unsigned *ccount;  // blocks of the displacement check that have finished (graph path)

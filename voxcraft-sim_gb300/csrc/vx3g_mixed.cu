@@ -82,7 +82,8 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
     const int r = (int)vi.x;
     if (d.status[r] != 0) return;
     const int n = d.nnb[s];
-    const int *lst = d.nbr + (size_t)s * kNbrCap;
+    const int *lst = d.nbr + s;  // slot-major: entry k at lst[k*ns]
+    const size_t ns = (size_t)d.ns;
     const float4 *P = reinterpret_cast<const float4 *>(d.pos);
     const float4 *LM = reinterpret_cast<const float4 *>(d.linmom);
     V3<float> acc{0, 0, 0};
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
         const float bv = pvH.w + pvL.w;  // baseSizeAverage = baseSize (isotropic)
         const VMat &mv = d.vmat[vi.y >> 8];
         for (int k = 0; k < n; k++) {
-            const int u = lst[k];  // partner voxel, ascending
+            const int u = lst[k * ns];  // partner voxel, ascending
             const float4 puH = P[2 * u], puL = P[2 * u + 1];
             // offset from the later surface voxel (voxel1) to the earlier one (voxel2)
             const float sg = u < v ? 1.0f : -1.0f;
