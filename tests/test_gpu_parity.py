@@ -106,6 +106,43 @@ def test_graph_chunks_match_single_steps():
     assert np.array_equal(a.time(), b.time())
 
 
+def _expanding(rng, grid_shape, p=1.0):
+    """A self-colliding body: 39 C actuation with CTE 0.01 and EnableExpansion grows
+    voxels to 1.39 voxel sizes, so diagonal neighbours (1.41 apart) touch."""
+    mats = [wl.Material(E=2e5, nu=0.35, cte=0.01), wl.Material(E=1e6, nu=0.35, cte=0.01)]
+    mask = wl.largest_component(rng.random(grid_shape) < p)
+    grid = np.where(mask, rng.integers(1, 3, size=grid_shape), 0).astype(np.uint8)
+    return wl.Robot(grid=grid, materials=mats, phase=rng.random(grid_shape), temp_vary=True, temp_amplitude=39.0,
+                    enable_collision=True, enable_expansion=1, z_offset=1)
+
+
+def test_both_list_builds_match_oracle():
+    """Contact forces and positions against the oracle for a batch that uses both
+    candidate-list builds: a 1030-long two-voxel strip (lattice coordinates past
+    1023, so its lists come from the global hashed grid) and a small body (lists
+    built per robot in shared memory)."""
+    rng = np.random.default_rng(31)
+    robots = [_expanding(rng, (1, 2, 1030)), _expanding(rng, (4, 5, 6), 0.85)]
+    b = abi.Batch(robots, abi.PRECISION_FP64)
+    sims = [ob.oracle_sim(r) for r in robots]
+    for _ in range(3):
+        b.step(20)
+        st, aux = b.state(), b.voxel_aux()
+        for i, (r, s) in enumerate(zip(robots, sims)):
+            s.step(20)
+            err = np.max(np.abs(_robot_slice(b, i, st["pos"]) - s.voxels()["pos"]))
+            assert err <= POS_TOL * r.vox_size, f"robot {i}: {err:.3e}"
+            c, ref = _robot_slice(b, i, aux["contact"]), s.last_contact()
+            assert np.count_nonzero(np.abs(ref).sum(1)) > 0, f"robot {i}: no contacts"
+            np.testing.assert_allclose(c, ref, rtol=1e-6, atol=1e-9 * np.abs(ref).max())
+    assert np.all(b.status() == 0)
+    m = abi.Batch(robots, abi.PRECISION_MIXED)
+    m.step(60)
+    assert np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - b.com(), axis=1) / np.linalg.norm(b.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
+
+
 def test_mixed_com_error_vs_fp64():
     rng = np.random.default_rng(21)
     mats = [wl.Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]

@@ -143,14 +143,19 @@ int recommended_dt_noalloc(const Dev &d, int device, double *out_host, cudaStrea
 // The reference tests every pair of surface voxels each step (gpu_update_attach,
 // VX3_VoxelyzeKernel.cu:833-843).  Here each surface voxel keeps a list of the
 // surface voxels of its robot that were within cutoff + skin when the list was
-// built (a Verlet list: uniform grid of cell edge cutoff + skin, hashed, counting
-// sort).  The lists are rebuilt in a step where any voxel has moved more than
-// half the skin since the last build, so every pair within the cutoff is in the
-// lists; each step the reference's exact test (handle_collision_attachment,
-// :682-704) runs on the listed pairs and the contact forces of VX3_Collision
-// (VX3_Collision.cu:3-31) are summed in ascending partner order -- the order in
-// which the reference's serial pair loop accumulates them -- without atomics.
-// The candidate set is therefore the reference's, pair for pair.
+// built (a Verlet list over a uniform grid of cell edge cutoff + skin).  A robot's
+// lists are rebuilt in a step where any of its voxels has moved more than half the
+// skin since its last build (robots never collide with each other, so the others
+// keep theirs); every pair within the cutoff is therefore listed.  Robots of up to
+// kLocalListMax collision-surface voxels build their lists in shared memory, one
+// CTA per chunk of the robot (k_coll_list_robot, from a work list of the robots
+// due); larger ones use one hashed grid in global memory with a counting sort
+// (k_coll_clear .. k_coll_list).  Each step the reference's exact test
+// (handle_collision_attachment, :682-704) runs on the listed pairs and the contact
+// forces of VX3_Collision (VX3_Collision.cu:3-31) are summed in ascending partner
+// order -- the order in which the reference's serial pair loop accumulates them --
+// without atomics.  A list may hold pairs that are out of reach; they add nothing,
+// so the forces are the reference's, pair for pair, whichever path built the list.
 __device__ __forceinline__ unsigned cell_hash(int cx, int cy, int cz, int r, int hmask) {
     unsigned h = (unsigned)cx * 73856093u ^ (unsigned)cy * 19349663u ^ (unsigned)cz * 83492791u ^ (unsigned)r * 2654435761u;
     h ^= h >> 15;
@@ -169,14 +174,28 @@ __device__ __forceinline__ float4 pos_f(const Dev &d, int v) {
     return make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
 }
 
-// 1. has any voxel moved more than half the skin since the last build?
+// robot r's lists are rebuilt this step; the first voxel to say so puts a robot of the
+// shared-memory path on the work list of k_coll_list_robot
+__device__ __forceinline__ void flag_robot(const Dev &d, int r) {
+    if (*(volatile int *)&d.cflag[1 + r]) return;
+    if (atomicOr(&d.cflag[1 + r], 1) != 0) return;
+    atomicOr(d.cflag, 1);
+    const int k = d.rp[r].lchunks;
+    if (k) {
+        const unsigned long long old = atomicAdd(d.lwork_ctr, (1ull << 32) | (unsigned long long)k);
+        if ((old >> 32) < (unsigned long long)d.nr) d.lwork[old >> 32] = make_int2(r, (int)(old & 0xffffffffull));
+    }
+}
+
+// 1. has a voxel moved more than half the skin since its robot's last build?
 __global__ void k_coll_check(Dev d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const float4 p = pos_f(d, v), q = d.cref[s];  // q.w: squared displacement limit
+    d.cposf[s] = p;  // the positions a rebuild on the shared-memory path lists from
     const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
-    if (ex * ex + ey * ey + ez * ez > q.w) atomicOr(d.cflag, 1);
+    if (ex * ex + ey * ey + ez * ez > q.w) flag_robot(d, (int)d.vinfo[v].x);
 }
 
 __global__ void k_coll_clear(Dev d) {
@@ -190,6 +209,7 @@ __global__ void k_coll_bin(Dev d) {
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
+    if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // rebuilt robots of the hashed-grid path only
     const double ic = d.rp[r].inv_list_cell;
     const double4 p = load_state(d, d.pos, v);
     const int4 c = make_int4((int)floor(p.x * ic), (int)floor(p.y * ic), (int)floor(p.z * ic), r);
@@ -236,6 +256,8 @@ __global__ void k_coll_scatter(Dev d) {
     if (!*d.cflag) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.ns) return;
+    const int r = (int)d.vinfo[d.csurf[s]].x;
+    if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // the voxels k_coll_bin binned this step
     const int4 c = d.ccell[s];
     const int slot = atomicAdd(&d.hfill[cell_hash(c.x, c.y, c.z, c.w, d.hsize - 1)], 1);
     d.hsorted[slot] = s;
@@ -248,6 +270,7 @@ __global__ void k_coll_list(Dev d) {
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
+    if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // lists still valid, or built in shared memory
     const int4 c = d.ccell[s];
     const float4 pf = d.cposf[s];
     const RobotP &rp = d.rp[r];
@@ -298,6 +321,293 @@ __global__ void k_coll_list(Dev d) {
     d.cref[s] = make_float4(pf.x, pf.y, pf.z, lim * lim);
 }
 
+// 2'. lists of the robots on the shared-memory path.  The work list holds the robots
+// due this step, each with its chunks of kLocalListChunk collision-surface voxels;
+// CTA b takes a contiguous range of those chunks.  For a chunk it bins every
+// collision-surface voxel of the chunk's robot into a cell grid in shared memory
+// (counting sort; kept while consecutive chunks belong to the same robot), then three
+// threads list the partners of each voxel of the chunk, in ascending order.  The grid
+// is dense over the robot's bounding box when that has at most kLocalHash cells (the
+// 3 x 3 x 3 neighbourhood is then 9 contiguous runs of buckets), else hashed, with
+// each candidate's cell compared.
+// Shared memory: P[lmax] (FP32 position from the displacement check; w holds the
+// packed lattice coordinates and fixed flag, cpk), cur/beg[kLocalHash] (bucket
+// ends and starts), srt[lmax] (local indices sorted by bucket),
+// cand[kNbrCap][kLocalListThreads] (each thread's sorted sub-list).
+size_t local_list_smem(int lmax) {
+    return (size_t)lmax * sizeof(float4) + 2 * (size_t)kLocalHash * sizeof(int) + (size_t)((lmax + 7) & ~7) * 2 +
+           (size_t)kNbrCap * kLocalListThreads * 2;
+}
+
+struct LocalGrid {
+    float3 mn;    // bounding-box corner
+    float ic;     // 1 / cell edge
+    int3 g;       // cells per axis (dense grid)
+    int dense;
+};
+
+__device__ __forceinline__ int3 local_cell(float4 p, const LocalGrid &G) {
+    int3 c = make_int3((int)floorf((p.x - G.mn.x) * G.ic), (int)floorf((p.y - G.mn.y) * G.ic),
+                       (int)floorf((p.z - G.mn.z) * G.ic));
+    if (G.dense) {
+        c.x = min(max(c.x, 0), G.g.x - 1);
+        c.y = min(max(c.y, 0), G.g.y - 1);
+        c.z = min(max(c.z, 0), G.g.z - 1);
+    }
+    return c;
+}
+
+__device__ __forceinline__ int local_bucket(int3 c, const LocalGrid &G) {
+    return G.dense ? (c.z * G.g.y + c.y) * G.g.x + c.x : (int)cell_hash(c.x, c.y, c.z, 0, kLocalHash - 1);
+}
+
+__global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_list_robot(Dev d) {
+    extern __shared__ __align__(16) unsigned char lsm[];
+    constexpr int T = kLocalListThreads, NW = T / 32;
+    __shared__ int wsum[NW];
+    __shared__ float wbox[6][NW];
+    __shared__ LocalGrid G;
+    float4 *P = reinterpret_cast<float4 *>(lsm);
+    int *cur = reinterpret_cast<int *>(P + d.lmax);
+    int *beg = cur + kLocalHash;
+    unsigned short *srt = reinterpret_cast<unsigned short *>(beg + kLocalHash);
+    unsigned short *cand = srt + ((d.lmax + 7) & ~7);
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+    const unsigned long long w = *d.lwork_ctr;
+    const int nrob = (int)min(w >> 32, (unsigned long long)d.nr), nitem = (int)(w & 0xffffffffull);
+    const int i0 = (int)((long long)nitem * blockIdx.x / gridDim.x);
+    const int i1 = (int)((long long)nitem * (blockIdx.x + 1) / gridDim.x);
+    int built = -1;
+    for (int item = i0; item < i1; item++) {
+        int lo = 0, hi = nrob - 1;  // the last work entry whose first chunk is <= item
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (d.lwork[mid].y <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        const int2 wk = d.lwork[lo];
+        const int r = wk.x;
+        if (r < 0 || r >= d.nr || item < wk.y) continue;  // (uniform) a work list the check did not write
+        const RobotP &rp = d.rp[r];
+        const int n = rp.ns, s0 = rp.soff;
+        if (!rp.lchunks || n > d.lmax) continue;
+        if (r != built) {  // uniform across the CTA
+            __syncthreads();  // the previous robot's table is no longer read
+            for (int h = tid; h < kLocalHash; h += T) cur[h] = 0;
+            float bx0 = INFINITY, by0 = INFINITY, bz0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY, bz1 = -INFINITY;
+            for (int i = tid; i < n; i += T) {
+                const float4 q = d.cposf[s0 + i];
+                P[i] = make_float4(q.x, q.y, q.z, __uint_as_float(d.cpk[s0 + i]));
+                bx0 = fminf(bx0, q.x), by0 = fminf(by0, q.y), bz0 = fminf(bz0, q.z);
+                bx1 = fmaxf(bx1, q.x), by1 = fmaxf(by1, q.y), bz1 = fmaxf(bz1, q.z);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+                by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+                bz0 = fminf(bz0, __shfl_xor_sync(0xffffffffu, bz0, o));
+                bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+                by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+                bz1 = fmaxf(bz1, __shfl_xor_sync(0xffffffffu, bz1, o));
+            }
+            if (lane == 0) {
+                wbox[0][wp] = bx0, wbox[1][wp] = by0, wbox[2][wp] = bz0;
+                wbox[3][wp] = bx1, wbox[4][wp] = by1, wbox[5][wp] = bz1;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                for (int k = 1; k < NW; k++) {
+                    bx0 = fminf(bx0, wbox[0][k]), by0 = fminf(by0, wbox[1][k]), bz0 = fminf(bz0, wbox[2][k]);
+                    bx1 = fmaxf(bx1, wbox[3][k]), by1 = fmaxf(by1, wbox[4][k]), bz1 = fmaxf(bz1, wbox[5][k]);
+                }
+                LocalGrid g;
+                g.ic = (float)rp.inv_list_cell;
+                g.mn = make_float3(bx0, by0, bz0);
+                const float ex = (bx1 - bx0) * g.ic, ey = (by1 - by0) * g.ic, ez = (bz1 - bz0) * g.ic;
+                g.dense = 0;
+                g.g = make_int3(1, 1, 1);
+                // finite extents below kLocalHash cells per axis (NaN fails every comparison)
+                if (ex >= 0.0f && ey >= 0.0f && ez >= 0.0f && ex < (float)kLocalHash && ey < (float)kLocalHash &&
+                    ez < (float)kLocalHash) {
+                    const int gx = (int)ex + 1, gy = (int)ey + 1, gz = (int)ez + 1;
+                    if ((long long)gx * gy * gz <= kLocalHash) {
+                        g.g = make_int3(gx, gy, gz);
+                        g.dense = 1;
+                    }
+                }
+                if (!g.dense && !(bx0 <= bx1 && by0 <= by1 && bz0 <= bz1))
+                    g.mn = make_float3(0.0f, 0.0f, 0.0f);  // non-finite box: absolute cells
+                G = g;
+            }
+            __syncthreads();
+            const LocalGrid g = G;
+            for (int i = tid; i < n; i += T) atomicAdd(&cur[local_bucket(local_cell(P[i], g), g)], 1);
+            __syncthreads();
+            // exclusive scan of the bucket counts, kLocalHash / T buckets per thread
+            constexpr int per = kLocalHash / T;
+            int sum = 0;
+#pragma unroll
+            for (int k = 0; k < per; k++) sum += cur[tid * per + k];
+            int x = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) wsum[wp] = x;
+            __syncthreads();
+            if (wp == 0) {
+                int t = lane < NW ? wsum[lane] : 0;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, t, o);
+                    if (lane >= o) t += y;
+                }
+                if (lane < NW) wsum[lane] = t;
+            }
+            __syncthreads();
+            int e = x - sum + (wp ? wsum[wp - 1] : 0);
+#pragma unroll
+            for (int k = 0; k < per; k++) {
+                const int ck = cur[tid * per + k];
+                beg[tid * per + k] = e;
+                cur[tid * per + k] = e;
+                e += ck;
+            }
+            __syncthreads();
+            for (int i = tid; i < n; i += T) {
+                const int slot = atomicAdd(&cur[local_bucket(local_cell(P[i], g), g)], 1);
+                if (slot < n) srt[slot] = (unsigned short)i;  // bucket h: srt[beg[h] .. cur[h])
+            }
+            __syncthreads();
+            built = r;
+        }
+        // three threads per voxel (a trio), thread q of the trio scanning the plane
+        // dz = q - 1 of the 3 x 3 x 3 neighbourhood; ten trios per warp, the voxels taken
+        // in bucket order so that a warp's trios work on neighbouring cells
+        const int trio = lane / 3, q = lane - 3 * trio, tb = lane - q;
+        const int pos = (item - wk.y) * kLocalListChunk + wp * 10 + trio;
+        const bool valid = lane < 30 && pos < n && item - wk.y < rp.lchunks;
+        unsigned short *my = cand + tid;  // this thread's sub-list, entry j at my[j*T]
+        int nc = 0, i = 0;
+        float4 pi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (valid) {
+            const LocalGrid g = G;
+            i = srt[pos];
+            pi = P[i];
+            const unsigned ki = __float_as_uint(pi.w);
+            const int3 c = local_cell(pi, g);
+            // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
+            const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
+            const int z = c.z + q - 1;
+            if (!g.dense || (z >= 0 && z < g.g.z)) {
+                for (int dy = -1; dy <= 1; dy++) {
+                    const int y = c.y + dy;
+                    if (g.dense && (y < 0 || y >= g.g.y)) continue;
+                    // dense grid: one run of buckets, cells x-1 .. x+1; hashed grid: the three
+                    // cells one by one, each candidate's cell compared
+                    for (int dx = -1; dx <= (g.dense ? -1 : 1); dx++) {
+                        int b, e;
+                        if (g.dense) {
+                            const int rw = (z * g.g.y + y) * g.g.x;
+                            b = beg[rw + max(c.x - 1, 0)];
+                            e = cur[rw + min(c.x + 1, g.g.x - 1)];
+                        } else {
+                            const int h = (int)cell_hash(c.x + dx, y, z, 0, kLocalHash - 1);
+                            b = beg[h];
+                            e = cur[h];
+                        }
+                        e = min(e, n);
+                        for (int k = b; k < e; k++) {
+                            const int t = srt[k];
+                            const float4 pt = P[t];
+                            const float ex = pt.x - pi.x, ey = pt.y - pi.y, ez = pt.z - pi.z;
+                            const unsigned kt = __float_as_uint(pt.w);
+                            // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): linked <=>
+                            // face-adjacent <=> the packed lattice difference is +-1, +-2^10 or +-2^20
+                            const int ad = abs((int)(ki & kPackMask) - (int)(kt & kPackMask));
+                            bool acc = ex * ex + ey * ey + ez * ez <= cut2 && t != i && ad != 1 && ad != (1 << 10) &&
+                                       ad != (1 << 20) && !(ki & kt & kPackFixed);
+                            if (!g.dense) {
+                                const int3 ct = local_cell(pt, g);
+                                acc = acc && ct.x == c.x + dx && ct.y == y && ct.z == z;  // same bucket, other cell
+                            }
+                            if (acc) {
+                                if (nc < kNbrCap) my[nc * T] = (unsigned short)t;
+                                nc++;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        const bool overflow = nc > kNbrCap;
+        nc = min(nc, kNbrCap);
+        for (int a2 = 1; a2 < nc; a2++) {  // ascending
+            const int x = my[a2 * T];
+            int j = a2;
+            while (j > 0 && my[(j - 1) * T] > x) {
+                my[j * T] = my[(j - 1) * T];
+                j--;
+            }
+            my[j * T] = (unsigned short)x;
+        }
+        // merge the trio's three disjoint sorted sub-lists: an entry's place in the list
+        // is its index in its own sub-list plus the entries below it in the other two
+        int c3[3];
+        bool ov3 = false;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            c3[k] = __shfl_sync(0xffffffffu, nc, (tb + k) & 31);
+            ov3 |= __shfl_sync(0xffffffffu, overflow ? 1 : 0, (tb + k) & 31) != 0;
+        }
+        __syncwarp();
+        if (valid) {
+            // the robot's collision-surface voxels are in ascending voxel order, so
+            // ascending local index is the ascending partner order of the reference
+            const int s = s0 + i;
+            int *out = d.nbr + s;
+            const size_t ns = (size_t)d.ns;
+            for (int j = 0; j < nc; j++) {
+                const int e = my[j * T];
+                int rank = j;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    if (k == q) continue;
+                    const unsigned short *o = cand + (tid - q + k);
+                    int m = 0;
+                    while (m < c3[k] && o[m * T] < e) m++;
+                    rank += m;
+                }
+                if (rank < kNbrCap) out[rank * ns] = d.csurf[s0 + e];
+            }
+            if (q == 0) {
+                const int total = c3[0] + c3[1] + c3[2];
+                d.nnb[s] = min(total, kNbrCap);
+                if (ov3 || total > kNbrCap) atomicOr(&d.status[r], 2);
+                const float lim = 0.49f * (float)rp.skin;  // rebuild when a voxel has moved farther than this
+                d.cref[s] = make_float4(pi.x, pi.y, pi.z, lim * lim);
+            }
+        }
+    }
+}
+
+cudaError_t init_collision(Dev &d) {
+    d.lgrid = 0;
+    if (!d.lmax) return cudaSuccess;
+    const size_t sm = local_list_smem(d.lmax);
+    cudaError_t e = cudaFuncSetAttribute(k_coll_list_robot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 0, occ = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_coll_list_robot, kLocalListThreads, sm)) !=
+        cudaSuccess)
+        return e;
+    d.lgrid = nsm * (occ > 0 ? occ : 1);
+    return cudaSuccess;
+}
+
 // force on voxel1 from the pair (voxel1, voxel2) as VX3_Collision computes it
 __device__ __forceinline__ V3<double> pair_force(const Dev &d, int v1, int v2, double bsa1, double bsa2) {
     const VMat &m1 = d.vmat[d.vinfo[v1].y >> 8];
@@ -320,10 +630,14 @@ __device__ __forceinline__ V3<double> pair_force(const Dev &d, int v1, int v2, d
 // 3. exact test and contact forces on the listed pairs, ascending partner order
 __global__ void k_coll_eval(Dev d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) *d.cflag = 0;  // the rebuild (if any) is done; the next check starts clear
+    if (s == 0) {  // the rebuild (if any) is done; the next check starts clear
+        *d.cflag = 0;
+        *d.lwork_ctr = 0ull;
+    }
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
+    if (d.cflag[1 + r]) d.cflag[1 + r] = 0;
     if (d.status[r] != 0) return;
     const int n = d.nnb[s];
     const int *lst = d.nbr + s;  // slot-major: entry k at lst[k*ns]
@@ -370,8 +684,9 @@ __global__ void k_coll_check_cond(Dev d, cudaGraphConditionalHandle h) {
     if (s < d.ns) {
         const int v = d.csurf[s];
         const float4 p = pos_f(d, v), q = d.cref[s];  // q.w: squared displacement limit
+        d.cposf[s] = p;  // the positions a rebuild on the shared-memory path lists from
         const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
-        if (ex * ex + ey * ey + ez * ez > q.w) atomicOr(d.cflag, 1);
+        if (ex * ex + ey * ey + ez * ez > q.w) flag_robot(d, (int)d.vinfo[v].x);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -386,12 +701,15 @@ __global__ void k_coll_check_cond(Dev d, cudaGraphConditionalHandle h) {
 }
 
 static void enqueue_rebuild(const Dev &d, int g, cudaStream_t s) {
-    k_coll_clear<<<152 * 4, 256, 0, s>>>(d);
-    k_coll_bin<<<g, 256, 0, s>>>(d);
-    k_scan_blocks<<<d.hsize / 1024, 1024, 0, s>>>(d);
-    k_scan_add<<<d.hsize / 1024, 1024, 0, s>>>(d);
-    k_coll_scatter<<<g, 256, 0, s>>>(d);
-    k_coll_list<<<g, 256, 0, s>>>(d);
+    if (d.nhash) {
+        k_coll_clear<<<152 * 4, 256, 0, s>>>(d);
+        k_coll_bin<<<g, 256, 0, s>>>(d);
+        k_scan_blocks<<<d.hsize / 1024, 1024, 0, s>>>(d);
+        k_scan_add<<<d.hsize / 1024, 1024, 0, s>>>(d);
+        k_coll_scatter<<<g, 256, 0, s>>>(d);
+        k_coll_list<<<g, 256, 0, s>>>(d);
+    }
+    if (d.lmax) k_coll_list_robot<<<d.lgrid, kLocalListThreads, local_list_smem(d.lmax), s>>>(d);
 }
 
 cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side) {
@@ -428,7 +746,8 @@ cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side) {
             return e;
     } else {
         // outside a graph: every rebuild kernel runs and returns at once unless the flag is set
-        cudaMemsetAsync(d.cflag, 0, sizeof(int), s);
+        cudaMemsetAsync(d.cflag, 0, sizeof(int) * (1 + (size_t)d.nr), s);
+        cudaMemsetAsync(d.lwork_ctr, 0, sizeof(unsigned long long), s);
         k_coll_check<<<g, 256, 0, s>>>(d);
         enqueue_rebuild(d, g, s);
     }

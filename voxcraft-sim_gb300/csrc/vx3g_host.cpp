@@ -423,6 +423,13 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             if (!interior && R.enable_collision) csurf.push_back(v);
         }
         rp.ns = (int)csurf.size() - rp.soff;
+        // lists in shared memory when the robot fits (lattice coordinates below 512, packed in 10 bits each)
+        int cmax = 0;
+        for (int k = 0; k < nvr; k++) {
+            const short4 q = c->ijk[v0 + k];
+            cmax = std::max(cmax, (int)std::max(q.x, std::max(q.y, q.z)));
+        }
+        rp.lchunks = rp.ns > 0 && rp.ns <= kLocalListMax && cmax < 512 ? (rp.ns + kLocalListChunk - 1) / kLocalListChunk : 0;
     }
     c->voff[c->nr] = (int)pos.size();
     c->loff[c->nr] = (int)c->ends.size();
@@ -465,17 +472,31 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     if ((rc = c->alloc(&d.dt, d.nr)) || (rc = c->alloc(&d.T, 2 * (size_t)d.nr)) || (rc = c->alloc(&d.status, d.nr)) ||
         (rc = c->alloc(&d.err, 1)) || (rc = c->alloc(&c->scratch, 4 * (size_t)d.nr + 4)))
         return rc;
-    // collision tables
+    // collision tables: robots on the shared-memory path (lchunks > 0) and the global hashed grid
+    d.lmax = 0;
+    d.nhash = 0;
+    std::vector<unsigned> cpk(csurf.size(), 0u);
+    for (const RobotP &q : rps) {
+        if (q.lchunks) d.lmax = std::max(d.lmax, q.ns);
+        else d.nhash += q.ns;
+        for (int k = 0; q.lchunks && k < q.ns; k++) {
+            const int v = csurf[q.soff + k];
+            const short4 l = c->ijk[v];
+            cpk[q.soff + k] = (unsigned)l.x | (unsigned)l.y << 10 | (unsigned)l.z << 20 | ((vinfo[v].y & VF_FIXED) ? kPackFixed : 0u);
+        }
+    }
     int hs = 1024;
-    while (hs < d.ns) hs <<= 1;
+    while (hs < d.nhash) hs <<= 1;
     d.hsize = hs;
     if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.cposf, d.ns)) ||
-        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1)) || (rc = c->alloc(&d.ccount, 1)) ||
+        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1 + (size_t)d.nr)) || (rc = c->alloc(&d.ccount, 1)) ||
         (rc = c->upload(&d.cref, std::vector<float4>((size_t)d.ns, make_float4(1e30f, 1e30f, 1e30f, 0.0f)))) ||
         (rc = c->alloc(&d.hcount, hs)) ||
         (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.hsorted, d.ns)) ||
-        (rc = c->alloc(&d.hblock, hs / 1024)))
+        (rc = c->alloc(&d.hblock, hs / 1024)) || (rc = c->alloc(&d.lwork, (size_t)d.nr)) || (rc = c->upload(&d.cpk, cpk)) ||
+        (rc = c->alloc(&d.lwork_ctr, 1)))
         return rc;
+    CU(init_collision(d));
 
     launch_init_temperature(d, c->precision == VX3G_PRECISION_MIXED, c->stream);
     launch_dt(d, c->scratch, c->stream);

@@ -67,11 +67,22 @@ struct RobotP {
     double inv_list_cell;  // 1 / (cell_size + skin): grid used to build the lists
     int voff, nv, loff, nl, soff, ns;
     int floor, vary_temp, expansion, collision;
+    int lchunks;  // > 0: lists built in shared memory (k_coll_list_robot), in this many chunks; 0: global hashed grid
 };
 
 template <class R> struct Slot { R f[3]; R m[3]; };
 
 constexpr int kNbrCap = 64;  // contact candidates kept per collision-surface voxel
+// per-robot list build in shared memory: robots with at most kLocalListMax collision-surface
+// voxels and lattice coordinates below 512, chunks of kLocalListChunk voxels (ten per warp,
+// three threads per voxel)
+constexpr int kLocalListMax = 6144;
+constexpr int kLocalListThreads = 512;
+constexpr int kLocalListChunk = kLocalListThreads / 32 * 10;
+// packed lattice word of a voxel on that path: x | y << 10 | z << 20 | fixed << 31 (coordinates
+// below 512, so the difference of two packed words is face-adjacent iff it is +-1, +-2^10 or +-2^20)
+constexpr unsigned kPackMask = 0x3fffffffu, kPackFixed = 0x80000000u;
+constexpr int kLocalHash = 4096;  // buckets of the shared-memory grid (power of two)
 
 struct Dev {
     // voxels
@@ -97,12 +108,18 @@ struct Dev {
     // collision
     int *csurf;     // collision surface list (global voxel index), NS entries
     int4 *ccell;    // cell coords + robot per collision-surface voxel
-    float4 *cposf;  // FP32 copy of the position (prefilter) per collision-surface voxel
+    float4 *cposf;  // FP32 position per collision-surface voxel, written by the displacement check
+    unsigned *cpk;  // per collision-surface voxel: packed lattice word (kPackMask, kPackFixed; shared-memory path)
     float4 *cref;   // position at the last list build (w: squared displacement that forces a rebuild)
     int *nbr;       // candidate lists, slot-major [kNbrCap][NS]: partner voxel indices, ascending
     int *nnb;       // candidate count per collision-surface voxel
-    int *cflag;     // 1: rebuild the candidate lists this step
+    int *cflag;     // [1 + NR]: [0] some robot's lists are rebuilt this step, [1 + r] robot r's are
     unsigned *ccount;  // blocks of the displacement check that have finished (graph path)
+    int2 *lwork;    // [NR] robots whose lists are rebuilt in shared memory this step: (robot, first chunk)
+    unsigned long long *lwork_ctr;  // (robots << 32) | chunks listed in lwork; cleared by the narrow phase
+    int lmax;       // most collision-surface voxels of a robot on the shared-memory path (0: none)
+    int lgrid;      // CTAs of k_coll_list_robot
+    int nhash;      // collision-surface voxels on the global hashed-grid path
     int *hcount, *hstart, *hfill, *hsorted, *hblock;
     int hsize;      // power of two
     int *err;       // device error word
@@ -137,6 +154,8 @@ void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 // surface-voxel collision of one step; `side` (optional) is a helper stream used when
 // `s` is being captured into a CUDA graph (the list rebuild becomes a conditional node)
 cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side);
+// one-time setup of the list-build kernels (shared-memory size, grid); fills d.lgrid
+cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);
 void launch_coll_eval(const Dev &d, cudaStream_t s);  // the contact evaluation alone
 void launch_com(const Dev &d, double *out4, cudaStream_t s);

@@ -75,11 +75,15 @@ __device__ __forceinline__ V3<float> rotvec_f(float w, V3<float> v) {
 // in ascending partner order as the FP64 pass does.
 __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) *d.cflag = 0;  // the rebuild (if any) is done; the next check starts clear
+    if (s == 0) {  // the rebuild (if any) is done; the next check starts clear
+        *d.cflag = 0;
+        *d.lwork_ctr = 0ull;
+    }
     if (s >= d.ns) return;
     const int v = d.csurf[s];
     const uint2 vi = d.vinfo[v];
     const int r = (int)vi.x;
+    if (d.cflag[1 + r]) d.cflag[1 + r] = 0;
     if (d.status[r] != 0) return;
     const int n = d.nnb[s];
     const int *lst = d.nbr + s;  // slot-major: entry k at lst[k*ns]
