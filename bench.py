@@ -323,8 +323,7 @@ def main():
     ap.add_argument("--tune-cache", default=None, help="JSON cache of tuned launch shapes (read and appended)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every step's kernels one by one instead of replaying CUDA graphs "
-                         "(what a per-kernel profiler can attribute; the list rebuild kernels then run "
-                         "every step and return at once unless a rebuild is due)")
+                         "(each launch then its own record in a per-kernel profiler)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

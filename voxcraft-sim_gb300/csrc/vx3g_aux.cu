@@ -148,9 +148,10 @@ int recommended_dt_noalloc(const Dev &d, int device, double *out_host, cudaStrea
 // skin since its last build (robots never collide with each other, so the others
 // keep theirs); every pair within the cutoff is therefore listed.  Robots of up to
 // kLocalListMax collision-surface voxels build their lists in shared memory, one
-// CTA per chunk of the robot (k_coll_list_robot, from a work list of the robots
+// CTA per chunk of the robot (coll_list_robots, from a work list of the robots
 // due); larger ones use one hashed grid in global memory with a counting sort
-// (k_coll_clear .. k_coll_list).  Each step the reference's exact test
+// (coll_bin .. coll_list).  The check and the rebuild run in one cooperative kernel
+// (k_coll_prepare).  Each step the reference's exact test
 // (handle_collision_attachment, :682-704) runs on the listed pairs and the contact
 // forces of VX3_Collision (VX3_Collision.cu:3-31) are summed in ascending partner
 // order -- the order in which the reference's serial pair loop accumulates them --
@@ -175,7 +176,7 @@ __device__ __forceinline__ float4 pos_f(const Dev &d, int v) {
 }
 
 // robot r's lists are rebuilt this step; the first voxel to say so puts a robot of the
-// shared-memory path on the work list of k_coll_list_robot
+// shared-memory path on the work list of coll_list_robots
 __device__ __forceinline__ void flag_robot(const Dev &d, int r) {
     if (*(volatile int *)&d.cflag[1 + r]) return;
     if (atomicOr(&d.cflag[1 + r], 1) != 0) return;
@@ -187,10 +188,8 @@ __device__ __forceinline__ void flag_robot(const Dev &d, int r) {
     }
 }
 
-// 1. has a voxel moved more than half the skin since its robot's last build?
-__global__ void k_coll_check(Dev d) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.ns) return;
+// 1. has surface voxel s moved more than half the skin since its robot's last build?
+__device__ __forceinline__ void coll_check(const Dev &d, int s) {
     const int v = d.csurf[s];
     const float4 p = pos_f(d, v), q = d.cref[s];  // q.w: squared displacement limit
     d.cposf[s] = p;  // the positions a rebuild on the shared-memory path lists from
@@ -198,15 +197,8 @@ __global__ void k_coll_check(Dev d) {
     if (ex * ex + ey * ey + ez * ez > q.w) flag_robot(d, (int)d.vinfo[v].x);
 }
 
-__global__ void k_coll_clear(Dev d) {
-    if (!*d.cflag) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.hsize; i += gridDim.x * blockDim.x) d.hcount[i] = 0;
-}
-
-__global__ void k_coll_bin(Dev d) {
-    if (!*d.cflag) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.ns) return;
+// hashed-grid path: bin the surface voxels of the due robots
+__device__ __forceinline__ void coll_bin(const Dev &d, int s) {
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
     if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // rebuilt robots of the hashed-grid path only
@@ -218,56 +210,77 @@ __global__ void k_coll_bin(Dev d) {
     atomicAdd(&d.hcount[cell_hash(c.x, c.y, c.z, c.w, d.hsize - 1)], 1);
 }
 
-// exclusive scan of hcount in blocks of 1024 (hsize is a multiple of 1024)
-__global__ void __launch_bounds__(1024) k_scan_blocks(Dev d) {
-    if (!*d.cflag) return;
-    __shared__ int sh[1024];
-    const int i = blockIdx.x * 1024 + threadIdx.x;
-    const int x = d.hcount[i];
-    sh[threadIdx.x] = x;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const int y = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
-        __syncthreads();
-        sh[threadIdx.x] += y;
-        __syncthreads();
+// exclusive scan of the inclusive-to-be value x over the kLocalListThreads threads of
+// the block; returns the exclusive prefix, *total the block's sum (wsum: NW ints)
+__device__ __forceinline__ int block_scan(int x, int *wsum, int *total) {
+    constexpr int NW = kLocalListThreads / 32;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    int y = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) y += t;
     }
-    d.hstart[i] = sh[threadIdx.x] - x;
-    if (threadIdx.x == 1023) d.hblock[blockIdx.x] = sh[1023];
+    __syncthreads();  // wsum is free
+    if (lane == 31) wsum[wp] = y;
+    __syncthreads();
+    if (wp == 0) {
+        int t = lane < NW ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += u;
+        }
+        if (lane < NW) wsum[lane] = t;
+    }
+    __syncthreads();
+    *total = wsum[NW - 1];
+    return y - x + (wp ? wsum[wp - 1] : 0);
 }
 
-__global__ void __launch_bounds__(1024) k_scan_add(Dev d) {
-    if (!*d.cflag) return;
-    __shared__ int base;
+// exclusive scan of hcount segment b (1024 buckets; hsize is a multiple of 1024), two
+// buckets per thread; the segment's sum goes to hblock[b]
+__device__ __forceinline__ void coll_scan_segment(const Dev &d, int b, int *wsum) {
+    const int i = b * 1024 + 2 * (int)threadIdx.x;
+    const int x0 = d.hcount[i], x1 = d.hcount[i + 1];
+    int total;
+    const int e = block_scan(x0 + x1, wsum, &total);
+    d.hstart[i] = e;
+    d.hstart[i + 1] = e + x0;
+    if (threadIdx.x == 0) d.hblock[b] = total;
+}
+
+// add the sums of the segments before b to segment b; fill cursors start there
+__device__ __forceinline__ void coll_scan_add(const Dev &d, int b, int *wsum) {
     if (threadIdx.x < 32) {
         int acc = 0;
-        for (int b = threadIdx.x; b < (int)blockIdx.x; b += 32) acc += d.hblock[b];
+        for (int k = threadIdx.x; k < b; k += 32) acc += d.hblock[k];
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (threadIdx.x == 0) base = acc;
+        __syncwarp();
+        if (threadIdx.x == 0) wsum[0] = acc;
     }
     __syncthreads();
-    const int i = blockIdx.x * 1024 + threadIdx.x;
-    const int v = d.hstart[i] + base;
-    d.hstart[i] = v;
-    d.hfill[i] = v;
+    const int base = wsum[0];
+    const int i = b * 1024 + 2 * (int)threadIdx.x;
+    const int v0 = d.hstart[i] + base, v1 = d.hstart[i + 1] + base;
+    d.hstart[i] = v0;
+    d.hstart[i + 1] = v1;
+    d.hfill[i] = v0;
+    d.hfill[i + 1] = v1;
+    __syncthreads();  // wsum is reused
 }
 
-__global__ void k_coll_scatter(Dev d) {
-    if (!*d.cflag) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.ns) return;
+__device__ __forceinline__ void coll_scatter(const Dev &d, int s) {
     const int r = (int)d.vinfo[d.csurf[s]].x;
-    if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // the voxels k_coll_bin binned this step
+    if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // the voxels coll_bin binned this step
     const int4 c = d.ccell[s];
     const int slot = atomicAdd(&d.hfill[cell_hash(c.x, c.y, c.z, c.w, d.hsize - 1)], 1);
     d.hsorted[slot] = s;
 }
 
 // 2. list every unlinked surface voxel of the same robot within cutoff + skin, ascending
-__global__ void k_coll_list(Dev d) {
-    if (!*d.cflag) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.ns) return;
+__device__ __forceinline__ void coll_list(const Dev &d, int s) {
     const int v = d.csurf[s];
     const int r = (int)d.vinfo[v].x;
     if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // lists still valid, or built in shared memory
@@ -361,10 +374,8 @@ __device__ __forceinline__ int local_bucket(int3 c, const LocalGrid &G) {
     return G.dense ? (c.z * G.g.y + c.y) * G.g.x + c.x : (int)cell_hash(c.x, c.y, c.z, 0, kLocalHash - 1);
 }
 
-__global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_list_robot(Dev d) {
-    extern __shared__ __align__(16) unsigned char lsm[];
+__device__ __forceinline__ void coll_list_robots(const Dev &d, unsigned char *lsm, int *wsum) {
     constexpr int T = kLocalListThreads, NW = T / 32;
-    __shared__ int wsum[NW];
     __shared__ float wbox[6][NW];
     __shared__ LocalGrid G;
     float4 *P = reinterpret_cast<float4 *>(lsm);
@@ -373,7 +384,7 @@ __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_list_robot(Dev d)
     unsigned short *srt = reinterpret_cast<unsigned short *>(beg + kLocalHash);
     unsigned short *cand = srt + ((d.lmax + 7) & ~7);
     const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
-    const unsigned long long w = *d.lwork_ctr;
+    const unsigned long long w = *(volatile unsigned long long *)d.lwork_ctr;
     const int nrob = (int)min(w >> 32, (unsigned long long)d.nr), nitem = (int)(w & 0xffffffffull);
     const int i0 = (int)((long long)nitem * blockIdx.x / gridDim.x);
     const int i1 = (int)((long long)nitem * (blockIdx.x + 1) / gridDim.x);
@@ -382,10 +393,10 @@ __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_list_robot(Dev d)
         int lo = 0, hi = nrob - 1;  // the last work entry whose first chunk is <= item
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (d.lwork[mid].y <= item) lo = mid;
+            if (__ldcg(&d.lwork[mid].y) <= item) lo = mid;
             else hi = mid - 1;
         }
-        const int2 wk = d.lwork[lo];
+        const int2 wk = __ldcg(&d.lwork[lo]);
         const int r = wk.x;
         if (r < 0 || r >= d.nr || item < wk.y) continue;  // (uniform) a work list the check did not write
         const RobotP &rp = d.rp[r];
@@ -396,7 +407,7 @@ __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_list_robot(Dev d)
             for (int h = tid; h < kLocalHash; h += T) cur[h] = 0;
             float bx0 = INFINITY, by0 = INFINITY, bz0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY, bz1 = -INFINITY;
             for (int i = tid; i < n; i += T) {
-                const float4 q = d.cposf[s0 + i];
+                const float4 q = __ldcg(&d.cposf[s0 + i]);
                 P[i] = make_float4(q.x, q.y, q.z, __uint_as_float(d.cpk[s0 + i]));
                 bx0 = fminf(bx0, q.x), by0 = fminf(by0, q.y), bz0 = fminf(bz0, q.z);
                 bx1 = fmaxf(bx1, q.x), by1 = fmaxf(by1, q.y), bz1 = fmaxf(bz1, q.z);
@@ -592,19 +603,80 @@ __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_list_robot(Dev d)
     }
 }
 
+// Barrier across the CTAs of the cooperative k_coll_prepare (a cooperative launch
+// keeps them all resident).  gbar[0] counts arrivals, gbar[1] is the generation; the
+// last CTA to arrive resets the count and advances the generation.  A CTA that has
+// waited kBarrierPolls polls records bit 1 in d.err and returns false.
+constexpr unsigned kBarrierPolls = 1u << 22;
+
+__device__ bool grid_barrier(const Dev &d) {
+    __shared__ int passed;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = d.gbar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(d.gbar, 1u) == gridDim.x - 1) {
+            atomicExch(d.gbar, 0u);
+            __threadfence();
+            atomicAdd(d.gbar + 1, 1u);
+            passed = 1;
+        } else {
+            unsigned k = 0;
+            while (*gen == g && ++k < kBarrierPolls) __nanosleep(32);
+            passed = *gen != g;
+            if (!passed) atomicOr(d.err, 1);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return passed != 0;
+}
+
+// The collision pass before the narrow phase, one cooperative launch per step: the
+// displacement check of every surface voxel; then, only in a step where some robot
+// is due, the rebuild of its lists (hashed-grid phases separated by grid barriers,
+// and the shared-memory path).  No host or graph decision sits between them.
+__global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_prepare(Dev d) {
+    extern __shared__ __align__(16) unsigned char lsm[];
+    __shared__ int wsum[kLocalListThreads / 32];
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    for (int s = gt; s < d.ns; s += gs) coll_check(d, s);
+    if (!grid_barrier(d)) return;
+    if (!*(volatile int *)d.cflag) return;  // (uniform) no robot is due
+    if (d.nhash) {
+        for (int i = gt; i < d.hsize; i += gs) d.hcount[i] = 0;
+        if (!grid_barrier(d)) return;
+        for (int s = gt; s < d.ns; s += gs) coll_bin(d, s);
+        if (!grid_barrier(d)) return;
+        for (int b = blockIdx.x; b < d.hsize / 1024; b += gridDim.x) coll_scan_segment(d, b, wsum);
+        if (!grid_barrier(d)) return;
+        for (int b = blockIdx.x; b < d.hsize / 1024; b += gridDim.x) coll_scan_add(d, b, wsum);
+        if (!grid_barrier(d)) return;
+        for (int s = gt; s < d.ns; s += gs) coll_scatter(d, s);
+        if (!grid_barrier(d)) return;
+        for (int s = gt; s < d.ns; s += gs) {
+            const int r = (int)d.vinfo[d.csurf[s]].x;
+            if (d.cflag[1 + r] && !d.rp[r].lchunks) coll_list(d, s);
+        }
+    }
+    if (d.lmax) coll_list_robots(d, lsm, wsum);
+}
+
 cudaError_t init_collision(Dev &d) {
-    d.lgrid = 0;
-    if (!d.lmax) return cudaSuccess;
-    const size_t sm = local_list_smem(d.lmax);
-    cudaError_t e = cudaFuncSetAttribute(k_coll_list_robot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    d.cgrid = 0;
+    if (!d.ns) return cudaSuccess;
+    const size_t sm = d.lmax ? local_list_smem(d.lmax) : 0;
+    cudaError_t e = cudaFuncSetAttribute(k_coll_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     int dev = 0, nsm = 0, occ = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_coll_list_robot, kLocalListThreads, sm)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_coll_prepare, kLocalListThreads, sm)) !=
         cudaSuccess)
         return e;
-    d.lgrid = nsm * (occ > 0 ? occ : 1);
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    d.cgrid = nsm * occ;  // every CTA resident: the grid barrier's premise
     return cudaSuccess;
 }
 
@@ -677,80 +749,28 @@ __global__ void k_coll_eval(Dev d) {
     d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
 }
 
-// 1'. the displacement check inside a CUDA graph: the last block to finish sets the
-// conditional node that runs the list rebuild (threadfence-reduction pattern, no wait)
-__global__ void k_coll_check_cond(Dev d, cudaGraphConditionalHandle h) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < d.ns) {
-        const int v = d.csurf[s];
-        const float4 p = pos_f(d, v), q = d.cref[s];  // q.w: squared displacement limit
-        d.cposf[s] = p;  // the positions a rebuild on the shared-memory path lists from
-        const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
-        if (ex * ex + ey * ey + ez * ez > q.w) flag_robot(d, (int)d.vinfo[v].x);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned prev = atomicAdd(d.ccount, 1u);
-        if (prev == gridDim.x - 1) {
-            __threadfence();
-            cudaGraphSetConditional(h, atomicOr(d.cflag, 0) ? 1u : 0u);
-            *d.ccount = 0;
-        }
-    }
-}
-
-static void enqueue_rebuild(const Dev &d, int g, cudaStream_t s) {
-    if (d.nhash) {
-        k_coll_clear<<<152 * 4, 256, 0, s>>>(d);
-        k_coll_bin<<<g, 256, 0, s>>>(d);
-        k_scan_blocks<<<d.hsize / 1024, 1024, 0, s>>>(d);
-        k_scan_add<<<d.hsize / 1024, 1024, 0, s>>>(d);
-        k_coll_scatter<<<g, 256, 0, s>>>(d);
-        k_coll_list<<<g, 256, 0, s>>>(d);
-    }
-    if (d.lmax) k_coll_list_robot<<<d.lgrid, kLocalListThreads, local_list_smem(d.lmax), s>>>(d);
-}
-
-cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side) {
+cudaError_t launch_collision(const Dev &d, cudaStream_t s) {
     if (!d.ns) return cudaSuccess;
-    const int g = (d.ns + 255) / 256;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaError_t e = cudaStreamIsCapturing(s, &cs);
     if (e != cudaSuccess) return e;
-    if (cs == cudaStreamCaptureStatusActive && side) {
-        // in a graph: check, then IF(rebuild due) { rebuild }, then the narrow phase
-        cudaGraph_t graph;
-        const cudaGraphNode_t *deps = nullptr;
-        size_t nd = 0;
-        if ((e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, nullptr, nullptr, nullptr)) != cudaSuccess) return e;
-        cudaGraphConditionalHandle h;
-        if ((e = cudaGraphConditionalHandleCreate(&h, graph, 0, 0)) != cudaSuccess) return e;
-        k_coll_check_cond<<<g, 256, 0, s>>>(d, h);
-        if ((e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &nd)) != cudaSuccess) return e;
-        cudaGraphNodeParams p{};
-        p.type = cudaGraphNodeTypeConditional;
-        p.conditional.handle = h;
-        p.conditional.type = cudaGraphCondTypeIf;
-        p.conditional.size = 1;
-        cudaGraphNode_t node;
-        if ((e = cudaGraphAddNode(&node, graph, deps, nullptr, nd, &p)) != cudaSuccess) return e;
-        cudaGraph_t body = p.conditional.phGraph_out[0];
-        if ((e = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
-            cudaSuccess)
+    if (cs == cudaStreamCaptureStatusNone) {
+        // single steps start from clear flags (inside graphs the narrow phase clears them)
+        if ((e = cudaMemsetAsync(d.cflag, 0, sizeof(int) * (1 + (size_t)d.nr), s)) != cudaSuccess ||
+            (e = cudaMemsetAsync(d.lwork_ctr, 0, sizeof(unsigned long long), s)) != cudaSuccess)
             return e;
-        enqueue_rebuild(d, g, side);
-        if ((e = cudaStreamEndCapture(side, &body)) != cudaSuccess) return e;
-        if ((e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
-            cudaSuccess)
-            return e;
-    } else {
-        // outside a graph: every rebuild kernel runs and returns at once unless the flag is set
-        cudaMemsetAsync(d.cflag, 0, sizeof(int) * (1 + (size_t)d.nr), s);
-        cudaMemsetAsync(d.lwork_ctr, 0, sizeof(unsigned long long), s);
-        k_coll_check<<<g, 256, 0, s>>>(d);
-        enqueue_rebuild(d, g, s);
     }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)d.cgrid);
+    cfg.blockDim = dim3(kLocalListThreads);
+    cfg.dynamicSmemBytes = d.lmax ? local_list_smem(d.lmax) : 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if ((e = cudaLaunchKernelEx(&cfg, k_coll_prepare, d)) != cudaSuccess) return e;
     launch_coll_eval(d, s);
     return cudaGetLastError();
 }

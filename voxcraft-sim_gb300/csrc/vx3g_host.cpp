@@ -174,7 +174,6 @@ void from_slot(const double4 &s, bool mixed, double out[4]) {
 struct vx3g_ctx {
     int precision = 0, chunk = 100, device = 0, nr = 0;
     cudaStream_t stream = nullptr;
-    cudaStream_t side = nullptr;  // helper stream for capturing conditional graph bodies
     Dev d{};
     std::vector<void *> allocs;
     double *scratch = nullptr;  // dt reduction / com output
@@ -238,7 +237,6 @@ struct vx3g_ctx {
         for (void *p : allocs) cudaFree(p);
         if (flush) cudaFree(flush);
         if (stage) cudaFree(stage);
-        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -257,7 +255,6 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     c->nr = desc->n_robots;
     CU(cudaSetDevice(c->device));
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
 
     std::vector<VMat> vmats;
     std::vector<LMat> lmats;
@@ -489,7 +486,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     while (hs < d.nhash) hs <<= 1;
     d.hsize = hs;
     if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.cposf, d.ns)) ||
-        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1 + (size_t)d.nr)) || (rc = c->alloc(&d.ccount, 1)) ||
+        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1 + (size_t)d.nr)) || (rc = c->alloc(&d.gbar, 2)) ||
         (rc = c->upload(&d.cref, std::vector<float4>((size_t)d.ns, make_float4(1e30f, 1e30f, 1e30f, 0.0f)))) ||
         (rc = c->alloc(&d.hcount, hs)) ||
         (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.hsorted, d.ns)) ||
@@ -516,7 +513,7 @@ void enqueue_voxels(vx3g_ctx *c, int parity) {
 
 cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
     enqueue_links(c);
-    const cudaError_t e = launch_collision(c->d, c->stream, c->side);
+    const cudaError_t e = launch_collision(c->d, c->stream);
     enqueue_voxels(c, parity);
     return e;
 }
@@ -842,7 +839,7 @@ int vx3g_time_passes(vx3g_ctx *c, int iters, float *ms4) {
         CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < iters; i++) {
             if (pass == 0) enqueue_links(c);
-            else if (pass == 1) launch_collision(d, c->stream, c->side);
+            else if (pass == 1) launch_collision(d, c->stream);
             else if (pass == 2) enqueue_voxels(c, (p0 + i) & 1);
             else launch_coll_eval(d, c->stream);
         }
@@ -908,7 +905,7 @@ int vx3g_autotune(vx3g_ctx *c, int n_steps, const char *cache_json) {
         CU(cudaEventRecord(ev[4 * i], c->stream));
         enqueue_links(c);
         CU(cudaEventRecord(ev[4 * i + 1], c->stream));
-        CU(launch_collision(c->d, c->stream, nullptr));
+        CU(launch_collision(c->d, c->stream));
         CU(cudaEventRecord(ev[4 * i + 2], c->stream));
         enqueue_voxels(c, parity);
         CU(cudaEventRecord(ev[4 * i + 3], c->stream));
@@ -1062,7 +1059,7 @@ cudaError_t enqueue_adj_segment(vx3g_ctx *c, const AdjBufs &a0, int len, int p0)
         ds.linmom = st.linmom;
         ds.vinfo = st.vinfo;
         ds.status = st.status;
-        e = launch_collision(ds, c->stream, c->side);
+        e = launch_collision(ds, c->stream);
         a.parity = (p0 + i) & 1;
         launch_adj_slots(d, st, a, c->stream);
         launch_adj_voxel_link(d, st, a, c->stream);

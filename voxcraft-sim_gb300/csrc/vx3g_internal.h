@@ -67,7 +67,7 @@ struct RobotP {
     double inv_list_cell;  // 1 / (cell_size + skin): grid used to build the lists
     int voff, nv, loff, nl, soff, ns;
     int floor, vary_temp, expansion, collision;
-    int lchunks;  // > 0: lists built in shared memory (k_coll_list_robot), in this many chunks; 0: global hashed grid
+    int lchunks;  // > 0: lists built in shared memory (coll_list_robots), in this many chunks; 0: global hashed grid
 };
 
 template <class R> struct Slot { R f[3]; R m[3]; };
@@ -114,11 +114,11 @@ struct Dev {
     int *nbr;       // candidate lists, slot-major [kNbrCap][NS]: partner voxel indices, ascending
     int *nnb;       // candidate count per collision-surface voxel
     int *cflag;     // [1 + NR]: [0] some robot's lists are rebuilt this step, [1 + r] robot r's are
-    unsigned *ccount;  // blocks of the displacement check that have finished (graph path)
+    unsigned *gbar;  // [2] grid barrier of k_coll_prepare: arrivals, generation
     int2 *lwork;    // [NR] robots whose lists are rebuilt in shared memory this step: (robot, first chunk)
     unsigned long long *lwork_ctr;  // (robots << 32) | chunks listed in lwork; cleared by the narrow phase
     int lmax;       // most collision-surface voxels of a robot on the shared-memory path (0: none)
-    int lgrid;      // CTAs of k_coll_list_robot
+    int cgrid;      // CTAs of the cooperative k_coll_prepare (all resident)
     int nhash;      // collision-surface voxels on the global hashed-grid path
     int *hcount, *hstart, *hfill, *hsorted, *hblock;
     int hsize;      // power of two
@@ -151,10 +151,10 @@ void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape = 0
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s);
 void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
-// surface-voxel collision of one step; `side` (optional) is a helper stream used when
-// `s` is being captured into a CUDA graph (the list rebuild becomes a conditional node)
-cudaError_t launch_collision(const Dev &d, cudaStream_t s, cudaStream_t side);
-// one-time setup of the list-build kernels (shared-memory size, grid); fills d.lgrid
+// surface-voxel collision of one step: displacement check and list rebuild (one
+// cooperative kernel), then the narrow phase
+cudaError_t launch_collision(const Dev &d, cudaStream_t s);
+// one-time setup of the collision kernels (shared-memory size, grid); fills d.cgrid
 cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);
 void launch_coll_eval(const Dev &d, cudaStream_t s);  // the contact evaluation alone
