@@ -140,6 +140,8 @@ int vx3g_get_surface(vx3g_ctx *ctx, int32_t *surface);
 int vx3g_com(vx3g_ctx *ctx, double *com /* 3 per robot */);
 int vx3g_dt(vx3g_ctx *ctx, double *dt /* per robot: the float step, widened */);
 int vx3g_time(vx3g_ctx *ctx, double *t /* per robot */);
+/* Per-robot status words.  Returns VX3G_ERR_DEVICE (status still filled) if a device
+ * wait of the collision pass gave up (bounded grid barrier; the state is then suspect). */
 int vx3g_status(vx3g_ctx *ctx, int32_t *status /* per robot */);
 /* Stops one robot: it no longer steps (CUDA_Simulation's per-simulation loop
  * exit when StopConditionMet(), src/VX3/VX3_SimulationManager.cu:63-64). */

@@ -781,11 +781,12 @@ int vx3g_time(vx3g_ctx *c, double *t) {
 
 int vx3g_status(vx3g_ctx *c, int32_t *st) {
     if (!c || !st) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_status");
-    std::vector<int> h;
+    std::vector<int> h, err;
     int rc = download(c, h, c->d.status, (size_t)c->nr);
-    if (rc) return rc;
+    if (rc || (rc = download(c, err, c->d.err, 1))) return rc;
     CU(cudaStreamSynchronize(c->stream));
     memcpy(st, h.data(), c->nr * sizeof(int));
+    if (err[0] & 1) return fail(VX3G_ERR_DEVICE, "collision pass: a grid barrier of k_coll_prepare timed out");
     return VX3G_OK;
 }
 
