@@ -824,13 +824,19 @@ void launch_unpack_state(const Dev &d, double *staged, const double4 *src, int c
 
 // ---------------------------------------------------------------- centre of mass
 // updateCurrentCenterOfMass (VX3_VoxelyzeKernel.cu:477-493): mass-weighted mean
-// of measured voxels, FP64, one block per robot with a fixed reduction order.
-__global__ void __launch_bounds__(256) k_com(Dev d, double *out) {
+// of measured voxels, FP64.  Two passes with a fixed partition and order (so the
+// result does not depend on scheduling): block (tile, robot) sums kComTile voxels
+// of the robot into partial[(r * com_tiles + tile) * 4 + {x, y, z, mass}]; then one
+// thread per robot and component adds the robot's tiles in tile order.
+__global__ void __launch_bounds__(256) k_com_tiles(Dev d) {
     __shared__ double sh[4][256];
-    const int r = blockIdx.x;
+    const int r = blockIdx.y, tile = blockIdx.x;
     const RobotP &rp = d.rp[r];
+    const int i0 = tile * kComTile;
+    if (i0 >= rp.nv) return;  // (uniform) past the robot's voxels
+    const int i1 = min(rp.nv, i0 + kComTile);
     double sx = 0, sy = 0, sz = 0, sm = 0;
-    for (int i = threadIdx.x; i < rp.nv; i += 256) {
+    for (int i = i0 + threadIdx.x; i < i1; i += 256) {
         const int v = rp.voff + i;
         const VMat &m = d.vmat[d.vinfo[v].y >> 8];
         if (!m.is_measured) continue;
@@ -848,17 +854,26 @@ __global__ void __launch_bounds__(256) k_com(Dev d, double *out) {
             for (int k = 0; k < 4; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        const double tot = sh[3][0];
-        double inv = tot != 0 ? 1.0 / tot : 0.0;
-        out[3 * r] = tot != 0 ? inv * sh[0][0] : 0.0;
-        out[3 * r + 1] = tot != 0 ? inv * sh[1][0] : 0.0;
-        out[3 * r + 2] = tot != 0 ? inv * sh[2][0] : 0.0;
-    }
+    if (threadIdx.x < 4) d.com_part[((size_t)r * d.com_tiles + tile) * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_com_sum(Dev d, double *out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * d.nr) return;
+    const int r = t >> 2, k = t & 3;
+    const int nt = (d.rp[r].nv + kComTile - 1) / kComTile;
+    const double *p = d.com_part + (size_t)r * d.com_tiles * 4;
+    double acc = 0;
+    for (int j = 0; j < nt; j++) acc += p[4 * j + k];
+    double tot = 0;
+    for (int j = 0; j < nt; j++) tot += p[4 * j + 3];
+    if (k < 3) out[3 * r + k] = tot != 0 ? (1.0 / tot) * acc : 0.0;
 }
 
 void launch_com(const Dev &d, double *out, cudaStream_t s) {
-    if (d.nr) k_com<<<d.nr, 256, 0, s>>>(d, out);
+    if (!d.nr) return;
+    k_com_tiles<<<dim3((unsigned)d.com_tiles, (unsigned)d.nr), 256, 0, s>>>(d);
+    k_com_sum<<<(4 * d.nr + 255) / 256, 256, 0, s>>>(d, out);
 }
 
 __global__ void k_or_status(Dev d, int r, int bits) { d.status[r] |= bits; }

@@ -469,6 +469,10 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     if ((rc = c->alloc(&d.dt, d.nr)) || (rc = c->alloc(&d.T, 2 * (size_t)d.nr)) || (rc = c->alloc(&d.status, d.nr)) ||
         (rc = c->alloc(&d.err, 1)) || (rc = c->alloc(&c->scratch, 4 * (size_t)d.nr + 4)))
         return rc;
+    int nvmax = 1;
+    for (const RobotP &q : rps) nvmax = std::max(nvmax, q.nv);
+    d.com_tiles = (nvmax + kComTile - 1) / kComTile;
+    if ((rc = c->alloc(&d.com_part, (size_t)d.nr * d.com_tiles * 4))) return rc;
     // collision tables: robots on the shared-memory path (lchunks > 0) and the global hashed grid
     d.lmax = 0;
     d.nhash = 0;

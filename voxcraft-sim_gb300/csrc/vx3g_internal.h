@@ -73,6 +73,7 @@ struct RobotP {
 template <class R> struct Slot { R f[3]; R m[3]; };
 
 constexpr int kNbrCap = 64;  // contact candidates kept per collision-surface voxel
+constexpr int kComTile = 2048;  // voxels per block of the centre-of-mass reduction
 // per-robot list build in shared memory: robots with at most kLocalListMax collision-surface
 // voxels and lattice coordinates below 512, chunks of kLocalListChunk voxels (ten per warp,
 // three threads per voxel)
@@ -123,6 +124,8 @@ struct Dev {
     int *hcount, *hstart, *hfill, *hsorted, *hblock;
     int hsize;      // power of two
     int *err;       // device error word
+    double *com_part;  // [NR][com_tiles][4] partial sums of the centre of mass
+    int com_tiles;     // tiles of kComTile voxels of the largest robot
     int nv, nl, nr, ns;
     int mixed;      // 1: voxel state is compensated FP32 (see below)
 };
