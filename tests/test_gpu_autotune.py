@@ -13,8 +13,8 @@ from vx3g import workloads as wl
 pytestmark = pytest.mark.gpu
 
 # the compiled shapes, (threads per block, minimum resident blocks), in index order
-LINK_SHAPES = [[256, 1], [256, 4], [128, 9], [128, 10]]
-VOXEL_SHAPES = [[256, 1], [256, 3], [128, 7], [128, 8]]
+LINK_SHAPES = [[256, 1], [256, 4], [128, 9], [128, 10], [64, 20], [256, 5]]
+VOXEL_SHAPES = [[256, 1], [256, 3], [128, 7], [128, 8], [64, 14], [64, 16]]
 
 
 def _robots():
@@ -32,7 +32,7 @@ def test_every_shape_gives_identical_states(tmp_path):
     ref.step(150)
     want = _state(ref)
     key = None
-    for k in range(4):
+    for k in range(len(LINK_SHAPES)):
         b = abi.Batch(robots, abi.PRECISION_MIXED)
         if key is None:  # learn the cache key from a tuning run
             path = tmp_path / "probe.json"

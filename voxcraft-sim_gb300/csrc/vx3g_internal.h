@@ -147,7 +147,7 @@ void launch_links_fp64(const Dev &d, cudaStream_t s);
 void launch_voxels_fp64(const Dev &d, int parity, cudaStream_t s);
 // launch shapes of the mixed-precision passes (vx3g_mixed.cu), chosen by vx3g_autotune
 struct LaunchShape { int threads, min_blocks; };
-constexpr int kMixedShapes = 4;
+constexpr int kMixedShapes = 6;
 extern const LaunchShape kLinkShapes[kMixedShapes], kVoxelShapes[kMixedShapes];
 void launch_links_mixed(const Dev &d, cudaStream_t s, int shape = 0);
 void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape = 0);

@@ -59,12 +59,40 @@ __device__ __forceinline__ V3<float> rotvec_f(float w, V3<float> v) {
     const float s2 = v.x * v.x + v.y * v.y + v.z * v.z;
     if (!(s2 > 0.0f)) return V3<float>{0, 0, 0};
     if (w > 0.0f && s2 < 1e-4f * (w * w)) {
-        const float iw = 1.0f / w;
+        const float iw = __frcp_rn(w);  // = 1.0f / w (both correctly rounded)
         const float x2 = s2 * (iw * iw);
         return scl(v, 2.0f * iw * (1.0f - x2 * (1.0f / 3.0f - x2 * 0.2f)));
     }
     const float s = sqrtf(s2);
     return scl(v, 2.0f * atan2f(s, w) / s);
+}
+
+// FromAngleToPosX (src/VX3/VX3_Quat3D.h:384-432) in FP32: the rotation taking r to
+// +x.  The reference forms theta = acos(n.x) for n = r/|r| and returns
+// (cos(theta/2), 0, n.z sin(theta/2)/|(n.y, n.z)|, -n.y sin(theta/2)/|(n.y, n.z)|).
+// With the half-angle identities cos(theta/2) = sqrt((1 + n.x)/2) and
+// sin(theta/2)/|(n.y, n.z)| = sqrt((1 - n.x)/2)/sqrt(1 - n.x^2) = 1/sqrt(2(1 + n.x))
+// that is (c/2, 0, n.z/c, -n.y/c) with c = sqrt(2(1 + n.x)): one square root and one
+// reciprocal instead of acos, sin and cos.  The small-angle shortcut and the
+// turned-around case (theta within 1e-7 of pi, where 1 + n.x underflows in FP32)
+// are the reference's.
+__device__ __forceinline__ Q4<float> from_angle_to_posx_f(Q4<float> q, V3<float> r) {
+    if (r.x == 0 && r.y == 0 && r.z == 0) return q;
+    const float yx = r.y / r.x, zx = r.z / r.x;
+    const float SA = 1.732e-2f;
+    if (yx < SA && yx > -SA && zx < SA && zx > -SA) {
+        q.x = 0;
+        q.y = 0.5f * zx;
+        q.z = -0.5f * yx;
+        q.w = 1 + 0.5f * (-q.y * q.y - q.z * q.z);
+        return q;
+    }
+    const float il = rsqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
+    const float nx = r.x * il, ny = r.y * il, nz = r.z * il;
+    const float t = 2.0f * (1.0f + nx);
+    if (!(t > 0.0f)) return Q4<float>{0, 0, 1, 0};
+    const float c = sqrtf(t), ic = __frcp_rn(c);
+    return Q4<float>{0.5f * c, 0, nz * ic, -ny * ic};
 }
 
 // ------------------------------------------------------------- collision narrow phase
@@ -195,14 +223,18 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     float py = 2.0f * L * (a1.x * a1.y - a1.w * a1.z) + rd.y;
     float pz = 2.0f * L * (a1.x * a1.z + a1.w * a1.y) + rd.z;
     const float px = L + pxm;
-    const float SmallTurn = (fabsf(pz) + fabsf(py)) / px;
-    const float ExtendPerc = fabsf(pxm / L);
+    // hysteresis on SmallTurn = (|pz| + |py|)/px and ExtendPerc = |pxm/L| (L > 0),
+    // compared without dividing: px < 0 (bent past 90 degrees) gives SmallTurn <= 0,
+    // px = 0 gives +inf (or NaN when the numerator is 0 too)
     const float HF = 1.2f, BEND = 0.05f, EXT = 0.50f;
+    const float turn = fabsf(pz) + fabsf(py), ext = fabsf(pxm);
+    const bool turnBelow = px > 0.0f ? turn < BEND * px : px < 0.0f;
+    const bool turnAbove = px > 0.0f ? turn > (HF * BEND) * px : (px == 0.0f && turn > 0.0f);
     bool small = (fl & LF_SMALL) != 0, lvv = (fl & LF_LVV) != 0;
-    if (!small && SmallTurn < BEND && ExtendPerc < EXT) {
+    if (!small && turnBelow && ext < EXT * L) {
         small = true;
         lvv = false;
-    } else if (small && (SmallTurn > HF * BEND || ExtendPerc > HF * EXT)) {
+    } else if (small && (turnAbove || ext > (HF * EXT) * L)) {
         small = false;
         lvv = false;
     }
@@ -213,7 +245,7 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     if (small) {
         pos2 = V3<float>{pxm, py, pz};
     } else {
-        angle1 = from_angle_to_posx(angle1, V3<float>{px, py, pz});
+        angle1 = from_angle_to_posx_f(angle1, V3<float>{px, py, pz});
         const Q4<float> a2 = qmul(angle1, Q4<float>{w2, v2.x, v2.y, v2.z});
         w2 = a2.w;
         v2 = V3<float>{a2.x, a2.y, a2.z};
@@ -466,8 +498,8 @@ template <int TPB, int MINB> __global__ void __launch_bounds__(TPB, MINB) k_voxe
     if (v < d.nv) voxels_mixed_body(d, v, parity);
 }
 
-const LaunchShape kLinkShapes[kMixedShapes] = {{256, 1}, {256, 4}, {128, 9}, {128, 10}};
-const LaunchShape kVoxelShapes[kMixedShapes] = {{256, 1}, {256, 3}, {128, 7}, {128, 8}};
+const LaunchShape kLinkShapes[kMixedShapes] = {{256, 1}, {256, 4}, {128, 9}, {128, 10}, {64, 20}, {256, 5}};
+const LaunchShape kVoxelShapes[kMixedShapes] = {{256, 1}, {256, 3}, {128, 7}, {128, 8}, {64, 14}, {64, 16}};
 
 // launch with programmatic stream serialization (see pdl_wait_then_release)
 template <typename... KArgs, typename... Args>
@@ -490,6 +522,8 @@ void launch_links_mixed(const Dev &d, cudaStream_t s, int shape) {
         case 1: launch_pdl(k_links_mixed<256, 4>, d.nl, 256, s, d); break;
         case 2: launch_pdl(k_links_mixed<128, 9>, d.nl, 128, s, d); break;
         case 3: launch_pdl(k_links_mixed<128, 10>, d.nl, 128, s, d); break;
+        case 4: launch_pdl(k_links_mixed<64, 20>, d.nl, 64, s, d); break;
+        case 5: launch_pdl(k_links_mixed<256, 5>, d.nl, 256, s, d); break;
         default: launch_pdl(k_links_mixed<256, 1>, d.nl, 256, s, d); break;
     }
 }
@@ -499,6 +533,8 @@ void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape) {
         case 1: launch_pdl(k_voxels_mixed<256, 3>, d.nv, 256, s, d, parity); break;
         case 2: launch_pdl(k_voxels_mixed<128, 7>, d.nv, 128, s, d, parity); break;
         case 3: launch_pdl(k_voxels_mixed<128, 8>, d.nv, 128, s, d, parity); break;
+        case 4: launch_pdl(k_voxels_mixed<64, 14>, d.nv, 64, s, d, parity); break;
+        case 5: launch_pdl(k_voxels_mixed<64, 16>, d.nv, 64, s, d, parity); break;
         default: launch_pdl(k_voxels_mixed<256, 1>, d.nv, 256, s, d, parity); break;
     }
 }
