@@ -64,6 +64,23 @@ typedef struct vx3g_material {
     double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
 } vx3g_material;
 
+/* One token of a math-tree program, the reference's VX3_MathTreeToken
+ * (src/Utils/VX3_MathTree.h:29-36) as VX3_SimulationManager::ParseMathTree
+ * (src/VX3/VX3_SimulationManager.cu:157-275) lays a formula out: op is the
+ * VX3_MathTreeOperator value -- mtEND 0, mtCONST 1, mtE 2, mtPI 3, mtVAR 4, mtADD 5,
+ * mtSUB 6, mtMUL 7, mtDIV 8, mtPOW 9, mtSQRT 10, mtSIN 11, mtCOS 12, mtTAN 13,
+ * mtATAN 14, mtLOG 15, mtINT 16, mtABS 17, mtNOT 18, mtGREATERTHAN 19, mtLESSTHAN 20,
+ * mtAND 21, mtOR 22, mtNORMALCDF 23 -- and value is mtCONST's constant or mtVAR's
+ * variable: x 0, y 1, z 2, hit 3, t 4, angle 5, targetCloseness 6, numClosePairs 7,
+ * num_voxel 8.  A program ends with mtEND and holds at most VX3G_MAX_MATH_TOKENS
+ * tokens including it. */
+typedef struct vx3g_math_token {
+    int32_t op;
+    int32_t reserved;
+    double value;
+} vx3g_math_token;
+#define VX3G_MAX_MATH_TOKENS 256
+
 /* One simulation: the content of a merged VXA document. */
 typedef struct vx3g_robot_desc {
     int nx, ny, nz;                 /* X_Voxels, Y_Voxels, Z_Voxels */
@@ -84,6 +101,13 @@ typedef struct vx3g_robot_desc {
     double bond_damping, col_damping, slow_damping; /* Simulator/Damping/{Bond,Col,Slow}DampingZ */
     const double *log10E;           /* nx*ny*nz per-voxel log10 Young's modulus overriding the palette's,
                                        or NULL (per-voxel stiffness is not expressible in a VXA palette) */
+    const vx3g_math_token *force_field[3]; /* Simulator/ForceField/{x,y,z}_forcefield programs or NULL
+                                       (0): the force added to every voxel each step
+                                       (VX3_Voxel::timeStep, src/VX3/VX3_Voxel.cu:178-184).  Variables
+                                       x, y, z (the voxel's position), t (the time at the start of the
+                                       step), num_voxel, and hit (the reference keeps it 0); programs
+                                       that read angle, targetCloseness or numClosePairs (target
+                                       tracking, not supported) are rejected with VX3G_ERR_UNSUPPORTED */
 } vx3g_robot_desc;
 
 typedef struct vx3g_batch_desc {

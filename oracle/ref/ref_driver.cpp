@@ -306,6 +306,21 @@ void *vx3ref_create(const char *vxa_text, int enable_collision, int enable_expan
     return S;
 }
 
+// Sets one force-field program (axis 0/1/2 = x/y/z) the way ParseMathTree fills
+// VX3_ForceField's token arrays (VX3_SimulationManager.cu:349-354): n tokens laid out
+// as {int op, int reserved, double value}, the last one mtEND.
+int vx3ref_set_force_field(void *h, int axis, const void *tokens, int n) {
+    struct Tok { int op, reserved; double value; };
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    VX3_MathTreeToken *dst = axis == 0 ? k->force_field.token_x_forcefield
+                             : axis == 1 ? k->force_field.token_y_forcefield
+                                         : k->force_field.token_z_forcefield;
+    if (axis < 0 || axis > 2 || n < 1 || n > 1024) return -1;
+    const Tok *t = (const Tok *)tokens;
+    for (int i = 0; i < n; i++) dst[i].set((VX3_MathTreeOperator)t[i].op, t[i].value);
+    return 0;
+}
+
 void vx3ref_destroy(void *h) { /* the reference frees nothing reliably either; leak in tests */ (void)h; }
 
 void vx3ref_counts(void *h, int *nv, int *nl, int *nsurf) {

@@ -7,8 +7,9 @@
  * float and double exactly (build with -ffp-contract=off).
  *
  * Scope: linear materials (MatModel 0/1), static lattice topology (no
- * attach/detach/removal), no boundary-condition regions, no signals/cilia,
- * force field = constant 0 (the reference default, VX3_ForceField.h:10-20).
+ * attach/detach/removal), no boundary-condition regions, no signals/cilia;
+ * force field: the robot's x/y/z math-tree programs (constant 0 when absent, the
+ * reference default, VX3_ForceField.h:10-20), target-tracking variables 0.
  */
 #include "vx3_oracle.h"
 
@@ -277,7 +278,54 @@ typedef struct {
     float dt;
     int surface_stale, diverged;
     int threads; /* > 1: timing mode, loops run under OpenMP */
+    vxo_math_token *ff[3]; /* force-field programs (copies) or NULL */
 } sim;
+
+/* VX3_MathTree::eval (src/Utils/VX3_MathTree.h:50-191): tokens in order, each result
+ * appended to a value queue, operators consuming the oldest unconsumed values (binary:
+ * values[pc + 1] op values[pc]); hit, angle, targetCloseness, numClosePairs are 0 here
+ * (the reference keeps collisionCount at 0; target tracking is not restated). */
+#define VXO_MAX_TOKENS 256
+static double math_eval(const vxo_math_token *tok, double x, double y, double z, double t, double num_voxel) {
+    double vals[VXO_MAX_TOKENS];
+    int vc = 0, pc = 0;
+    for (int i = 0; i < VXO_MAX_TOKENS; i++) {
+        double r, w;
+        switch (tok[i].op) {
+        case 0: return vals[pc < vc ? pc : 0];
+        case 1: r = tok[i].value; break;
+        case 2: r = 2.71828182845904523536; break;
+        case 3: r = 3.14159265358979323846; break;
+        case 4:
+            w = tok[i].value;
+            r = w < 0.5 ? x : w < 1.5 ? y : w < 2.5 ? z : (w >= 3.5 && w < 4.5) ? t : (w >= 7.5 && w < 8.5) ? num_voxel : 0.0;
+            break;
+        case 5: r = vals[pc + 1] + vals[pc]; pc += 2; break;
+        case 6: r = vals[pc + 1] - vals[pc]; pc += 2; break;
+        case 7: r = vals[pc + 1] * vals[pc]; pc += 2; break;
+        case 8: r = vals[pc + 1] / vals[pc]; pc += 2; break;
+        case 9: r = pow(vals[pc + 1], vals[pc]); pc += 2; break;
+        case 10: r = sqrt(vals[pc]); pc++; break;
+        case 11: r = sin(vals[pc]); pc++; break;
+        case 12: r = cos(vals[pc]); pc++; break;
+        case 13: r = tan(vals[pc]); pc++; break;
+        case 14: r = atan(vals[pc]); pc++; break;
+        case 15: r = log(vals[pc]); pc++; break;
+        case 16: r = rint(vals[pc]); pc++; break;
+        case 17: r = fabs(vals[pc]); pc++; break;
+        case 18: r = !vals[pc]; pc++; break;
+        case 19: r = vals[pc + 1] > vals[pc]; pc += 2; break;
+        case 20: r = vals[pc + 1] < vals[pc]; pc += 2; break;
+        case 21: r = vals[pc + 1] && vals[pc]; pc += 2; break;
+        case 22: r = vals[pc + 1] || vals[pc]; pc += 2; break;
+        case 23: r = 0.5 * erfc(-vals[pc] / sqrt(2.0)); pc++; break;
+        default: return 0.0;
+        }
+        if (pc > vc) return 0.0;
+        vals[vc++] = r;
+    }
+    return 0.0;
+}
 
 /* VX3_Voxel::baseSize(axis) (VX3_Voxel.h:96-100); material size() = nomSize*extScale(1,1,1) */
 static double base_size(const sim *S, const voxel *v) {
@@ -306,6 +354,14 @@ static void update_rest(sim *S, link *L) {
 void *vxo_create(const vxo_robot *r) {
     sim *S = (sim *)calloc(1, sizeof(sim));
     S->r = *r;
+    for (int k = 0; k < 3; k++) {
+        S->r.force_field[k] = NULL;
+        if (!r->force_field[k]) continue;
+        int n = 0;
+        while (n < VXO_MAX_TOKENS - 1 && r->force_field[k][n].op != 0) n++;
+        S->ff[k] = (vxo_math_token *)calloc((size_t)n + 1, sizeof(vxo_math_token));
+        memcpy(S->ff[k], r->force_field[k], sizeof(vxo_math_token) * (size_t)n);
+    }
     int nx = r->nx, ny = r->ny, nz = r->nz, ncell = nx * ny * nz;
     S->nvm = r->n_materials;
     S->vm = (vmat *)calloc(S->nvm ? S->nvm : 1, sizeof(vmat));
@@ -380,6 +436,7 @@ void vxo_destroy(void *h) {
     sim *S = (sim *)h;
     if (!S) return;
     free(S->vm); free(S->lm); free(S->v); free(S->l); free(S->surf); free(S->last_contact);
+    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]);
     free(S);
 }
 
@@ -515,8 +572,10 @@ static void voxel_update(sim *S, voxel *v, float dtf) {
     F = vsub(F, v->contact);
     v->contact = V(0, 0, 0);
     F = vadd(F, V(0.0 * 0.0, 0.0 * 0.0, 0.0 * 0.0)); /* CiliaForce * Cilia, both zero */
-    /* force field, constant 0 (VX3_Voxel.cu:179-184) */
-    F.x += 0.0; F.y += 0.0; F.z += 0.0;
+    /* force field (VX3_Voxel.cu:178-184; constant 0 unless the VXA gives one) */
+    F.x += S->ff[0] ? math_eval(S->ff[0], v->pos.x, v->pos.y, v->pos.z, S->t, S->nv) : 0.0;
+    F.y += S->ff[1] ? math_eval(S->ff[1], v->pos.x, v->pos.y, v->pos.z, S->t, S->nv) : 0.0;
+    F.z += S->ff[2] ? math_eval(S->ff[2], v->pos.x, v->pos.y, v->pos.z, S->t, S->nv) : 0.0;
     vec fric = F;
     if (v->flags & F_FLOOR) floor_force(S, v, &F);
     fric = vsub(F, fric);

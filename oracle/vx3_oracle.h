@@ -25,6 +25,13 @@ typedef struct vxo_material {
     double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
 } vxo_material;
 
+/* A math-tree token (VX3_MathTreeToken, src/Utils/VX3_MathTree.h:29-36): op is the
+ * VX3_MathTreeOperator value, value the constant or the variable index. */
+typedef struct vxo_math_token {
+    int op, reserved;
+    double value;
+} vxo_math_token;
+
 /* One simulation (one merged VXA). */
 typedef struct vxo_robot {
     int nx, ny, nz;
@@ -37,6 +44,7 @@ typedef struct vxo_robot {
     double temp_amplitude, temp_period, temp_base;
     int temp_enabled, vary_temp, enable_expansion, enable_collision, volume_effects;
     double bond_damping, col_damping, slow_damping;
+    const vxo_math_token *force_field[3]; /* ForceField x/y/z programs (mtEND-terminated) or NULL */
 } vxo_robot;
 
 void *vxo_create(const vxo_robot *r);

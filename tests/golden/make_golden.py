@@ -56,6 +56,18 @@ def cases():
     brittle = [wl.Material(E=2e4, nu=0.0, fail_stress=40.0, mu_static=0.2, mu_kinetic=0.1)]
     out["brittle_failure"] = (wl.Robot(grid=grid.copy(), materials=brittle, volume_effects=False, z_offset=0),
                               900, 300)
+    # Simulator/ForceField programs (VX3_Voxel.cu:178-184): time, position and voxel-count terms
+    C = lambda v: ("mtCONST", v)  # noqa: E731
+    V = lambda n: ("mtVAR", n)  # noqa: E731
+    ff = [("mtMUL", C(1e-2), ("mtSIN", ("mtMUL", C(31.4), V("t")))),
+          ("mtSUB", ("mtMUL", C(-0.5), V("y")), ("mtDIV", V("num_voxel"), C(1e5))),
+          ("mtADD", ("mtMUL", C(6e-3), ("mtNORMALCDF", ("mtDIV", ("mtSUB", V("z"), C(0.02)), C(0.01)))),
+                    ("mtMUL", C(2e-3), ("mtATAN", ("mtPOW", ("mtMUL", V("t"), C(10.0)), C(2.0)))))]
+    ffmats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=3e5, nu=0.35, cte=0.0)]
+    rng = np.random.default_rng(7)
+    out["bern5_force_field"] = (
+        wl.bernoulli_body(rng, (5, 4, 3), 0.8, ffmats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
+                          force_field=ff, z_offset=1), 300, 100)
     return out
 
 
@@ -77,7 +89,7 @@ def robot_record(r):
                     slow_damping=r.slow_damping, gravity=r.gravity, grav_acc=r.grav_acc, floor=r.floor,
                     temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,
                     temp_base=r.temp_base, enable_expansion=r.enable_expansion, enable_collision=r.enable_collision,
-                    volume_effects=r.volume_effects)
+                    volume_effects=r.volume_effects, force_field=r.force_field)
     return dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
                 settings=np.array(json.dumps(settings)))
 

@@ -18,6 +18,9 @@ def names():
 def load(name):
     d = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
     s = json.loads(str(d["settings"]))
+    if s.get("force_field") is not None:  # math trees were stored as nested JSON lists
+        tup = lambda n: tuple(tup(c) if isinstance(c, list) else c for c in n)  # noqa: E731
+        s["force_field"] = [None if t is None else tup(t) for t in s["force_field"]]
     mats = [wl.Material(E=m[0], nu=m[1], rho=m[2], cte=m[3], mu_static=m[4], mu_kinetic=m[5], fail_stress=m[6],
                         fixed=int(m[7]), is_measured=int(m[8])) for m in d["materials"]]
     phase = d["phase"] if d["phase"].size else None

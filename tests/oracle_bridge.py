@@ -37,7 +37,8 @@ class VxoRobot(ctypes.Structure):
                 ("temp_amplitude", ctypes.c_double), ("temp_period", ctypes.c_double), ("temp_base", ctypes.c_double),
                 ("temp_enabled", ctypes.c_int), ("vary_temp", ctypes.c_int), ("enable_expansion", ctypes.c_int),
                 ("enable_collision", ctypes.c_int), ("volume_effects", ctypes.c_int),
-                ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double)]
+                ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
+                ("force_field", ctypes.c_void_p * 3)]
 
 
 def build_oracle():
@@ -191,7 +192,17 @@ def robot_struct(robot):
                  robot.temp_amplitude, robot.temp_period, robot.temp_base, 0, int(robot.temp_vary),
                  int(robot.enable_expansion), int(robot.enable_collision), int(robot.volume_effects),
                  robot.bond_damping, robot.col_damping, robot.slow_damping)
-    return r, (lattice, phase, mats)
+    progs = _force_field_tokens(robot)
+    for k, t in enumerate(progs):
+        if t is not None:
+            r.force_field[k] = _P(t)
+    return r, (lattice, phase, mats, progs)
+
+
+def _force_field_tokens(robot):
+    from vx3g.workloads import math_tokens
+    ff = getattr(robot, "force_field", None) or [None] * 3
+    return [None if t is None else np.ascontiguousarray(math_tokens(t)) for t in ff]
 
 
 def oracle_sim(robot) -> Sim:
@@ -213,4 +224,10 @@ def ref_sim(robot) -> Sim:
     lib.vx3ref_create.restype = ctypes.c_void_p
     lib.vx3ref_create.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
     h = lib.vx3ref_create(to_vxa(robot).encode(), int(robot.enable_collision), int(robot.enable_expansion))
-    return Sim(lib, "vx3ref_", h, None)
+    lib.vx3ref_set_force_field.restype = ctypes.c_int
+    lib.vx3ref_set_force_field.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    progs = _force_field_tokens(robot)
+    for k, t in enumerate(progs):
+        if t is not None:
+            assert lib.vx3ref_set_force_field(h, k, _P(t), len(t)) == 0
+    return Sim(lib, "vx3ref_", h, progs)

@@ -35,3 +35,30 @@ def test_loader_is_loud_when_library_missing(tmp_path):
             abi.load(str(tmp_path / "nope.so"))
     finally:
         abi._lib = saved
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors in abi.py have the C structs' sizes and field offsets."""
+    import subprocess
+    fields = {"vx3g_material": (abi.Material, ["E", "fail_stress", "model", "is_measured", "thermal_on_after"]),
+              "vx3g_robot_desc": (abi.RobotDesc, ["lattice", "materials", "vox_size", "floor_enabled",
+                                                  "volume_effects", "slow_damping", "log10E", "force_field"]),
+              "vx3g_batch_desc": (abi.BatchDesc, ["robots", "precision", "graph_chunk"])}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vx3g.h"', "int main(void) {"]
+    for st, (_, names) in fields.items():
+        lines.append(f'printf("%zu\\n", sizeof({st}));')
+        lines += [f'printf("%zu\\n", offsetof({st}, {n}));' for n in names]
+    lines.append('printf("%zu\\n", sizeof(vx3g_math_token));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    want = []
+    for st, (cls, names) in fields.items():
+        want.append(ctypes.sizeof(cls))
+        want += [getattr(cls, n).offset for n in names]
+    from vx3g import workloads as wl
+    want.append(wl.math_tokens(("mtCONST", 0.0)).dtype.itemsize)
+    assert got == want

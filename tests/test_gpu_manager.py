@@ -73,3 +73,31 @@ def test_runner_history_text(tmp_path):
     recs = [x for x in body.split(";") if x]
     assert len(recs) == 26
     assert all(len(x.rstrip(",").split(",")) == 15 for x in recs)
+
+
+def test_runner_force_field_matches_oracle(tmp_path):
+    """Simulator/ForceField in the VXA: the runner's token programs (built from the
+    XML the way ParseMathTree lays them out) move the robot as the oracle does."""
+    vbuild.build()
+    exe = os.path.join(os.path.dirname(vbuild.LIB), "vx3g_sim")
+    C = lambda v: ("mtCONST", v)  # noqa: E731
+    V = lambda n: ("mtVAR", n)  # noqa: E731
+    ff = [("mtMUL", C(1e-2), ("mtCOS", ("mtMUL", C(20.0), V("t")))),
+          ("mtMUL", C(-0.3), ("mtSUB", V("y"), C(0.02))),
+          ("mtDIV", ("mtSQRT", V("num_voxel")), C(2e3))]
+    rng = np.random.default_rng(8)
+    mats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=3e5, nu=0.35, cte=0.0)]
+    robot = wl.bernoulli_body(rng, (4, 4, 3), 0.85, mats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
+                              stop_time=0.01, fitness_x=True, force_field=ff)
+    (tmp_path / "base.vxa").write_text(wl.to_vxa(robot))
+    (tmp_path / "r.vxd").write_text("<VXD>\n</VXD>\n")
+    out = tmp_path / "report.xml"
+    r = subprocess.run([exe, "-i", str(tmp_path), "-o", str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    node = ET.parse(out).getroot().find("detail/r")
+    s, c0, _ = _oracle_until(robot, 0.01)
+    com = [float(node.find(f"currentCenterOfMass/{k}").text) for k in "xyz"]
+    np.testing.assert_allclose(com, s.com(), rtol=0, atol=1e-6 * robot.vox_size)
+    free = wl.Robot(**{**robot.__dict__, "force_field": None})
+    f, _, _ = _oracle_until(free, 0.01)
+    assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size  # the field moved the robot

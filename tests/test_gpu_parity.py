@@ -143,6 +143,70 @@ def test_both_list_builds_match_oracle():
     assert np.all(rel <= 1e-5), rel
 
 
+def _ff(*trees):
+    return list(trees)
+
+
+def test_force_field_programs_are_checked():
+    """Programs are validated at create: target-tracking variables are unsupported,
+    an operator without operands or a program without mtEND's single value is invalid."""
+    base = wl.solid_block(3)
+    C = lambda v: ("mtCONST", v)  # noqa: E731
+    ok = wl.Robot(**{**base.__dict__, "force_field": _ff(("mtMUL", C(1e-3), ("mtVAR", "t")), None, None)})
+    abi.Batch([ok], abi.PRECISION_FP64).close()
+    angle = wl.Robot(**{**base.__dict__, "force_field": _ff(("mtVAR", "angle"), None, None)})
+    with pytest.raises(abi.Vx3gError, match="target tracking"):
+        abi.Batch([angle], abi.PRECISION_FP64)
+    lib = abi.load()
+    d, keep = abi.robot_desc(base)
+    for toks in ([(5, 0, 0.0), (0, 0, 0.0)],                 # mtADD with nothing to add
+                 [(1, 0, 1.0), (1, 0, 2.0), (0, 0, 0.0)],    # two values left at mtEND
+                 [(1, 0, 1.0)] * 300):                        # no mtEND
+        arr = np.array(toks, dtype=[("op", np.int32), ("reserved", np.int32), ("value", np.float64)])
+        d.force_field[2] = arr.ctypes.data
+        bd = abi.BatchDesc(1, abi.ctypes.pointer(d), abi.PRECISION_FP64, 0, 100)
+        st = abi.ctypes.c_int(0)
+        assert not lib.vx3g_create(abi.ctypes.byref(bd), abi.ctypes.byref(st))
+        assert st.value == -1, lib.vx3g_last_error()
+
+
+def test_adjoint_with_force_fields():
+    """record() refuses a force field that reads the position; a time-only field is
+    part of the recomputed forward step, so backward() still matches central
+    differences (4 phases, 120 steps, eps = 1e-6, within 3%)."""
+    base = wl.c4_differentiable(0)[0]
+    C = lambda v: ("mtCONST", v)  # noqa: E731
+    pos = wl.Robot(**{**base.__dict__, "force_field": _ff(None, ("mtMUL", C(-0.1), ("mtVAR", "y")), None)})
+    b = abi.Batch([pos], abi.PRECISION_FP64)
+    with pytest.raises(abi.Vx3gError, match="position"):
+        b.record(10, 5)
+    ff = _ff(("mtMUL", C(3e-3), ("mtSIN", ("mtMUL", C(31.4), ("mtVAR", "t")))), None,
+             ("mtMUL", C(1e-8), ("mtVAR", "num_voxel")))
+    robot = wl.Robot(**{**base.__dict__, "force_field": ff})
+    n = 120
+    b = abi.Batch([robot], abi.PRECISION_FP64)
+    b.record(n, 40)
+    gp, _ = b.backward(np.array([[-1.0, 0.0, 0.0]]))
+    ph = robot.phase.reshape(-1)
+    idx = np.flatnonzero(robot.grid.reshape(-1) > 0)
+    rng = np.random.default_rng(3)
+    errs = []
+    for k in rng.choice(len(idx), 4, replace=False):
+        cell, eps = idx[k], 1e-6
+        f = []
+        for sgn in (1, -1):
+            p = ph.copy()
+            p[cell] += sgn * eps
+            r2 = wl.Robot(**{**robot.__dict__, "phase": p.reshape(robot.phase.shape)})
+            c = abi.Batch([r2], abi.PRECISION_FP64)
+            c0 = c.com()[0, 0]
+            c.step(n)
+            f.append(-(c.com()[0, 0] - c0))
+        fd = (f[0] - f[1]) / (2 * eps)
+        errs.append(abs(gp[k] - fd) / max(abs(fd), abs(gp[k]), 1e-2 * np.abs(gp).max()))
+    assert np.median(errs) <= 0.03, errs
+
+
 def test_mixed_com_error_vs_fp64():
     rng = np.random.default_rng(21)
     mats = [wl.Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]

@@ -46,7 +46,7 @@ class RobotDesc(ctypes.Structure):
                 ("temp_enabled", ctypes.c_int), ("vary_temp", ctypes.c_int), ("enable_expansion", ctypes.c_int),
                 ("enable_collision", ctypes.c_int), ("volume_effects", ctypes.c_int),
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
-                ("log10E", ctypes.c_void_p)]
+                ("log10E", ctypes.c_void_p), ("force_field", ctypes.c_void_p * 3)]
 
 
 class BatchDesc(ctypes.Structure):
@@ -135,7 +135,13 @@ def robot_desc(robot):
                   int(robot.temp_vary), int(robot.enable_expansion), int(robot.enable_collision),
                   int(robot.volume_effects), robot.bond_damping, robot.col_damping, robot.slow_damping,
                   _P(log10E))
-    return d, (lattice, phase, mats, log10E)
+    from . import workloads as wl  # noqa: E402  (math-tree token layout)
+    progs = []
+    for k, tree in enumerate(getattr(robot, "force_field", None) or [None] * 3):
+        if tree is not None:
+            progs.append(np.ascontiguousarray(wl.math_tokens(tree)))
+            d.force_field[k] = _P(progs[-1])
+    return d, (lattice, phase, mats, log10E, progs)
 
 
 class Batch:

@@ -377,6 +377,12 @@ __device__ __forceinline__ void adj_voxel(const Dev &d, const Snap &s, const Adj
         F = sub(F, V{c.x, c.y, c.z});
     }
     F = add(F, V{0.0, 0.0, 0.0});
+    if (rp.ff[0] >= 0 || rp.ff[1] >= 0 || rp.ff[2] >= 0) {  // force field: depends on time only (record checks)
+        const V ff = force_field(d, rp, p4.x, p4.y, p4.z, s.T[(size_t)a.parity * d.nr + r]);
+        F.x += ff.x;
+        F.y += ff.y;
+        F.z += ff.z;
+    }
     V fric = F;
     bool contact = false, kinetic = false;
     V u{0, 0, 0};

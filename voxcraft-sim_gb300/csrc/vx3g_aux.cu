@@ -139,6 +139,27 @@ int recommended_dt_noalloc(const Dev &d, int device, double *out_host, cudaStrea
     return 0;
 }
 
+// ---------------------------------------------------------------- force field
+// VX3_Voxel::timeStep adds the three force-field programs evaluated at the voxel's
+// position and the current time (VX3_Voxel.cu:178-184).  They are evaluated here,
+// in FP64, before the voxel pass (positions and time are those the voxel pass
+// starts from), so the voxel kernels only add the stored force at the reference's
+// place in the sum.
+__global__ void k_force_field(Dev d, int parity) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= d.nv) return;
+    const int r = (int)d.vinfo[v].x;
+    const RobotP &rp = d.rp[r];
+    if (!rp.ff_any) return;
+    const double4 p = load_state(d, d.pos, v);
+    const V3<double> f = force_field(d, rp, p.x, p.y, p.z, d.T[(size_t)parity * d.nr + r]);
+    d.ffv[v] = make_double4(f.x, f.y, f.z, 0.0);
+}
+
+void launch_force_field(const Dev &d, int parity, cudaStream_t s) {
+    if (d.ffv && d.nv) k_force_field<<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity);
+}
+
 // ---------------------------------------------------------------- collision
 // The reference tests every pair of surface voxels each step (gpu_update_attach,
 // VX3_VoxelyzeKernel.cu:833-843).  Here each surface voxel keeps a list of the

@@ -186,6 +186,8 @@ struct vx3g_ctx {
     std::vector<unsigned char> vfixed;
     int64_t steps = 0;
     int shape_links = 0, shape_voxels = 0;  // launch shapes of the mixed passes (vx3g_autotune)
+    bool ff_pos = false;  // some robot's force field reads the voxel position
+    bool any_ff = false;  // some robot has a force field
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -243,6 +245,52 @@ struct vx3g_ctx {
 
 namespace {
 
+// Checks a math-tree program the way VX3_MathTree::eval would run it
+// (src/Utils/VX3_MathTree.h:50-191): known operators and variables, operators never
+// consume values not yet produced, mtEND within VX3G_MAX_MATH_TOKENS with exactly one
+// value left.  Sets *len (tokens including mtEND) and *reads_pos (x, y or z read).
+int check_math_program(const vx3g_math_token *t, int *len, bool *reads_pos, std::string *why) {
+    int vc = 0, pc = 0;
+    *reads_pos = false;
+    for (int i = 0; i < VX3G_MAX_MATH_TOKENS; i++) {
+        const int op = t[i].op;
+        if (op == 0) {
+            if (vc - pc != 1) {
+                *why = "the program leaves " + std::to_string(vc - pc) + " values (1 expected)";
+                return VX3G_ERR_INVALID;
+            }
+            *len = i + 1;
+            return VX3G_OK;
+        }
+        if (op == 4) {
+            const double w = t[i].value;
+            if (!(w >= -0.5 && w < 8.5)) {
+                *why = "mtVAR names no variable";
+                return VX3G_ERR_INVALID;
+            }
+            if (w < 2.5) *reads_pos = true;
+            if (w >= 4.5 && w < 7.5) {
+                *why = "variables angle, targetCloseness and numClosePairs (target tracking) are not supported";
+                return VX3G_ERR_UNSUPPORTED;
+            }
+        } else if ((op >= 5 && op <= 9) || (op >= 19 && op <= 22)) {
+            pc += 2;
+        } else if ((op >= 10 && op <= 18) || op == 23) {
+            pc += 1;
+        } else if (op < 1 || op > 3) {
+            *why = "unknown operator " + std::to_string(op);
+            return VX3G_ERR_INVALID;
+        }
+        if (pc > vc) {
+            *why = "an operator at token " + std::to_string(i) + " lacks operands";
+            return VX3G_ERR_INVALID;
+        }
+        vc++;
+    }
+    *why = "no mtEND within " + std::to_string(VX3G_MAX_MATH_TOKENS) + " tokens";
+    return VX3G_ERR_INVALID;
+}
+
 int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     if (!desc || desc->n_robots <= 0 || !desc->robots) return fail(VX3G_ERR_INVALID, "empty batch descriptor");
     if (desc->precision != VX3G_PRECISION_FP64 && desc->precision != VX3G_PRECISION_MIXED)
@@ -264,6 +312,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     std::vector<double> phase;
     std::vector<uint2> vinfo, linfo;
     std::vector<int> csurf;
+    std::vector<MathTok> ftok;
     c->voff.assign(c->nr + 1, 0);
     c->loff.assign(c->nr + 1, 0);
 
@@ -396,6 +445,22 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         rp.vary_temp = R.vary_temp ? 1 : 0;
         rp.expansion = R.enable_expansion ? 1 : 0;
         rp.collision = R.enable_collision ? 1 : 0;
+        rp.ff_pos = 0;
+        for (int k = 0; k < 3; k++) {  // Simulator/ForceField programs
+            rp.ff[k] = -1;
+            if (!R.force_field[k]) continue;
+            int len = 0, rc;
+            bool reads_pos = false;
+            std::string why;
+            if ((rc = check_math_program(R.force_field[k], &len, &reads_pos, &why)))
+                return fail(rc, "robot " + std::to_string(r) + ": force_field[" + std::to_string(k) + "]: " + why);
+            rp.ff[k] = (int)ftok.size();
+            for (int i = 0; i < len; i++) ftok.push_back(MathTok{R.force_field[k][i].op, 0, R.force_field[k][i].value});
+            rp.ff_pos |= reads_pos ? 1 : 0;
+            rp.ff_any = 1;
+            c->ff_pos |= reads_pos;
+            c->any_ff = true;
+        }
         // largest base size over the run bounds the envelope cutoff 1.25*bs
         // the envelope cutoff (bsa1+bsa2)*0.625 is at most 1.25*vox_size*fmax, fmax the largest
         // base-size factor 1+T*cte any voxel can reach: T spans the initial temperature and,
@@ -466,6 +531,11 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     d.rp = drp;
     d.vmat = dvm;
     d.lmat = dlm;
+    MathTok *dft;
+    if ((rc = c->upload(&dft, ftok))) return rc;
+    d.ftok = dft;
+    d.ffv = nullptr;
+    if (c->any_ff && (rc = c->alloc(&d.ffv, d.nv))) return rc;
     if ((rc = c->alloc(&d.dt, d.nr)) || (rc = c->alloc(&d.T, 2 * (size_t)d.nr)) || (rc = c->alloc(&d.status, d.nr)) ||
         (rc = c->alloc(&d.err, 1)) || (rc = c->alloc(&c->scratch, 4 * (size_t)d.nr + 4)))
         return rc;
@@ -511,6 +581,7 @@ void enqueue_links(vx3g_ctx *c) {
     else launch_links_mixed(c->d, c->stream, c->shape_links);
 }
 void enqueue_voxels(vx3g_ctx *c, int parity) {
+    launch_force_field(c->d, parity, c->stream);  // robots with a Simulator/ForceField only
     if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(c->d, parity, c->stream);
     else launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels);
 }
@@ -1106,6 +1177,8 @@ extern "C" {
 int vx3g_record(vx3g_ctx *c, int n, int k) {
     if (!c || n < 0 || k <= 0) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_record");
     if (c->precision != VX3G_PRECISION_FP64) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint runs on FP64 contexts");
+    if (c->ff_pos)
+        return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a force field that reads the voxel position is not implemented");
     CU(cudaSetDevice(c->device));
     CU(cudaStreamSynchronize(c->stream));
     c->free_record();

@@ -68,6 +68,15 @@ struct RobotP {
     int voff, nv, loff, nl, soff, ns;
     int floor, vary_temp, expansion, collision;
     int lchunks;  // > 0: lists built in shared memory (coll_list_robots), in this many chunks; 0: global hashed grid
+    int ff[3] = {-1, -1, -1};  // force-field programs (x, y, z): token offset in Dev::ftok, or -1 for none
+    int ff_pos = 0;            // 1: a force-field program reads the voxel position
+    int ff_any = 0;            // 1: the robot has a force field (k_force_field fills Dev::ffv)
+};
+
+// a math-tree token as vx3g_math_token lays it out (op, reserved, value)
+struct MathTok {
+    int op, reserved;
+    double value;
 };
 
 template <class R> struct Slot { R f[3]; R m[3]; };
@@ -124,6 +133,8 @@ struct Dev {
     int *hcount, *hstart, *hfill, *hsorted, *hblock;
     int hsize;      // power of two
     int *err;       // device error word
+    const MathTok *ftok;  // force-field programs of all robots, back to back
+    double4 *ffv;         // per voxel: this step's force-field force (robots with ff_any), or NULL
     double *com_part;  // [NR][com_tiles][4] partial sums of the centre of mass
     int com_tiles;     // tiles of kComTile voxels of the largest robot
     int nv, nl, nr, ns;
@@ -157,6 +168,8 @@ void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 // surface-voxel collision of one step: displacement check and list rebuild (one
 // cooperative kernel), then the narrow phase
 cudaError_t launch_collision(const Dev &d, cudaStream_t s);
+// the force field of every voxel of the robots that have one, into d.ffv (step parity's time)
+void launch_force_field(const Dev &d, int parity, cudaStream_t s);
 // one-time setup of the collision kernels (shared-memory size, grid); fills d.cgrid
 cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);

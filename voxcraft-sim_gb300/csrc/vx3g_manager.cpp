@@ -91,6 +91,49 @@ bool uses_only_time(const Node *n) {
     return true;
 }
 
+// The token program VX3_SimulationManager::ParseMathTree (src/VX3/VX3_SimulationManager.cu:
+// 157-275) writes for a formula element: every element below it, breadth first in
+// document order, pushed on a stack above mtEND and popped back (leaves first, mtEND
+// last); operator codes and variable indices as in include/vx3g.h.
+std::vector<vx3g_math_token> math_program(const Node *holder, const std::string &where) {
+    static const char *ops[] = {"mtEND", "mtCONST", "mtE", "mtPI", "mtVAR", "mtADD", "mtSUB", "mtMUL",
+                                "mtDIV", "mtPOW", "mtSQRT", "mtSIN", "mtCOS", "mtTAN", "mtATAN", "mtLOG",
+                                "mtINT", "mtABS", "mtNOT", "mtGREATERTHAN", "mtLESSTHAN", "mtAND", "mtOR", "mtNORMALCDF"};
+    static const char *vars[] = {"x", "y", "z", "hit", "t", "angle", "targetCloseness", "numClosePairs", "num_voxel"};
+    std::vector<const Node *> order, frontier{holder};
+    while (!frontier.empty()) {
+        std::vector<const Node *> next;
+        for (const Node *n : frontier)
+            for (auto &c : n->children) {
+                order.push_back(c.get());
+                next.push_back(c.get());
+            }
+        frontier.swap(next);
+    }
+    std::vector<vx3g_math_token> prog;
+    for (auto it = order.rbegin(); it != order.rend(); ++it) {
+        const Node *n = *it;
+        vx3g_math_token t{};
+        int op = -1;
+        for (int k = 1; k < 24; k++)
+            if (n->name == ops[k]) op = k;
+        if (op < 0) throw std::runtime_error(where + ": unknown math-tree operator " + n->name);
+        t.op = op;
+        const std::string text = vx3g::xml::trim(n->text);
+        if (op == 1) t.value = std::strtod(text.c_str(), nullptr);
+        if (op == 4) {
+            int v = -1;
+            for (int k = 0; k < 9; k++)
+                if (text == vars[k]) v = k;
+            if (v < 0) throw std::runtime_error(where + ": unknown math-tree variable " + text);
+            t.value = v;
+        }
+        prog.push_back(t);
+    }
+    prog.push_back(vx3g_math_token{});  // mtEND
+    return prog;
+}
+
 const Node *formula_root(const Node *holder) {  // the single operator element inside a formula holder
     if (!holder) return nullptr;
     for (auto &c : holder->children)
@@ -123,6 +166,7 @@ struct RobotSpec {
     std::vector<int> mat_rgba;  // 4 ints per material
     vx3g_robot_desc desc{};
     const Node *stop = nullptr, *fitness = nullptr;
+    std::vector<vx3g_math_token> ff[3];  // force-field programs (desc.force_field points here)
     std::unique_ptr<Node> doc;
     int record_step = 0, record_voxel = 1, record_link = 0, save_all = 0;
 };
@@ -151,10 +195,13 @@ void read_spec(RobotSpec &S) {
     if (vx3g::xml::get_int(root, "VXA.Simulator.EnableCilia", 0) || vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0) ||
         vx3g::xml::get_int(root, "VXA.Simulator.SecondaryExperiment", 0))
         throw std::runtime_error(S.filename + ": cilia, signals and secondary experiments are not supported");
-    for (const char *ax : {"x_forcefield", "y_forcefield", "z_forcefield"}) {
-        const Node *f = formula_root(vx3g::xml::find(root, std::string("VXA.Simulator.ForceField.") + ax));
-        if (f && !(f->name == "mtCONST" && eval_tree(f, MathVars{}) == 0.0))
-            throw std::runtime_error(S.filename + ": a non-zero force field is not supported");
+    const char *axes[3] = {"x_forcefield", "y_forcefield", "z_forcefield"};
+    for (int k = 0; k < 3; k++) {  // Simulator/ForceField (VX3_SimulationManager.cu:349-354)
+        const std::string key = std::string("VXA.Simulator.ForceField.") + axes[k];
+        const Node *holder = vx3g::xml::find(root, key);
+        if (!holder || !formula_root(holder)) continue;
+        S.ff[k] = math_program(holder, S.filename + ": " + key);
+        d.force_field[k] = S.ff[k].data();
     }
     d.enable_expansion = vx3g::xml::get_int(root, "VXA.Simulator.EnableExpansion", 0);
     S.record_step = vx3g::xml::get_int(root, "VXA.Simulator.RecordHistory.RecordStepSize", 0);

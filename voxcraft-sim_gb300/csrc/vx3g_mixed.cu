@@ -401,6 +401,10 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
             const double4 c = d.contact[v];
             F = sub(F, V3<float>{(float)c.x, (float)c.y, (float)c.z});
         }
+        if (rp.ff_any) {  // force field (VX3_Voxel.cu:178-184), evaluated in FP64 by k_force_field
+            const double4 ff = d.ffv[v];
+            F = add(F, V3<float>{(float)ff.x, (float)ff.y, (float)ff.z});
+        }
         // floor penetration bsa/2 - nom/2 - z with bsa = base size (VX3_Voxel.h:185-188)
         const float pen = 0.5f * ((pH.w - m.nom_hi) + (pL.w - m.nom_lo)) - (pH.z + pL.z);
         V3<float> fric = F;

@@ -152,6 +152,70 @@ template <class R> __device__ __forceinline__ void store_slot(Slot<R> *s, V3<R> 
     *s = o;
 }
 
+// VX3_MathTree::eval (src/Utils/VX3_MathTree.h:50-191): the token program is read in
+// order; each token's result is appended to a value queue and operators consume the
+// oldest unconsumed values (binary: values[pc + 1] op values[pc]).  Programs are
+// validated when the context is created (known operators, the consumption cursor
+// never passes the append cursor, mtEND within VX3G_MAX_MATH_TOKENS with exactly one
+// value left), so the queue indices stay in bounds.  Variables hit, angle,
+// targetCloseness and numClosePairs are 0 (the validated programs read none but hit,
+// which the reference never changes from 0).
+constexpr int kMaxMathTokens = 256;
+#if !defined(__CUDACC__)
+// host builds of this header (the host-compiled adjoint checks): Phi(x) = erfc(-x/sqrt 2)/2
+inline double normcdf(double x) { return 0.5 * std::erfc(-x / std::sqrt(2.0)); }
+#endif
+
+__device__ inline double math_eval(const MathTok *tok, double x, double y, double z, double t, double num_voxel) {
+    double vals[kMaxMathTokens];
+    int vc = 0, pc = 0;
+    for (int i = 0; i < kMaxMathTokens; i++) {
+        const MathTok k = tok[i];
+        double r;
+        switch (k.op) {
+            case 0: return vals[pc < vc ? pc : 0];  // mtEND
+            case 1: r = k.value; break;
+            case 2: r = 2.71828182845904523536; break;
+            case 3: r = 3.14159265358979323846; break;
+            case 4: {
+                const double w = k.value;
+                r = w < 0.5 ? x : w < 1.5 ? y : w < 2.5 ? z : (w >= 3.5 && w < 4.5) ? t : (w >= 7.5 && w < 8.5) ? num_voxel : 0.0;
+                break;
+            }
+            case 5: r = vals[pc + 1] + vals[pc]; pc += 2; break;
+            case 6: r = vals[pc + 1] - vals[pc]; pc += 2; break;
+            case 7: r = vals[pc + 1] * vals[pc]; pc += 2; break;
+            case 8: r = vals[pc + 1] / vals[pc]; pc += 2; break;
+            case 9: r = pow(vals[pc + 1], vals[pc]); pc += 2; break;
+            case 10: r = sqrt(vals[pc]); pc++; break;
+            case 11: r = sin(vals[pc]); pc++; break;
+            case 12: r = cos(vals[pc]); pc++; break;
+            case 13: r = tan(vals[pc]); pc++; break;
+            case 14: r = atan(vals[pc]); pc++; break;
+            case 15: r = log(vals[pc]); pc++; break;
+            case 16: r = rint(vals[pc]); pc++; break;
+            case 17: r = fabs(vals[pc]); pc++; break;
+            case 18: r = !vals[pc]; pc++; break;
+            case 19: r = vals[pc + 1] > vals[pc]; pc += 2; break;
+            case 20: r = vals[pc + 1] < vals[pc]; pc += 2; break;
+            case 21: r = vals[pc + 1] && vals[pc]; pc += 2; break;
+            case 22: r = vals[pc + 1] || vals[pc]; pc += 2; break;
+            case 23: r = normcdf(vals[pc]); pc++; break;
+            default: return 0.0;
+        }
+        vals[vc++] = r;
+    }
+    return 0.0;
+}
+
+// the force field of robot rp at position (x, y, z) and time t (VX3_Voxel.cu:178-184)
+__device__ inline V3<double> force_field(const Dev &d, const RobotP &rp, double x, double y, double z, double t) {
+    const double nv = (double)rp.nv;
+    return V3<double>{rp.ff[0] >= 0 ? math_eval(d.ftok + rp.ff[0], x, y, z, t, nv) : 0.0,
+                      rp.ff[1] >= 0 ? math_eval(d.ftok + rp.ff[1], x, y, z, t, nv) : 0.0,
+                      rp.ff[2] >= 0 ? math_eval(d.ftok + rp.ff[2], x, y, z, t, nv) : 0.0};
+}
+
 // ------------------------------------------------------------- link pass
 template <class R> __device__ __forceinline__ void link_update(const Dev &d, int l) {
     const uint2 li = d.linfo[l];
@@ -360,7 +424,13 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
             const double4 c = d.contact[v];
             F = sub(F, V3<double>{c.x, c.y, c.z});
         }
-        F = add(F, V3<double>{0.0, 0.0, 0.0});  // cilia (zero) and the constant-0 force field
+        F = add(F, V3<double>{0.0, 0.0, 0.0});  // cilia (zero, VX3_Voxel.cu:377)
+        if (rp.ff_any) {  // force field (VX3_Voxel.cu:178-184), evaluated by k_force_field
+            const double4 ff = d.ffv[v];
+            F.x += ff.x;
+            F.y += ff.y;
+            F.z += ff.z;
+        }
         V3<double> fric = F;
         if (floorOn) {  // floorForce (VX3_Voxel.cu:399-426)
             if (pen >= 0) {
@@ -406,6 +476,10 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
         if (rp.collision) {
             const double4 c = d.contact[v];
             F = sub(F, V3<float>{(float)c.x, (float)c.y, (float)c.z});
+        }
+        if (rp.ff_any) {
+            const double4 ff = d.ffv[v];
+            F = add(F, V3<float>{(float)ff.x, (float)ff.y, (float)ff.z});
         }
         V3<float> fric = F;
         if (floorOn) {

@@ -59,6 +59,7 @@ class Robot:
     enable_collision: bool = False
     volume_effects: bool = True
     log10E: Optional[np.ndarray] = None   # float64 [Z, Y, X] per-voxel log10 E (C ABI only; not in VXA)
+    force_field: Optional[list] = None    # Simulator/ForceField: [x, y, z] math trees (see math_tokens) or None
     stop_time: Optional[float] = None     # StopConditionFormula "t - stop_time" (> 0 stops)
     fitness_x: bool = False               # FitnessFunction "x" (COM displacement along x)
     record_step: int = 0                  # RecordHistory/RecordStepSize
@@ -127,6 +128,55 @@ def bernoulli_body(rng: np.random.Generator, dims: Sequence[int], p: float, mate
     return Robot(grid=grid, materials=materials, phase=phase, **kw)
 
 
+# ------------------------------------------------------------------ math trees
+# A math tree is a nested tuple (op, arg...): ("mtCONST", 1.5), ("mtVAR", "z"),
+# ("mtSUB", a, b) = a - b.  Operator codes are VX3_MathTreeOperator's order
+# (src/Utils/VX3_MathTree.h:4-28); variables are the mtVAR names of
+# VX3_SimulationManager::ParseMathTree (src/VX3/VX3_SimulationManager.cu:193-217).
+MT_OPS = ["mtEND", "mtCONST", "mtE", "mtPI", "mtVAR", "mtADD", "mtSUB", "mtMUL", "mtDIV", "mtPOW", "mtSQRT", "mtSIN",
+          "mtCOS", "mtTAN", "mtATAN", "mtLOG", "mtINT", "mtABS", "mtNOT", "mtGREATERTHAN", "mtLESSTHAN", "mtAND",
+          "mtOR", "mtNORMALCDF"]
+MT_VARS = ["x", "y", "z", "hit", "t", "angle", "targetCloseness", "numClosePairs", "num_voxel"]
+
+
+def math_tokens(tree) -> np.ndarray:
+    """(op, value) tokens of a math tree in the order ParseMathTree writes them
+    (src/VX3/VX3_SimulationManager.cu:157-275): every element below the formula
+    element, breadth first in document order, pushed on a stack after mtEND and
+    popped back, so the program runs leaves-first and ends with mtEND."""
+    order = []
+    frontier = [tree]
+    order.append(tree)
+    while frontier:
+        nxt = []
+        for node in frontier:
+            for child in node[1:]:
+                if isinstance(child, tuple):
+                    order.append(child)
+                    nxt.append(child)
+        frontier = nxt
+    toks = []
+    for node in reversed(order):
+        op = node[0]
+        if op == "mtCONST":
+            toks.append((1, 0, float(node[1])))
+        elif op == "mtVAR":
+            toks.append((4, 0, float(MT_VARS.index(node[1]))))
+        else:
+            toks.append((MT_OPS.index(op), 0, 0.0))
+    toks.append((0, 0, 0.0))
+    return np.array(toks, dtype=[("op", np.int32), ("reserved", np.int32), ("value", np.float64)])
+
+
+def math_tree_xml(tree) -> str:
+    op = tree[0]
+    if op == "mtCONST":
+        return f"<mtCONST>{_fmt(tree[1])}</mtCONST>"
+    if op == "mtVAR":
+        return f"<mtVAR>{tree[1]}</mtVAR>"
+    return f"<{op}>" + "".join(math_tree_xml(c) for c in tree[1:]) + f"</{op}>"
+
+
 def _fmt(v: float) -> str:
     return repr(float(v))
 
@@ -176,6 +226,9 @@ def to_vxa(r: Robot) -> str:
            *([f"<StopCondition><StopConditionFormula><mtSUB><mtVAR>t</mtVAR><mtCONST>{_fmt(r.stop_time)}</mtCONST>"
               "</mtSUB></StopConditionFormula></StopCondition>"] if r.stop_time is not None else []),
            *(["<FitnessFunction><mtVAR>x</mtVAR></FitnessFunction>"] if r.fitness_x else []),
+           *(["<ForceField>" + "".join(f"<{a}_forcefield>{math_tree_xml(t)}</{a}_forcefield>"
+                                        for a, t in zip("xyz", r.force_field) if t is not None) + "</ForceField>"]
+             if r.force_field else []),
            *([f"<RecordHistory><RecordStepSize>{int(r.record_step)}</RecordStepSize><RecordVoxel>1</RecordVoxel>"
               "<RecordLink>0</RecordLink></RecordHistory>"] if r.record_step else []),
            "</Simulator>",
