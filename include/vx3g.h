@@ -62,6 +62,8 @@ typedef struct vx3g_material {
     int fixed;            /* Fixed */
     int is_measured;      /* isMeasured (counts toward the centre of mass) */
     double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
+    double cilia;            /* Cilia: scale of the cilia force (VX3_Voxel::force, src/VX3/VX3_Voxel.cu:376) */
+    double cilia_on_after;   /* TurnOnCiliaAfterThisManySeconds */
 } vx3g_material;
 
 /* One token of a math-tree program, the reference's VX3_MathTreeToken
@@ -108,6 +110,10 @@ typedef struct vx3g_robot_desc {
                                        step), num_voxel, and hit (the reference keeps it 0); programs
                                        that read angle, targetCloseness or numClosePairs (target
                                        tracking, not supported) are rejected with VX3G_ERR_UNSUPPORTED */
+    int enable_cilia;               /* Simulator/EnableCilia: gpu_update_cilia_force (VX3_VoxelyzeKernel.cu:846-859) */
+    const double *cilia_base;       /* nx*ny*nz*3 Structure/BaseCiliaForce vectors (per cell) or NULL for 0 */
+    const double *cilia_shift;      /* nx*ny*nz*3 Structure/ShiftCiliaForce vectors or NULL; scaled by the
+                                       voxel's signal, which stays 0 (signals are not supported) */
 } vx3g_robot_desc;
 
 typedef struct vx3g_batch_desc {

@@ -247,6 +247,16 @@ bool do_time_step(RefSim &S) {
         S.last_contact[3 * i + 2] = k->d_voxels[i].contactForce.z;
     }
 
+    // gpu_update_cilia_force (:846-859), before the voxel pass (:296-303)
+    if (k->EnableCilia) {
+        for (VX3_Voxel *v : S.surface) {
+            if (v->removed) continue;
+            if (v->mat->Cilia == 0) continue;
+            if (v->mat->TurnOnCiliaAfterThisManySeconds > k->currentTime) continue;
+            v->CiliaForce = v->orient.RotateVec3D(v->baseCiliaForce + v->localSignal * v->shiftCiliaForce);
+        }
+    }
+
     // gpu_update_voxels (:582-623), physics part
     for (int i = 0; i < k->num_d_voxels; i++) {
         VX3_Voxel *t = &k->d_voxels[i];
@@ -320,6 +330,10 @@ int vx3ref_set_force_field(void *h, int axis, const void *tokens, int n) {
     for (int i = 0; i < n; i++) dst[i].set((VX3_MathTreeOperator)t[i].op, t[i].value);
     return 0;
 }
+
+// VXA.Simulator.EnableCilia, read by VX3_SimulationManager::readVXD through the
+// property tree (VX3_SimulationManager.cu:360)
+void vx3ref_set_cilia(void *h, int enable) { ((RefSim *)h)->k->EnableCilia = enable; }
 
 void vx3ref_destroy(void *h) { /* the reference frees nothing reliably either; leak in tests */ (void)h; }
 

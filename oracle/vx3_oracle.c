@@ -7,7 +7,8 @@
  * float and double exactly (build with -ffp-contract=off).
  *
  * Scope: linear materials (MatModel 0/1), static lattice topology (no
- * attach/detach/removal), no boundary-condition regions, no signals/cilia;
+ * attach/detach/removal), no boundary-condition regions, no signals (cilia
+ * with the signal at 0);
  * force field: the robot's x/y/z math-tree programs (constant 0 when absent, the
  * reference default, VX3_ForceField.h:10-20), target-tracking variables 0.
  */
@@ -144,6 +145,7 @@ typedef struct {
     float mass, mass_inv, sqrt_mass, mom_inertia, mom_inertia_inv, c2xSqMxExS, c2xSqIxExSxSxS;
     int fixed, is_measured;
     double thermal_on_after;
+    double cilia, cilia_on_after; /* Cilia, TurnOnCiliaAfterThisManySeconds (VX_Object.cpp:1429,1437) */
 } vmat;
 
 typedef struct {
@@ -176,6 +178,8 @@ static void vmat_derive(vmat *m) {
  * 145-148; setters src/old/VX_Material.cpp:372-532). */
 static void vmat_import(vmat *m, const vxo_material *in, const vxo_robot *r) {
     memset(m, 0, sizeof(*m));
+    m->cilia = in->cilia;
+    m->cilia_on_after = in->cilia_on_after;
     float E = (float)in->E;
     float fail = in->model == 1 ? (float)in->fail_stress : -1.0f;
     m->E = E;
@@ -279,6 +283,7 @@ typedef struct {
     int surface_stale, diverged;
     int threads; /* > 1: timing mode, loops run under OpenMP */
     vxo_math_token *ff[3]; /* force-field programs (copies) or NULL */
+    vec *cilia_base;       /* per voxel: BaseCiliaForce + 0 * ShiftCiliaForce (the signal stays 0), or NULL */
 } sim;
 
 /* VX3_MathTree::eval (src/Utils/VX3_MathTree.h:50-191): tokens in order, each result
@@ -354,6 +359,7 @@ static void update_rest(sim *S, link *L) {
 void *vxo_create(const vxo_robot *r) {
     sim *S = (sim *)calloc(1, sizeof(sim));
     S->r = *r;
+    S->r.cilia_base = S->r.cilia_shift = NULL;
     for (int k = 0; k < 3; k++) {
         S->r.force_field[k] = NULL;
         if (!r->force_field[k]) continue;
@@ -417,6 +423,16 @@ void *vxo_create(const vxo_robot *r) {
             S->nl++;
         }
     }
+    if (r->enable_cilia) { /* VX_Sim.cpp:102-105: per-voxel cilia vectors in voxel order */
+        S->cilia_base = (vec *)calloc(S->nv ? S->nv : 1, sizeof(vec));
+        for (int c = 0; c < ncell; c++) {
+            if (vid[c] < 0) continue;
+            vec b = V(0, 0, 0), sh = V(0, 0, 0);
+            if (r->cilia_base) b = V(r->cilia_base[3 * c], r->cilia_base[3 * c + 1], r->cilia_base[3 * c + 2]);
+            if (r->cilia_shift) sh = V(r->cilia_shift[3 * c], r->cilia_shift[3 * c + 1], r->cilia_shift[3 * c + 2]);
+            S->cilia_base[vid[c]] = vadd(b, vscale(sh, 0.0)); /* base + localSignal * shift, signal 0 */
+        }
+    }
     free(vid);
     for (int i = 0; i < S->nl; i++) update_rest(S, &S->l[i]);
     S->surf = (int *)malloc(sizeof(int) * (S->nv ? S->nv : 1));
@@ -436,7 +452,7 @@ void vxo_destroy(void *h) {
     sim *S = (sim *)h;
     if (!S) return;
     free(S->vm); free(S->lm); free(S->v); free(S->l); free(S->surf); free(S->last_contact);
-    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]);
+    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]); free(S->cilia_base);
     free(S);
 }
 
@@ -571,7 +587,13 @@ static void voxel_update(sim *S, voxel *v, float dtf) {
     F.z += -m->mass * 9.80665f * m->grav_mult;
     F = vsub(F, v->contact);
     v->contact = V(0, 0, 0);
-    F = vadd(F, V(0.0 * 0.0, 0.0 * 0.0, 0.0 * 0.0)); /* CiliaForce * Cilia, both zero */
+    {   /* CiliaForce * Cilia (VX3_Voxel.cu:376); CiliaForce from gpu_update_cilia_force
+         * (VX3_VoxelyzeKernel.cu:846-859) for surface voxels, before the voxel pass */
+        vec cf = V(0, 0, 0);
+        if (S->cilia_base && !(v->flags & F_SURFACE) && m->cilia != 0 && !(m->cilia_on_after > S->t))
+            cf = qrot(v->orient, S->cilia_base[v - S->v]);
+        F = vadd(F, vscale(cf, m->cilia));
+    }
     /* force field (VX3_Voxel.cu:178-184; constant 0 unless the VXA gives one) */
     F.x += S->ff[0] ? math_eval(S->ff[0], v->pos.x, v->pos.y, v->pos.z, S->t, S->nv) : 0.0;
     F.y += S->ff[1] ? math_eval(S->ff[1], v->pos.x, v->pos.y, v->pos.z, S->t, S->nv) : 0.0;

@@ -23,6 +23,7 @@ typedef struct vxo_material {
     int model;               /* 0 = MDL_LINEAR, 1 = MDL_LINEAR_FAIL */
     int fixed, is_measured;
     double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
+    double cilia, cilia_on_after; /* Cilia, TurnOnCiliaAfterThisManySeconds */
 } vxo_material;
 
 /* A math-tree token (VX3_MathTreeToken, src/Utils/VX3_MathTree.h:29-36): op is the
@@ -45,6 +46,8 @@ typedef struct vxo_robot {
     int temp_enabled, vary_temp, enable_expansion, enable_collision, volume_effects;
     double bond_damping, col_damping, slow_damping;
     const vxo_math_token *force_field[3]; /* ForceField x/y/z programs (mtEND-terminated) or NULL */
+    int enable_cilia;                     /* Simulator/EnableCilia */
+    const double *cilia_base, *cilia_shift; /* nx*ny*nz*3 Base/ShiftCiliaForce per cell, or NULL */
 } vxo_robot;
 
 void *vxo_create(const vxo_robot *r);

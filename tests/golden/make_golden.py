@@ -68,6 +68,16 @@ def cases():
     out["bern5_force_field"] = (
         wl.bernoulli_body(rng, (5, 4, 3), 0.8, ffmats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
                           force_field=ff, z_offset=1), 300, 100)
+    # EnableCilia: per-voxel BaseCiliaForce/ShiftCiliaForce, a negative Cilia and a turn-on time
+    rng = np.random.default_rng(9)
+    cmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),
+             wl.Material(E=3e5, nu=0.35, cilia=-0.5, cilia_on_after=0.003), wl.Material(E=5e5, nu=0.35)]
+    cil = wl.bernoulli_body(rng, (5, 4, 3), 0.85, cmats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
+                            z_offset=1)
+    cil.enable_cilia = True
+    cil.cilia_base = 2e-2 * rng.standard_normal(cil.grid.shape + (3,))
+    cil.cilia_shift = 1e-2 * rng.standard_normal(cil.grid.shape + (3,))
+    out["bern5_cilia"] = (cil, 300, 100)
     return out
 
 
@@ -83,15 +93,19 @@ def snapshot(s):
 
 def robot_record(r):
     g, ph = r.padded()
-    mats = np.array([[m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress, m.fixed, m.is_measured]
-                     for m in r.materials], np.float64)
+    mats = np.array([[m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress, m.fixed, m.is_measured,
+                      m.cilia, m.cilia_on_after] for m in r.materials], np.float64)
     settings = dict(vox_size=r.vox_size, dt_frac=r.dt_frac, bond_damping=r.bond_damping, col_damping=r.col_damping,
                     slow_damping=r.slow_damping, gravity=r.gravity, grav_acc=r.grav_acc, floor=r.floor,
                     temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,
                     temp_base=r.temp_base, enable_expansion=r.enable_expansion, enable_collision=r.enable_collision,
-                    volume_effects=r.volume_effects, force_field=r.force_field)
-    return dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
-                settings=np.array(json.dumps(settings)))
+                    volume_effects=r.volume_effects, force_field=r.force_field, enable_cilia=r.enable_cilia)
+    rec = dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
+               settings=np.array(json.dumps(settings)))
+    for name in ("cilia_base", "cilia_shift"):  # per cell of the padded lattice, 3 values each
+        a = r.padded_cells(getattr(r, name))
+        rec[name] = a.reshape(g.shape + (3,)) if a is not None else np.zeros(0)
+    return rec
 
 
 def main():

@@ -22,7 +22,12 @@ def load(name):
         tup = lambda n: tuple(tup(c) if isinstance(c, list) else c for c in n)  # noqa: E731
         s["force_field"] = [None if t is None else tup(t) for t in s["force_field"]]
     mats = [wl.Material(E=m[0], nu=m[1], rho=m[2], cte=m[3], mu_static=m[4], mu_kinetic=m[5], fail_stress=m[6],
-                        fixed=int(m[7]), is_measured=int(m[8])) for m in d["materials"]]
+                        fixed=int(m[7]), is_measured=int(m[8]),
+                        cilia=float(m[9]) if len(m) > 9 else 0.0, cilia_on_after=float(m[10]) if len(m) > 10 else 0.0)
+            for m in d["materials"]]
     phase = d["phase"] if d["phase"].size else None
     robot = wl.Robot(grid=d["lattice"], materials=mats, phase=phase, z_offset=0, **s)
+    for name in ("cilia_base", "cilia_shift"):
+        if name in d.files and d[name].size:
+            setattr(robot, name, d[name])
     return robot, d

@@ -25,7 +25,8 @@ class VxoMaterial(ctypes.Structure):
     _fields_ = [("E", ctypes.c_double), ("nu", ctypes.c_double), ("rho", ctypes.c_double),
                 ("cte", ctypes.c_double), ("mu_static", ctypes.c_double), ("mu_kinetic", ctypes.c_double),
                 ("fail_stress", ctypes.c_double), ("model", ctypes.c_int), ("fixed", ctypes.c_int),
-                ("is_measured", ctypes.c_int), ("thermal_on_after", ctypes.c_double)]
+                ("is_measured", ctypes.c_int), ("thermal_on_after", ctypes.c_double),
+                ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double)]
 
 
 class VxoRobot(ctypes.Structure):
@@ -38,7 +39,8 @@ class VxoRobot(ctypes.Structure):
                 ("temp_enabled", ctypes.c_int), ("vary_temp", ctypes.c_int), ("enable_expansion", ctypes.c_int),
                 ("enable_collision", ctypes.c_int), ("volume_effects", ctypes.c_int),
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
-                ("force_field", ctypes.c_void_p * 3)]
+                ("force_field", ctypes.c_void_p * 3),
+                ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p)]
 
 
 def build_oracle():
@@ -185,7 +187,8 @@ def robot_struct(robot):
     mats = (VxoMaterial * max(len(robot.materials), 1))()
     for i, m in enumerate(robot.materials):
         mats[i] = VxoMaterial(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic,
-                              m.fail_stress, 0 if m.fail_stress == 0 else 1, m.fixed, m.is_measured, 0.0)
+                              m.fail_stress, 0 if m.fail_stress == 0 else 1, m.fixed, m.is_measured, 0.0,
+                              m.cilia, m.cilia_on_after)
     Z, Y, X = g.shape
     r = VxoRobot(X, Y, Z, _P(lattice), None if phase is None else _P(phase), len(robot.materials), mats,
                  robot.vox_size, robot.dt_frac, robot.grav_acc, int(robot.floor),
@@ -196,7 +199,15 @@ def robot_struct(robot):
     for k, t in enumerate(progs):
         if t is not None:
             r.force_field[k] = _P(t)
-    return r, (lattice, phase, mats, progs)
+    cil = []
+    if robot.enable_cilia:
+        r.enable_cilia = 1
+        for name in ("cilia_base", "cilia_shift"):
+            a = robot.padded_cells(getattr(robot, name))
+            if a is not None:
+                cil.append(a)
+                setattr(r, name, _P(a))
+    return r, (lattice, phase, mats, progs, cil)
 
 
 def _force_field_tokens(robot):
@@ -230,4 +241,7 @@ def ref_sim(robot) -> Sim:
     for k, t in enumerate(progs):
         if t is not None:
             assert lib.vx3ref_set_force_field(h, k, _P(t), len(t)) == 0
+    lib.vx3ref_set_cilia.restype = None
+    lib.vx3ref_set_cilia.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.vx3ref_set_cilia(h, int(robot.enable_cilia))
     return Sim(lib, "vx3ref_", h, progs)

@@ -101,3 +101,30 @@ def test_runner_force_field_matches_oracle(tmp_path):
     free = wl.Robot(**{**robot.__dict__, "force_field": None})
     f, _, _ = _oracle_until(free, 0.01)
     assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size  # the field moved the robot
+
+
+def test_runner_cilia_matches_oracle(tmp_path):
+    """EnableCilia with Structure/BaseCiliaForce and ShiftCiliaForce rows and per-material
+    Cilia / TurnOnCiliaAfterThisManySeconds, through the runner, against the oracle."""
+    vbuild.build()
+    exe = os.path.join(os.path.dirname(vbuild.LIB), "vx3g_sim")
+    rng = np.random.default_rng(12)
+    mats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),
+            wl.Material(E=3e5, nu=0.35, cilia=0.7, cilia_on_after=0.004)]
+    robot = wl.bernoulli_body(rng, (4, 4, 3), 0.85, mats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
+                              stop_time=0.01, fitness_x=True)
+    robot.enable_cilia = True
+    robot.cilia_base = 2e-2 * rng.standard_normal(robot.grid.shape + (3,))
+    robot.cilia_shift = 1e-2 * rng.standard_normal(robot.grid.shape + (3,))
+    (tmp_path / "base.vxa").write_text(wl.to_vxa(robot))
+    (tmp_path / "r.vxd").write_text("<VXD>\n</VXD>\n")
+    out = tmp_path / "report.xml"
+    r = subprocess.run([exe, "-i", str(tmp_path), "-o", str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    node = ET.parse(out).getroot().find("detail/r")
+    s, _, _ = _oracle_until(robot, 0.01)
+    com = [float(node.find(f"currentCenterOfMass/{k}").text) for k in "xyz"]
+    np.testing.assert_allclose(com, s.com(), rtol=0, atol=1e-6 * robot.vox_size)
+    free = wl.Robot(**{**robot.__dict__, "enable_cilia": False})
+    f, _, _ = _oracle_until(free, 0.01)
+    assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size  # the cilia moved the robot

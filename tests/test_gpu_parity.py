@@ -207,6 +207,20 @@ def test_adjoint_with_force_fields():
     assert np.median(errs) <= 0.03, errs
 
 
+def test_cilia_mixed_and_adjoint_guard():
+    """Cilia in a mixed-precision context stay within the mixed COM bar of the FP64
+    run, and the adjoint refuses cilia (its derivative is not formed)."""
+    robot, _ = golden_cases.load("bern5_cilia")
+    f = abi.Batch([robot], abi.PRECISION_FP64)
+    m = abi.Batch([robot], abi.PRECISION_MIXED)
+    f.step(300)
+    m.step(300)
+    rel = np.linalg.norm(m.com() - f.com(), axis=1) / np.linalg.norm(f.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
+    with pytest.raises(abi.Vx3gError, match="cilia"):
+        abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
+
+
 def test_mixed_com_error_vs_fp64():
     rng = np.random.default_rng(21)
     mats = [wl.Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]

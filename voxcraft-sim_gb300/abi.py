@@ -33,7 +33,7 @@ class Material(ctypes.Structure):
     _fields_ = [("E", ctypes.c_double), ("nu", ctypes.c_double), ("rho", ctypes.c_double), ("cte", ctypes.c_double),
                 ("mu_static", ctypes.c_double), ("mu_kinetic", ctypes.c_double), ("fail_stress", ctypes.c_double),
                 ("model", ctypes.c_int), ("fixed", ctypes.c_int), ("is_measured", ctypes.c_int),
-                ("thermal_on_after", ctypes.c_double)]
+                ("thermal_on_after", ctypes.c_double), ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double)]
 
 
 class RobotDesc(ctypes.Structure):
@@ -46,7 +46,8 @@ class RobotDesc(ctypes.Structure):
                 ("temp_enabled", ctypes.c_int), ("vary_temp", ctypes.c_int), ("enable_expansion", ctypes.c_int),
                 ("enable_collision", ctypes.c_int), ("volume_effects", ctypes.c_int),
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
-                ("log10E", ctypes.c_void_p), ("force_field", ctypes.c_void_p * 3)]
+                ("log10E", ctypes.c_void_p), ("force_field", ctypes.c_void_p * 3),
+                ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p)]
 
 
 class BatchDesc(ctypes.Structure):
@@ -122,7 +123,8 @@ def robot_desc(robot):
     mats = (Material * len(robot.materials))()
     for i, m in enumerate(robot.materials):
         mats[i] = Material(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress,
-                           0 if m.fail_stress == 0 else 1, int(m.fixed), int(m.is_measured), 0.0)
+                           0 if m.fail_stress == 0 else 1, int(m.fixed), int(m.is_measured), 0.0,
+                           float(m.cilia), float(m.cilia_on_after))
     Z, Y, X = g.shape
     log10E = getattr(robot, "log10E", None)
     if log10E is not None:
@@ -141,7 +143,15 @@ def robot_desc(robot):
         if tree is not None:
             progs.append(np.ascontiguousarray(wl.math_tokens(tree)))
             d.force_field[k] = _P(progs[-1])
-    return d, (lattice, phase, mats, log10E, progs)
+    cil = []
+    if robot.enable_cilia:
+        d.enable_cilia = 1
+        for name in ("cilia_base", "cilia_shift"):
+            a = robot.padded_cells(getattr(robot, name))
+            if a is not None:
+                cil.append(a)
+                setattr(d, name, _P(a))
+    return d, (lattice, phase, mats, log10E, progs, cil)
 
 
 class Batch:

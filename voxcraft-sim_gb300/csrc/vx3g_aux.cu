@@ -139,25 +139,39 @@ int recommended_dt_noalloc(const Dev &d, int device, double *out_host, cudaStrea
     return 0;
 }
 
-// ---------------------------------------------------------------- force field
+// ---------------------------------------------------------------- force field and cilia
 // VX3_Voxel::timeStep adds the three force-field programs evaluated at the voxel's
-// position and the current time (VX3_Voxel.cu:178-184).  They are evaluated here,
-// in FP64, before the voxel pass (positions and time are those the voxel pass
-// starts from), so the voxel kernels only add the stored force at the reference's
-// place in the sum.
-__global__ void k_force_field(Dev d, int parity) {
+// position and the current time (VX3_Voxel.cu:178-184), and force() adds
+// CiliaForce * Cilia (:376), CiliaForce being set for surface voxels by
+// gpu_update_cilia_force (VX3_VoxelyzeKernel.cu:846-859) as R(orient) (base + signal
+// * shift), the signal staying 0 here.  Both are evaluated in FP64 before the voxel
+// pass (from the position, orientation and time it starts with), so the voxel
+// kernels only add the stored forces at the reference's places in the sum.
+__global__ void k_extra_forces(Dev d, int parity) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= d.nv) return;
     const int r = (int)d.vinfo[v].x;
     const RobotP &rp = d.rp[r];
-    if (!rp.ff_any) return;
-    const double4 p = load_state(d, d.pos, v);
-    const V3<double> f = force_field(d, rp, p.x, p.y, p.z, d.T[(size_t)parity * d.nr + r]);
-    d.ffv[v] = make_double4(f.x, f.y, f.z, 0.0);
+    if (!rp.ff_any && !rp.cilia) return;
+    const double t = d.T[(size_t)parity * d.nr + r];
+    if (rp.cilia) {
+        const double4 c = d.cil[v];
+        V3<double> cf{0, 0, 0};
+        if (!(d.cil_on[v] > t)) {
+            const double4 q = load_state(d, d.quat, v);
+            cf = qrot(Q4<double>{q.x, q.y, q.z, q.w}, V3<double>{c.x, c.y, c.z});
+        }
+        d.cfv[v] = make_double4(cf.x * c.w, cf.y * c.w, cf.z * c.w, 0.0);
+    }
+    if (rp.ff_any) {
+        const double4 p = load_state(d, d.pos, v);
+        const V3<double> f = force_field(d, rp, p.x, p.y, p.z, t);
+        d.ffv[v] = make_double4(f.x, f.y, f.z, 0.0);
+    }
 }
 
-void launch_force_field(const Dev &d, int parity, cudaStream_t s) {
-    if (d.ffv && d.nv) k_force_field<<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity);
+void launch_extra_forces(const Dev &d, int parity, cudaStream_t s) {
+    if ((d.ffv || d.cfv) && d.nv) k_extra_forces<<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity);
 }
 
 // ---------------------------------------------------------------- collision

@@ -188,6 +188,7 @@ struct vx3g_ctx {
     int shape_links = 0, shape_voxels = 0;  // launch shapes of the mixed passes (vx3g_autotune)
     bool ff_pos = false;  // some robot's force field reads the voxel position
     bool any_ff = false;  // some robot has a force field
+    bool any_cilia = false;  // some robot has cilia
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -313,6 +314,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     std::vector<uint2> vinfo, linfo;
     std::vector<int> csurf;
     std::vector<MathTok> ftok;
+    std::vector<double4> cil_h;
+    std::vector<double> cil_on_h;
     c->voff.assign(c->nr + 1, 0);
     c->loff.assign(c->nr + 1, 0);
 
@@ -485,6 +488,32 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             if (!interior && R.enable_collision) csurf.push_back(v);
         }
         rp.ns = (int)csurf.size() - rp.soff;
+        // cilia (gpu_update_cilia_force, VX3_VoxelyzeKernel.cu:846-859): surface voxels of a
+        // material with Cilia != 0, once TurnOnCiliaAfterThisManySeconds has passed
+        cil_h.resize(pos.size(), make_double4(0, 0, 0, 0));
+        cil_on_h.resize(pos.size(), INFINITY);
+        rp.cilia = 0;
+        if (R.enable_cilia) {
+            for (int k = 0; k < nvr; k++) {
+                const int v = v0 + k;
+                const vx3g_material &M = R.materials[c->vmat_local[v]];
+                const short4 q = c->ijk[v];
+                const size_t cell = (size_t)q.x + (size_t)R.nx * ((size_t)q.y + (size_t)R.ny * (size_t)q.z);
+                double b[3] = {0, 0, 0}, sh[3] = {0, 0, 0};
+                for (int j = 0; j < 3; j++) {
+                    if (R.cilia_base) b[j] = R.cilia_base[3 * cell + j];
+                    if (R.cilia_shift) sh[j] = R.cilia_shift[3 * cell + j];
+                }
+                const double sig = 0.0;  // localSignal: signals are not simulated
+                cil_h[v] = make_double4(b[0] + sig * sh[0], b[1] + sig * sh[1], b[2] + sig * sh[2], M.cilia);
+                const bool interior = (vinfo[v].y & VF_LINKMASK) == VF_LINKMASK;
+                if (!interior && M.cilia != 0) {
+                    cil_on_h[v] = M.cilia_on_after;
+                    rp.cilia = 1;
+                }
+            }
+            c->any_cilia |= rp.cilia != 0;
+        }
         // lists in shared memory when the robot fits (lattice coordinates below 512, packed in 10 bits each)
         int cmax = 0;
         for (int k = 0; k < nvr; k++) {
@@ -536,6 +565,12 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     d.ftok = dft;
     d.ffv = nullptr;
     if (c->any_ff && (rc = c->alloc(&d.ffv, d.nv))) return rc;
+    d.cil = nullptr;
+    d.cil_on = nullptr;
+    d.cfv = nullptr;
+    if (c->any_cilia &&
+        ((rc = c->upload(&d.cil, cil_h)) || (rc = c->upload(&d.cil_on, cil_on_h)) || (rc = c->alloc(&d.cfv, d.nv))))
+        return rc;
     if ((rc = c->alloc(&d.dt, d.nr)) || (rc = c->alloc(&d.T, 2 * (size_t)d.nr)) || (rc = c->alloc(&d.status, d.nr)) ||
         (rc = c->alloc(&d.err, 1)) || (rc = c->alloc(&c->scratch, 4 * (size_t)d.nr + 4)))
         return rc;
@@ -581,7 +616,7 @@ void enqueue_links(vx3g_ctx *c) {
     else launch_links_mixed(c->d, c->stream, c->shape_links);
 }
 void enqueue_voxels(vx3g_ctx *c, int parity) {
-    launch_force_field(c->d, parity, c->stream);  // robots with a Simulator/ForceField only
+    launch_extra_forces(c->d, parity, c->stream);  // robots with a force field or cilia only
     if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(c->d, parity, c->stream);
     else launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels);
 }
@@ -1179,6 +1214,7 @@ int vx3g_record(vx3g_ctx *c, int n, int k) {
     if (c->precision != VX3G_PRECISION_FP64) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint runs on FP64 contexts");
     if (c->ff_pos)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a force field that reads the voxel position is not implemented");
+    if (c->any_cilia) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of cilia forces is not implemented");
     CU(cudaSetDevice(c->device));
     CU(cudaStreamSynchronize(c->stream));
     c->free_record();

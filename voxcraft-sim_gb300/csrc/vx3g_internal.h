@@ -70,7 +70,8 @@ struct RobotP {
     int lchunks;  // > 0: lists built in shared memory (coll_list_robots), in this many chunks; 0: global hashed grid
     int ff[3] = {-1, -1, -1};  // force-field programs (x, y, z): token offset in Dev::ftok, or -1 for none
     int ff_pos = 0;            // 1: a force-field program reads the voxel position
-    int ff_any = 0;            // 1: the robot has a force field (k_force_field fills Dev::ffv)
+    int ff_any = 0;            // 1: the robot has a force field (k_extra_forces fills Dev::ffv)
+    int cilia = 0;             // 1: EnableCilia with some cilia voxel (k_extra_forces fills Dev::cfv)
 };
 
 // a math-tree token as vx3g_math_token lays it out (op, reserved, value)
@@ -135,6 +136,9 @@ struct Dev {
     int *err;       // device error word
     const MathTok *ftok;  // force-field programs of all robots, back to back
     double4 *ffv;         // per voxel: this step's force-field force (robots with ff_any), or NULL
+    double4 *cil;         // per voxel: BaseCiliaForce + 0 * ShiftCiliaForce, material Cilia (robots with cilia)
+    double *cil_on;       // per voxel: the time cilia switch on (+inf: never; interior or Cilia 0)
+    double4 *cfv;         // per voxel: this step's CiliaForce * Cilia (robots with cilia), or NULL
     double *com_part;  // [NR][com_tiles][4] partial sums of the centre of mass
     int com_tiles;     // tiles of kComTile voxels of the largest robot
     int nv, nl, nr, ns;
@@ -168,8 +172,9 @@ void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 // surface-voxel collision of one step: displacement check and list rebuild (one
 // cooperative kernel), then the narrow phase
 cudaError_t launch_collision(const Dev &d, cudaStream_t s);
-// the force field of every voxel of the robots that have one, into d.ffv (step parity's time)
-void launch_force_field(const Dev &d, int parity, cudaStream_t s);
+// the force field (d.ffv) and the cilia force (d.cfv) of the voxels of robots that have
+// them, at the start of the step of the given time parity
+void launch_extra_forces(const Dev &d, int parity, cudaStream_t s);
 // one-time setup of the collision kernels (shared-memory size, grid); fills d.cgrid
 cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);

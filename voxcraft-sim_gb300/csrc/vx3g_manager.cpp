@@ -162,6 +162,7 @@ struct RobotSpec {
     std::string filename;
     std::vector<uint8_t> lattice;
     std::vector<double> phase;
+    std::vector<double> cilia_base, cilia_shift;  // 3 per cell, or empty
     std::vector<vx3g_material> mats;
     std::vector<int> mat_rgba;  // 4 ints per material
     vx3g_robot_desc desc{};
@@ -192,9 +193,9 @@ void read_spec(RobotSpec &S) {
     if (vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableAttach", false) ||
         vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableDetach", false))
         throw std::runtime_error(S.filename + ": runtime attach/detach is not supported");
-    if (vx3g::xml::get_int(root, "VXA.Simulator.EnableCilia", 0) || vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0) ||
-        vx3g::xml::get_int(root, "VXA.Simulator.SecondaryExperiment", 0))
-        throw std::runtime_error(S.filename + ": cilia, signals and secondary experiments are not supported");
+    if (vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0) || vx3g::xml::get_int(root, "VXA.Simulator.SecondaryExperiment", 0))
+        throw std::runtime_error(S.filename + ": signals and secondary experiments are not supported");
+    d.enable_cilia = vx3g::xml::get_int(root, "VXA.Simulator.EnableCilia", 0);  // VX3_SimulationManager.cu:360
     const char *axes[3] = {"x_forcefield", "y_forcefield", "z_forcefield"};
     for (int k = 0; k < 3; k++) {  // Simulator/ForceField (VX3_SimulationManager.cu:349-354)
         const std::string key = std::string("VXA.Simulator.ForceField.") + axes[k];
@@ -255,6 +256,8 @@ void read_spec(RobotSpec &S) {
             M.fixed = vx3g::xml::get_int(mech, "Fixed", 0);
             M.is_measured = vx3g::xml::get_int(mech, "isMeasured", 1);
             M.thermal_on_after = vx3g::xml::get_double(mech, "TurnOnThermalExpansionAfterThisManySeconds", 0.0);
+            M.cilia = vx3g::xml::get_double(mech, "Cilia", 0.0);  // VX_Object.cpp:1429, 1437
+            M.cilia_on_after = vx3g::xml::get_double(mech, "TurnOnCiliaAfterThisManySeconds", 0.0);
             S.mats.push_back(M);
             const Node *disp = m->child("Display");
             for (const char *c : {"Red", "Green", "Blue", "Alpha"})
@@ -303,6 +306,31 @@ void read_spec(RobotSpec &S) {
             }
         }
     }
+    // BaseCiliaForce / ShiftCiliaForce (VX_Object.cpp:1886-1958): three comma-separated values
+    // per cell of each layer, read for occupied cells, 0 where a row is short
+    for (int which = 0; which < 2; which++) {
+        const Node *cf = st->child(which ? "ShiftCiliaForce" : "BaseCiliaForce");
+        std::vector<double> &dst = which ? S.cilia_shift : S.cilia_base;
+        if (!cf) continue;
+        dst.assign(3 * S.lattice.size(), 0.0);
+        auto rows = cf->all("Layer");
+        for (int z = 0; z < d.nz && z < (int)rows.size(); z++) {
+            std::vector<double> vals;
+            const std::string &row = rows[z]->text;
+            size_t a = 0;
+            while (a <= row.size()) {
+                size_t b = row.find(',', a);
+                if (b == std::string::npos) b = row.size();
+                vals.push_back(std::atof(row.substr(a, b - a).c_str()));
+                a = b + 1;
+            }
+            for (size_t k = 0; k < layer; k++)
+                if (S.lattice[z * layer + k] > 0 && vals.size() > 3 * k + 2)
+                    for (int j = 0; j < 3; j++) dst[3 * (z * layer + k) + j] = vals[3 * k + j];
+        }
+    }
+    d.cilia_base = S.cilia_base.empty() ? nullptr : S.cilia_base.data();
+    d.cilia_shift = S.cilia_shift.empty() ? nullptr : S.cilia_shift.data();
     d.lattice = S.lattice.data();
     d.phase = S.phase.data();
     d.n_materials = (int)S.mats.size();

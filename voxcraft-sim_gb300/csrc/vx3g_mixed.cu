@@ -401,7 +401,11 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
             const double4 c = d.contact[v];
             F = sub(F, V3<float>{(float)c.x, (float)c.y, (float)c.z});
         }
-        if (rp.ff_any) {  // force field (VX3_Voxel.cu:178-184), evaluated in FP64 by k_force_field
+        if (rp.cilia) {  // CiliaForce * Cilia (VX3_Voxel.cu:376), evaluated in FP64 by k_extra_forces
+            const double4 c = d.cfv[v];
+            F = add(F, V3<float>{(float)c.x, (float)c.y, (float)c.z});
+        }
+        if (rp.ff_any) {  // force field (VX3_Voxel.cu:178-184), evaluated in FP64 by k_extra_forces
             const double4 ff = d.ffv[v];
             F = add(F, V3<float>{(float)ff.x, (float)ff.y, (float)ff.z});
         }

@@ -424,8 +424,13 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
             const double4 c = d.contact[v];
             F = sub(F, V3<double>{c.x, c.y, c.z});
         }
-        F = add(F, V3<double>{0.0, 0.0, 0.0});  // cilia (zero, VX3_Voxel.cu:377)
-        if (rp.ff_any) {  // force field (VX3_Voxel.cu:178-184), evaluated by k_force_field
+        if (rp.cilia) {  // CiliaForce * Cilia (VX3_Voxel.cu:376), from k_extra_forces
+            const double4 c = d.cfv[v];
+            F = add(F, V3<double>{c.x, c.y, c.z});
+        } else {
+            F = add(F, V3<double>{0.0, 0.0, 0.0});  // no cilia: CiliaForce is 0
+        }
+        if (rp.ff_any) {  // force field (VX3_Voxel.cu:178-184), evaluated by k_extra_forces
             const double4 ff = d.ffv[v];
             F.x += ff.x;
             F.y += ff.y;
@@ -476,6 +481,10 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
         if (rp.collision) {
             const double4 c = d.contact[v];
             F = sub(F, V3<float>{(float)c.x, (float)c.y, (float)c.z});
+        }
+        if (rp.cilia) {
+            const double4 c = d.cfv[v];
+            F = add(F, V3<float>{(float)c.x, (float)c.y, (float)c.z});
         }
         if (rp.ff_any) {
             const double4 ff = d.ffv[v];

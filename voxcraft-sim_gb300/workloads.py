@@ -33,6 +33,8 @@ class Material:
     fail_stress: float = 0.0   # 0 -> linear model without failure (MatModel 0)
     fixed: int = 0
     is_measured: int = 1
+    cilia: float = 0.0         # Cilia (scale of the cilia force)
+    cilia_on_after: float = 0.0  # TurnOnCiliaAfterThisManySeconds
     name: str = "mat"
 
 
@@ -60,12 +62,24 @@ class Robot:
     volume_effects: bool = True
     log10E: Optional[np.ndarray] = None   # float64 [Z, Y, X] per-voxel log10 E (C ABI only; not in VXA)
     force_field: Optional[list] = None    # Simulator/ForceField: [x, y, z] math trees (see math_tokens) or None
+    enable_cilia: bool = False            # Simulator/EnableCilia
+    cilia_base: Optional[np.ndarray] = None   # float64 [Z, Y, X, 3] BaseCiliaForce (only occupied cells read)
+    cilia_shift: Optional[np.ndarray] = None  # float64 [Z, Y, X, 3] ShiftCiliaForce
     stop_time: Optional[float] = None     # StopConditionFormula "t - stop_time" (> 0 stops)
     fitness_x: bool = False               # FitnessFunction "x" (COM displacement along x)
     record_step: int = 0                  # RecordHistory/RecordStepSize
 
     def occupied(self) -> np.ndarray:
         return self.grid > 0
+
+    def padded_cells(self, a):
+        """A per-cell [Z, Y, X, ...] array with the z_offset empty layers below, flattened
+        (x fastest), or None."""
+        if a is None:
+            return None
+        if self.z_offset:
+            a = np.concatenate([np.zeros((self.z_offset,) + a.shape[1:], a.dtype), a], axis=0)
+        return np.ascontiguousarray(a.reshape(-1).astype(np.float64))
 
     def padded(self):
         """Lattice with z_offset empty layers underneath, as written to the VXA."""
@@ -197,6 +211,14 @@ def structure_xml(r: Robot, replace: Optional[str] = None) -> str:
         for z in range(Z):
             out.append("<Layer><![CDATA[" + ",".join(repr(float(v)) for v in ph[z].reshape(-1)) + "]]></Layer>")
         out.append("</PhaseOffset>")
+    for tag, a in (("BaseCiliaForce", r.cilia_base), ("ShiftCiliaForce", r.cilia_shift)):
+        if a is None:
+            continue
+        cells = r.padded_cells(a).reshape(Z, Y * X * 3)
+        out.append(f"<{tag}>")
+        for z in range(Z):
+            out.append("<Layer><![CDATA[" + ",".join(repr(float(v)) for v in cells[z]) + "]]></Layer>")
+        out.append(f"</{tag}>")
     out.append("</Structure>")
     return "\n".join(out)
 
@@ -223,6 +245,7 @@ def to_vxa(r: Robot) -> str:
            f"<AttachDetach><EnableCollision>{int(r.enable_collision)}</EnableCollision>"
            "<EnableAttach>0</EnableAttach><EnableDetach>0</EnableDetach></AttachDetach>",
            f"<EnableExpansion>{int(r.enable_expansion)}</EnableExpansion>",
+           *([f"<EnableCilia>1</EnableCilia>"] if r.enable_cilia else []),
            *([f"<StopCondition><StopConditionFormula><mtSUB><mtVAR>t</mtVAR><mtCONST>{_fmt(r.stop_time)}</mtCONST>"
               "</mtSUB></StopConditionFormula></StopCondition>"] if r.stop_time is not None else []),
            *(["<FitnessFunction><mtVAR>x</mtVAR></FitnessFunction>"] if r.fitness_x else []),
@@ -252,6 +275,8 @@ def to_vxa(r: Robot) -> str:
             f"<Elastic_Mod>{_fmt(m.E)}</Elastic_Mod><Fail_Stress>{_fmt(m.fail_stress)}</Fail_Stress>"
             f"<Density>{_fmt(m.rho)}</Density><Poissons_Ratio>{_fmt(m.nu)}</Poissons_Ratio>"
             f"<CTE>{_fmt(m.cte)}</CTE><MaterialTempPhase>0</MaterialTempPhase>"
+            f"<Cilia>{_fmt(m.cilia)}</Cilia><TurnOnCiliaAfterThisManySeconds>{_fmt(m.cilia_on_after)}"
+            "</TurnOnCiliaAfterThisManySeconds>"
             f"<uStatic>{_fmt(m.mu_static)}</uStatic><uDynamic>{_fmt(m.mu_kinetic)}</uDynamic>"
             f"<Fixed>{int(m.fixed)}</Fixed><isMeasured>{int(m.is_measured)}</isMeasured>"
             "</Mechanical></Material>")
