@@ -114,6 +114,10 @@ typedef struct vx3g_robot_desc {
     const double *cilia_base;       /* nx*ny*nz*3 Structure/BaseCiliaForce vectors (per cell) or NULL for 0 */
     const double *cilia_shift;      /* nx*ny*nz*3 Structure/ShiftCiliaForce vectors or NULL; scaled by the
                                        voxel's signal, which stays 0 (signals are not supported) */
+    int enable_detach;              /* Simulator/AttachDetach/EnableDetach: a failed link leaves both voxels'
+                                       link tables after the collision pass (gpu_update_detach,
+                                       VX3_VoxelyzeKernel.cu:946-967); the surface, and the contact
+                                       candidates, follow from the next step (not with enable_cilia) */
 } vx3g_robot_desc;
 
 typedef struct vx3g_batch_desc {
@@ -164,7 +168,8 @@ int vx3g_get_links(vx3g_ctx *ctx, float *strain, float *max_strain, double *loca
  * link ends (neg, pos voxel indices, packed global), link axis (0 x, 1 y, 2 z). */
 int vx3g_get_topology(vx3g_ctx *ctx, int32_t *voxel_ijk, int32_t *voxel_mat, int32_t *link_ends,
                       int32_t *link_axis);
-/* Surface voxels (fewer than six links), global voxel indices in voxel order. */
+/* Surface voxels (fewer than six links), global voxel indices in voxel order; with
+ * enable_detach the set grows as links detach (vx3g_counts gives its current size). */
 int vx3g_get_surface(vx3g_ctx *ctx, int32_t *surface);
 
 int vx3g_com(vx3g_ctx *ctx, double *com /* 3 per robot */);

@@ -247,6 +247,22 @@ bool do_time_step(RefSim &S) {
         S.last_contact[3 * i + 2] = k->d_voxels[i].contactForce.z;
     }
 
+    // updateDetach / gpu_update_detach (:292-294, :946-967), after the collision pass
+    if (k->enableDetach) {
+        for (int i = 0; i < k->num_d_links; i++) {
+            VX3_Link *t = &k->d_links[i];
+            if (t->removed || t->isDetached) continue;
+            if (t->isFailed()) {
+                t->isDetached = true;
+                for (int j = 0; j < 6; j++) {
+                    if (t->pVNeg->links[j] == t) t->pVNeg->links[j] = NULL;
+                    if (t->pVPos->links[j] == t) t->pVPos->links[j] = NULL;
+                }
+                k->isSurfaceChanged = true;
+            }
+        }
+    }
+
     // gpu_update_cilia_force (:846-859), before the voxel pass (:296-303)
     if (k->EnableCilia) {
         for (VX3_Voxel *v : S.surface) {
@@ -334,6 +350,8 @@ int vx3ref_set_force_field(void *h, int axis, const void *tokens, int n) {
 // VXA.Simulator.EnableCilia, read by VX3_SimulationManager::readVXD through the
 // property tree (VX3_SimulationManager.cu:360)
 void vx3ref_set_cilia(void *h, int enable) { ((RefSim *)h)->k->EnableCilia = enable; }
+// VXA.Simulator.AttachDetach.EnableDetach (VX3_SimulationManager.cu:330)
+void vx3ref_set_detach(void *h, int enable) { ((RefSim *)h)->k->enableDetach = enable != 0; }
 
 void vx3ref_destroy(void *h) { /* the reference frees nothing reliably either; leak in tests */ (void)h; }
 

@@ -267,6 +267,7 @@ typedef struct {
     float strain, maxStrain, area, tss;
     double rest;
     int small, states;
+    int gone; /* detached (gpu_update_detach): no longer updated, no longer any voxel's link */
 } link;
 
 typedef struct {
@@ -748,6 +749,7 @@ static int do_step(sim *S) {
 #pragma omp parallel for if (S->threads > 1) schedule(static) reduction(| : div)
     for (int i = 0; i < S->nl; i++) {
         link *L = &S->l[i];
+        if (L->gone) continue;
         if (S->vm[S->v[L->neg].mat].fixed && S->vm[S->v[L->pos].mat].fixed) continue;
         link_update(S, L);
         if (L->strain > 100) div = 1;
@@ -770,6 +772,22 @@ static int do_step(sim *S) {
         else
             for (int a = 0; a < S->ns; a++)
                 for (int b = 0; b < a; b++) collide(S, &S->v[S->surf[a]], &S->v[S->surf[b]], S->surf[a], S->surf[b]);
+    }
+    /* gpu_update_detach (:946-967), after the collision pass: a failed link leaves both
+     * voxels' link tables; the surface is regenerated at the start of the next step */
+    if (r->enable_detach) {
+        for (int i = 0; i < S->nl; i++) {
+            link *L = &S->l[i];
+            if (L->gone) continue;
+            const lmat *m = &S->lm[L->mat];
+            if (!(m->eps_fail != -1.0f && L->maxStrain > m->eps_fail)) continue; /* VX3_Link::isFailed */
+            L->gone = 1;
+            for (int d = 0; d < 6; d++) {
+                if (S->v[L->neg].links[d] == i) S->v[L->neg].links[d] = -1;
+                if (S->v[L->pos].links[d] == i) S->v[L->pos].links[d] = -1;
+            }
+            S->surface_stale = 1;
+        }
     }
     for (int i = 0; i < S->nv; i++) {
         S->last_contact[3 * i] = S->v[i].contact.x;

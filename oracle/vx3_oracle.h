@@ -48,6 +48,7 @@ typedef struct vxo_robot {
     const vxo_math_token *force_field[3]; /* ForceField x/y/z programs (mtEND-terminated) or NULL */
     int enable_cilia;                     /* Simulator/EnableCilia */
     const double *cilia_base, *cilia_shift; /* nx*ny*nz*3 Base/ShiftCiliaForce per cell, or NULL */
+    int enable_detach;                    /* Simulator/AttachDetach/EnableDetach */
 } vxo_robot;
 
 void *vxo_create(const vxo_robot *r);

@@ -78,6 +78,14 @@ def cases():
     cil.cilia_base = 2e-2 * rng.standard_normal(cil.grid.shape + (3,))
     cil.cilia_shift = 1e-2 * rng.standard_normal(cil.grid.shape + (3,))
     out["bern5_cilia"] = (cil, 300, 100)
+    # EnableDetach: a brittle, thermally driven block; links fail in the first steps, interior
+    # voxels become surface voxels and the loose pieces collide
+    rng = np.random.default_rng(6)
+    bmats = [wl.Material(E=1e5, nu=0.0, fail_stress=2500.0, mu_static=0.2, mu_kinetic=0.1, cte=0.001)]
+    out["block4_detach"] = (wl.Robot(grid=np.ones((4, 4, 4), np.uint8), materials=bmats, volume_effects=False,
+                                     z_offset=0, enable_collision=True, enable_detach=True,
+                                     phase=rng.random((4, 4, 4)), temp_vary=True, temp_amplitude=30.0,
+                                     enable_expansion=1), 300, 100)
     return out
 
 
@@ -99,7 +107,8 @@ def robot_record(r):
                     slow_damping=r.slow_damping, gravity=r.gravity, grav_acc=r.grav_acc, floor=r.floor,
                     temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,
                     temp_base=r.temp_base, enable_expansion=r.enable_expansion, enable_collision=r.enable_collision,
-                    volume_effects=r.volume_effects, force_field=r.force_field, enable_cilia=r.enable_cilia)
+                    volume_effects=r.volume_effects, force_field=r.force_field, enable_cilia=r.enable_cilia,
+                    enable_detach=r.enable_detach)
     rec = dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
                settings=np.array(json.dumps(settings)))
     for name in ("cilia_base", "cilia_shift"):  # per cell of the padded lattice, 3 values each

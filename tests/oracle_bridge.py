@@ -40,7 +40,8 @@ class VxoRobot(ctypes.Structure):
                 ("enable_collision", ctypes.c_int), ("volume_effects", ctypes.c_int),
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
                 ("force_field", ctypes.c_void_p * 3),
-                ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p)]
+                ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
+                ("enable_detach", ctypes.c_int)]
 
 
 def build_oracle():
@@ -207,6 +208,7 @@ def robot_struct(robot):
             if a is not None:
                 cil.append(a)
                 setattr(r, name, _P(a))
+    r.enable_detach = int(robot.enable_detach)
     return r, (lattice, phase, mats, progs, cil)
 
 
@@ -244,4 +246,7 @@ def ref_sim(robot) -> Sim:
     lib.vx3ref_set_cilia.restype = None
     lib.vx3ref_set_cilia.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.vx3ref_set_cilia(h, int(robot.enable_cilia))
+    lib.vx3ref_set_detach.restype = None
+    lib.vx3ref_set_detach.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.vx3ref_set_detach(h, int(robot.enable_detach))
     return Sim(lib, "vx3ref_", h, progs)

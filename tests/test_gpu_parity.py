@@ -221,6 +221,27 @@ def test_cilia_mixed_and_adjoint_guard():
         abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
 
 
+def test_detach_surface_and_guards():
+    """EnableDetach: the surface grows as links detach (mixed and FP64 agree on it),
+    the adjoint refuses a changing link table, and cilia with detach is refused."""
+    robot, d = golden_cases.load("block4_detach")
+    f = abi.Batch([robot], abi.PRECISION_FP64)
+    m = abi.Batch([robot], abi.PRECISION_MIXED)
+    n0 = len(f.surface())
+    f.step(300)
+    m.step(300)
+    assert len(f.surface()) > n0
+    assert np.array_equal(f.surface(), d["s300_surface"])
+    assert np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - f.com(), axis=1) / np.linalg.norm(f.com(), axis=1)
+    assert np.all(rel <= 1e-4), rel
+    with pytest.raises(abi.Vx3gError, match="detach"):
+        abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
+    both = wl.Robot(**{**robot.__dict__, "enable_cilia": True})
+    with pytest.raises(abi.Vx3gError, match="detach"):
+        abi.Batch([both], abi.PRECISION_FP64)
+
+
 def test_mixed_com_error_vs_fp64():
     rng = np.random.default_rng(21)
     mats = [wl.Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]

@@ -47,7 +47,8 @@ class RobotDesc(ctypes.Structure):
                 ("enable_collision", ctypes.c_int), ("volume_effects", ctypes.c_int),
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
                 ("log10E", ctypes.c_void_p), ("force_field", ctypes.c_void_p * 3),
-                ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p)]
+                ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
+                ("enable_detach", ctypes.c_int)]
 
 
 class BatchDesc(ctypes.Structure):
@@ -143,6 +144,7 @@ def robot_desc(robot):
         if tree is not None:
             progs.append(np.ascontiguousarray(wl.math_tokens(tree)))
             d.force_field[k] = _P(progs[-1])
+    d.enable_detach = int(robot.enable_detach)
     cil = []
     if robot.enable_cilia:
         d.enable_cilia = 1
@@ -239,9 +241,12 @@ class Batch:
         return dict(ijk=ijk, mat=mat, negpos=ends, axis=axis)
 
     def surface(self):
-        s = np.zeros(max(self.ns, 1), np.int32)
+        """Surface voxels (fewer than six links) now; the set grows when links detach."""
+        nv, nl, ns = (ctypes.c_int(), ctypes.c_int(), ctypes.c_int())
+        _check(self.lib.vx3g_counts(self.h, ctypes.byref(nv), ctypes.byref(nl), ctypes.byref(ns)), "vx3g_counts")
+        s = np.zeros(max(ns.value, 1), np.int32)
         _check(self.lib.vx3g_get_surface(self.h, _P(s)), "vx3g_get_surface")
-        return s[:self.ns]
+        return s[:ns.value]
 
     def com(self):
         c = np.zeros((self.n_robots, 3))

@@ -174,6 +174,33 @@ void launch_extra_forces(const Dev &d, int parity, cudaStream_t s) {
     if ((d.ffv || d.cfv) && d.nv) k_extra_forces<<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity);
 }
 
+// ---------------------------------------------------------------- detach
+// gpu_update_detach (VX3_VoxelyzeKernel.cu:946-967), after the collision pass: a link
+// that has failed (VX3_Link::isFailed, maxStrain past the failure strain, VX3_Link.cu:78)
+// leaves the link tables of both voxels; the robot's surface, and so its contact
+// candidate lists, change from the next step on (regenerateSurfaceVoxels, :283-286).
+__global__ void k_detach(Dev d) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= d.nl) return;
+    const uint2 li = d.linfo[l];
+    const int r = (int)li.x;
+    if (!d.rp[r].detach || d.status[r] != 0) return;
+    const uint32_t fl = li.y;
+    if (fl & LF_GONE) return;
+    const LMat &m = d.lmat[fl >> 8];
+    if (!(m.eps_fail != -1.0f && d.strain[l].y > m.eps_fail)) return;
+    d.linfo[l].y = fl | LF_GONE;
+    const int a = (int)(fl & LF_AXIS);
+    const int2 e = d.ends[l];
+    atomicAnd(&d.vinfo[e.x].y, ~(1u << (2 * a)));      // the negative end's link toward +axis
+    atomicAnd(&d.vinfo[e.y].y, ~(1u << (2 * a + 1)));  // the positive end's link toward -axis
+    d.srf[r] = 1;
+}
+
+void launch_detach(const Dev &d, cudaStream_t s) {
+    if (d.any_detach && d.nl) k_detach<<<(d.nl + 255) / 256, 256, 0, s>>>(d);
+}
+
 // ---------------------------------------------------------------- collision
 // The reference tests every pair of surface voxels each step (gpu_update_attach,
 // VX3_VoxelyzeKernel.cu:833-843).  Here each surface voxel keeps a list of the
@@ -228,6 +255,15 @@ __device__ __forceinline__ void coll_check(const Dev &d, int s) {
     const int v = d.csurf[s];
     const float4 p = pos_f(d, v), q = d.cref[s];  // q.w: squared displacement limit
     d.cposf[s] = p;  // the positions a rebuild on the shared-memory path lists from
+    if (d.any_detach) {  // robots whose surface follows their link table
+        const uint2 vi = d.vinfo[v];
+        const RobotP &rp = d.rp[vi.x];
+        if (rp.detach && s == rp.soff && d.srf[vi.x]) {  // a link detached last step: new surface
+            d.srf[vi.x] = 0;
+            flag_robot(d, (int)vi.x);
+        }
+        if ((vi.y & VF_LINKMASK) == VF_LINKMASK) return;  // interior: not a surface voxel now
+    }
     const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
     if (ex * ex + ey * ey + ez * ez > q.w) flag_robot(d, (int)d.vinfo[v].x);
 }
@@ -315,16 +351,29 @@ __device__ __forceinline__ void coll_scatter(const Dev &d, int s) {
 }
 
 // 2. list every unlinked surface voxel of the same robot within cutoff + skin, ascending
+// the link-table bit of a voxel toward a face neighbour at lattice offset (dx, dy, dz):
+// bit 2a for +a, 2a + 1 for -a
+__device__ __forceinline__ int link_bit(int dx, int dy, int dz) {
+    return dx ? (dx > 0 ? 0 : 1) : dy ? (dy > 0 ? 2 : 3) : (dz > 0 ? 4 : 5);
+}
+
 __device__ __forceinline__ void coll_list(const Dev &d, int s) {
     const int v = d.csurf[s];
+    const uint32_t vfl = d.vinfo[v].y;
     const int r = (int)d.vinfo[v].x;
     if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // lists still valid, or built in shared memory
     const int4 c = d.ccell[s];
     const float4 pf = d.cposf[s];
     const RobotP &rp = d.rp[r];
+    const float lim = 0.49f * (float)rp.skin;  // rebuild when a voxel has moved farther than this
+    if ((vfl & VF_LINKMASK) == VF_LINKMASK) {  // interior (EnableDetach robots): no surface pairs
+        d.nnb[s] = 0;
+        d.cref[s] = make_float4(pf.x, pf.y, pf.z, lim * lim);
+        return;
+    }
     // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
     const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
-    const bool fixed = (d.vinfo[v].y & VF_FIXED) != 0;
+    const bool fixed = (vfl & VF_FIXED) != 0;
     const short4 ij = d.ijk[v];
     int *out = d.nbr + s;  // entry j at out[j*ns]: slot-major, so list reads coalesce across a warp
     const size_t ns = (size_t)d.ns;
@@ -345,10 +394,14 @@ __device__ __forceinline__ void coll_list(const Dev &d, int s) {
                     const float ex = tf.x - pf.x, ey = tf.y - pf.y, ez = tf.z - pf.z;
                     if (ex * ex + ey * ey + ez * ez > cut2) continue;
                     const int u = d.csurf[t];
-                    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): linked <=> face-adjacent in the lattice
+                    const uint32_t ufl = d.vinfo[u].y;
+                    if ((ufl & VF_LINKMASK) == VF_LINKMASK) continue;  // interior partner
+                    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them (face
+                    // neighbours whose link has not detached)
                     const short4 ik = d.ijk[u];
-                    if (abs(ik.x - ij.x) + abs(ik.y - ij.y) + abs(ik.z - ij.z) == 1) continue;
-                    if (fixed && (d.vinfo[u].y & VF_FIXED)) continue;
+                    const int ddx = ik.x - ij.x, ddy = ik.y - ij.y, ddz = ik.z - ij.z;
+                    if (abs(ddx) + abs(ddy) + abs(ddz) == 1 && ((vfl >> link_bit(ddx, ddy, ddz)) & 1u)) continue;
+                    if (fixed && (ufl & VF_FIXED)) continue;
                     if (nc == kNbrCap) {
                         overflow = true;
                         continue;
@@ -365,7 +418,6 @@ __device__ __forceinline__ void coll_list(const Dev &d, int s) {
             }
     if (overflow) atomicOr(&d.status[r], 2);
     d.nnb[s] = nc;
-    const float lim = 0.49f * (float)rp.skin;  // rebuild when a voxel has moved farther than this
     d.cref[s] = make_float4(pf.x, pf.y, pf.z, lim * lim);
 }
 
@@ -443,7 +495,9 @@ __device__ __forceinline__ void coll_list_robots(const Dev &d, unsigned char *ls
             float bx0 = INFINITY, by0 = INFINITY, bz0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY, bz1 = -INFINITY;
             for (int i = tid; i < n; i += T) {
                 const float4 q = __ldcg(&d.cposf[s0 + i]);
-                P[i] = make_float4(q.x, q.y, q.z, __uint_as_float(d.cpk[s0 + i]));
+                unsigned pk = d.cpk[s0 + i];
+                if (rp.detach && (d.vinfo[d.csurf[s0 + i]].y & VF_LINKMASK) == VF_LINKMASK) pk |= kPackInterior;
+                P[i] = make_float4(q.x, q.y, q.z, __uint_as_float(pk));
                 bx0 = fminf(bx0, q.x), by0 = fminf(by0, q.y), bz0 = fminf(bz0, q.z);
                 bx1 = fmaxf(bx1, q.x), by1 = fmaxf(by1, q.y), bz1 = fmaxf(bz1, q.z);
             }
@@ -538,10 +592,14 @@ __device__ __forceinline__ void coll_list_robots(const Dev &d, unsigned char *ls
         int nc = 0, i = 0;
         float4 pi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (valid) {
-            const LocalGrid g = G;
             i = srt[pos];
             pi = P[i];
+        }
+        if (valid && !(__float_as_uint(pi.w) & kPackInterior)) {  // interior voxels list nothing
+            const LocalGrid g = G;
             const unsigned ki = __float_as_uint(pi.w);
+            // the voxel's link table: face neighbours are excluded only while a link joins them
+            const unsigned imask = rp.detach ? d.vinfo[d.csurf[s0 + i]].y & VF_LINKMASK : VF_LINKMASK;
             const int3 c = local_cell(pi, g);
             // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
             const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
@@ -569,11 +627,15 @@ __device__ __forceinline__ void coll_list_robots(const Dev &d, unsigned char *ls
                             const float4 pt = P[t];
                             const float ex = pt.x - pi.x, ey = pt.y - pi.y, ez = pt.z - pi.z;
                             const unsigned kt = __float_as_uint(pt.w);
-                            // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): linked <=>
-                            // face-adjacent <=> the packed lattice difference is +-1, +-2^10 or +-2^20
-                            const int ad = abs((int)(ki & kPackMask) - (int)(kt & kPackMask));
-                            bool acc = ex * ex + ey * ey + ez * ez <= cut2 && t != i && ad != 1 && ad != (1 << 10) &&
-                                       ad != (1 << 20) && !(ki & kt & kPackFixed);
+                            // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them;
+                            // face neighbours have a packed lattice difference of +-1, +-2^10 or +-2^20
+                            const int dl = (int)(ki & kPackMask) - (int)(kt & kPackMask);
+                            const int ad = abs(dl);
+                            const bool face = ad == 1 || ad == (1 << 10) || ad == (1 << 20);
+                            const int bit = (ad == 1 ? 0 : ad == (1 << 10) ? 2 : 4) + (dl > 0 ? 1 : 0);
+                            const bool linked = face && ((imask >> bit) & 1u);
+                            bool acc = ex * ex + ey * ey + ez * ez <= cut2 && t != i && !linked &&
+                                       !(ki & kt & kPackFixed) && !(kt & kPackInterior);
                             if (!g.dense) {
                                 const int3 ct = local_cell(pt, g);
                                 acc = acc && ct.x == c.x + dx && ct.y == y && ct.z == z;  // same bucket, other cell

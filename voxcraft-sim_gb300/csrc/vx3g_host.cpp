@@ -189,6 +189,7 @@ struct vx3g_ctx {
     bool ff_pos = false;  // some robot's force field reads the voxel position
     bool any_ff = false;  // some robot has a force field
     bool any_cilia = false;  // some robot has cilia
+    bool any_detach = false;  // some robot has EnableDetach
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -448,6 +449,10 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         rp.vary_temp = R.vary_temp ? 1 : 0;
         rp.expansion = R.enable_expansion ? 1 : 0;
         rp.collision = R.enable_collision ? 1 : 0;
+        rp.detach = R.enable_detach ? 1 : 0;
+        c->any_detach |= R.enable_detach != 0;
+        if (R.enable_detach && R.enable_cilia)
+            return fail(VX3G_ERR_UNSUPPORTED, "robot " + std::to_string(r) + ": cilia together with detach (cilia act on the surface at creation)");
         rp.ff_pos = 0;
         for (int k = 0; k < 3; k++) {  // Simulator/ForceField programs
             rp.ff[k] = -1;
@@ -485,7 +490,9 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             const int v = v0 + k;
             const bool interior = (vinfo[v].y & VF_LINKMASK) == VF_LINKMASK;
             if (!interior) c->surface.push_back(v);
-            if (!interior && R.enable_collision) csurf.push_back(v);
+            // EnableDetach: any voxel may become a surface voxel, so all take part (interior
+            // ones are skipped while their six links hold)
+            if ((!interior || R.enable_detach) && R.enable_collision) csurf.push_back(v);
         }
         rp.ns = (int)csurf.size() - rp.soff;
         // cilia (gpu_update_cilia_force, VX3_VoxelyzeKernel.cu:846-859): surface voxels of a
@@ -571,6 +578,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     if (c->any_cilia &&
         ((rc = c->upload(&d.cil, cil_h)) || (rc = c->upload(&d.cil_on, cil_on_h)) || (rc = c->alloc(&d.cfv, d.nv))))
         return rc;
+    d.any_detach = c->any_detach ? 1 : 0;
+    if ((rc = c->alloc(&d.srf, (size_t)d.nr))) return rc;
     if ((rc = c->alloc(&d.dt, d.nr)) || (rc = c->alloc(&d.T, 2 * (size_t)d.nr)) || (rc = c->alloc(&d.status, d.nr)) ||
         (rc = c->alloc(&d.err, 1)) || (rc = c->alloc(&c->scratch, 4 * (size_t)d.nr + 4)))
         return rc;
@@ -616,9 +625,10 @@ void enqueue_links(vx3g_ctx *c) {
     else launch_links_mixed(c->d, c->stream, c->shape_links);
 }
 void enqueue_voxels(vx3g_ctx *c, int parity) {
+    launch_detach(c->d, c->stream);                // EnableDetach robots only (after the collision pass)
     launch_extra_forces(c->d, parity, c->stream);  // robots with a force field or cilia only
     if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(c->d, parity, c->stream);
-    else launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels);
+    else launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, !c->any_detach);  // detach writes voxel info
 }
 
 cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
@@ -708,11 +718,32 @@ int vx3g_synchronize(vx3g_ctx *c) {
 void *vx3g_stream(vx3g_ctx *c) { return c ? (void *)c->stream : nullptr; }
 int64_t vx3g_steps_taken(vx3g_ctx *c) { return c ? c->steps : -1; }
 
+// The surface voxels (fewer than six links) in voxel order: fixed at creation, or read
+// from the current link table when links can detach.
+static int current_surface(vx3g_ctx *c, std::vector<int> &out) {
+    if (!c->any_detach) {
+        out = c->surface;
+        return VX3G_OK;
+    }
+    std::vector<uint2> vi((size_t)c->d.nv);
+    if (c->d.nv) CU(cudaMemcpyAsync(vi.data(), c->d.vinfo, sizeof(uint2) * vi.size(), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    out.clear();
+    for (size_t v = 0; v < vi.size(); v++)
+        if ((vi[v].y & VF_LINKMASK) != VF_LINKMASK) out.push_back((int)v);
+    return VX3G_OK;
+}
+
 int vx3g_counts(vx3g_ctx *c, int *nv, int *nl, int *ns) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
     if (nv) *nv = c->d.nv;
     if (nl) *nl = c->d.nl;
-    if (ns) *ns = (int)c->surface.size();
+    if (ns) {
+        std::vector<int> cur;
+        int rc = current_surface(c, cur);
+        if (rc) return rc;
+        *ns = (int)cur.size();
+    }
     return VX3G_OK;
 }
 
@@ -852,7 +883,10 @@ int vx3g_get_topology(vx3g_ctx *c, int32_t *ijk, int32_t *vmat, int32_t *ends, i
 
 int vx3g_get_surface(vx3g_ctx *c, int32_t *surface) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
-    for (size_t i = 0; i < c->surface.size(); i++) surface[i] = c->surface[i];
+    std::vector<int> cur;
+    int rc = current_surface(c, cur);
+    if (rc) return rc;
+    for (size_t i = 0; i < cur.size(); i++) surface[i] = cur[i];
     return VX3G_OK;
 }
 
@@ -1215,6 +1249,7 @@ int vx3g_record(vx3g_ctx *c, int n, int k) {
     if (c->ff_pos)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a force field that reads the voxel position is not implemented");
     if (c->any_cilia) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of cilia forces is not implemented");
+    if (c->any_detach) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a changing link table (detach) is not implemented");
     CU(cudaSetDevice(c->device));
     CU(cudaStreamSynchronize(c->stream));
     c->free_record();

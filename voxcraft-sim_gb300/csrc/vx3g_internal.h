@@ -33,6 +33,7 @@ enum : uint32_t {
     LF_SMALL = 1u << 2,       // smallAngle
     LF_LVV = 1u << 3,         // LOCAL_VELOCITY_VALID
     LF_BOTH_FIXED = 1u << 4,  // both ends fixed: gpu_update_links skips the link
+    LF_GONE = 1u << 5,        // detached (gpu_update_detach): no longer updated, no voxel's link
 };
 
 struct VMat {  // one voxel material (global index), constants as the reference derives them
@@ -72,6 +73,7 @@ struct RobotP {
     int ff_pos = 0;            // 1: a force-field program reads the voxel position
     int ff_any = 0;            // 1: the robot has a force field (k_extra_forces fills Dev::ffv)
     int cilia = 0;             // 1: EnableCilia with some cilia voxel (k_extra_forces fills Dev::cfv)
+    int detach = 0;            // 1: EnableDetach (failed links leave; the surface follows the link table)
 };
 
 // a math-tree token as vx3g_math_token lays it out (op, reserved, value)
@@ -93,6 +95,7 @@ constexpr int kLocalListChunk = kLocalListThreads / 32 * 10;
 // packed lattice word of a voxel on that path: x | y << 10 | z << 20 | fixed << 31 (coordinates
 // below 512, so the difference of two packed words is face-adjacent iff it is +-1, +-2^10 or +-2^20)
 constexpr unsigned kPackMask = 0x3fffffffu, kPackFixed = 0x80000000u;
+constexpr unsigned kPackInterior = 0x40000000u;  // set while a voxel of an EnableDetach robot has six links
 constexpr int kLocalHash = 4096;  // buckets of the shared-memory grid (power of two)
 
 struct Dev {
@@ -139,6 +142,8 @@ struct Dev {
     double4 *cil;         // per voxel: BaseCiliaForce + 0 * ShiftCiliaForce, material Cilia (robots with cilia)
     double *cil_on;       // per voxel: the time cilia switch on (+inf: never; interior or Cilia 0)
     double4 *cfv;         // per voxel: this step's CiliaForce * Cilia (robots with cilia), or NULL
+    int *srf;             // [NR] a link of the robot detached this step: rebuild its lists next step
+    int any_detach;       // some robot has EnableDetach
     double *com_part;  // [NR][com_tiles][4] partial sums of the centre of mass
     int com_tiles;     // tiles of kComTile voxels of the largest robot
     int nv, nl, nr, ns;
@@ -165,7 +170,8 @@ struct LaunchShape { int threads, min_blocks; };
 constexpr int kMixedShapes = 6;
 extern const LaunchShape kLinkShapes[kMixedShapes], kVoxelShapes[kMixedShapes];
 void launch_links_mixed(const Dev &d, cudaStream_t s, int shape = 0);
-void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape = 0);
+// pdl = false when the kernel before it wrote voxel info (detach): no early start
+void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape = 0, bool pdl = true);
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s);
 void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
@@ -175,6 +181,8 @@ cudaError_t launch_collision(const Dev &d, cudaStream_t s);
 // the force field (d.ffv) and the cilia force (d.cfv) of the voxels of robots that have
 // them, at the start of the step of the given time parity
 void launch_extra_forces(const Dev &d, int parity, cudaStream_t s);
+// gpu_update_detach (VX3_VoxelyzeKernel.cu:946-967) for robots with EnableDetach
+void launch_detach(const Dev &d, cudaStream_t s);
 // one-time setup of the collision kernels (shared-memory size, grid); fills d.cgrid
 cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);

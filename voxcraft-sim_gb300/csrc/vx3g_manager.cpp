@@ -190,9 +190,9 @@ void read_spec(RobotSpec &S) {
     }
     d.volume_effects = vx3g::xml::get_bool(root, "VXA.Simulator.Features.VolumeEffectsEnabled", false);
     d.enable_collision = vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableCollision", true);
-    if (vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableAttach", false) ||
-        vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableDetach", false))
-        throw std::runtime_error(S.filename + ": runtime attach/detach is not supported");
+    if (vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableAttach", false))
+        throw std::runtime_error(S.filename + ": runtime attachment is not supported");
+    d.enable_detach = vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableDetach", false);  // :330
     if (vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0) || vx3g::xml::get_int(root, "VXA.Simulator.SecondaryExperiment", 0))
         throw std::runtime_error(S.filename + ": signals and secondary experiments are not supported");
     d.enable_cilia = vx3g::xml::get_int(root, "VXA.Simulator.EnableCilia", 0);  // VX3_SimulationManager.cu:360

@@ -198,7 +198,7 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     const int r = (int)li.x;
     if (d.status[r] != 0) return;
     const uint32_t fl = li.y;
-    if (fl & LF_BOTH_FIXED) return;
+    if (fl & (LF_BOTH_FIXED | LF_GONE)) return;
     const int axis = fl & LF_AXIS;
     const LMat &m = d.lmat[fl >> 8];
 
@@ -511,7 +511,7 @@ const LaunchShape kVoxelShapes[kMixedShapes] = {{256, 1}, {256, 3}, {128, 7}, {1
 
 // launch with programmatic stream serialization (see pdl_wait_then_release)
 template <typename... KArgs, typename... Args>
-static void launch_pdl(void (*kernel)(KArgs...), int n, int threads, cudaStream_t s, Args... args) {
+static void launch_pdl(void (*kernel)(KArgs...), int n, int threads, cudaStream_t s, bool pdl, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)((n + threads - 1) / threads));
     cfg.blockDim = dim3((unsigned)threads);
@@ -520,30 +520,30 @@ static void launch_pdl(void (*kernel)(KArgs...), int n, int threads, cudaStream_
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = pdl ? 1 : 0;
     cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
 void launch_links_mixed(const Dev &d, cudaStream_t s, int shape) {
     if (!d.nl) return;
     switch (shape) {
-        case 1: launch_pdl(k_links_mixed<256, 4>, d.nl, 256, s, d); break;
-        case 2: launch_pdl(k_links_mixed<128, 9>, d.nl, 128, s, d); break;
-        case 3: launch_pdl(k_links_mixed<128, 10>, d.nl, 128, s, d); break;
-        case 4: launch_pdl(k_links_mixed<64, 20>, d.nl, 64, s, d); break;
-        case 5: launch_pdl(k_links_mixed<256, 5>, d.nl, 256, s, d); break;
-        default: launch_pdl(k_links_mixed<256, 1>, d.nl, 256, s, d); break;
+        case 1: launch_pdl(k_links_mixed<256, 4>, d.nl, 256, s, true, d); break;
+        case 2: launch_pdl(k_links_mixed<128, 9>, d.nl, 128, s, true, d); break;
+        case 3: launch_pdl(k_links_mixed<128, 10>, d.nl, 128, s, true, d); break;
+        case 4: launch_pdl(k_links_mixed<64, 20>, d.nl, 64, s, true, d); break;
+        case 5: launch_pdl(k_links_mixed<256, 5>, d.nl, 256, s, true, d); break;
+        default: launch_pdl(k_links_mixed<256, 1>, d.nl, 256, s, true, d); break;
     }
 }
-void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape) {
+void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape, bool pdl) {
     if (!d.nv) return;
     switch (shape) {
-        case 1: launch_pdl(k_voxels_mixed<256, 3>, d.nv, 256, s, d, parity); break;
-        case 2: launch_pdl(k_voxels_mixed<128, 7>, d.nv, 128, s, d, parity); break;
-        case 3: launch_pdl(k_voxels_mixed<128, 8>, d.nv, 128, s, d, parity); break;
-        case 4: launch_pdl(k_voxels_mixed<64, 14>, d.nv, 64, s, d, parity); break;
-        case 5: launch_pdl(k_voxels_mixed<64, 16>, d.nv, 64, s, d, parity); break;
-        default: launch_pdl(k_voxels_mixed<256, 1>, d.nv, 256, s, d, parity); break;
+        case 1: launch_pdl(k_voxels_mixed<256, 3>, d.nv, 256, s, pdl, d, parity); break;
+        case 2: launch_pdl(k_voxels_mixed<128, 7>, d.nv, 128, s, pdl, d, parity); break;
+        case 3: launch_pdl(k_voxels_mixed<128, 8>, d.nv, 128, s, pdl, d, parity); break;
+        case 4: launch_pdl(k_voxels_mixed<64, 14>, d.nv, 64, s, pdl, d, parity); break;
+        case 5: launch_pdl(k_voxels_mixed<64, 16>, d.nv, 64, s, pdl, d, parity); break;
+        default: launch_pdl(k_voxels_mixed<256, 1>, d.nv, 256, s, pdl, d, parity); break;
     }
 }
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s) {

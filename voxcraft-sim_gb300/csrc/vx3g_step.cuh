@@ -222,7 +222,7 @@ template <class R> __device__ __forceinline__ void link_update(const Dev &d, int
     const int r = (int)li.x;
     if (d.status[r] != 0) return;
     uint32_t fl = li.y;
-    if (fl & LF_BOTH_FIXED) return;
+    if (fl & (LF_BOTH_FIXED | LF_GONE)) return;  // gpu_update_links skips both-fixed and detached links
     const int axis = fl & LF_AXIS;
     const int2 e = d.ends[l];
     const double4 pn = d.pos[e.x], pp = d.pos[e.y];

@@ -63,6 +63,7 @@ class Robot:
     log10E: Optional[np.ndarray] = None   # float64 [Z, Y, X] per-voxel log10 E (C ABI only; not in VXA)
     force_field: Optional[list] = None    # Simulator/ForceField: [x, y, z] math trees (see math_tokens) or None
     enable_cilia: bool = False            # Simulator/EnableCilia
+    enable_detach: bool = False           # Simulator/AttachDetach/EnableDetach (failed links leave the lattice)
     cilia_base: Optional[np.ndarray] = None   # float64 [Z, Y, X, 3] BaseCiliaForce (only occupied cells read)
     cilia_shift: Optional[np.ndarray] = None  # float64 [Z, Y, X, 3] ShiftCiliaForce
     stop_time: Optional[float] = None     # StopConditionFormula "t - stop_time" (> 0 stops)
@@ -243,7 +244,7 @@ def to_vxa(r: Robot) -> str:
            "</Damping>",
            f"<Features><VolumeEffectsEnabled>{int(r.volume_effects)}</VolumeEffectsEnabled></Features>",
            f"<AttachDetach><EnableCollision>{int(r.enable_collision)}</EnableCollision>"
-           "<EnableAttach>0</EnableAttach><EnableDetach>0</EnableDetach></AttachDetach>",
+           f"<EnableAttach>0</EnableAttach><EnableDetach>{int(r.enable_detach)}</EnableDetach></AttachDetach>",
            f"<EnableExpansion>{int(r.enable_expansion)}</EnableExpansion>",
            *([f"<EnableCilia>1</EnableCilia>"] if r.enable_cilia else []),
            *([f"<StopCondition><StopConditionFormula><mtSUB><mtVAR>t</mtVAR><mtCONST>{_fmt(r.stop_time)}</mtCONST>"
