@@ -268,19 +268,6 @@ __device__ __forceinline__ void coll_check(const Dev &d, int s) {
     if (ex * ex + ey * ey + ez * ez > q.w) flag_robot(d, (int)d.vinfo[v].x);
 }
 
-// hashed-grid path: bin the surface voxels of the due robots
-__device__ __forceinline__ void coll_bin(const Dev &d, int s) {
-    const int v = d.csurf[s];
-    const int r = (int)d.vinfo[v].x;
-    if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // rebuilt robots of the hashed-grid path only
-    const double ic = d.rp[r].inv_list_cell;
-    const double4 p = load_state(d, d.pos, v);
-    const int4 c = make_int4((int)floor(p.x * ic), (int)floor(p.y * ic), (int)floor(p.z * ic), r);
-    d.ccell[s] = c;
-    d.cposf[s] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.0f);
-    atomicAdd(&d.hcount[cell_hash(c.x, c.y, c.z, c.w, d.hsize - 1)], 1);
-}
-
 // exclusive scan of the inclusive-to-be value x over the kLocalListThreads threads of
 // the block; returns the exclusive prefix, *total the block's sum (wsum: NW ints)
 __device__ __forceinline__ int block_scan(int x, int *wsum, int *total) {
@@ -342,83 +329,271 @@ __device__ __forceinline__ void coll_scan_add(const Dev &d, int b, int *wsum) {
     __syncthreads();  // wsum is reused
 }
 
-__device__ __forceinline__ void coll_scatter(const Dev &d, int s) {
-    const int r = (int)d.vinfo[d.csurf[s]].x;
-    if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // the voxels coll_bin binned this step
-    const int4 c = d.ccell[s];
-    const int slot = atomicAdd(&d.hfill[cell_hash(c.x, c.y, c.z, c.w, d.hsize - 1)], 1);
-    d.hsorted[slot] = s;
-}
-
-// 2. list every unlinked surface voxel of the same robot within cutoff + skin, ascending
 // the link-table bit of a voxel toward a face neighbour at lattice offset (dx, dy, dz):
 // bit 2a for +a, 2a + 1 for -a
 __device__ __forceinline__ int link_bit(int dx, int dy, int dz) {
     return dx ? (dx > 0 ? 0 : 1) : dy ? (dy > 0 ? 2 : 3) : (dz > 0 ? 4 : 5);
 }
 
-__device__ __forceinline__ void coll_list(const Dev &d, int s) {
-    const int v = d.csurf[s];
-    const uint32_t vfl = d.vinfo[v].y;
-    const int r = (int)d.vinfo[v].x;
-    if (!d.cflag[1 + r] || d.rp[r].lchunks) return;  // lists still valid, or built in shared memory
-    const int4 c = d.ccell[s];
-    const float4 pf = d.cposf[s];
-    const RobotP &rp = d.rp[r];
-    const float lim = 0.49f * (float)rp.skin;  // rebuild when a voxel has moved farther than this
-    if ((vfl & VF_LINKMASK) == VF_LINKMASK) {  // interior (EnableDetach robots): no surface pairs
-        d.nnb[s] = 0;
-        d.cref[s] = make_float4(pf.x, pf.y, pf.z, lim * lim);
+// 2. lists of the robots too large for shared memory (the 64^3 body): one grid over all
+// of them in global memory.  Each due robot's surface voxels are binned into a dense
+// cell grid over its bounding box (cells of edge cutoff + skin), the robots' grids
+// back to back in the bucket table; if they do not fit, cells are hashed with the
+// robot id instead and each candidate's cell is compared.  A counting sort stores every
+// binned voxel's position and voxel index (spos) and lattice word (sij) in cell order,
+// so a candidate costs two independent loads; in a dense grid the 3 x 3 x 3
+// neighbourhood is 9 contiguous runs of buckets.  Three lanes per voxel scan one
+// dz-plane each, voxels taken in cell order, appending partners to sub-lists in shared
+// memory that are sorted and merged by rank, as on the shared-memory path.
+__device__ __forceinline__ unsigned fkey(float f) {  // order-preserving float -> unsigned
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(unsigned k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__device__ __forceinline__ bool grid_voxel(const Dev &d, int s, int *v, int *r) {  // a due voxel of a large robot
+    *v = d.csurf[s];
+    const uint2 vi = d.vinfo[*v];
+    *r = (int)vi.x;
+    return d.cflag[1 + *r] && !d.rp[*r].lchunks;
+}
+
+__device__ __forceinline__ int3 grid_cell(const GridP &g, float4 p, bool dense) {
+    int3 c = make_int3((int)floorf((p.x - g.mnx) * g.ic), (int)floorf((p.y - g.mny) * g.ic), (int)floorf((p.z - g.mnz) * g.ic));
+    if (dense) {
+        c.x = min(max(c.x, 0), g.gx - 1);
+        c.y = min(max(c.y, 0), g.gy - 1);
+        c.z = min(max(c.z, 0), g.gz - 1);
+    }
+    return c;
+}
+
+__device__ __forceinline__ int grid_bucket(const Dev &d, const GridP &g, int3 c, int r, bool dense) {
+    return dense ? g.base + (c.z * g.gy + c.y) * g.gx + c.x : (int)cell_hash(c.x, c.y, c.z, r, d.hsize - 1);
+}
+
+// (a) bounding boxes of the due robots' surface voxels; called by every thread of the
+// grid for the same s sequence (warp-uniform), a warp whose voxels are one robot's
+// reduces first so that the atomics are one per warp, not per voxel
+__device__ __forceinline__ void grid_box(const Dev &d, int s) {
+    int v = 0, r = -1;
+    bool valid = s < d.ns && grid_voxel(d, s, &v, &r) && (d.vinfo[v].y & VF_LINKMASK) != VF_LINKMASK;
+    unsigned k[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+    if (valid) {
+        const float4 p = d.cposf[s];
+        k[0] = k[3] = fkey(p.x);
+        k[1] = k[4] = fkey(p.y);
+        k[2] = k[5] = fkey(p.z);
+    }
+    const unsigned any = __ballot_sync(0xffffffffu, valid);
+    if (!any) return;
+    const int r0 = __shfl_sync(0xffffffffu, r, __ffs(any) - 1);
+    if (__all_sync(0xffffffffu, !valid || r == r0)) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            k[0] = min(k[0], __shfl_xor_sync(0xffffffffu, k[0], o));
+            k[1] = min(k[1], __shfl_xor_sync(0xffffffffu, k[1], o));
+            k[2] = min(k[2], __shfl_xor_sync(0xffffffffu, k[2], o));
+            k[3] = max(k[3], __shfl_xor_sync(0xffffffffu, k[3], o));
+            k[4] = max(k[4], __shfl_xor_sync(0xffffffffu, k[4], o));
+            k[5] = max(k[5], __shfl_xor_sync(0xffffffffu, k[5], o));
+        }
+        if ((threadIdx.x & 31) != 0) return;
+        r = r0;
+    } else if (!valid) {
         return;
     }
-    // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
-    const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
-    const bool fixed = (vfl & VF_FIXED) != 0;
+    unsigned *b = d.gbox + 6 * (size_t)r;
+    atomicMin(b + 0, k[0]), atomicMin(b + 1, k[1]), atomicMin(b + 2, k[2]);
+    atomicMax(b + 3, k[3]), atomicMax(b + 4, k[4]), atomicMax(b + 5, k[5]);
+}
+
+// (b) one thread: grid of every due robot, dense if all fit the bucket table
+__device__ void grid_params(const Dev &d) {
+    long long total = 0;
+    bool fits = true;
+    for (int r = 0; r < d.nr; r++) {
+        const RobotP &rp = d.rp[r];
+        if (rp.lchunks || !rp.ns || !d.cflag[1 + r]) continue;
+        unsigned *b = d.gbox + 6 * (size_t)r;
+        GridP g;
+        g.ic = (float)rp.inv_list_cell;
+        g.mnx = fkey_inv(b[0]), g.mny = fkey_inv(b[1]), g.mnz = fkey_inv(b[2]);
+        const float ex = (fkey_inv(b[3]) - g.mnx) * g.ic, ey = (fkey_inv(b[4]) - g.mny) * g.ic,
+                    ez = (fkey_inv(b[5]) - g.mnz) * g.ic;
+        g.gx = g.gy = g.gz = 1;
+        if (ex >= 0.0f && ey >= 0.0f && ez >= 0.0f && ex < 65536.0f && ey < 65536.0f && ez < 65536.0f) {
+            g.gx = (int)ex + 1, g.gy = (int)ey + 1, g.gz = (int)ez + 1;
+            const long long cells = (long long)g.gx * g.gy * g.gz;
+            g.base = (int)min(total, (long long)INT_MAX);
+            total += cells;
+        } else {
+            if (!(ex >= 0.0f && ey >= 0.0f && ez >= 0.0f)) g.mnx = g.mny = g.mnz = 0.0f;  // no finite box
+            fits = false;
+        }
+        d.ggrid[r] = g;
+        b[0] = b[1] = b[2] = 0xffffffffu;  // ready for the next rebuild
+        b[3] = b[4] = b[5] = 0u;
+    }
+    if (total > d.hsize) fits = false;
+    const int used = fits ? (int)((total + 1023) / 1024 * 1024) : d.hsize;
+    d.gmode[0] = fits ? 1 : 0;
+    d.gmode[1] = used;
+}
+
+// (c) count the due surface voxels per bucket
+__device__ __forceinline__ void grid_count(const Dev &d, int s) {
+    int v, r;
+    if (!grid_voxel(d, s, &v, &r)) return;
+    const RobotP &rp = d.rp[r];
+    const float4 p = d.cposf[s];
+    if ((d.vinfo[v].y & VF_LINKMASK) == VF_LINKMASK) {  // interior (EnableDetach): lists nothing
+        const float lim = 0.49f * (float)rp.skin;
+        d.nnb[s] = 0;
+        d.cref[s] = make_float4(p.x, p.y, p.z, lim * lim);
+        d.ccell[s].x = -1;
+        return;
+    }
+    const bool dense = d.gmode[0] != 0;
+    const GridP g = d.ggrid[r];
+    const int bk = grid_bucket(d, g, grid_cell(g, p, dense), r, dense);
+    d.ccell[s].x = bk;
+    atomicAdd(&d.hcount[bk], 1);
+}
+
+// (d) scatter into cell order: position + voxel index, lattice word, surface index
+__device__ __forceinline__ void grid_scatter(const Dev &d, int s) {
+    int v, r;
+    if (!grid_voxel(d, s, &v, &r)) return;
+    const int bk = d.ccell[s].x;
+    if (bk < 0) return;
+    const int slot = atomicAdd(&d.hfill[bk], 1);
+    if (slot < 0 || slot >= d.ns) return;
+    const float4 p = d.cposf[s];
     const short4 ij = d.ijk[v];
-    int *out = d.nbr + s;  // entry j at out[j*ns]: slot-major, so list reads coalesce across a warp
+    d.spos[slot] = make_float4(p.x, p.y, p.z, __int_as_float(v));
+    d.sij[slot] = make_short4(ij.x, ij.y, ij.z, (d.vinfo[v].y & VF_FIXED) ? 1 : 0);
+    d.ssurf[slot] = s;
+}
+
+// (e) the lists, three lanes per voxel in cell order; cand: kNbrCap ints per thread
+__device__ void grid_list(const Dev &d, int *cand) {
+    constexpr int T = kLocalListThreads;
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+    const int trio = lane / 3, q = lane - 3 * trio, tb = lane - q;
+    const bool dense = d.gmode[0] != 0;
+    const int used = d.gmode[1];
+    const int nbin = min(d.hstart[used - 1] + d.hcount[used - 1], d.ns);  // voxels binned
     const size_t ns = (size_t)d.ns;
-    int nc = 0;
-    bool overflow = false;
-    for (int dz = -1; dz <= 1; dz++)
-        for (int dy = -1; dy <= 1; dy++)
-            for (int dx = -1; dx <= 1; dx++) {
-                const int cx = c.x + dx, cy = c.y + dy, cz = c.z + dz;
-                const unsigned h = cell_hash(cx, cy, cz, r, d.hsize - 1);
-                const int b = d.hstart[h], n = d.hcount[h];
-                for (int k = 0; k < n; k++) {
-                    const int t = d.hsorted[b + k];
-                    if (t == s) continue;
-                    const int4 ct = d.ccell[t];
-                    if (ct.x != cx || ct.y != cy || ct.z != cz || ct.w != r) continue;
-                    const float4 tf = d.cposf[t];
-                    const float ex = tf.x - pf.x, ey = tf.y - pf.y, ez = tf.z - pf.z;
-                    if (ex * ex + ey * ey + ez * ez > cut2) continue;
-                    const int u = d.csurf[t];
-                    const uint32_t ufl = d.vinfo[u].y;
-                    if ((ufl & VF_LINKMASK) == VF_LINKMASK) continue;  // interior partner
-                    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them (face
-                    // neighbours whose link has not detached)
-                    const short4 ik = d.ijk[u];
-                    const int ddx = ik.x - ij.x, ddy = ik.y - ij.y, ddz = ik.z - ij.z;
-                    if (abs(ddx) + abs(ddy) + abs(ddz) == 1 && ((vfl >> link_bit(ddx, ddy, ddz)) & 1u)) continue;
-                    if (fixed && (ufl & VF_FIXED)) continue;
-                    if (nc == kNbrCap) {
-                        overflow = true;
-                        continue;
+    const int per_pass = gridDim.x * (T / 32) * 10;  // voxels per pass of the grid
+    for (int base = 0; base < nbin; base += per_pass) {  // uniform over the grid
+        const int k = base + (blockIdx.x * (T / 32) + wp) * 10 + trio;
+        const bool valid = lane < 30 && k < nbin;
+        int *my = cand + tid;  // this thread's sub-list, entry j at my[j*T]
+        int nc = 0, v = 0, s = 0;
+        float4 pv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (valid) {
+            s = d.ssurf[k];
+            pv = d.spos[k];
+            v = __float_as_int(pv.w);
+            const short4 ij = d.sij[k];
+            const uint2 vi = d.vinfo[v];
+            const int r = (int)vi.x;
+            const RobotP &rp = d.rp[r];
+            const GridP g = d.ggrid[r];
+            const int3 c = grid_cell(g, pv, dense);
+            // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
+            const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
+            const int z = c.z + q - 1;
+            if (!dense || (z >= 0 && z < g.gz)) {
+                for (int dy = -1; dy <= 1; dy++) {
+                    const int y = c.y + dy;
+                    if (dense && (y < 0 || y >= g.gy)) continue;
+                    for (int dx = -1; dx <= (dense ? -1 : 1); dx++) {
+                        int b, e;
+                        if (dense) {
+                            const int rw = g.base + (z * g.gy + y) * g.gx;
+                            b = d.hstart[rw + max(c.x - 1, 0)];
+                            e = d.hfill[rw + min(c.x + 1, g.gx - 1)];  // the bucket's end after the scatter
+                        } else {
+                            const int h = (int)cell_hash(c.x + dx, y, z, r, d.hsize - 1);
+                            b = d.hstart[h];
+                            e = d.hfill[h];
+                        }
+                        e = min(e, nbin);
+                        for (int j = b; j < e; j++) {
+                            const float4 pu = d.spos[j];
+                            const int u = __float_as_int(pu.w);
+                            const float ex = pu.x - pv.x, ey = pu.y - pv.y, ez = pu.z - pv.z;
+                            bool acc = u != v && ex * ex + ey * ey + ez * ez <= cut2;
+                            if (acc) {
+                                const short4 ik = d.sij[j];
+                                if (!dense) {  // another cell in the same bucket, or another robot
+                                    const int3 cu = grid_cell(g, pu, false);
+                                    acc = cu.x == c.x + dx && cu.y == y && cu.z == z && (int)d.vinfo[u].x == r;
+                                }
+                                // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them
+                                const int ddx = ik.x - ij.x, ddy = ik.y - ij.y, ddz = ik.z - ij.z;
+                                if (abs(ddx) + abs(ddy) + abs(ddz) == 1 && ((vi.y >> link_bit(ddx, ddy, ddz)) & 1u))
+                                    acc = false;
+                                if ((ij.w & 1) && (ik.w & 1)) acc = false;  // both fixed
+                            }
+                            if (acc) {
+                                if (nc < kNbrCap) my[nc * T] = u;
+                                nc++;
+                            }
+                        }
                     }
-                    // the list holds voxel indices in ascending order: csurf is ascending, so
-                    // this is the ascending surface-index order of the reference's pair loop
-                    int j = nc++;
-                    while (j > 0 && out[(j - 1) * ns] > u) {
-                        out[j * ns] = out[(j - 1) * ns];
-                        j--;
-                    }
-                    out[j * ns] = u;
                 }
             }
-    if (overflow) atomicOr(&d.status[r], 2);
-    d.nnb[s] = nc;
-    d.cref[s] = make_float4(pf.x, pf.y, pf.z, lim * lim);
+        }
+        const bool overflow = nc > kNbrCap;
+        nc = min(nc, kNbrCap);
+        for (int a2 = 1; a2 < nc; a2++) {  // ascending voxel index
+            const int x = my[a2 * T];
+            int j = a2;
+            while (j > 0 && my[(j - 1) * T] > x) {
+                my[j * T] = my[(j - 1) * T];
+                j--;
+            }
+            my[j * T] = x;
+        }
+        int c3[3];
+        bool ov3 = false;
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            c3[kk] = __shfl_sync(0xffffffffu, nc, (tb + kk) & 31);
+            ov3 |= __shfl_sync(0xffffffffu, overflow ? 1 : 0, (tb + kk) & 31) != 0;
+        }
+        __syncwarp();
+        if (valid) {
+            int *out = d.nbr + s;
+            for (int j = 0; j < nc; j++) {
+                const int e = my[j * T];
+                int rank = j;
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++) {
+                    if (kk == q) continue;
+                    const int *o = cand + (tid - q + kk);
+                    int m = 0;
+                    while (m < c3[kk] && o[m * T] < e) m++;
+                    rank += m;
+                }
+                if (rank < kNbrCap) out[rank * ns] = e;
+            }
+            if (q == 0) {
+                const int r = (int)d.vinfo[v].x;
+                const int total = c3[0] + c3[1] + c3[2];
+                d.nnb[s] = min(total, kNbrCap);
+                if (ov3 || total > kNbrCap) atomicOr(&d.status[r], 2);
+                const float lim = 0.49f * (float)d.rp[r].skin;  // rebuild when a voxel has moved farther than this
+                d.cref[s] = make_float4(pv.x, pv.y, pv.z, lim * lim);
+            }
+        }
+        __syncwarp();
+    }
 }
 
 // 2'. lists of the robots on the shared-memory path.  The work list holds the robots
@@ -741,29 +916,40 @@ __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_prepare(Dev d) {
     for (int s = gt; s < d.ns; s += gs) coll_check(d, s);
     if (!grid_barrier(d)) return;
     if (!*(volatile int *)d.cflag) return;  // (uniform) no robot is due
-    if (d.nhash) {
-        for (int i = gt; i < d.hsize; i += gs) d.hcount[i] = 0;
+    if (d.nhash) {  // robots too large for shared memory, if any is due
+        for (int s0 = 0; s0 < d.ns; s0 += gs) grid_box(d, s0 + gt);  // warp-uniform trip count
         if (!grid_barrier(d)) return;
-        for (int s = gt; s < d.ns; s += gs) coll_bin(d, s);
+        if (gt == 0) grid_params(d);
         if (!grid_barrier(d)) return;
-        for (int b = blockIdx.x; b < d.hsize / 1024; b += gridDim.x) coll_scan_segment(d, b, wsum);
+        const int used = d.gmode[1];
+        for (int i = gt; i < used; i += gs) d.hcount[i] = 0;
         if (!grid_barrier(d)) return;
-        for (int b = blockIdx.x; b < d.hsize / 1024; b += gridDim.x) coll_scan_add(d, b, wsum);
+        for (int s = gt; s < d.ns; s += gs) grid_count(d, s);
         if (!grid_barrier(d)) return;
-        for (int s = gt; s < d.ns; s += gs) coll_scatter(d, s);
+        for (int b = blockIdx.x; b < used / 1024; b += gridDim.x) coll_scan_segment(d, b, wsum);
         if (!grid_barrier(d)) return;
-        for (int s = gt; s < d.ns; s += gs) {
-            const int r = (int)d.vinfo[d.csurf[s]].x;
-            if (d.cflag[1 + r] && !d.rp[r].lchunks) coll_list(d, s);
-        }
+        for (int b = blockIdx.x; b < used / 1024; b += gridDim.x) coll_scan_add(d, b, wsum);
+        if (!grid_barrier(d)) return;
+        for (int s = gt; s < d.ns; s += gs) grid_scatter(d, s);
+        if (!grid_barrier(d)) return;
+        grid_list(d, reinterpret_cast<int *>(lsm));
+        __syncthreads();  // the shared-memory path below reuses lsm
     }
     if (d.lmax) coll_list_robots(d, lsm, wsum);
+}
+
+// dynamic shared memory of k_coll_prepare: the shared-memory path's tables, or the
+// large-robot path's sub-lists (kNbrCap ints per thread), whichever is larger
+static size_t coll_prepare_smem(const Dev &d) {
+    size_t sm = d.lmax ? local_list_smem(d.lmax) : 0;
+    if (d.nhash) sm = std::max(sm, (size_t)kNbrCap * kLocalListThreads * sizeof(int));
+    return sm;
 }
 
 cudaError_t init_collision(Dev &d) {
     d.cgrid = 0;
     if (!d.ns) return cudaSuccess;
-    const size_t sm = d.lmax ? local_list_smem(d.lmax) : 0;
+    const size_t sm = coll_prepare_smem(d);
     cudaError_t e = cudaFuncSetAttribute(k_coll_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     int dev = 0, nsm = 0, occ = 0;
@@ -860,7 +1046,7 @@ cudaError_t launch_collision(const Dev &d, cudaStream_t s) {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)d.cgrid);
     cfg.blockDim = dim3(kLocalListThreads);
-    cfg.dynamicSmemBytes = d.lmax ? local_list_smem(d.lmax) : 0;
+    cfg.dynamicSmemBytes = coll_prepare_smem(d);
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeCooperative;

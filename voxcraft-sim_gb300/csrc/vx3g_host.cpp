@@ -578,6 +578,11 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     if (c->any_cilia &&
         ((rc = c->upload(&d.cil, cil_h)) || (rc = c->upload(&d.cil_on, cil_on_h)) || (rc = c->alloc(&d.cfv, d.nv))))
         return rc;
+    {  // large-robot grid: empty bounding boxes (min keys at the top, max keys at the bottom)
+        std::vector<unsigned> box(6 * (size_t)d.nr, 0u);
+        for (size_t r = 0; r < (size_t)d.nr; r++) box[6 * r] = box[6 * r + 1] = box[6 * r + 2] = 0xffffffffu;
+        if ((rc = c->upload(&d.gbox, box))) return rc;
+    }
     d.any_detach = c->any_detach ? 1 : 0;
     if ((rc = c->alloc(&d.srf, (size_t)d.nr))) return rc;
     if ((rc = c->alloc(&d.dt, d.nr)) || (rc = c->alloc(&d.T, 2 * (size_t)d.nr)) || (rc = c->alloc(&d.status, d.nr)) ||
@@ -601,13 +606,14 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         }
     }
     int hs = 1024;
-    while (hs < d.nhash) hs <<= 1;
+    while (hs < 2 * (long long)d.nhash) hs <<= 1;  // room for a dense grid over the robots' boxes
     d.hsize = hs;
     if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.cposf, d.ns)) ||
         (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1 + (size_t)d.nr)) || (rc = c->alloc(&d.gbar, 2)) ||
         (rc = c->upload(&d.cref, std::vector<float4>((size_t)d.ns, make_float4(1e30f, 1e30f, 1e30f, 0.0f)))) ||
         (rc = c->alloc(&d.hcount, hs)) ||
-        (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.hsorted, d.ns)) ||
+        (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.spos, d.ns)) || (rc = c->alloc(&d.sij, d.ns)) ||
+        (rc = c->alloc(&d.ssurf, d.ns)) || (rc = c->alloc(&d.ggrid, (size_t)d.nr)) || (rc = c->alloc(&d.gmode, 3)) ||
         (rc = c->alloc(&d.hblock, hs / 1024)) || (rc = c->alloc(&d.lwork, (size_t)d.nr)) || (rc = c->upload(&d.cpk, cpk)) ||
         (rc = c->alloc(&d.lwork_ctr, 1)))
         return rc;

@@ -76,6 +76,12 @@ struct RobotP {
     int detach = 0;            // 1: EnableDetach (failed links leave; the surface follows the link table)
 };
 
+// grid of one robot on the large-robot list path (bounding box in cells of cutoff + skin)
+struct GridP {
+    float mnx, mny, mnz, ic;  // bounding-box corner, 1 / cell edge
+    int gx, gy, gz, base;     // cells per axis, first bucket (dense grid)
+};
+
 // a math-tree token as vx3g_math_token lays it out (op, reserved, value)
 struct MathTok {
     int op, reserved;
@@ -121,7 +127,7 @@ struct Dev {
     const LMat *lmat;
     // collision
     int *csurf;     // collision surface list (global voxel index), NS entries
-    int4 *ccell;    // cell coords + robot per collision-surface voxel
+    int4 *ccell;    // x: the bucket of a collision-surface voxel in the large-robot grid (-1: not binned)
     float4 *cposf;  // FP32 position per collision-surface voxel, written by the displacement check
     unsigned *cpk;  // per collision-surface voxel: packed lattice word (kPackMask, kPackFixed; shared-memory path)
     float4 *cref;   // position at the last list build (w: squared displacement that forces a rebuild)
@@ -134,7 +140,13 @@ struct Dev {
     int lmax;       // most collision-surface voxels of a robot on the shared-memory path (0: none)
     int cgrid;      // CTAs of the cooperative k_coll_prepare (all resident)
     int nhash;      // collision-surface voxels on the global hashed-grid path
-    int *hcount, *hstart, *hfill, *hsorted, *hblock;
+    int *hcount, *hstart, *hfill, *hblock;  // bucket counts, starts, ends (after the scatter), segment sums
+    unsigned *gbox;      // [NR][6] bounding-box accumulators of the large-robot grid (order-preserving keys)
+    GridP *ggrid;        // [NR] that grid's corner, cell edge, size and first bucket
+    int *gmode;          // [3] dense grid (1) or hashed (0), buckets in use
+    float4 *spos;        // [NS] binned voxels in cell order: FP32 position, voxel index in w
+    short4 *sij;         // [NS] their lattice coordinates, w = fixed
+    int *ssurf;          // [NS] their collision-surface index
     int hsize;      // power of two
     int *err;       // device error word
     const MathTok *ftok;  // force-field programs of all robots, back to back
