@@ -12,6 +12,10 @@ library's stream; the L2 cache is flushed (512 MB overwrite) before every timed
 chunk.  The default workload is the single large body (64^3 Bernoulli(0.6),
 collisions + floor, mixed precision).  Under torchrun each rank runs its own
 replica of the workload on its own GPU (robots are independent; no collective).
+
+"e2e" replays the same window (same warm-up, then the same K chunks of the same
+trajectory) on a fresh batch through the C ABI with the voxel state in pinned
+host memory: each chunk uploads the state, steps, reads the state and the COM back.
 """
 
 import argparse
@@ -362,20 +366,6 @@ def main():
     vox_steps = b.nv * C * K * world
     value = vox_steps / (total_ms / 1e3)
 
-    # e2e through the C ABI with host buffers: upload state from pinned host memory,
-    # run a chunk, read COM back
-    st = pinned_copy(b.state())
-    h2d = sum(a.nbytes for a in st.values())
-    t0 = time.perf_counter()
-    E = max(3, K // 5)
-    for _ in range(E):
-        b.set_state(**st)
-        b.step(C)
-        com = b.com()
-    e2e_s = time.perf_counter() - t0
-    d2h = com.nbytes
-    e2e_value = b.nv * C * E * world / e2e_s
-
     # per-pass device times (after the measured run); the dominant kernel is the
     # single kernel with the largest time: the link pass, the voxel pass or the
     # contact evaluation (the collision pass's other kernels are the small check and
@@ -391,9 +381,34 @@ def main():
     peak, peak_kind = peaks()
     achieved = kernel_bytes[dom] / (kernel_ms[dom] / 1e3) / 1e9 if kernel_ms[dom] > 0 else 0.0
     traffic = ncu_traffic(args.workload, args.precision, dom)
-    # link pass + voxel pass; collision: displacement check, 6 list-rebuild kernels
-    # (they return at once unless a rebuild is due) and the contact evaluation
-    kernels_per_step = 2 + (8 if ns_coll else 0)
+    # link pass + voxel pass; collision: the cooperative check/list-rebuild kernel and
+    # the contact evaluation
+    kernels_per_step = 2 + (2 if ns_coll else 0)
+    shapes = [int(x) for x in b.launch_shapes()]
+    b.close()
+
+    # e2e through the C ABI with host buffers: a fresh batch of the same robots runs
+    # the same warm-up steps and then the same K chunks of the same trajectory, the
+    # voxel state living in pinned host memory: every chunk uploads it, steps, reads
+    # it back and reads the COM
+    b2 = abi.Batch(robots, prec, device=dev, graph_chunk=-1 if args.no_graphs else args.chunk)
+    b2.autotune(max(16, (W - 1) * C), args.tune_cache)
+    b2.step(C)
+    host = pinned_copy(b2.state())
+    b2.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        b2.set_state(**host)
+        b2.step(C)
+        b2.state(out=host)
+        com = b2.com()
+    e2e_s = barrier_and_max(time.perf_counter() - t0, world)
+    h2d = sum(a.nbytes for a in host.values())
+    d2h = h2d + com.nbytes
+    e2e_value = b2.nv * C * K * world / e2e_s
+    b2.close()
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -402,8 +417,7 @@ def main():
         "config": {"workload": desc, "robots": len(robots), "voxels": b.nv, "links": b.nl,
                    "collision_surface_voxels": ns_coll, "precision": args.precision,
                    "physics_steps_per_bench_step": C, "cuda_graphs": not args.no_graphs,
-                   "launch_shapes": {"links": [int(x) for x in b.launch_shapes()[:2]],
-                                     "voxels": [int(x) for x in b.launch_shapes()[2:]]},
+                   "launch_shapes": {"links": shapes[:2], "voxels": shapes[2:]},
                    "l2": "512 MB overwrite before every timed chunk", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,

@@ -206,11 +206,20 @@ class Batch:
     def steps_taken(self) -> int:
         return self.lib.vx3g_steps_taken(self.h)
 
-    def state(self):
-        pos, lm, am = (np.zeros((self.nv, 3)) for _ in range(3))
-        orient = np.zeros((self.nv, 4))
-        _check(self.lib.vx3g_get_state(self.h, _P(pos), _P(orient), _P(lm), _P(am)), "vx3g_get_state")
-        return dict(pos=pos, orient=orient, linmom=lm, angmom=am)
+    def state(self, out=None):
+        """Voxel state as float64 arrays; `out` (a dict of C-contiguous float64 arrays
+        with the keys and shapes returned here) is filled in place instead."""
+        if out is None:
+            pos, lm, am = (np.zeros((self.nv, 3)) for _ in range(3))
+            orient = np.zeros((self.nv, 4))
+            out = dict(pos=pos, orient=orient, linmom=lm, angmom=am)
+        for k, comps in (("pos", 3), ("orient", 4), ("linmom", 3), ("angmom", 3)):
+            a = out[k]
+            if a.dtype != np.float64 or a.shape != (self.nv, comps) or not a.flags.c_contiguous:
+                raise ValueError(f"state(out=...): {k} must be a C-contiguous float64 array of shape ({self.nv}, {comps})")
+        _check(self.lib.vx3g_get_state(self.h, _P(out["pos"]), _P(out["orient"]), _P(out["linmom"]),
+                                       _P(out["angmom"])), "vx3g_get_state")
+        return out
 
     def set_state(self, pos=None, orient=None, linmom=None, angmom=None):
         c = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
