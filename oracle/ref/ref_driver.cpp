@@ -188,6 +188,37 @@ void collide_pair(VX3_Voxel *voxel1, VX3_Voxel *voxel2, VX3_VoxelyzeKernel *k) {
     }
 }
 
+// removeVoxels (VX3_VoxelyzeKernel.cu:365-397), restated over the kernel's arrays: once a
+// material's RemoveFromSimulationAfterThisManySeconds (> 0) is below the current time,
+// every voxel of it and each of their links leave the simulation
+void remove_voxels(VX3_VoxelyzeKernel *k) {
+    for (int i = 0; i < k->num_d_voxelMats; i++) {
+        VX3_MaterialVoxel *m = &k->d_voxelMats[i];
+        if (m->removed || !(m->RemoveFromSimulationAfterThisManySeconds > 0) ||
+            !(m->RemoveFromSimulationAfterThisManySeconds < k->currentTime))
+            continue;
+        for (int j = 0; j < k->num_d_voxels; j++) {
+            VX3_Voxel *v = &k->d_voxels[j];
+            if (v->mat != m || v->removed) continue;
+            v->removed = true;
+            for (int d = 0; d < 6; d++) {
+                VX3_Link *L = v->links[d];
+                if (!L) continue;
+                L->removed = true;
+                VX3_Voxel *other = (L->pVNeg == v) ? L->pVPos : L->pVNeg;
+                for (int q = 0; q < 6; q++)
+                    if (other->links[q] == L) {
+                        other->links[q] = NULL;
+                        break;
+                    }
+                v->links[d] = NULL;
+            }
+        }
+        m->removed = true;
+        k->isSurfaceChanged = true;
+    }
+}
+
 // doTimeStep (VX3_VoxelyzeKernel.cu:237-359) with dt = -1
 bool do_time_step(RefSim &S) {
     VX3_VoxelyzeKernel *k = S.k;
@@ -280,6 +311,9 @@ bool do_time_step(RefSim &S) {
         if (t->mat->fixed) continue;
         t->timeStep(dt, k->currentTime, k);
     }
+    // SecondaryExperiment (:335-349): material removal at the end of the step, before the
+    // time advances (the initial-position reset there is the caller's bookkeeping)
+    if (k->SecondaryExperiment) remove_voxels(k);
     k->currentTime += dt;
     return true;
 }
@@ -324,6 +358,7 @@ void *vx3ref_create(const char *vxa_text, int enable_collision, int enable_expan
     S->k->EnableCollision = enable_collision != 0;
     S->k->enableAttach = false;
     S->k->enableDetach = false;
+    S->k->SecondaryExperiment = 0;
     S->k->EnableExpansion = enable_expansion;
     // CUDA_Simulation prologue (:54-57): initial COM and two recommendedTimeStep calls
     double c[3];
@@ -352,6 +387,8 @@ int vx3ref_set_force_field(void *h, int axis, const void *tokens, int n) {
 void vx3ref_set_cilia(void *h, int enable) { ((RefSim *)h)->k->EnableCilia = enable; }
 // VXA.Simulator.AttachDetach.EnableDetach (VX3_SimulationManager.cu:330)
 void vx3ref_set_detach(void *h, int enable) { ((RefSim *)h)->k->enableDetach = enable != 0; }
+// VXA.Simulator.SecondaryExperiment (VX3_SimulationManager.cu:364)
+void vx3ref_set_secondary(void *h, int enable) { ((RefSim *)h)->k->SecondaryExperiment = enable; }
 
 void vx3ref_destroy(void *h) { /* the reference frees nothing reliably either; leak in tests */ (void)h; }
 

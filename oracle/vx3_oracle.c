@@ -6,9 +6,9 @@
  * written so that C's usual conversions reproduce the reference's mix of
  * float and double exactly (build with -ffp-contract=off).
  *
- * Scope: linear materials (MatModel 0/1), static lattice topology (no
- * attach/detach/removal), no boundary-condition regions, no signals (cilia
- * with the signal at 0);
+ * Scope: linear materials (MatModel 0/1); the link table changes only by detach
+ * and by material removal (no attachment); no boundary-condition regions, no
+ * signals (cilia with the signal at 0);
  * force field: the robot's x/y/z math-tree programs (constant 0 when absent, the
  * reference default, VX3_ForceField.h:10-20), target-tracking variables 0.
  */
@@ -146,6 +146,7 @@ typedef struct {
     int fixed, is_measured;
     double thermal_on_after;
     double cilia, cilia_on_after; /* Cilia, TurnOnCiliaAfterThisManySeconds (VX_Object.cpp:1429,1437) */
+    double remove_after;          /* RemoveFromSimulationAfterThisManySeconds (VX_Object.cpp:1427) */
 } vmat;
 
 typedef struct {
@@ -180,6 +181,7 @@ static void vmat_import(vmat *m, const vxo_material *in, const vxo_robot *r) {
     memset(m, 0, sizeof(*m));
     m->cilia = in->cilia;
     m->cilia_on_after = in->cilia_on_after;
+    m->remove_after = in->remove_after;
     float E = (float)in->E;
     float fail = in->model == 1 ? (float)in->fail_stress : -1.0f;
     m->E = E;
@@ -257,6 +259,7 @@ typedef struct {
     quat orient;
     float tempe, prevDt;
     int flags;
+    int removed; /* removeVoxels (SecondaryExperiment): no longer stepped, linked or collided */
     double phase;
 } voxel;
 
@@ -285,6 +288,7 @@ typedef struct {
     int threads; /* > 1: timing mode, loops run under OpenMP */
     vxo_math_token *ff[3]; /* force-field programs (copies) or NULL */
     vec *cilia_base;       /* per voxel: BaseCiliaForce + 0 * ShiftCiliaForce (the signal stays 0), or NULL */
+    int *mat_removed;      /* per material: removeVoxels has removed it (VX3_MaterialVoxel::removed) */
 } sim;
 
 /* VX3_MathTree::eval (src/Utils/VX3_MathTree.h:50-191): tokens in order, each result
@@ -373,6 +377,7 @@ void *vxo_create(const vxo_robot *r) {
     S->nvm = r->n_materials;
     S->vm = (vmat *)calloc(S->nvm ? S->nvm : 1, sizeof(vmat));
     for (int i = 0; i < S->nvm; i++) vmat_import(&S->vm[i], &r->materials[i], r);
+    S->mat_removed = (int *)calloc(S->nvm ? S->nvm : 1, sizeof(int));
 
     int *vid = (int *)malloc(sizeof(int) * (ncell ? ncell : 1));
     S->nv = 0;
@@ -453,7 +458,7 @@ void vxo_destroy(void *h) {
     sim *S = (sim *)h;
     if (!S) return;
     free(S->vm); free(S->lm); free(S->v); free(S->l); free(S->surf); free(S->last_contact);
-    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]); free(S->cilia_base);
+    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]); free(S->cilia_base); free(S->mat_removed);
     free(S);
 }
 
@@ -722,6 +727,34 @@ static void collide_rows_threaded(sim *S, int row_begin, int row_end) {
     }
 }
 
+/* removeVoxels (VX3_VoxelyzeKernel.cu:365-397), at the end of a step of a SecondaryExperiment
+ * (:335-349), before the time advances: every voxel of a material whose
+ * RemoveFromSimulationAfterThisManySeconds (> 0) is below the current time leaves the
+ * simulation together with its links; the surface is regenerated in the next step. */
+static void remove_voxels(sim *S) {
+    for (int i = 0; i < S->nvm; i++) {
+        const vmat *m = &S->vm[i];
+        if (S->mat_removed[i] || !(m->remove_after > 0) || !(m->remove_after < S->t)) continue;
+        for (int j = 0; j < S->nv; j++) {
+            voxel *v = &S->v[j];
+            if (v->mat != i || v->removed) continue;
+            v->removed = 1;
+            for (int k = 0; k < 6; k++) {
+                const int li = v->links[k];
+                if (li < 0) continue;
+                link *L = &S->l[li];
+                L->gone = 1; /* VX3_Link::removed: skipped by the link and detach passes */
+                voxel *nb = &S->v[L->neg == j ? L->pos : L->neg];
+                for (int q = 0; q < 6; q++)
+                    if (nb->links[q] == li) { nb->links[q] = -1; break; }
+                v->links[k] = -1;
+            }
+        }
+        S->mat_removed[i] = 1;
+        S->surface_stale = 1;
+    }
+}
+
 /* doTimeStep (VX3_VoxelyzeKernel.cu:237-359) */
 static int do_step(sim *S) {
     const vxo_robot *r = &S->r;
@@ -731,6 +764,7 @@ static int do_step(sim *S) {
         for (int i = 0; i < S->nv; i++) {
             voxel *v = &S->v[i];
             const vmat *m = &S->vm[v->mat];
+            if (v->removed) continue;
             if (m->thermal_on_after > S->t) continue;
             if (m->fixed) continue;
             double T = r->temp_amplitude * sin(2 * 3.1415926f * (S->t / r->temp_period + v->phase));
@@ -763,7 +797,7 @@ static int do_step(sim *S) {
             int interior = 1;
             for (int d = 0; d < 6; d++) if (S->v[i].links[d] < 0) interior = 0;
             if (interior) S->v[i].flags |= F_SURFACE; else S->v[i].flags &= ~F_SURFACE;
-            if (!interior) S->surf[S->ns++] = i;
+            if (!interior && !S->v[i].removed) S->surf[S->ns++] = i;
         }
     }
     /* gpu_update_attach (:833-843): pairs first > second in surface order */
@@ -797,9 +831,11 @@ static int do_step(sim *S) {
     /* gpu_update_voxels (:582-623) */
 #pragma omp parallel for if (S->threads > 1) schedule(static)
     for (int i = 0; i < S->nv; i++) {
+        if (S->v[i].removed) continue;
         if (S->vm[S->v[i].mat].fixed) continue;
         voxel_update(S, &S->v[i], dt);
     }
+    if (r->secondary_experiment) remove_voxels(S);
     S->t += dt;
     return 1;
 }

@@ -24,6 +24,7 @@ typedef struct vxo_material {
     int fixed, is_measured;
     double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
     double cilia, cilia_on_after; /* Cilia, TurnOnCiliaAfterThisManySeconds */
+    double remove_after;          /* RemoveFromSimulationAfterThisManySeconds (SecondaryExperiment) */
 } vxo_material;
 
 /* A math-tree token (VX3_MathTreeToken, src/Utils/VX3_MathTree.h:29-36): op is the
@@ -49,6 +50,7 @@ typedef struct vxo_robot {
     int enable_cilia;                     /* Simulator/EnableCilia */
     const double *cilia_base, *cilia_shift; /* nx*ny*nz*3 Base/ShiftCiliaForce per cell, or NULL */
     int enable_detach;                    /* Simulator/AttachDetach/EnableDetach */
+    int secondary_experiment;             /* Simulator/SecondaryExperiment: material removal */
 } vxo_robot;
 
 void *vxo_create(const vxo_robot *r);

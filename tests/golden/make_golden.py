@@ -3,7 +3,7 @@
 Run where the reference tree is mounted:
 
     make -C oracle ref            # compiles the reference sources into oracle/_ref/
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 Each case is a small seeded robot.  The VXA document is fed to the
 reference's own reader (CXML_Rip + CVX_Sim::ReadVXA/Import) and stepped by the
@@ -86,6 +86,18 @@ def cases():
                                      z_offset=0, enable_collision=True, enable_detach=True,
                                      phase=rng.random((4, 4, 4)), temp_vary=True, temp_amplitude=30.0,
                                      enable_expansion=1), 300, 100)
+    # SecondaryExperiment: two materials leave the simulation at different times; the
+    # exposed voxels join the collision surface and, with cilia on, get cilia forces
+    rng = np.random.default_rng(11)
+    rmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),
+             wl.Material(E=3e5, nu=0.35, remove_after=0.002),
+             wl.Material(E=5e5, nu=0.35, cilia=-0.5, remove_after=0.006)]
+    rem = wl.bernoulli_body(rng, (6, 5, 4), 0.9, rmats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
+                            enable_collision=True, z_offset=1)
+    rem.enable_cilia = True
+    rem.secondary_experiment = True
+    rem.cilia_base = 2e-2 * rng.standard_normal(rem.grid.shape + (3,))
+    out["bern6_removal"] = (rem, 300, 100)
     return out
 
 
@@ -102,13 +114,13 @@ def snapshot(s):
 def robot_record(r):
     g, ph = r.padded()
     mats = np.array([[m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress, m.fixed, m.is_measured,
-                      m.cilia, m.cilia_on_after] for m in r.materials], np.float64)
+                      m.cilia, m.cilia_on_after, m.remove_after] for m in r.materials], np.float64)
     settings = dict(vox_size=r.vox_size, dt_frac=r.dt_frac, bond_damping=r.bond_damping, col_damping=r.col_damping,
                     slow_damping=r.slow_damping, gravity=r.gravity, grav_acc=r.grav_acc, floor=r.floor,
                     temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,
                     temp_base=r.temp_base, enable_expansion=r.enable_expansion, enable_collision=r.enable_collision,
                     volume_effects=r.volume_effects, force_field=r.force_field, enable_cilia=r.enable_cilia,
-                    enable_detach=r.enable_detach)
+                    enable_detach=r.enable_detach, secondary_experiment=r.secondary_experiment)
     rec = dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
                settings=np.array(json.dumps(settings)))
     for name in ("cilia_base", "cilia_shift"):  # per cell of the padded lattice, 3 values each
@@ -117,10 +129,12 @@ def robot_record(r):
     return rec
 
 
-def main():
+def main(only=()):
     if not ob.ref_available():
         sys.exit("reference build missing: run `make -C oracle ref` first")
     for name, (robot, steps, every) in cases().items():
+        if only and name not in only:
+            continue
         s = ob.ref_sim(robot)
         nv, nl, _ = s.counts()
         rec = robot_record(robot)
@@ -145,4 +159,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])  # optional case names: regenerate only those

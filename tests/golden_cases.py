@@ -23,7 +23,8 @@ def load(name):
         s["force_field"] = [None if t is None else tup(t) for t in s["force_field"]]
     mats = [wl.Material(E=m[0], nu=m[1], rho=m[2], cte=m[3], mu_static=m[4], mu_kinetic=m[5], fail_stress=m[6],
                         fixed=int(m[7]), is_measured=int(m[8]),
-                        cilia=float(m[9]) if len(m) > 9 else 0.0, cilia_on_after=float(m[10]) if len(m) > 10 else 0.0)
+                        cilia=float(m[9]) if len(m) > 9 else 0.0, cilia_on_after=float(m[10]) if len(m) > 10 else 0.0,
+                        remove_after=float(m[11]) if len(m) > 11 else 0.0)
             for m in d["materials"]]
     phase = d["phase"] if d["phase"].size else None
     robot = wl.Robot(grid=d["lattice"], materials=mats, phase=phase, z_offset=0, **s)

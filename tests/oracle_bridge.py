@@ -26,7 +26,7 @@ class VxoMaterial(ctypes.Structure):
                 ("cte", ctypes.c_double), ("mu_static", ctypes.c_double), ("mu_kinetic", ctypes.c_double),
                 ("fail_stress", ctypes.c_double), ("model", ctypes.c_int), ("fixed", ctypes.c_int),
                 ("is_measured", ctypes.c_int), ("thermal_on_after", ctypes.c_double),
-                ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double)]
+                ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double), ("remove_after", ctypes.c_double)]
 
 
 class VxoRobot(ctypes.Structure):
@@ -41,7 +41,7 @@ class VxoRobot(ctypes.Structure):
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
                 ("force_field", ctypes.c_void_p * 3),
                 ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
-                ("enable_detach", ctypes.c_int)]
+                ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int)]
 
 
 def build_oracle():
@@ -189,7 +189,7 @@ def robot_struct(robot):
     for i, m in enumerate(robot.materials):
         mats[i] = VxoMaterial(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic,
                               m.fail_stress, 0 if m.fail_stress == 0 else 1, m.fixed, m.is_measured, 0.0,
-                              m.cilia, m.cilia_on_after)
+                              m.cilia, m.cilia_on_after, m.remove_after)
     Z, Y, X = g.shape
     r = VxoRobot(X, Y, Z, _P(lattice), None if phase is None else _P(phase), len(robot.materials), mats,
                  robot.vox_size, robot.dt_frac, robot.grav_acc, int(robot.floor),
@@ -209,6 +209,7 @@ def robot_struct(robot):
                 cil.append(a)
                 setattr(r, name, _P(a))
     r.enable_detach = int(robot.enable_detach)
+    r.secondary_experiment = int(robot.secondary_experiment)
     return r, (lattice, phase, mats, progs, cil)
 
 
@@ -249,4 +250,7 @@ def ref_sim(robot) -> Sim:
     lib.vx3ref_set_detach.restype = None
     lib.vx3ref_set_detach.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.vx3ref_set_detach(h, int(robot.enable_detach))
+    lib.vx3ref_set_secondary.restype = None
+    lib.vx3ref_set_secondary.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.vx3ref_set_secondary(h, int(robot.secondary_experiment))
     return Sim(lib, "vx3ref_", h, progs)

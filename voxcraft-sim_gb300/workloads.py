@@ -35,6 +35,7 @@ class Material:
     is_measured: int = 1
     cilia: float = 0.0         # Cilia (scale of the cilia force)
     cilia_on_after: float = 0.0  # TurnOnCiliaAfterThisManySeconds
+    remove_after: float = 0.0  # RemoveFromSimulationAfterThisManySeconds (SecondaryExperiment; 0: never)
     name: str = "mat"
 
 
@@ -64,6 +65,8 @@ class Robot:
     force_field: Optional[list] = None    # Simulator/ForceField: [x, y, z] math trees (see math_tokens) or None
     enable_cilia: bool = False            # Simulator/EnableCilia
     enable_detach: bool = False           # Simulator/AttachDetach/EnableDetach (failed links leave the lattice)
+    secondary_experiment: bool = False    # Simulator/SecondaryExperiment (material removal, initial-position reset)
+    reinit_after: float = 0.0             # Simulator/ReinitializeInitialPositionAfterThisManySeconds
     cilia_base: Optional[np.ndarray] = None   # float64 [Z, Y, X, 3] BaseCiliaForce (only occupied cells read)
     cilia_shift: Optional[np.ndarray] = None  # float64 [Z, Y, X, 3] ShiftCiliaForce
     stop_time: Optional[float] = None     # StopConditionFormula "t - stop_time" (> 0 stops)
@@ -247,6 +250,9 @@ def to_vxa(r: Robot) -> str:
            f"<EnableAttach>0</EnableAttach><EnableDetach>{int(r.enable_detach)}</EnableDetach></AttachDetach>",
            f"<EnableExpansion>{int(r.enable_expansion)}</EnableExpansion>",
            *([f"<EnableCilia>1</EnableCilia>"] if r.enable_cilia else []),
+           *([f"<SecondaryExperiment>1</SecondaryExperiment><ReinitializeInitialPositionAfterThisManySeconds>"
+              f"{_fmt(r.reinit_after)}</ReinitializeInitialPositionAfterThisManySeconds>"]
+             if r.secondary_experiment else []),
            *([f"<StopCondition><StopConditionFormula><mtSUB><mtVAR>t</mtVAR><mtCONST>{_fmt(r.stop_time)}</mtCONST>"
               "</mtSUB></StopConditionFormula></StopCondition>"] if r.stop_time is not None else []),
            *(["<FitnessFunction><mtVAR>x</mtVAR></FitnessFunction>"] if r.fitness_x else []),
@@ -278,6 +284,7 @@ def to_vxa(r: Robot) -> str:
             f"<CTE>{_fmt(m.cte)}</CTE><MaterialTempPhase>0</MaterialTempPhase>"
             f"<Cilia>{_fmt(m.cilia)}</Cilia><TurnOnCiliaAfterThisManySeconds>{_fmt(m.cilia_on_after)}"
             "</TurnOnCiliaAfterThisManySeconds>"
+            f"<RemoveFromSimulationAfterThisManySeconds>{_fmt(m.remove_after)}</RemoveFromSimulationAfterThisManySeconds>"
             f"<uStatic>{_fmt(m.mu_static)}</uStatic><uDynamic>{_fmt(m.mu_kinetic)}</uDynamic>"
             f"<Fixed>{int(m.fixed)}</Fixed><isMeasured>{int(m.is_measured)}</isMeasured>"
             "</Mechanical></Material>")
