@@ -64,6 +64,9 @@ typedef struct vx3g_material {
     double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
     double cilia;            /* Cilia: scale of the cilia force (VX3_Voxel::force, src/VX3/VX3_Voxel.cu:376) */
     double cilia_on_after;   /* TurnOnCiliaAfterThisManySeconds */
+    double remove_after;     /* RemoveFromSimulationAfterThisManySeconds: with secondary_experiment, the
+                                material's voxels leave the simulation at the end of the first step that
+                                starts later than this (> 0; 0 never) */
 } vx3g_material;
 
 /* One token of a math-tree program, the reference's VX3_MathTreeToken
@@ -116,8 +119,14 @@ typedef struct vx3g_robot_desc {
                                        voxel's signal, which stays 0 (signals are not supported) */
     int enable_detach;              /* Simulator/AttachDetach/EnableDetach: a failed link leaves both voxels'
                                        link tables after the collision pass (gpu_update_detach,
-                                       VX3_VoxelyzeKernel.cu:946-967); the surface, and the contact
-                                       candidates, follow from the next step (not with enable_cilia) */
+                                       VX3_VoxelyzeKernel.cu:946-967); the surface, the contact
+                                       candidates and the cilia follow from the next step */
+    int secondary_experiment;       /* Simulator/SecondaryExperiment: material removal (removeVoxels,
+                                       VX3_VoxelyzeKernel.cu:335-397): a removed voxel is no longer
+                                       stepped, loses its links, leaves the surface and the contact
+                                       candidates, and keeps counting toward the centre of mass; the
+                                       initial-position reset of the same block is the caller's (it
+                                       touches only the report) */
 } vx3g_robot_desc;
 
 typedef struct vx3g_batch_desc {
@@ -161,15 +170,17 @@ int vx3g_set_state(vx3g_ctx *ctx, const double *pos, const double *orient, const
 int vx3g_get_voxel_aux(vx3g_ctx *ctx, float *tempe, int32_t *flags, double *contact);
 /* Link state in the reference's link order: strain, maxStrain (float),
  * local9 = pos2, angle1v, angle2v (9 doubles), forces12 = forceNeg, forcePos,
- * momentNeg, momentPos (12 doubles), small = small-angle flag. */
+ * momentNeg, momentPos (12 doubles), small = small-angle flag (bit 0) | 2 once the
+ * link has left the lattice (detached or removed: no voxel's link any more). */
 int vx3g_get_links(vx3g_ctx *ctx, float *strain, float *max_strain, double *local9, double *forces12,
                    int32_t *small);
 /* Topology: voxel lattice indices (3 ints), voxel palette index (0-based),
  * link ends (neg, pos voxel indices, packed global), link axis (0 x, 1 y, 2 z). */
 int vx3g_get_topology(vx3g_ctx *ctx, int32_t *voxel_ijk, int32_t *voxel_mat, int32_t *link_ends,
                       int32_t *link_axis);
-/* Surface voxels (fewer than six links), global voxel indices in voxel order; with
- * enable_detach the set grows as links detach (vx3g_counts gives its current size). */
+/* Surface voxels (fewer than six links, not removed), global voxel indices in voxel
+ * order; with enable_detach or secondary_experiment the set follows the link table
+ * (vx3g_counts gives its current size). */
 int vx3g_get_surface(vx3g_ctx *ctx, int32_t *surface);
 
 int vx3g_com(vx3g_ctx *ctx, double *com /* 3 per robot */);

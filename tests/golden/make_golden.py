@@ -86,6 +86,14 @@ def cases():
                                      z_offset=0, enable_collision=True, enable_detach=True,
                                      phase=rng.random((4, 4, 4)), temp_vary=True, temp_amplitude=30.0,
                                      enable_expansion=1), 300, 100)
+    # detach with cilia: voxels exposed by failed links get cilia forces from the step after
+    rng = np.random.default_rng(13)
+    dcm = [wl.Material(E=1e5, nu=0.0, fail_stress=2500.0, mu_static=0.2, mu_kinetic=0.1, cte=0.001, cilia=0.8)]
+    dc = wl.Robot(grid=np.ones((4, 4, 4), np.uint8), materials=dcm, volume_effects=False, z_offset=0,
+                  enable_collision=True, enable_detach=True, phase=rng.random((4, 4, 4)), temp_vary=True,
+                  temp_amplitude=30.0, enable_expansion=1, enable_cilia=True)
+    dc.cilia_base = 1e-2 * rng.standard_normal((4, 4, 4, 3))
+    out["block4_detach_cilia"] = (dc, 300, 100)
     # SecondaryExperiment: two materials leave the simulation at different times; the
     # exposed voxels join the collision surface and, with cilia on, get cilia forces
     rng = np.random.default_rng(11)

@@ -128,3 +128,106 @@ def test_runner_cilia_matches_oracle(tmp_path):
     free = wl.Robot(**{**robot.__dict__, "enable_cilia": False})
     f, _, _ = _oracle_until(free, 0.01)
     assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size  # the cilia moved the robot
+
+
+def _eval_tree(tree, v):
+    """A math tree over the operators these tests use, operands in document order."""
+    op = tree[0]
+    if op == "mtCONST":
+        return float(tree[1])
+    if op == "mtVAR":
+        return float(v.get(tree[1], 0.0))
+    a = [_eval_tree(c, v) for c in tree[1:]]
+    return {"mtADD": lambda: a[0] + a[1], "mtSUB": lambda: a[0] - a[1], "mtMUL": lambda: a[0] * a[1],
+            "mtDIV": lambda: a[0] / a[1], "mtGREATERTHAN": lambda: float(a[0] > a[1]),
+            "mtLESSTHAN": lambda: float(a[0] < a[1])}[op]()
+
+
+def _reference_run(robot, stop, max_steps=100000, fresh_com=False):
+    """CUDA_Simulation (VX3_SimulationManager.cu:54-118) over the oracle: StopConditionMet
+    before every step reads currentCenterOfMass, which doTimeStep refreshes only when the
+    step count is a multiple of CycleStep = int(TempPeriod / dt) (VX3_VoxelyzeKernel.cu:
+    313-320); a SecondaryExperiment takes the initial COM (that value) and the initial
+    voxel positions again at the end of the first step that starts after
+    ReinitializeInitialPositionAfterThisManySeconds (:344-348).  fresh_com=True reads the
+    current COM instead (what the runner must NOT do)."""
+    s = ob.oracle_sim(robot)
+    nv = s.counts()[0]
+    com0 = s.com()
+    com_s, init, n, reset = com0.copy(), s.voxels()["pos"].copy(), 0, False
+    while n < max_steps:
+        t = s.time()
+        c = s.com() if fresh_com else com_s
+        if _eval_tree(stop, dict(x=c[0], y=c[1], z=c[2], t=t, num_voxel=nv)) > 0:
+            break
+        s.step(1)
+        n += 1
+        cyc = int(robot.temp_period / float(np.float32(s.dt())))
+        if cyc > 0 and n % cyc == 0:
+            com_s = s.com()
+        if robot.secondary_experiment and not reset and robot.reinit_after < t:
+            reset = True
+            com0, init = com_s.copy(), s.voxels()["pos"].copy()
+    return s, n, com0, init
+
+
+def _run_runner(tmp_path, robot):
+    vbuild.build()
+    exe = os.path.join(os.path.dirname(vbuild.LIB), "vx3g_sim")
+    (tmp_path / "base.vxa").write_text(wl.to_vxa(robot))
+    (tmp_path / "r.vxd").write_text("<VXD>\n</VXD>\n")
+    out = tmp_path / "report.xml"
+    r = subprocess.run([exe, "-i", str(tmp_path), "-o", str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return ET.parse(out).getroot().find("detail/r")
+
+
+def _xyz(node, tag):
+    return np.array([float(node.find(f"{tag}/{k}").text) for k in "xyz"])
+
+
+def test_runner_com_stop_condition_reads_the_sampled_com(tmp_path):
+    """A StopConditionFormula on the centre of mass stops where the reference's does: the
+    COM it reads is the one sampled every int(TempPeriod/dt) steps, not the current one."""
+    rng = np.random.default_rng(14)
+    mats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=3e5, nu=0.35)]
+    robot = wl.bernoulli_body(rng, (4, 3, 3), 0.9, mats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
+                              temp_period=0.003, z_offset=2, fitness_x=True)
+    z0 = ob.oracle_sim(robot).com()[2]
+    robot.stop_formula = ("mtLESSTHAN", ("mtVAR", "z"), ("mtCONST", z0 - 0.004))
+    s, n, c0, _ = _reference_run(robot, robot.stop_formula)
+    _, n_fresh, _, _ = _reference_run(robot, robot.stop_formula, fresh_com=True)
+    assert n_fresh < n  # the sampled COM lags: the two readings stop at different steps
+    node = _run_runner(tmp_path, robot)
+    assert float(node.find("currentTime").text) == pytest.approx(s.time(), rel=1e-12)
+    np.testing.assert_allclose(_xyz(node, "currentCenterOfMass"), s.com(), rtol=0, atol=1e-6 * robot.vox_size)
+    np.testing.assert_allclose(_xyz(node, "initialCenterOfMass"), c0, rtol=0, atol=1e-9 * robot.vox_size)
+
+
+def test_runner_secondary_experiment_matches_oracle(tmp_path):
+    """SecondaryExperiment through the runner: a material leaves the simulation
+    (RemoveFromSimulationAfterThisManySeconds) and the initial COM and positions are taken
+    again (ReinitializeInitialPositionAfterThisManySeconds), as the reference's loop does."""
+    rng = np.random.default_rng(15)
+    mats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=3e5, nu=0.35, remove_after=0.002),
+            wl.Material(E=5e5, nu=0.35, is_measured=0)]
+    robot = wl.bernoulli_body(rng, (5, 4, 3), 0.9, mats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
+                              temp_period=0.001, enable_collision=True, stop_time=0.006, fitness_x=True, z_offset=1)
+    robot.secondary_experiment = True
+    robot.reinit_after = 0.003
+    robot.stop_formula = ("mtSUB", ("mtVAR", "t"), ("mtCONST", 0.006))
+    s, n, c0, init = _reference_run(robot, robot.stop_formula)
+    node = _run_runner(tmp_path, robot)
+    assert float(node.find("currentTime").text) == pytest.approx(s.time(), rel=1e-12)
+    com = _xyz(node, "currentCenterOfMass")
+    np.testing.assert_allclose(com, s.com(), rtol=0, atol=1e-6 * robot.vox_size)
+    np.testing.assert_allclose(_xyz(node, "initialCenterOfMass"), c0, rtol=0, atol=1e-6 * robot.vox_size)
+    assert float(node.find("fitness_score").text) == pytest.approx(s.com()[0] - c0[0], abs=1e-6 * robot.vox_size)
+    # total_distance_of_all_voxels: measured voxels' distance from the positions at the reset
+    pos = s.voxels()["pos"]
+    mat = s.topology()["mat"]
+    meas = np.array([robot.materials[k].is_measured for k in mat], bool)
+    want = np.linalg.norm(pos[meas] - init[meas], axis=1).sum()
+    assert float(node.find("total_distance_of_all_voxels").text) == pytest.approx(
+        want, rel=0, abs=1e-6 * robot.vox_size * meas.sum())
+    assert int(node.find("num_measured_voxel").text) == int(meas.sum())

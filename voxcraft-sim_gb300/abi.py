@@ -33,7 +33,8 @@ class Material(ctypes.Structure):
     _fields_ = [("E", ctypes.c_double), ("nu", ctypes.c_double), ("rho", ctypes.c_double), ("cte", ctypes.c_double),
                 ("mu_static", ctypes.c_double), ("mu_kinetic", ctypes.c_double), ("fail_stress", ctypes.c_double),
                 ("model", ctypes.c_int), ("fixed", ctypes.c_int), ("is_measured", ctypes.c_int),
-                ("thermal_on_after", ctypes.c_double), ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double)]
+                ("thermal_on_after", ctypes.c_double), ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double),
+                ("remove_after", ctypes.c_double)]
 
 
 class RobotDesc(ctypes.Structure):
@@ -48,7 +49,7 @@ class RobotDesc(ctypes.Structure):
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
                 ("log10E", ctypes.c_void_p), ("force_field", ctypes.c_void_p * 3),
                 ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
-                ("enable_detach", ctypes.c_int)]
+                ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int)]
 
 
 class BatchDesc(ctypes.Structure):
@@ -125,7 +126,7 @@ def robot_desc(robot):
     for i, m in enumerate(robot.materials):
         mats[i] = Material(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress,
                            0 if m.fail_stress == 0 else 1, int(m.fixed), int(m.is_measured), 0.0,
-                           float(m.cilia), float(m.cilia_on_after))
+                           float(m.cilia), float(m.cilia_on_after), float(m.remove_after))
     Z, Y, X = g.shape
     log10E = getattr(robot, "log10E", None)
     if log10E is not None:
@@ -145,6 +146,7 @@ def robot_desc(robot):
             progs.append(np.ascontiguousarray(wl.math_tokens(tree)))
             d.force_field[k] = _P(progs[-1])
     d.enable_detach = int(robot.enable_detach)
+    d.secondary_experiment = int(robot.secondary_experiment)
     cil = []
     if robot.enable_cilia:
         d.enable_cilia = 1

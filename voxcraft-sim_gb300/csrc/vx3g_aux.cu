@@ -145,8 +145,9 @@ int recommended_dt_noalloc(const Dev &d, int device, double *out_host, cudaStrea
 // CiliaForce * Cilia (:376), CiliaForce being set for surface voxels by
 // gpu_update_cilia_force (VX3_VoxelyzeKernel.cu:846-859) as R(orient) (base + signal
 // * shift), the signal staying 0 here.  Both are evaluated in FP64 before the voxel
-// pass (from the position, orientation and time it starts with), so the voxel
-// kernels only add the stored forces at the reference's places in the sum.
+// pass and the step's detach (from the position, orientation and time the step starts
+// with), so the voxel kernels only add the stored forces at the reference's places in
+// the sum.
 __global__ void k_extra_forces(Dev d, int parity) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= d.nv) return;
@@ -157,7 +158,11 @@ __global__ void k_extra_forces(Dev d, int parity) {
     if (rp.cilia) {
         const double4 c = d.cil[v];
         V3<double> cf{0, 0, 0};
-        if (!(d.cil_on[v] > t)) {
+        // surface voxels only; a voxel joins the surface once it has lost a link (detach,
+        // removal of a neighbour) -- this kernel runs before the step's detach, so with the
+        // link table the reference regenerated its surface list from
+        const bool surface = (d.vinfo[v].y & VF_LINKMASK) != VF_LINKMASK;
+        if (surface && !(d.cil_on[v] > t)) {
             const double4 q = load_state(d, d.quat, v);
             cf = qrot(Q4<double>{q.x, q.y, q.z, q.w}, V3<double>{c.x, c.y, c.z});
         }
@@ -199,6 +204,49 @@ __global__ void k_detach(Dev d) {
 
 void launch_detach(const Dev &d, cudaStream_t s) {
     if (d.any_detach && d.nl) k_detach<<<(d.nl + 255) / 256, 256, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------- material removal
+// removeVoxels (VX3_VoxelyzeKernel.cu:365-397), at the end of a SecondaryExperiment step
+// (:335-349): once the step's start time is past a material's
+// RemoveFromSimulationAfterThisManySeconds (> 0), each voxel of it leaves the simulation.
+// It no longer steps (VF_FIXED: the voxel pass skips it, as gpu_update_voxels skips a
+// removed voxel, :586), keeps the temperature of the step just taken (gpu_update_temperature
+// skips it, :632), still counts toward the centre of mass (:477-493), and every link of it
+// leaves the lattice (LF_GONE, the direction bits of both ends cleared).  Its robot's
+// contact lists are rebuilt in the next step without it.  Whether a voxel leaves in this
+// step depends on its own time test only, so link threads and voxel threads need no
+// ordering among themselves.
+__device__ __forceinline__ bool removed_by(const Dev &d, int v, int parity) {
+    const int r = (int)d.vinfo[v].x;
+    return d.status[r] == 0 && d.rm_at[v] < d.T[(size_t)parity * d.nr + r];
+}
+
+__global__ void k_remove(Dev d, int parity) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.nl) {
+        const uint2 li = d.linfo[i];
+        if (d.rp[li.x].remove && !(li.y & LF_GONE)) {
+            const int2 e = d.ends[i];
+            if (removed_by(d, e.x, parity) || removed_by(d, e.y, parity)) {
+                d.linfo[i].y = li.y | LF_GONE;
+                const int a = (int)(li.y & LF_AXIS);
+                atomicAnd(&d.vinfo[e.x].y, ~(1u << (2 * a)));      // the negative end's link toward +axis
+                atomicAnd(&d.vinfo[e.y].y, ~(1u << (2 * a + 1)));  // the positive end's toward -axis
+            }
+        }
+    }
+    if (i < d.nv && !d.vgone[i] && removed_by(d, i, parity)) {
+        d.vgone[i] = 1;
+        atomicOr(&d.vinfo[i].y, VF_FIXED);
+        d.tempe[(size_t)(parity ^ 1) * d.nv + i] = d.tempe[(size_t)parity * d.nv + i];
+        d.srf[d.vinfo[i].x] = 1;
+    }
+}
+
+void launch_remove(const Dev &d, int parity, cudaStream_t s) {
+    const int n = d.nv > d.nl ? d.nv : d.nl;
+    if (d.any_remove && n) k_remove<<<(n + 255) / 256, 256, 0, s>>>(d, parity);
 }
 
 // ---------------------------------------------------------------- collision
@@ -255,14 +303,15 @@ __device__ __forceinline__ void coll_check(const Dev &d, int s) {
     const int v = d.csurf[s];
     const float4 p = pos_f(d, v), q = d.cref[s];  // q.w: squared displacement limit
     d.cposf[s] = p;  // the positions a rebuild on the shared-memory path lists from
-    if (d.any_detach) {  // robots whose surface follows their link table
+    if (d.any_dyn) {  // robots whose surface follows their link table
         const uint2 vi = d.vinfo[v];
         const RobotP &rp = d.rp[vi.x];
-        if (rp.detach && s == rp.soff && d.srf[vi.x]) {  // a link detached last step: new surface
+        if (rp.dyn && s == rp.soff && d.srf[vi.x]) {  // a link or a voxel left last step: new surface
             d.srf[vi.x] = 0;
             flag_robot(d, (int)vi.x);
         }
-        if ((vi.y & VF_LINKMASK) == VF_LINKMASK) return;  // interior: not a surface voxel now
+        // interior or removed: not a surface voxel now
+        if ((vi.y & VF_LINKMASK) == VF_LINKMASK || (d.vgone && d.vgone[v])) return;
     }
     const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
     if (ex * ex + ey * ey + ez * ez > q.w) flag_robot(d, (int)d.vinfo[v].x);
@@ -379,7 +428,8 @@ __device__ __forceinline__ int grid_bucket(const Dev &d, const GridP &g, int3 c,
 // reduces first so that the atomics are one per warp, not per voxel
 __device__ __forceinline__ void grid_box(const Dev &d, int s) {
     int v = 0, r = -1;
-    bool valid = s < d.ns && grid_voxel(d, s, &v, &r) && (d.vinfo[v].y & VF_LINKMASK) != VF_LINKMASK;
+    bool valid = s < d.ns && grid_voxel(d, s, &v, &r) && (d.vinfo[v].y & VF_LINKMASK) != VF_LINKMASK &&
+                 !(d.vgone && d.vgone[v]);
     unsigned k[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
     if (valid) {
         const float4 p = d.cposf[s];
@@ -449,7 +499,7 @@ __device__ __forceinline__ void grid_count(const Dev &d, int s) {
     if (!grid_voxel(d, s, &v, &r)) return;
     const RobotP &rp = d.rp[r];
     const float4 p = d.cposf[s];
-    if ((d.vinfo[v].y & VF_LINKMASK) == VF_LINKMASK) {  // interior (EnableDetach): lists nothing
+    if ((d.vinfo[v].y & VF_LINKMASK) == VF_LINKMASK || (d.vgone && d.vgone[v])) {  // interior or removed: lists nothing
         const float lim = 0.49f * (float)rp.skin;
         d.nnb[s] = 0;
         d.cref[s] = make_float4(p.x, p.y, p.z, lim * lim);
@@ -671,7 +721,10 @@ __device__ __forceinline__ void coll_list_robots(const Dev &d, unsigned char *ls
             for (int i = tid; i < n; i += T) {
                 const float4 q = __ldcg(&d.cposf[s0 + i]);
                 unsigned pk = d.cpk[s0 + i];
-                if (rp.detach && (d.vinfo[d.csurf[s0 + i]].y & VF_LINKMASK) == VF_LINKMASK) pk |= kPackInterior;
+                if (rp.dyn) {  // interior or removed: neither lists nor is listed
+                    const int v = d.csurf[s0 + i];
+                    if ((d.vinfo[v].y & VF_LINKMASK) == VF_LINKMASK || (d.vgone && d.vgone[v])) pk |= kPackInterior;
+                }
                 P[i] = make_float4(q.x, q.y, q.z, __uint_as_float(pk));
                 bx0 = fminf(bx0, q.x), by0 = fminf(by0, q.y), bz0 = fminf(bz0, q.z);
                 bx1 = fmaxf(bx1, q.x), by1 = fmaxf(by1, q.y), bz1 = fmaxf(bz1, q.z);
@@ -774,7 +827,7 @@ __device__ __forceinline__ void coll_list_robots(const Dev &d, unsigned char *ls
             const LocalGrid g = G;
             const unsigned ki = __float_as_uint(pi.w);
             // the voxel's link table: face neighbours are excluded only while a link joins them
-            const unsigned imask = rp.detach ? d.vinfo[d.csurf[s0 + i]].y & VF_LINKMASK : VF_LINKMASK;
+            const unsigned imask = rp.dyn ? d.vinfo[d.csurf[s0 + i]].y & VF_LINKMASK : VF_LINKMASK;
             const int3 c = local_cell(pi, g);
             // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
             const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;

@@ -190,6 +190,8 @@ struct vx3g_ctx {
     bool any_ff = false;  // some robot has a force field
     bool any_cilia = false;  // some robot has cilia
     bool any_detach = false;  // some robot has EnableDetach
+    bool any_remove = false;  // some robot removes voxels (SecondaryExperiment)
+    bool any_dyn = false;     // some robot's surface follows its link table (detach or removal)
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -317,6 +319,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     std::vector<MathTok> ftok;
     std::vector<double4> cil_h;
     std::vector<double> cil_on_h;
+    std::vector<double> rm_h;  // per voxel: removal time (+inf: never)
     c->voff.assign(c->nr + 1, 0);
     c->loff.assign(c->nr + 1, 0);
 
@@ -451,8 +454,22 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         rp.collision = R.enable_collision ? 1 : 0;
         rp.detach = R.enable_detach ? 1 : 0;
         c->any_detach |= R.enable_detach != 0;
-        if (R.enable_detach && R.enable_cilia)
-            return fail(VX3G_ERR_UNSUPPORTED, "robot " + std::to_string(r) + ": cilia together with detach (cilia act on the surface at creation)");
+        // SecondaryExperiment: the voxels of a material with RemoveFromSimulationAfterThisManySeconds > 0
+        // leave at the end of the first step that starts later (removeVoxels, VX3_VoxelyzeKernel.cu:365-397)
+        rm_h.resize(pos.size(), INFINITY);
+        rp.remove = 0;
+        if (R.secondary_experiment) {
+            for (int k = 0; k < nvr; k++) {
+                const double ra = R.materials[c->vmat_local[v0 + k]].remove_after;
+                if (ra > 0) {
+                    rm_h[v0 + k] = ra;
+                    rp.remove = 1;
+                }
+            }
+        }
+        c->any_remove |= rp.remove != 0;
+        rp.dyn = rp.detach || rp.remove ? 1 : 0;
+        c->any_dyn |= rp.dyn != 0;
         rp.ff_pos = 0;
         for (int k = 0; k < 3; k++) {  // Simulator/ForceField programs
             rp.ff[k] = -1;
@@ -490,13 +507,14 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             const int v = v0 + k;
             const bool interior = (vinfo[v].y & VF_LINKMASK) == VF_LINKMASK;
             if (!interior) c->surface.push_back(v);
-            // EnableDetach: any voxel may become a surface voxel, so all take part (interior
-            // ones are skipped while their six links hold)
-            if ((!interior || R.enable_detach) && R.enable_collision) csurf.push_back(v);
+            // detach or removal: any voxel may become a surface voxel, so all take part
+            // (interior ones are skipped while their six links hold, removed ones for good)
+            if ((!interior || rp.dyn) && R.enable_collision) csurf.push_back(v);
         }
         rp.ns = (int)csurf.size() - rp.soff;
         // cilia (gpu_update_cilia_force, VX3_VoxelyzeKernel.cu:846-859): surface voxels of a
-        // material with Cilia != 0, once TurnOnCiliaAfterThisManySeconds has passed
+        // material with Cilia != 0, once TurnOnCiliaAfterThisManySeconds has passed (k_extra_forces
+        // reads the surface from the current link table)
         cil_h.resize(pos.size(), make_double4(0, 0, 0, 0));
         cil_on_h.resize(pos.size(), INFINITY);
         rp.cilia = 0;
@@ -513,8 +531,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
                 }
                 const double sig = 0.0;  // localSignal: signals are not simulated
                 cil_h[v] = make_double4(b[0] + sig * sh[0], b[1] + sig * sh[1], b[2] + sig * sh[2], M.cilia);
-                const bool interior = (vinfo[v].y & VF_LINKMASK) == VF_LINKMASK;
-                if (!interior && M.cilia != 0) {
+                if (M.cilia != 0) {
                     cil_on_h[v] = M.cilia_on_after;
                     rp.cilia = 1;
                 }
@@ -584,6 +601,11 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         if ((rc = c->upload(&d.gbox, box))) return rc;
     }
     d.any_detach = c->any_detach ? 1 : 0;
+    d.any_remove = c->any_remove ? 1 : 0;
+    d.any_dyn = c->any_dyn ? 1 : 0;
+    d.vgone = nullptr;
+    d.rm_at = nullptr;
+    if (c->any_remove && ((rc = c->alloc(&d.vgone, (size_t)d.nv)) || (rc = c->upload(&d.rm_at, rm_h)))) return rc;
     if ((rc = c->alloc(&d.srf, (size_t)d.nr))) return rc;
     if ((rc = c->alloc(&d.dt, d.nr)) || (rc = c->alloc(&d.T, 2 * (size_t)d.nr)) || (rc = c->alloc(&d.status, d.nr)) ||
         (rc = c->alloc(&d.err, 1)) || (rc = c->alloc(&c->scratch, 4 * (size_t)d.nr + 4)))
@@ -628,13 +650,14 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
 
 void enqueue_links(vx3g_ctx *c) {
     if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(c->d, c->stream);
-    else launch_links_mixed(c->d, c->stream, c->shape_links);
+    else launch_links_mixed(c->d, c->stream, c->shape_links, !c->any_remove);  // removal writes link info
 }
 void enqueue_voxels(vx3g_ctx *c, int parity) {
-    launch_detach(c->d, c->stream);                // EnableDetach robots only (after the collision pass)
     launch_extra_forces(c->d, parity, c->stream);  // robots with a force field or cilia only
+    launch_detach(c->d, c->stream);                // EnableDetach robots only (after the collision pass)
     if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(c->d, parity, c->stream);
     else launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, !c->any_detach);  // detach writes voxel info
+    launch_remove(c->d, parity, c->stream);        // SecondaryExperiment robots only (end of the step)
 }
 
 cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
@@ -724,19 +747,22 @@ int vx3g_synchronize(vx3g_ctx *c) {
 void *vx3g_stream(vx3g_ctx *c) { return c ? (void *)c->stream : nullptr; }
 int64_t vx3g_steps_taken(vx3g_ctx *c) { return c ? c->steps : -1; }
 
-// The surface voxels (fewer than six links) in voxel order: fixed at creation, or read
-// from the current link table when links can detach.
+// The surface voxels (fewer than six links, not removed) in voxel order: fixed at
+// creation, or read from the current link table when links can detach or voxels leave.
 static int current_surface(vx3g_ctx *c, std::vector<int> &out) {
-    if (!c->any_detach) {
+    if (!c->any_dyn) {
         out = c->surface;
         return VX3G_OK;
     }
     std::vector<uint2> vi((size_t)c->d.nv);
+    std::vector<unsigned char> gone((size_t)c->d.nv, 0);
     if (c->d.nv) CU(cudaMemcpyAsync(vi.data(), c->d.vinfo, sizeof(uint2) * vi.size(), cudaMemcpyDeviceToHost, c->stream));
+    if (c->d.nv && c->d.vgone)
+        CU(cudaMemcpyAsync(gone.data(), c->d.vgone, gone.size(), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     out.clear();
     for (size_t v = 0; v < vi.size(); v++)
-        if ((vi[v].y & VF_LINKMASK) != VF_LINKMASK) out.push_back((int)v);
+        if ((vi[v].y & VF_LINKMASK) != VF_LINKMASK && !gone[v]) out.push_back((int)v);
     return VX3G_OK;
 }
 
@@ -857,7 +883,7 @@ int vx3g_get_links(vx3g_ctx *c, float *strain, float *max_strain, double *local9
     for (size_t l = 0; l < nl; l++) {
         if (strain) strain[l] = sm[l].x;
         if (max_strain) max_strain[l] = sm[l].y;
-        if (small) small[l] = (li[l].y & LF_SMALL) ? 1 : 0;
+        if (small) small[l] = ((li[l].y & LF_SMALL) ? 1 : 0) | ((li[l].y & LF_GONE) ? 2 : 0);
         if (local9)
             for (int k = 0; k < 9; k++) local9[9 * l + k] = rd(ls, (size_t)k * nl + l);
         if (forces12) {
@@ -1255,7 +1281,8 @@ int vx3g_record(vx3g_ctx *c, int n, int k) {
     if (c->ff_pos)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a force field that reads the voxel position is not implemented");
     if (c->any_cilia) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of cilia forces is not implemented");
-    if (c->any_detach) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a changing link table (detach) is not implemented");
+    if (c->any_detach || c->any_remove)
+        return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a changing link table (detach, removal) is not implemented");
     CU(cudaSetDevice(c->device));
     CU(cudaStreamSynchronize(c->stream));
     c->free_record();

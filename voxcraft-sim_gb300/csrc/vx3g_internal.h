@@ -73,7 +73,9 @@ struct RobotP {
     int ff_pos = 0;            // 1: a force-field program reads the voxel position
     int ff_any = 0;            // 1: the robot has a force field (k_extra_forces fills Dev::ffv)
     int cilia = 0;             // 1: EnableCilia with some cilia voxel (k_extra_forces fills Dev::cfv)
-    int detach = 0;            // 1: EnableDetach (failed links leave; the surface follows the link table)
+    int detach = 0;            // 1: EnableDetach (failed links leave)
+    int remove = 0;            // 1: SecondaryExperiment with a material that leaves (k_remove)
+    int dyn = 0;               // detach || remove: the surface follows the link table
 };
 
 // grid of one robot on the large-robot list path (bounding box in cells of cutoff + skin)
@@ -101,7 +103,9 @@ constexpr int kLocalListChunk = kLocalListThreads / 32 * 10;
 // packed lattice word of a voxel on that path: x | y << 10 | z << 20 | fixed << 31 (coordinates
 // below 512, so the difference of two packed words is face-adjacent iff it is +-1, +-2^10 or +-2^20)
 constexpr unsigned kPackMask = 0x3fffffffu, kPackFixed = 0x80000000u;
-constexpr unsigned kPackInterior = 0x40000000u;  // set while a voxel of an EnableDetach robot has six links
+// set while a voxel of a robot whose surface follows its link table has six links, or
+// after it was removed: it neither lists nor is listed
+constexpr unsigned kPackInterior = 0x40000000u;
 constexpr int kLocalHash = 4096;  // buckets of the shared-memory grid (power of two)
 
 struct Dev {
@@ -154,8 +158,12 @@ struct Dev {
     double4 *cil;         // per voxel: BaseCiliaForce + 0 * ShiftCiliaForce, material Cilia (robots with cilia)
     double *cil_on;       // per voxel: the time cilia switch on (+inf: never; interior or Cilia 0)
     double4 *cfv;         // per voxel: this step's CiliaForce * Cilia (robots with cilia), or NULL
-    int *srf;             // [NR] a link of the robot detached this step: rebuild its lists next step
+    int *srf;             // [NR] a link of the robot detached or a voxel left this step: rebuild its lists next step
     int any_detach;       // some robot has EnableDetach
+    int any_remove;       // some robot removes voxels (k_remove)
+    int any_dyn;          // some robot's surface follows its link table (detach or removal)
+    unsigned char *vgone; // per voxel: removed (removeVoxels), or NULL when no robot removes voxels
+    double *rm_at;        // per voxel: the time after which it is removed (+inf: never), or NULL
     double *com_part;  // [NR][com_tiles][4] partial sums of the centre of mass
     int com_tiles;     // tiles of kComTile voxels of the largest robot
     int nv, nl, nr, ns;
@@ -181,7 +189,8 @@ void launch_voxels_fp64(const Dev &d, int parity, cudaStream_t s);
 struct LaunchShape { int threads, min_blocks; };
 constexpr int kMixedShapes = 6;
 extern const LaunchShape kLinkShapes[kMixedShapes], kVoxelShapes[kMixedShapes];
-void launch_links_mixed(const Dev &d, cudaStream_t s, int shape = 0);
+// pdl = false when the kernel before it wrote link info (removal): no early start
+void launch_links_mixed(const Dev &d, cudaStream_t s, int shape = 0, bool pdl = true);
 // pdl = false when the kernel before it wrote voxel info (detach): no early start
 void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape = 0, bool pdl = true);
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
@@ -195,6 +204,8 @@ cudaError_t launch_collision(const Dev &d, cudaStream_t s);
 void launch_extra_forces(const Dev &d, int parity, cudaStream_t s);
 // gpu_update_detach (VX3_VoxelyzeKernel.cu:946-967) for robots with EnableDetach
 void launch_detach(const Dev &d, cudaStream_t s);
+// removeVoxels (VX3_VoxelyzeKernel.cu:365-397) at the end of the step of the given parity
+void launch_remove(const Dev &d, int parity, cudaStream_t s);
 // one-time setup of the collision kernels (shared-memory size, grid); fills d.cgrid
 cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);

@@ -170,6 +170,7 @@ struct RobotSpec {
     std::vector<vx3g_math_token> ff[3];  // force-field programs (desc.force_field points here)
     std::unique_ptr<Node> doc;
     int record_step = 0, record_voxel = 1, record_link = 0, save_all = 0;
+    double reinit_after = 0.0;  // ReinitializeInitialPositionAfterThisManySeconds (SecondaryExperiment)
 };
 
 void read_spec(RobotSpec &S) {
@@ -193,8 +194,12 @@ void read_spec(RobotSpec &S) {
     if (vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableAttach", false))
         throw std::runtime_error(S.filename + ": runtime attachment is not supported");
     d.enable_detach = vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableDetach", false);  // :330
-    if (vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0) || vx3g::xml::get_int(root, "VXA.Simulator.SecondaryExperiment", 0))
-        throw std::runtime_error(S.filename + ": signals and secondary experiments are not supported");
+    if (vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0))
+        throw std::runtime_error(S.filename + ": signals are not supported");
+    // SecondaryExperiment (VX3_SimulationManager.cu:364-365): material removal on the device,
+    // the initial-position reset here
+    d.secondary_experiment = vx3g::xml::get_int(root, "VXA.Simulator.SecondaryExperiment", 0);
+    S.reinit_after = vx3g::xml::get_double(root, "VXA.Simulator.ReinitializeInitialPositionAfterThisManySeconds", 0.0);
     d.enable_cilia = vx3g::xml::get_int(root, "VXA.Simulator.EnableCilia", 0);  // VX3_SimulationManager.cu:360
     const char *axes[3] = {"x_forcefield", "y_forcefield", "z_forcefield"};
     for (int k = 0; k < 3; k++) {  // Simulator/ForceField (VX3_SimulationManager.cu:349-354)
@@ -258,6 +263,7 @@ void read_spec(RobotSpec &S) {
             M.thermal_on_after = vx3g::xml::get_double(mech, "TurnOnThermalExpansionAfterThisManySeconds", 0.0);
             M.cilia = vx3g::xml::get_double(mech, "Cilia", 0.0);  // VX_Object.cpp:1429, 1437
             M.cilia_on_after = vx3g::xml::get_double(mech, "TurnOnCiliaAfterThisManySeconds", 0.0);
+            M.remove_after = vx3g::xml::get_double(mech, "RemoveFromSimulationAfterThisManySeconds", 0.0);  // :1427
             S.mats.push_back(M);
             const Node *disp = m->child("Display");
             for (const char *c : {"Red", "Green", "Blue", "Alpha"})
@@ -348,15 +354,16 @@ void print_history(FILE *out, vx3g_ctx *ctx, int robot, const RobotSpec &S, long
     check(vx3g_counts(ctx, &nv, &nl, &ns), "vx3g_counts");
     std::vector<double> pos(3 * (size_t)nv), orient(4 * (size_t)nv);
     std::vector<float> tempe(nv), strain(nl), maxs(nl);
-    std::vector<int32_t> ends(2 * (size_t)nl), axis(nl), vmat(nv), surf(ns);
+    std::vector<int32_t> ends(2 * (size_t)nl), axis(nl), vmat(nv), surf(ns), lflag(nl);
     check(vx3g_get_state(ctx, pos.data(), orient.data(), nullptr, nullptr), "vx3g_get_state");
     check(vx3g_get_voxel_aux(ctx, tempe.data(), nullptr, nullptr), "vx3g_get_voxel_aux");
-    check(vx3g_get_links(ctx, strain.data(), maxs.data(), nullptr, nullptr, nullptr), "vx3g_get_links");
+    check(vx3g_get_links(ctx, strain.data(), maxs.data(), nullptr, nullptr, lflag.data()), "vx3g_get_links");
     check(vx3g_get_topology(ctx, nullptr, vmat.data(), ends.data(), axis.data()), "vx3g_get_topology");
     check(vx3g_get_surface(ctx, surf.data()), "vx3g_get_surface");
-    // per voxel: link in each direction
+    // per voxel: link in each direction (detached and removed links are no voxel's any more)
     std::vector<int> slot(6 * (size_t)nv, -1);
     for (int l = loff[robot]; l < loff[robot + 1]; l++) {
+        if (lflag[l] & 2) continue;
         slot[6 * (size_t)ends[2 * l] + 2 * axis[l]] = l;
         slot[6 * (size_t)ends[2 * l + 1] + 2 * axis[l] + 1] = l;
     }
@@ -402,6 +409,7 @@ void print_history(FILE *out, vx3g_ctx *ctx, int robot, const RobotSpec &S, long
     if (S.record_link) {
         fprintf(out, "|[[[%ld]]]", step);
         for (int l = loff[robot]; l < loff[robot + 1]; l++) {
+            if (lflag[l] & 2) continue;  // removed or detached (:98-103)
             const double *a = &pos[3 * (size_t)ends[2 * l + 1]], *b = &pos[3 * (size_t)ends[2 * l]];
             fprintf(out, "%.4f,%.4f,%.4f,%.4f,%.4f,%.4f,;", a[0], a[1], a[2], b[0], b[1], b[2]);
         }
@@ -461,30 +469,79 @@ void VX3_SimulationManager::start() {
             v.num_voxel = voff[r + 1] - voff[r];
             return eval_tree(specs[r]->stop, v) > 0;
         };
+        // currentCenterOfMass, which StopConditionMet reads before every step
+        // (VX3_SimulationManager.cu:62-64), is refreshed only at the end of every step whose
+        // count is a multiple of CycleStep = int(TempPeriod / dt) (VX3_VoxelyzeKernel.cu:313-320);
+        // com_s is that value.  (CycleStep 0, TempPeriod below dt, leaves the reference with a
+        // modulo by zero; here the value then stays the initial one.)
+        std::vector<long> cycle(R, 0);
+        for (int r = 0; r < R; r++) cycle[r] = (long)(specs[r]->desc.temp_period / (double)(float)dt[r]);
+        std::vector<double> com_s(com0);
+        // SecondaryExperiment: the initial centre of mass (that value) and the voxels' initial
+        // positions are taken again at the end of the first step that starts later than
+        // ReinitializeInitialPositionAfterThisManySeconds (:344-348)
+        std::vector<long> reinit_step(R, -1);
+        std::vector<std::vector<double>> init_pos(R);
+        for (int r = 0; r < R; r++) {
+            if (!specs[r]->desc.secondary_experiment) continue;
+            double tt = 0.0;  // start time of step n
+            long n = 1;
+            while (!(specs[r]->reinit_after < tt) && n <= max_steps) {
+                tt += (float)dt[r];
+                n++;
+            }
+            if (n <= max_steps) reinit_step[r] = n;
+        }
         long loop = 0;
         const bool history = std::any_of(stride.begin(), stride.end(), [](long s) { return s > 0; });
         while (true) {
             check(vx3g_time(ctx, t.data()), "vx3g_time");
             check(vx3g_status(ctx, st.data()), "vx3g_status");
             check(vx3g_com(ctx, com.data()), "vx3g_com");
+            bool snap = false;
+            for (int r = 0; r < R; r++) {  // the end of step `loop` for the robots still stepping
+                if (done[r] || loop == 0) continue;
+                if (cycle[r] > 0 && loop % cycle[r] == 0)
+                    for (int k = 0; k < 3; k++) com_s[3 * r + k] = com[3 * r + k];
+                if (loop == reinit_step[r]) {
+                    for (int k = 0; k < 3; k++) com0[3 * r + k] = com_s[3 * r + k];
+                    snap = true;
+                }
+            }
+            if (snap) {
+                int nv_all = 0;
+                check(vx3g_counts(ctx, &nv_all, nullptr, nullptr), "vx3g_counts");
+                std::vector<double> p(3 * (size_t)nv_all);
+                check(vx3g_get_state(ctx, p.data(), nullptr, nullptr, nullptr), "vx3g_get_state");
+                for (int r = 0; r < R; r++)
+                    if (!done[r] && loop == reinit_step[r])
+                        init_pos[r].assign(p.begin() + 3 * (size_t)voff[r], p.begin() + 3 * (size_t)voff[r + 1]);
+            }
             int active = 0;
             long chunk = 100;
             for (int r = 0; r < R; r++) {
                 if (done[r]) continue;
-                if (st[r] != VX3G_ROBOT_OK || loop >= max_steps || stop_met(r, t[r], &com[3 * r])) {
+                if (st[r] != VX3G_ROBOT_OK || loop >= max_steps || stop_met(r, t[r], &com_s[3 * r])) {
                     done[r] = 1;
                     continue;
                 }
                 active++;
-                // a time-only stop condition gives the exact number of steps left (time accumulates float dt in double)
-                if (specs[r]->stop && uses_only_time(specs[r]->stop)) {
+                if (specs[r]->stop) {
+                    // the exact number of steps before the condition holds: time accumulates the
+                    // float dt in double, and the COM it reads changes only at the next CycleStep
+                    long lim = chunk;
+                    if (!uses_only_time(specs[r]->stop) && cycle[r] > 0) lim = std::min(lim, (loop / cycle[r] + 1) * cycle[r] - loop);
                     double tt = t[r];
                     long k = 0;
-                    while (k < chunk && !stop_met(r, tt, &com[3 * r])) {
+                    while (k < lim && !stop_met(r, tt, &com_s[3 * r])) {
                         tt += (float)dt[r];
                         k++;
                     }
                     chunk = std::max(1L, std::min(chunk, k));
+                }
+                if (reinit_step[r] > loop) {  // the reset reads the COM sampled at the last CycleStep before it
+                    chunk = std::min(chunk, reinit_step[r] - loop);
+                    if (cycle[r] > 0) chunk = std::min(chunk, (loop / cycle[r] + 1) * cycle[r] - loop);
                 }
             }
             if (!active) break;
@@ -533,7 +590,13 @@ void VX3_SimulationManager::start() {
             res.status = st[r];
             res.steps = steps[r];
             for (int v = voff[r]; v < voff[r + 1]; v++) {
+                // saveInitialPosition (VX3_VoxelyzeKernel.cu:155-161): the lattice positions, or
+                // the positions at the SecondaryExperiment reset
                 VX3_Vec3 p0{ijk[3 * v] * S.desc.vox_size, ijk[3 * v + 1] * S.desc.vox_size, ijk[3 * v + 2] * S.desc.vox_size};
+                if (!init_pos[r].empty()) {
+                    const double *q = &init_pos[r][3 * (size_t)(v - voff[r])];
+                    p0 = VX3_Vec3{q[0], q[1], q[2]};
+                }
                 VX3_Vec3 p{pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
                 res.voxel_init_pos.push_back(p0);
                 res.voxel_position.push_back(p);

@@ -524,15 +524,15 @@ static void launch_pdl(void (*kernel)(KArgs...), int n, int threads, cudaStream_
     cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
-void launch_links_mixed(const Dev &d, cudaStream_t s, int shape) {
+void launch_links_mixed(const Dev &d, cudaStream_t s, int shape, bool pdl) {
     if (!d.nl) return;
     switch (shape) {
-        case 1: launch_pdl(k_links_mixed<256, 4>, d.nl, 256, s, true, d); break;
-        case 2: launch_pdl(k_links_mixed<128, 9>, d.nl, 128, s, true, d); break;
-        case 3: launch_pdl(k_links_mixed<128, 10>, d.nl, 128, s, true, d); break;
-        case 4: launch_pdl(k_links_mixed<64, 20>, d.nl, 64, s, true, d); break;
-        case 5: launch_pdl(k_links_mixed<256, 5>, d.nl, 256, s, true, d); break;
-        default: launch_pdl(k_links_mixed<256, 1>, d.nl, 256, s, true, d); break;
+        case 1: launch_pdl(k_links_mixed<256, 4>, d.nl, 256, s, pdl, d); break;
+        case 2: launch_pdl(k_links_mixed<128, 9>, d.nl, 128, s, pdl, d); break;
+        case 3: launch_pdl(k_links_mixed<128, 10>, d.nl, 128, s, pdl, d); break;
+        case 4: launch_pdl(k_links_mixed<64, 20>, d.nl, 64, s, pdl, d); break;
+        case 5: launch_pdl(k_links_mixed<256, 5>, d.nl, 256, s, pdl, d); break;
+        default: launch_pdl(k_links_mixed<256, 1>, d.nl, 256, s, pdl, d); break;
     }
 }
 void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape, bool pdl) {

@@ -70,6 +70,7 @@ class Robot:
     cilia_base: Optional[np.ndarray] = None   # float64 [Z, Y, X, 3] BaseCiliaForce (only occupied cells read)
     cilia_shift: Optional[np.ndarray] = None  # float64 [Z, Y, X, 3] ShiftCiliaForce
     stop_time: Optional[float] = None     # StopConditionFormula "t - stop_time" (> 0 stops)
+    stop_formula: Optional[tuple] = None  # or any StopConditionFormula math tree (see math_tokens)
     fitness_x: bool = False               # FitnessFunction "x" (COM displacement along x)
     record_step: int = 0                  # RecordHistory/RecordStepSize
 
@@ -255,6 +256,8 @@ def to_vxa(r: Robot) -> str:
              if r.secondary_experiment else []),
            *([f"<StopCondition><StopConditionFormula><mtSUB><mtVAR>t</mtVAR><mtCONST>{_fmt(r.stop_time)}</mtCONST>"
               "</mtSUB></StopConditionFormula></StopCondition>"] if r.stop_time is not None else []),
+           *([f"<StopCondition><StopConditionFormula>{math_tree_xml(r.stop_formula)}</StopConditionFormula>"
+              "</StopCondition>"] if r.stop_formula is not None and r.stop_time is None else []),
            *(["<FitnessFunction><mtVAR>x</mtVAR></FitnessFunction>"] if r.fitness_x else []),
            *(["<ForceField>" + "".join(f"<{a}_forcefield>{math_tree_xml(t)}</{a}_forcefield>"
                                         for a, t in zip("xyz", r.force_field) if t is not None) + "</ForceField>"]
