@@ -1085,7 +1085,7 @@ __global__ void k_coll_eval(Dev d) {
     d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
 }
 
-cudaError_t launch_collision(const Dev &d, cudaStream_t s) {
+cudaError_t launch_coll_prepare(const Dev &d, cudaStream_t s) {
     if (!d.ns) return cudaSuccess;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaError_t e = cudaStreamIsCapturing(s, &cs);
@@ -1106,7 +1106,13 @@ cudaError_t launch_collision(const Dev &d, cudaStream_t s) {
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    if ((e = cudaLaunchKernelEx(&cfg, k_coll_prepare, d)) != cudaSuccess) return e;
+    return cudaLaunchKernelEx(&cfg, k_coll_prepare, d);
+}
+
+cudaError_t launch_collision(const Dev &d, cudaStream_t s) {
+    if (!d.ns) return cudaSuccess;
+    const cudaError_t e = launch_coll_prepare(d, s);
+    if (e != cudaSuccess) return e;
     launch_coll_eval(d, s);
     return cudaGetLastError();
 }

@@ -174,6 +174,11 @@ void from_slot(const double4 &s, bool mixed, double out[4]) {
 struct vx3g_ctx {
     int precision = 0, chunk = 100, device = 0, nr = 0;
     cudaStream_t stream = nullptr;
+    // mixed precision with collisions: the contact evaluation runs on `side`, beside the
+    // link pass (both read only the state the step starts with), forked and joined by events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool overlap = false;
     Dev d{};
     std::vector<void *> allocs;
     double *scratch = nullptr;  // dt reduction / com output
@@ -243,6 +248,10 @@ struct vx3g_ctx {
         for (void *p : allocs) cudaFree(p);
         if (flush) cudaFree(flush);
         if (stage) cudaFree(stage);
+        if (side) cudaStreamSynchronize(side);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -640,6 +649,12 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         (rc = c->alloc(&d.lwork_ctr, 1)))
         return rc;
     CU(init_collision(d));
+    if (d.mixed && d.ns) {
+        CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+        c->overlap = true;
+    }
 
     launch_init_temperature(d, c->precision == VX3G_PRECISION_MIXED, c->stream);
     launch_dt(d, c->scratch, c->stream);
@@ -661,10 +676,29 @@ void enqueue_voxels(vx3g_ctx *c, int parity) {
 }
 
 cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
-    enqueue_links(c);
-    const cudaError_t e = launch_collision(c->d, c->stream);
-    enqueue_voxels(c, parity);
-    return e;
+    if (!c->overlap) {
+        enqueue_links(c);
+        const cudaError_t e = launch_collision(c->d, c->stream);
+        enqueue_voxels(c, parity);
+        return e;
+    }
+    // the check / list rebuild, then the contact evaluation on the side stream beside the
+    // link pass (disjoint outputs: contact forces; link forces and link state), joined
+    // before the voxel pass, which reads both
+    cudaError_t e = launch_coll_prepare(c->d, c->stream);
+    if (e != cudaSuccess || (e = cudaEventRecord(c->ev_fork, c->stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(c->side, c->ev_fork, 0)) != cudaSuccess)
+        return e;
+    launch_coll_eval(c->d, c->side);
+    launch_links_mixed(c->d, c->stream, c->shape_links, false);
+    if ((e = cudaEventRecord(c->ev_join, c->side)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(c->stream, c->ev_join, 0)) != cudaSuccess)
+        return e;
+    launch_extra_forces(c->d, parity, c->stream);
+    launch_detach(c->d, c->stream);
+    launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, false);
+    launch_remove(c->d, parity, c->stream);
+    return cudaSuccess;
 }
 
 int get_graph(vx3g_ctx *c, int parity, cudaGraphExec_t *out) {

@@ -199,6 +199,7 @@ void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 // surface-voxel collision of one step: displacement check and list rebuild (one
 // cooperative kernel), then the narrow phase
 cudaError_t launch_collision(const Dev &d, cudaStream_t s);
+cudaError_t launch_coll_prepare(const Dev &d, cudaStream_t s);  // the check / rebuild kernel alone
 // the force field (d.ffv) and the cilia force (d.cfv) of the voxels of robots that have
 // them, at the start of the step of the given time parity
 void launch_extra_forces(const Dev &d, int parity, cudaStream_t s);

@@ -112,7 +112,10 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
     const uint2 vi = d.vinfo[v];
     const int r = (int)vi.x;
     if (d.cflag[1 + r]) d.cflag[1 + r] = 0;
-    if (d.status[r] != 0) return;
+    // stopped robots and robots flagged before this step keep their contact forces; the
+    // divergence bit is left out because the link pass, which may set it, runs beside
+    // this kernel (a diverged robot never steps again, so its contacts feed nothing)
+    if (d.status[r] & ~1) return;
     const int n = d.nnb[s];
     const int *lst = d.nbr + s;  // slot-major: entry k at lst[k*ns]
     const size_t ns = (size_t)d.ns;
