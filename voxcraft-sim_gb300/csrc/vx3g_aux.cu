@@ -573,26 +573,35 @@ __device__ void grid_list(const Dev &d, int *cand) {
                             e = d.hfill[h];
                         }
                         e = min(e, nbin);
-                        for (int j = b; j < e; j++) {
-                            const float4 pu = d.spos[j];
-                            const int u = __float_as_int(pu.w);
-                            const float ex = pu.x - pv.x, ey = pu.y - pv.y, ez = pu.z - pv.z;
-                            bool acc = u != v && ex * ex + ey * ey + ez * ez <= cut2;
-                            if (acc) {
-                                const short4 ik = d.sij[j];
-                                if (!dense) {  // another cell in the same bucket, or another robot
-                                    const int3 cu = grid_cell(g, pu, false);
-                                    acc = cu.x == c.x + dx && cu.y == y && cu.z == z && (int)d.vinfo[u].x == r;
+                        // four candidates' positions are loaded before any is tested, so
+                        // four gathers are in flight (the appends keep candidate order)
+                        for (int j0 = b; j0 < e; j0 += 4) {
+                            float4 pq[4];
+#pragma unroll
+                            for (int t = 0; t < 4; t++) pq[t] = j0 + t < e ? d.spos[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                            for (int t = 0; t < 4; t++) {
+                                const int j = j0 + t;
+                                const float4 pu = pq[t];
+                                const int u = __float_as_int(pu.w);
+                                const float ex = pu.x - pv.x, ey = pu.y - pv.y, ez = pu.z - pv.z;
+                                bool acc = j < e && u != v && ex * ex + ey * ey + ez * ez <= cut2;
+                                if (acc) {
+                                    const short4 ik = d.sij[j];
+                                    if (!dense) {  // another cell in the same bucket, or another robot
+                                        const int3 cu = grid_cell(g, pu, false);
+                                        acc = cu.x == c.x + dx && cu.y == y && cu.z == z && (int)d.vinfo[u].x == r;
+                                    }
+                                    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them
+                                    const int ddx = ik.x - ij.x, ddy = ik.y - ij.y, ddz = ik.z - ij.z;
+                                    if (abs(ddx) + abs(ddy) + abs(ddz) == 1 && ((vi.y >> link_bit(ddx, ddy, ddz)) & 1u))
+                                        acc = false;
+                                    if ((ij.w & 1) && (ik.w & 1)) acc = false;  // both fixed
                                 }
-                                // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them
-                                const int ddx = ik.x - ij.x, ddy = ik.y - ij.y, ddz = ik.z - ij.z;
-                                if (abs(ddx) + abs(ddy) + abs(ddz) == 1 && ((vi.y >> link_bit(ddx, ddy, ddz)) & 1u))
-                                    acc = false;
-                                if ((ij.w & 1) && (ik.w & 1)) acc = false;  // both fixed
-                            }
-                            if (acc) {
-                                if (nc < kNbrCap) my[nc * T] = u;
-                                nc++;
+                                if (acc) {
+                                    if (nc < kNbrCap) my[nc * T] = u;
+                                    nc++;
+                                }
                             }
                         }
                     }
