@@ -832,6 +832,20 @@ static int ensure_stage(vx3g_ctx *c) {
     return VX3G_OK;
 }
 
+// The device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister), or
+// nullptr for pageable or device memory: vx3g_set_state's kernel reads page-locked
+// buffers in place instead of staging them through a device copy (0.17 -> 0.12 ms for
+// the 16 MB of a 64^3 body).  vx3g_get_state stages its writes: kernel stores into host
+// memory were slower than the copy engine (0.21 -> 0.31 ms).
+static const void *pinned_device_pointer(const void *p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // not a CUDA pointer: clear the error
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int vx3g_get_state(vx3g_ctx *c, double *pos, double *orient, double *linmom, double *angmom) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
     CU(cudaSetDevice(c->device));
@@ -862,8 +876,12 @@ int vx3g_set_state(vx3g_ctx *c, const double *pos, const double *orient, const d
     for (int k = 0; k < 4; k++) {
         if (!in[k]) continue;
         const int comps = k == 1 ? 4 : 3;
-        CU(cudaMemcpyAsync(c->stage, in[k], comps * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-        launch_pack_state(c->d, dst[k], c->stage, comps, k == 0, c->stream);  // pos keeps its base size
+        const double *from = (const double *)pinned_device_pointer(in[k]);  // page-locked: read in place
+        if (!from) {
+            CU(cudaMemcpyAsync(c->stage, in[k], comps * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+            from = c->stage;
+        }
+        launch_pack_state(c->d, dst[k], from, comps, k == 0, c->stream);  // pos keeps its base size
     }
     CU(cudaStreamSynchronize(c->stream));
     CU(cudaGetLastError());

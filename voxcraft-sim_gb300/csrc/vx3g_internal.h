@@ -212,7 +212,8 @@ cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);
 void launch_coll_eval(const Dev &d, cudaStream_t s);  // the contact evaluation alone
 void launch_com(const Dev &d, double *out4, cudaStream_t s);
-// state exchange with plain doubles (comps = 3 or 4 per voxel) staged in device memory
+// state exchange with plain doubles (comps = 3 or 4 per voxel) in device memory, or, for
+// the pack, in page-locked host memory it reads in place
 void launch_pack_state(const Dev &d, double4 *dst, const double *staged, int comps, int keep_w, cudaStream_t s);
 void launch_unpack_state(const Dev &d, double *staged, const double4 *src, int comps, cudaStream_t s);
 void launch_or_status(const Dev &d, int robot, int bits, cudaStream_t s);
