@@ -381,9 +381,9 @@ def main():
     peak, peak_kind = peaks()
     achieved = kernel_bytes[dom] / (kernel_ms[dom] / 1e3) / 1e9 if kernel_ms[dom] > 0 else 0.0
     traffic = ncu_traffic(args.workload, args.precision, dom)
-    # link pass + voxel pass; collision: the cooperative check/list-rebuild kernel and
-    # the contact evaluation
-    kernels_per_step = 2 + (2 if ns_coll else 0)
+    # link pass + voxel pass; collision: the displacement check, the cooperative list
+    # rebuild kernel (it returns at once unless a rebuild is due) and the contact evaluation
+    kernels_per_step = 2 + (3 if ns_coll else 0)
     shapes = [int(x) for x in b.launch_shapes()]
     b.close()
 

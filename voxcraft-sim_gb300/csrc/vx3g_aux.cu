@@ -971,13 +971,18 @@ __device__ bool grid_barrier(const Dev &d) {
 // displacement check of every surface voxel; then, only in a step where some robot
 // is due, the rebuild of its lists (hashed-grid phases separated by grid barriers,
 // and the shared-memory path).  No host or graph decision sits between them.
+// the displacement check of every collision-surface voxel, at full occupancy, just
+// before k_coll_prepare
+__global__ void __launch_bounds__(256) k_coll_check(Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < d.ns) coll_check(d, s);
+}
+
 __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_prepare(Dev d) {
     extern __shared__ __align__(16) unsigned char lsm[];
     __shared__ int wsum[kLocalListThreads / 32];
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
-    for (int s = gt; s < d.ns; s += gs) coll_check(d, s);
-    if (!grid_barrier(d)) return;
-    if (!*(volatile int *)d.cflag) return;  // (uniform) no robot is due
+    if (!*(volatile int *)d.cflag) return;  // (uniform: k_coll_check has finished) no robot is due
     if (d.nhash) {  // robots too large for shared memory, if any is due
         for (int s0 = 0; s0 < d.ns; s0 += gs) grid_box(d, s0 + gt);  // warp-uniform trip count
         if (!grid_barrier(d)) return;
@@ -1105,6 +1110,7 @@ cudaError_t launch_coll_prepare(const Dev &d, cudaStream_t s) {
             (e = cudaMemsetAsync(d.lwork_ctr, 0, sizeof(unsigned long long), s)) != cudaSuccess)
             return e;
     }
+    k_coll_check<<<(d.ns + 255) / 256, 256, 0, s>>>(d);
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)d.cgrid);
     cfg.blockDim = dim3(kLocalListThreads);
