@@ -59,3 +59,31 @@ def test_cached_choice_is_applied(tmp_path):
     c.autotune(10, path)  # cached: no timing, same shapes
     assert np.array_equal(c.launch_shapes(), chosen)
     assert c.steps_taken() == 10
+
+
+def test_fork_points_give_identical_states(tmp_path):
+    """The overlapped mixed step forks its side stream after the rebuild kernel or
+    before the displacement check (vx3g_autotune picks one): the states are identical,
+    in graphs and in single steps, and the tuner's choice lands in the cache."""
+    rng = np.random.default_rng(8)
+    mats = [wl.Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(3)]
+    robots = [wl.bernoulli_body(rng, tuple(int(x) for x in rng.integers(6, 11, size=3)), 0.7, mats,
+                                random_phase=True, temp_vary=True, temp_amplitude=39.0, enable_collision=True,
+                                z_offset=1) for _ in range(5)]
+    probe = tmp_path / "probe.json"
+    t = abi.Batch(robots, abi.PRECISION_MIXED)
+    t.autotune(64, probe)  # shapes, then whole steps at both fork points
+    assert t.steps_taken() == 64
+    key, entry = next(iter(json.loads(probe.read_text()).items()))
+    assert len(entry) == 3 and entry[2] in (0, 1)
+    states = []
+    for fk in (0, 1):
+        path = tmp_path / f"fork{fk}.json"
+        path.write_text(json.dumps({key: [entry[0], entry[1], fk]}))
+        b = abi.Batch(robots, abi.PRECISION_MIXED)
+        b.autotune(0, path)
+        b.step(200)  # graph chunks
+        b.step(7)    # single steps
+        assert np.all(b.status() == 0)
+        states.append(_state(b))
+    assert np.array_equal(states[0], states[1])

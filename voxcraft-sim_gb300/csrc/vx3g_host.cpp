@@ -179,6 +179,11 @@ struct vx3g_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool overlap = false;
+    // where the side stream forks: 0 after the cooperative rebuild kernel (best when
+    // rebuilds are rare), 1 before the displacement check, so that the check, any rebuild
+    // and the contact evaluation all run beside the link pass (best when some robot
+    // rebuilds in most steps); chosen by vx3g_autotune, results do not depend on it
+    int fork_early = 0;
     Dev d{};
     std::vector<void *> allocs;
     double *scratch = nullptr;  // dt reduction / com output
@@ -685,9 +690,10 @@ cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
     // the check / list rebuild, then the contact evaluation on the side stream beside the
     // link pass (disjoint outputs: contact forces; link forces and link state), joined
     // before the voxel pass, which reads both
-    cudaError_t e = launch_coll_prepare(c->d, c->stream);
+    cudaError_t e = c->fork_early ? cudaSuccess : launch_coll_prepare(c->d, c->stream);
     if (e != cudaSuccess || (e = cudaEventRecord(c->ev_fork, c->stream)) != cudaSuccess ||
-        (e = cudaStreamWaitEvent(c->side, c->ev_fork, 0)) != cudaSuccess)
+        (e = cudaStreamWaitEvent(c->side, c->ev_fork, 0)) != cudaSuccess ||
+        (c->fork_early && (e = launch_coll_prepare(c->d, c->side)) != cudaSuccess))
         return e;
     launch_coll_eval(c->d, c->side);
     launch_links_mixed(c->d, c->stream, c->shape_links, false);
@@ -1110,25 +1116,30 @@ int vx3g_autotune(vx3g_ctx *c, int n_steps, const char *cache_json) {
             fclose(f);
         }
         const size_t at = cache.find("\"" + key + "\": [");
-        int a = -1, b = -1;
+        int a = -1, b = -1, fk = 0;
         if (at != std::string::npos &&
-            sscanf(cache.c_str() + at + key.size() + 5, "%d, %d", &a, &b) == 2 && a >= 0 && a < kMixedShapes &&
+            sscanf(cache.c_str() + at + key.size() + 5, "%d, %d, %d", &a, &b, &fk) >= 2 && a >= 0 && a < kMixedShapes &&
             b >= 0 && b < kMixedShapes) {
-            if (a != c->shape_links || b != c->shape_voxels) {
+            fk = (fk == 1 && c->overlap) ? 1 : 0;
+            if (a != c->shape_links || b != c->shape_voxels || fk != c->fork_early) {
                 for (auto &g : c->graph)
                     if (g) cudaGraphExecDestroy(g), g = nullptr;
             }
             c->shape_links = a;
             c->shape_voxels = b;
+            c->fork_early = fk;
             return vx3g_step(c, n_steps);
         }
     }
-    // time the passes of real steps, cycling through the shapes (results do not depend on them)
+    // time the passes of real steps, cycling through the shapes (results do not depend on them),
+    // then whole steps alternating the fork point of the overlapped step
     const int warm = 2 * kMixedShapes;
     if (n_steps < warm + 2 * kMixedShapes) return vx3g_step(c, n_steps);
+    const int n_fork = c->overlap && n_steps >= 2 * (warm + 2 * kMixedShapes) ? std::min(n_steps / 2, 64) : 0;
+    const int n_shape = n_steps - n_fork;
     std::vector<cudaEvent_t> ev(4 * (size_t)n_steps);
     for (auto &e : ev) CU(cudaEventCreate(&e));
-    for (int i = 0; i < n_steps; i++) {
+    for (int i = 0; i < n_shape; i++) {
         const int parity = (int)(c->steps & 1);
         c->shape_links = c->shape_voxels = i % kMixedShapes;
         CU(cudaEventRecord(ev[4 * i], c->stream));
@@ -1142,14 +1153,13 @@ int vx3g_autotune(vx3g_ctx *c, int n_steps, const char *cache_json) {
     }
     CU(cudaStreamSynchronize(c->stream));
     double tl[kMixedShapes] = {}, tv[kMixedShapes] = {};
-    for (int i = warm; i < n_steps; i++) {
+    for (int i = warm; i < n_shape; i++) {
         float a = 0, b = 0;
         CU(cudaEventElapsedTime(&a, ev[4 * i], ev[4 * i + 1]));
         CU(cudaEventElapsedTime(&b, ev[4 * i + 2], ev[4 * i + 3]));
         tl[i % kMixedShapes] += a;
         tv[i % kMixedShapes] += b;
     }
-    for (auto &e : ev) cudaEventDestroy(e);
     int bl = 0, bv = 0;
     for (int k = 1; k < kMixedShapes; k++) {
         if (tl[k] < tl[bl]) bl = k;
@@ -1157,12 +1167,61 @@ int vx3g_autotune(vx3g_ctx *c, int n_steps, const char *cache_json) {
     }
     c->shape_links = bl;
     c->shape_voxels = bv;
+    // the fork point: graphs of G whole overlapped steps (the form vx3g_step runs them in),
+    // one per fork point, launched alternately; the first launch of each is not counted
+    constexpr int G = 8;
+    const int reps = n_fork / (2 * G);
+    double tf[2] = {0.0, 0.0};
+    if (reps >= 2) {
+        cudaGraphExec_t gx[2] = {nullptr, nullptr};
+        const int p0 = (int)(c->steps & 1);  // G is even: every launch starts at this parity
+        for (int m = 0; m < 2; m++) {
+            c->fork_early = m;
+            cudaGraph_t gr;
+            CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t ce = cudaSuccess;
+            for (int i = 0; i < G && ce == cudaSuccess; i++) ce = enqueue_step(c, (p0 + i) & 1);
+            const cudaError_t ee = cudaStreamEndCapture(c->stream, &gr);
+            if (ce != cudaSuccess || ee != cudaSuccess) {
+                if (ee == cudaSuccess) cudaGraphDestroy(gr);
+                if (gx[0]) cudaGraphExecDestroy(gx[0]);
+                return fail(VX3G_ERR_CUDA, "autotune graph capture");
+            }
+            const cudaError_t ie = cudaGraphInstantiate(&gx[m], gr, 0);
+            cudaGraphDestroy(gr);
+            if (ie != cudaSuccess) {
+                if (gx[0]) cudaGraphExecDestroy(gx[0]);
+                return fail(VX3G_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+            }
+        }
+        for (int k = 0; k < 2 * reps; k++) {
+            CU(cudaEventRecord(ev[2 * k], c->stream));
+            CU(cudaGraphLaunch(gx[k & 1], c->stream));
+            CU(cudaEventRecord(ev[2 * k + 1], c->stream));
+            c->steps += G;
+        }
+        CU(cudaStreamSynchronize(c->stream));
+        for (int k = 2; k < 2 * reps; k++) {
+            float a = 0;
+            CU(cudaEventElapsedTime(&a, ev[2 * k], ev[2 * k + 1]));
+            tf[k & 1] += a;
+        }
+        cudaGraphExecDestroy(gx[0]);
+        cudaGraphExecDestroy(gx[1]);
+    }
+    c->fork_early = reps >= 2 && tf[1] < tf[0] ? 1 : 0;
+    for (int i = 2 * reps * G; i < n_fork; i++) {  // the rest of the n_steps, at the chosen point
+        CU(enqueue_step(c, (int)(c->steps & 1)));
+        c->steps++;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
     for (auto &g : c->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
-    if (cache_json) {  // flat JSON object {"<gpu>|mixed|nv|nl|ns": [link shape, voxel shape], ...}
+    if (cache_json) {  // flat JSON object {"<gpu>|mixed|nv|nl|ns": [link shape, voxel shape, fork point], ...}
         std::string body = cache;
         const size_t close = body.rfind('}');
-        const std::string entry = "\"" + key + "\": [" + std::to_string(bl) + ", " + std::to_string(bv) + "]";
+        const std::string entry = "\"" + key + "\": [" + std::to_string(bl) + ", " + std::to_string(bv) + ", " +
+                                  std::to_string(c->fork_early) + "]";
         if (close == std::string::npos || body.find('"') == std::string::npos) {
             body = "{\n  " + entry + "\n}\n";
         } else {
