@@ -40,9 +40,12 @@ def test_loader_is_loud_when_library_missing(tmp_path):
 def test_ctypes_structs_match_the_header(tmp_path):
     """The ctypes mirrors in abi.py have the C structs' sizes and field offsets."""
     import subprocess
-    fields = {"vx3g_material": (abi.Material, ["E", "fail_stress", "model", "is_measured", "thermal_on_after"]),
+    fields = {"vx3g_material": (abi.Material, ["E", "fail_stress", "model", "is_measured", "thermal_on_after",
+                                                "cilia", "cilia_on_after", "remove_after"]),
               "vx3g_robot_desc": (abi.RobotDesc, ["lattice", "materials", "vox_size", "floor_enabled",
-                                                  "volume_effects", "slow_damping", "log10E", "force_field"]),
+                                                  "volume_effects", "slow_damping", "log10E", "force_field",
+                                                  "enable_cilia", "cilia_base", "cilia_shift", "enable_detach",
+                                                  "secondary_experiment"]),
               "vx3g_batch_desc": (abi.BatchDesc, ["robots", "precision", "graph_chunk"])}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vx3g.h"', "int main(void) {"]
     for st, (_, names) in fields.items():
