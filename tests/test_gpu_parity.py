@@ -324,3 +324,24 @@ def test_full_size_single_body_properties():
     p = st["linmom"].sum(0)
     assert np.all(np.abs(p) <= 1e-6 * np.abs(st["linmom"]).sum())
     assert np.all(runs[0].status() == 0)
+
+
+def test_fp64_feature_mix_batch_matches_oracle():
+    """Eight seeded robots combining collision, detach, material removal, cilia and
+    force fields, in one batch: the FP64 kernels follow the oracle robot by robot
+    (positions within 1e-6 voxel sizes, identical surface sets)."""
+    import feature_mix
+    robots = [feature_mix.robot(s) for s in range(8)]
+    b = abi.Batch(robots, abi.PRECISION_FP64)
+    sims = [ob.oracle_sim(r) for r in robots]
+    off = b.voxel_offset
+    for _ in range(4):
+        b.step(60)
+        pos, surf = b.state()["pos"], b.surface()
+        for i, (r, s) in enumerate(zip(robots, sims)):
+            s.step(60)
+            err = np.max(np.abs(_robot_slice(b, i, pos) - s.voxels()["pos"]))
+            assert err <= POS_TOL * r.vox_size, f"robot {i}: {err:.3e}"
+            mine = surf[(surf >= off[i]) & (surf < off[i + 1])] - off[i]
+            assert np.array_equal(mine, s.surface()), f"robot {i}: surface"
+    assert np.all(b.status() == 0)
