@@ -6,11 +6,15 @@
 // stands in for boost::filesystem::path.  Each sub-batch (one per device) is
 // read the way readVXD does it (base VXA + each VXD merged by its
 // replace="..." children, src/Utils/ctool.h:49-57), simulated as one vx3g
-// batch until each robot's StopConditionFormula holds (or it diverges), and
+// batch until each robot's StopConditionFormula holds (or it diverges; the formula
+// reads the centre of mass as the reference samples it, every int(TempPeriod / dt)
+// steps, src/VX3/VX3_VoxelyzeKernel.cu:313-320), and
 // collected into VX3_SimulationResult records sorted by fitness
 // (VX3_SimulationResult.h:26-33).  With RecordStepSize > 0 the history text of
 // CUDA_Simulation (src/VX3/VX3_SimulationManager.cu:40-114) is written to
-// `history` (stdout by default).
+// `history` (stdout by default).  Simulator/SecondaryExperiment: material removal
+// runs inside the step, the initial-position reset
+// (ReinitializeInitialPositionAfterThisManySeconds, :344-348) here between chunks.
 #pragma once
 
 #include <cstdio>
