@@ -7,7 +7,8 @@ The default line also carries the adjoint's backward/forward time ratio on the
 differentiable 12x12x6 robot ("adjoint"; --no-adjoint leaves it out).
 
 A bench "step" is one CUDA-graph chunk of --chunk (default 100) physics time
-steps over the whole batch.  Timed steps are bracketed by CUDA events on the
+steps over the whole batch; the default 200 timed chunks cover the 20,000 steps
+of the single-body configuration (after 500 warm-up steps).  Timed steps are bracketed by CUDA events on the
 library's stream; the L2 cache is flushed (512 MB overwrite) before every timed
 chunk.  The default workload is the single large body (64^3 Bernoulli(0.6),
 collisions + floor, mixed precision).  Under torchrun each rank runs its own
@@ -315,7 +316,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)  # 200 chunks of 100: the 64^3 body's 20,000-step run
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="vx3g", choices=["vx3g", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
