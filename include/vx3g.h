@@ -218,8 +218,13 @@ int vx3g_backward(vx3g_ctx *ctx, const double *dL_dcom, double *dL_dphase, doubl
  * vx3g_recommended_dt_noalloc: rdt[r] = recommendedTimeStep of robot r in its
  *   current state (seconds, before DtFrac and the 1e-10 floor; vx3g_create sets
  *   the context's dt to (float)(DtFrac * max(rdt, 1e-10))).  With Poisson's ratio
- *   on, the stiffness term follows the links' current strain, so the value
- *   changes as the robot deforms.
+ *   on, the stiffness term eHat*A/((strain+1)*L) takes the links' current strain
+ *   and rest length, so the value changes as the robot deforms, and the transverse
+ *   area A fixed when the link was created -- the area the step itself uses (the
+ *   reference's link update never refreshes it, VX3_Link.cu:147-150).  The
+ *   reference's VX3_Link::axialStiffness refreshes A from the voxels' current
+ *   Poisson strain (VX3_Link.cu:269-278); the two agree at step 0, where the
+ *   reference calls it.
  *   For callers that must not allocate device memory at this point: a control
  *   loop re-checking the stable step between chunks in a process whose device
  *   memory budget is fixed, or code that runs while the device is in use by work
@@ -258,6 +263,16 @@ int vx3g_launch_shapes(vx3g_ctx *ctx, int32_t *shapes4);
 int vx3g_time_steps(vx3g_ctx *ctx, int n_steps, float *ms);
 int vx3g_flush_l2(vx3g_ctx *ctx, size_t bytes);
 int vx3g_time_passes(vx3g_ctx *ctx, int iters, float *ms4);
+
+/* ---- fault-path test hook (no counterpart in the reference) ---------------
+ * vx3g_debug_barrier: sets the grid barrier of the collision list rebuild to give up
+ *   after `polls` polls of 32 ns or more each (0: the default limit, 2^22 polls)
+ *   with `arrivals` arrivals already counted, and, for polls > 0, makes every
+ *   robot's contact lists due so that the next step runs the barrier.  A large
+ *   pre-counted arrival makes every wait run out: the kernel returns, later rebuilds
+ *   are skipped until the next vx3g_status reports VX3G_ERR_DEVICE and clears the
+ *   barrier and the error, and the step after that rebuilds every list.  Tests only. */
+int vx3g_debug_barrier(vx3g_ctx *ctx, uint32_t polls, uint32_t arrivals);
 
 #ifdef __cplusplus
 }

@@ -6,7 +6,7 @@ vx3g_create sets dt = (float)(DtFrac * max(recommendedTimeStep, 1e-10)); at step
 recommendedTimeStep, so the float dt it implies must equal vx3g_dt bit for bit, on
 two calls in a row.  Covers palettes with Poisson's ratio off and on (the
 strain-dependent stiffness branch), FP64 and mixed-precision contexts, several
-robots, and the 4096-robot limit."""
+robots, a deformed state against the oracle, and the 4096-robot limit."""
 
 import numpy as np
 import pytest
@@ -38,6 +38,30 @@ def test_noalloc_dt_matches_create_time_dt(precision):
         rdt = b.recommended_dt_noalloc()
         got = (frac * np.maximum(rdt, 1e-10)).astype(np.float32)
         assert np.array_equal(got, ref), (got, ref)
+    b.close()
+
+
+@pytest.mark.parametrize("precision,tol", [(abi.PRECISION_FP64, 1e-12), (abi.PRECISION_MIXED, 1e-6)])
+def test_noalloc_dt_follows_the_deformed_state(precision, tol):
+    """After 300 steps of falling and landing, the links are strained: the
+    strain-dependent stiffness branch (Poisson's ratio on) moves the stable step
+    away from its step-0 value.  Against the oracle's recommendedTimeStep on its own
+    run of the same robots (creation-time transverse area, current strain and rest
+    length), on two calls in a row."""
+    import oracle_bridge as ob
+    robots = _robots()
+    b = abi.Batch(robots, precision)
+    step0 = b.recommended_dt_noalloc()
+    b.step(300)
+    sims = [ob.oracle_sim(r) for r in robots]
+    for s in sims:
+        s.step(300)
+    ref = np.array([s.recommended_dt() for s in sims])
+    for _ in range(2):
+        got = b.recommended_dt_noalloc()
+        assert np.allclose(got, ref, rtol=tol, atol=0), (got, ref)
+    moved = np.abs(ref / step0 - 1)
+    assert np.all(moved[[bool(r.volume_effects) for r in robots]] > 1e-9)  # the strain branch is exercised
     b.close()
 
 

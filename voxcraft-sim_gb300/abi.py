@@ -26,6 +26,7 @@ EXPORTS = [
     "vx3g_get_topology", "vx3g_get_surface", "vx3g_com", "vx3g_dt", "vx3g_time", "vx3g_status",
     "vx3g_steps_taken", "vx3g_time_steps", "vx3g_flush_l2", "vx3g_time_passes", "vx3g_stop_robot",
     "vx3g_record", "vx3g_backward", "vx3g_recommended_dt_noalloc", "vx3g_autotune", "vx3g_launch_shapes",
+    "vx3g_debug_barrier",
 ]
 
 
@@ -100,6 +101,7 @@ def load(path: str = LIB_PATH):
     lib.vx3g_autotune.argtypes = [vp, ip, ctypes.c_char_p]
     lib.vx3g_launch_shapes.argtypes = [vp, vp]
     lib.vx3g_backward.argtypes = [vp, dp, dp, dp]
+    lib.vx3g_debug_barrier.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
     _lib = lib
     return lib
 
@@ -311,6 +313,10 @@ class Batch:
         out = np.zeros(self.n_robots)
         _check(self.lib.vx3g_recommended_dt_noalloc(self.h, _P(out)), "vx3g_recommended_dt_noalloc")
         return out
+
+    def debug_barrier(self, polls: int, arrivals: int):
+        """Test hook: make the next list rebuild's grid barrier give up (vx3g_debug_barrier)."""
+        _check(self.lib.vx3g_debug_barrier(self.h, int(polls), int(arrivals)), "vx3g_debug_barrier")
 
     def stop_robot(self, r: int):
         _check(self.lib.vx3g_stop_robot(self.h, int(r)), "vx3g_stop_robot")

@@ -940,15 +940,15 @@ __device__ __forceinline__ void coll_list_robots(const Dev &d, unsigned char *ls
 // Barrier across the CTAs of the cooperative k_coll_prepare (a cooperative launch
 // keeps them all resident).  gbar[0] counts arrivals, gbar[1] is the generation; the
 // last CTA to arrive resets the count and advances the generation.  A CTA that has
-// waited kBarrierPolls polls records bit 1 in d.err and returns false.
-constexpr unsigned kBarrierPolls = 1u << 22;
-
+// waited gbar[2] polls (kBarrierPolls unless a test lowered it) records bit 1 in d.err
+// and returns false; vx3g_status reports it and clears gbar[0..1] and the error word.
 __device__ bool grid_barrier(const Dev &d) {
     __shared__ int passed;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *gen = d.gbar + 1;
         const unsigned g = *gen;
+        const unsigned limit = *(volatile unsigned *)(d.gbar + 2);
         __threadfence();
         if (atomicAdd(d.gbar, 1u) == gridDim.x - 1) {
             atomicExch(d.gbar, 0u);
@@ -957,7 +957,7 @@ __device__ bool grid_barrier(const Dev &d) {
             passed = 1;
         } else {
             unsigned k = 0;
-            while (*gen == g && ++k < kBarrierPolls) __nanosleep(32);
+            while (*gen == g && ++k < limit) __nanosleep(32);
             passed = *gen != g;
             if (!passed) atomicOr(d.err, 1);
         }
@@ -983,6 +983,9 @@ __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_prepare(Dev d) {
     __shared__ int wsum[kLocalListThreads / 32];
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
     if (!*(volatile int *)d.cflag) return;  // (uniform: k_coll_check has finished) no robot is due
+    // a barrier gave up in an earlier launch and vx3g_status has not cleared it yet: the
+    // arrival count may be stale, so no barrier of this launch could be trusted
+    if (*(volatile int *)d.err & 1) return;
     if (d.nhash) {  // robots too large for shared memory, if any is due
         for (int s0 = 0; s0 < d.ns; s0 += gs) grid_box(d, s0 + gt);  // warp-uniform trip count
         if (!grid_barrier(d)) return;

@@ -645,7 +645,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     while (hs < 2 * (long long)d.nhash) hs <<= 1;  // room for a dense grid over the robots' boxes
     d.hsize = hs;
     if ((rc = c->upload(&d.csurf, csurf)) || (rc = c->alloc(&d.ccell, d.ns)) || (rc = c->alloc(&d.cposf, d.ns)) ||
-        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1 + (size_t)d.nr)) || (rc = c->alloc(&d.gbar, 2)) ||
+        (rc = c->alloc(&d.nbr, (size_t)d.ns * kNbrCap)) || (rc = c->alloc(&d.nnb, d.ns)) || (rc = c->alloc(&d.cflag, 1 + (size_t)d.nr)) || (rc = c->upload(&d.gbar, std::vector<unsigned>{0u, 0u, kBarrierPolls})) ||
         (rc = c->upload(&d.cref, std::vector<float4>((size_t)d.ns, make_float4(1e30f, 1e30f, 1e30f, 0.0f)))) ||
         (rc = c->alloc(&d.hcount, hs)) ||
         (rc = c->alloc(&d.hstart, hs)) || (rc = c->alloc(&d.hfill, hs)) || (rc = c->alloc(&d.spos, d.ns)) || (rc = c->alloc(&d.sij, d.ns)) ||
@@ -1020,7 +1020,33 @@ int vx3g_status(vx3g_ctx *c, int32_t *st) {
     if (rc || (rc = download(c, err, c->d.err, 1))) return rc;
     CU(cudaStreamSynchronize(c->stream));
     memcpy(st, h.data(), c->nr * sizeof(int));
-    if (err[0] & 1) return fail(VX3G_ERR_DEVICE, "collision pass: a grid barrier of k_coll_prepare timed out");
+    if (err[0] & 1) {
+        // a grid barrier gave up: CTAs that left early may have left a stale arrival count
+        // and half-built candidate lists.  With nothing in flight (the stream is idle),
+        // clear the barrier words and the error word and make every robot's lists due, so
+        // the next step rebuilds them from scratch; the report stands for the steps taken.
+        CU(cudaMemsetAsync(c->d.gbar, 0, 2 * sizeof(unsigned), c->stream));
+        CU(cudaMemsetAsync(c->d.err, 0, sizeof(int), c->stream));
+        if (c->d.ns) {
+            const std::vector<float4> far((size_t)c->d.ns, make_float4(1e30f, 1e30f, 1e30f, 0.0f));
+            CU(cudaMemcpyAsync(c->d.cref, far.data(), far.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+        }
+        CU(cudaStreamSynchronize(c->stream));
+        return fail(VX3G_ERR_DEVICE, "collision pass: a grid barrier of k_coll_prepare timed out");
+    }
+    return VX3G_OK;
+}
+
+int vx3g_debug_barrier(vx3g_ctx *c, uint32_t polls, uint32_t arrivals) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    CU(cudaSetDevice(c->device));
+    const unsigned w[3] = {arrivals, 0u, polls ? polls : kBarrierPolls};
+    CU(cudaMemcpyAsync(c->d.gbar, w, sizeof w, cudaMemcpyHostToDevice, c->stream));
+    if (polls && c->d.ns) {  // make every robot's lists due, so the next step runs the barriers
+        const std::vector<float4> far((size_t)c->d.ns, make_float4(1e30f, 1e30f, 1e30f, 0.0f));
+        CU(cudaMemcpyAsync(c->d.cref, far.data(), far.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    }
+    CU(cudaStreamSynchronize(c->stream));
     return VX3G_OK;
 }
 

@@ -107,6 +107,9 @@ constexpr unsigned kPackMask = 0x3fffffffu, kPackFixed = 0x80000000u;
 // after it was removed: it neither lists nor is listed
 constexpr unsigned kPackInterior = 0x40000000u;
 constexpr int kLocalHash = 4096;  // buckets of the shared-memory grid (power of two)
+// polls (each with a 32 ns back-off) after which a CTA waiting at a grid barrier of
+// k_coll_prepare gives up, records the error and returns
+constexpr unsigned kBarrierPolls = 1u << 22;
 
 struct Dev {
     // voxels
@@ -138,7 +141,7 @@ struct Dev {
     int *nbr;       // candidate lists, slot-major [kNbrCap][NS]: partner voxel indices, ascending
     int *nnb;       // candidate count per collision-surface voxel
     int *cflag;     // [1 + NR]: [0] some robot's lists are rebuilt this step, [1 + r] robot r's are
-    unsigned *gbar;  // [2] grid barrier of k_coll_prepare: arrivals, generation
+    unsigned *gbar;  // [3] grid barrier of k_coll_prepare: arrivals, generation, poll limit
     int2 *lwork;    // [NR] robots whose lists are rebuilt in shared memory this step: (robot, first chunk)
     unsigned long long *lwork_ctr;  // (robots << 32) | chunks listed in lwork; cleared by the narrow phase
     int lmax;       // most collision-surface voxels of a robot on the shared-memory path (0: none)
