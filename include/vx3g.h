@@ -57,8 +57,15 @@ typedef struct vx3g_material {
     double cte;           /* CTE (1/degC) */
     double mu_static;     /* uStatic */
     double mu_kinetic;    /* uDynamic */
-    double fail_stress;   /* Fail_Stress (Pa), used when model == 1 */
-    int model;            /* MatModel: 0 linear, 1 linear with failure; others -> VX3G_ERR_UNSUPPORTED */
+    double fail_stress;   /* Fail_Stress (Pa): models 1 and 2 (-1: no failure) */
+    int model;            /* MatModel: 0 linear, 1 linear with failure, 2 bilinear (elastic-plastic),
+                             3 stress-strain data points; others -> VX3G_ERR_UNSUPPORTED.  A model
+                             the reference's setters reject (E <= 0; model 1 with fail_stress <= 0;
+                             model 2 unless 0 < plastic_mod < E, yield_stress > 0 and fail_stress
+                             > yield_stress or -1; model 3 without a positive first point or with
+                             strain not increasing) leaves the reference's default material model,
+                             as VX3_SimulationManager does: linear, E = 1e6 Pa, no failure
+                             (src/old/VX_Material.cpp:300-446, src/old/Voxelyze.cpp:357-365) */
     int fixed;            /* Fixed */
     int is_measured;      /* isMeasured (counts toward the centre of mass) */
     double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
@@ -67,7 +74,13 @@ typedef struct vx3g_material {
     double remove_after;     /* RemoveFromSimulationAfterThisManySeconds: with secondary_experiment, the
                                 material's voxels leave the simulation at the end of the first step that
                                 starts later than this (> 0; 0 never) */
+    double plastic_mod;      /* Plastic_Mod (Pa), model 2: the modulus past yield */
+    double yield_stress;     /* Yield_Stress (Pa), model 2 */
+    int n_data;              /* model 3: SSData NumDataPts (a leading (0,0) point is skipped), at most
+                                VX3G_MAX_MODEL_POINTS */
+    const double *strain_data, *stress_data; /* model 3: SSData StrainData / StressData values */
 } vx3g_material;
+#define VX3G_MAX_MODEL_POINTS 32
 
 /* One token of a math-tree program, the reference's VX3_MathTreeToken
  * (src/Utils/VX3_MathTree.h:29-36) as VX3_SimulationManager::ParseMathTree

@@ -508,6 +508,23 @@ void vx3ref_link_mats(void *h, float *f16, int *lmat_of_link) {
     for (int i = 0; i < k->num_d_links; i++) lmat_of_link[i] = (int)(k->d_links[i].mat - k->d_linkMats);
 }
 
+// per link: the plastic strain offset (VX3_Link::strainOffset) of non-linear materials
+void vx3ref_link_offsets(void *h, float *off) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_links; i++) off[i] = k->d_links[i].strainOffset;
+}
+
+// stress-strain points of link material i ((0,0) first); returns their count, copies at most cap
+int vx3ref_link_curve(void *h, int i, float *strain, float *stress, int cap) {
+    VX3_MaterialLink &m = ((RefSim *)h)->k->d_linkMats[i];
+    const int n = (int)m.d_strainData.size();
+    for (int j = 0; j < n && j < cap; j++) {
+        strain[j] = m.d_strainData[j];
+        stress[j] = m.d_stressData[j];
+    }
+    return n;
+}
+
 // link transverse info frozen at init: area, strainSum
 void vx3ref_link_transverse(void *h, float *area, float *ssum) {
     VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;

@@ -136,10 +136,164 @@ static vec to_axis_original(int axis, vec v) {
     return v;
 }
 
+/* ------------------------------------------------------- stress-strain curves */
+/* The piecewise-linear stress-strain model of a material: points (0,0),
+ * (strain[1], stress[1]), ... in float, initial modulus E, failure stress and
+ * strain (-1: none), linear flag.  Setters as CVX_Material's
+ * (src/old/VX_Material.cpp:300-446); each returns 0 where the reference's setter
+ * returns false, the caller then keeping the default curve (setModelLinear(1e6),
+ * the CVX_Material constructor's, src/old/VX_Material.cpp:15-22). */
+#define VXO_MAX_PTS 72
+typedef struct {
+    int linear, n;
+    float E, sigma_fail, eps_fail;
+    float strain[VXO_MAX_PTS], stress[VXO_MAX_PTS];
+} curve;
+
+static int curve_linear(curve *c, float E, float fail) {
+    if (E <= 0) return 0;
+    if (fail != -1.0f && fail <= 0) return 0;
+    float fs = fail == -1.0f ? 1000000.0f : fail;
+    float fe = fs / E;
+    c->n = 2;
+    c->strain[0] = 0.0f; c->stress[0] = 0.0f;
+    c->strain[1] = fe; c->stress[1] = fs;
+    c->linear = 1;
+    c->E = E;
+    c->sigma_fail = fail;
+    c->eps_fail = fail == -1.0f ? -1.0f : fe;
+    return 1;
+}
+
+static void curve_default(curve *c) { curve_linear(c, 1e6f, -1.0f); }
+
+static int curve_bilinear(curve *c, float E, float Ep, float sy, float fail) {
+    if (E <= 0 || Ep <= 0 || Ep >= E || sy <= 0) return 0;
+    if (fail != -1.0f && fail <= sy) return 0;
+    float ys = sy / E;
+    float fs = fail == -1.0f ? 3 * sy : fail;
+    float b = sy - Ep * ys;
+    float fe = (fs - b) / Ep;
+    c->n = 3;
+    c->strain[0] = 0.0f; c->stress[0] = 0.0f;
+    c->strain[1] = ys; c->stress[1] = sy;
+    c->strain[2] = fe; c->stress[2] = fs;
+    c->linear = 0;
+    c->E = E;
+    c->sigma_fail = fail;
+    c->eps_fail = fail == -1.0f ? -1.0f : fe;
+    return 1;
+}
+
+/* setModel: a leading (0,0) is dropped; the rest must begin positive with strictly
+ * increasing strain; the point (0,0) is put back in front */
+static int curve_points(curve *c, int n, const float *e, const float *s) {
+    int k = 0;
+    if (n > 0 && e[0] == 0 && s[0] == 0) k = 1;
+    int m = n - k;
+    if (m <= 0 || m + 1 > VXO_MAX_PTS) return 0;
+    if (e[k] <= 0 || s[k] <= 0) return 0;
+    float last = 0.0f;
+    for (int i = k; i < n; i++) {
+        if (e[i] <= last) return 0;
+        last = e[i];
+    }
+    c->n = m + 1;
+    c->strain[0] = 0.0f; c->stress[0] = 0.0f;
+    for (int i = 0; i < m; i++) { c->strain[i + 1] = e[k + i]; c->stress[i + 1] = s[k + i]; }
+    c->E = c->stress[1] / c->strain[1];
+    c->sigma_fail = c->stress[c->n - 1];
+    c->eps_fail = c->strain[c->n - 1];
+    c->linear = m == 1;
+    return 1;
+}
+
+static int curve_failed(const curve *c, float eps) { return c->eps_fail != -1.0f && eps > c->eps_fail; }
+
+/* CVX_Material::modulus (src/old/VX_Material.cpp:231-243) */
+static float curve_modulus(const curve *c, float eps) {
+    if (curve_failed(c, eps)) return 0.0f;
+    if (eps <= c->strain[1] || c->linear) return c->E;
+    for (int i = 2; i < c->n; i++)
+        if (eps <= c->strain[i] || i == c->n - 1) return (c->stress[i] - c->stress[i - 1]) / (c->strain[i] - c->strain[i - 1]);
+    return 0.0f;
+}
+
+/* CVX_Material::strain(stress) (src/old/VX_Material.cpp:214-228) */
+static float curve_strain_of(const curve *c, float sig) {
+    if (sig <= c->stress[1] || c->linear) return sig / c->E;
+    for (int i = 2; i < c->n; i++) {
+        if (sig <= c->stress[i] || i == c->n - 1) {
+            float perc = (sig - c->stress[i - 1]) / (c->stress[i] - c->stress[i - 1]);
+            return c->strain[i - 1] + perc * (c->strain[i] - c->strain[i - 1]);
+        }
+    }
+    return 0.0f;
+}
+
+/* VX3_Material::stress (src/VX3/VX3_Material.cu:90-124) on the device copy of the
+ * curve: VX3_Material::syncVectors (VX3_Material.cu:463-481) puts one more 0 in front
+ * of the host points, so the device arrays read 0, 0, strain_1, ... and the stress
+ * function's first-segment test compares with that second 0 */
+static float curve_stress(const curve *c, float nu, float eHat, float eps, float tss, int force_linear) {
+    float ds[VXO_MAX_PTS + 1], dS[VXO_MAX_PTS + 1];
+    int n = c->n + 1;
+    ds[0] = 0.0f; dS[0] = 0.0f;
+    for (int i = 0; i < c->n; i++) { ds[i + 1] = c->strain[i]; dS[i + 1] = c->stress[i]; }
+    if (curve_failed(c, eps)) return 0.0f;
+    if (eps <= ds[1] || c->linear || force_linear) {
+        if (nu == 0.0f) return c->E * eps;
+        return eHat * ((1 - nu) * eps + nu * tss);
+    }
+    for (int i = 2; i < n; i++) {
+        if (eps <= ds[i] || i == n - 1) {
+            float perc = (eps - ds[i - 1]) / (ds[i] - ds[i - 1]);
+            float basic = dS[i - 1] + perc * (dS[i] - dS[i - 1]);
+            if (nu == 0.0f) return basic;
+            float modulus = (dS[i] - dS[i - 1]) / (ds[i] - ds[i - 1]);
+            float modulusHat = modulus / ((1 - 2 * nu) * (1 + nu));
+            float eff = basic / modulus;
+            float effT = tss * (eff / eps);
+            return modulusHat * ((1 - nu) * eff + nu * effT);
+        }
+    }
+    return 0.0f;
+}
+
+/* the link curve of CVX_MaterialLink::updateAll (src/old/VX_MaterialLink.cpp:66-97) */
+static void curve_link(curve *out, const curve *a, const curve *b) {
+    float fail;
+    if (a->sigma_fail == -1.0f) fail = b->sigma_fail;
+    else if (b->sigma_fail == -1.0f) fail = a->sigma_fail;
+    else fail = a->sigma_fail < b->sigma_fail ? a->sigma_fail : b->sigma_fail;
+    if (a->linear && b->linear) {
+        if (!curve_linear(out, 2.0f * a->E * b->E / (a->E + b->E), fail)) curve_default(out);
+        return;
+    }
+    float e[VXO_MAX_PTS], s[VXO_MAX_PTS];
+    int n = 1, ia = 1, ib = 1;
+    e[0] = 0.0f; s[0] = 0.0f;
+    while (ia < a->n && ib < b->n && n < VXO_MAX_PTS) {
+        float x = a->strain[ia];
+        if (b->strain[ib] < x) x = b->strain[ib];
+        if (x == a->strain[ia]) ia++;
+        if (x == b->strain[ib]) ib++;
+        float k1 = curve_modulus(a, x - FLT_EPSILON), k2 = curve_modulus(b, x - FLT_EPSILON);
+        float k = 2.0f * k1 * k2 / (k1 + k2);
+        e[n] = x;
+        s[n] = s[n - 1] + k * (x - e[n - 1]);
+        n++;
+    }
+    if (!curve_points(out, n, e, s)) curve_default(out);
+    out->sigma_fail = fail;
+    out->eps_fail = fail == -1.0f ? -1.0f : curve_strain_of(out, fail);
+}
+
 /* ------------------------------------------------------------- materials */
 typedef struct {
     float E, nu, rho, cte, mu_s, mu_k, z_int, z_glob, z_col, eHat;
     float sigma_fail, eps_fail;
+    curve cv;
     double nom_size;
     float grav_mult;
     float mass, mass_inv, sqrt_mass, mom_inertia, mom_inertia_inv, c2xSqMxExS, c2xSqIxExSxSxS;
@@ -153,6 +307,7 @@ typedef struct {
     int m1, m2; /* vox1Mat, vox2Mat indices */
     float E, nu, eHat, eps_fail, cte;
     float a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp;
+    curve cv;
 } lmat;
 
 /* CVX_Material::updateDerived _eHat (src/old/VX_Material.cpp:542-549) */
@@ -182,11 +337,21 @@ static void vmat_import(vmat *m, const vxo_material *in, const vxo_robot *r) {
     m->cilia = in->cilia;
     m->cilia_on_after = in->cilia_on_after;
     m->remove_after = in->remove_after;
-    float E = (float)in->E;
-    float fail = in->model == 1 ? (float)in->fail_stress : -1.0f;
-    m->E = E;
-    m->sigma_fail = fail;
-    m->eps_fail = (fail == -1.0f) ? -1.0f : fail / E; /* setModelLinear (VX_Material.cpp:372-392) */
+    /* the model as CVX_Sim::CopyMat sets it (VX_Sim.cpp:390-409) */
+    int ok = 0;
+    if (in->model == 0) ok = curve_linear(&m->cv, (float)in->E, -1.0f);
+    else if (in->model == 1) ok = curve_linear(&m->cv, (float)in->E, (float)in->fail_stress);
+    else if (in->model == 2)
+        ok = curve_bilinear(&m->cv, (float)in->E, (float)in->plastic_mod, (float)in->yield_stress, (float)in->fail_stress);
+    else if (in->model == 3 && in->n_data > 0 && in->n_data < VXO_MAX_PTS) {
+        float e[VXO_MAX_PTS], sg[VXO_MAX_PTS];
+        for (int i = 0; i < in->n_data; i++) { e[i] = (float)in->strain_data[i]; sg[i] = (float)in->stress_data[i]; }
+        ok = curve_points(&m->cv, in->n_data, e, sg);
+    }
+    if (!ok) curve_default(&m->cv);
+    m->E = m->cv.E;
+    m->sigma_fail = m->cv.sigma_fail;
+    m->eps_fail = m->cv.eps_fail;
     float nu = (float)in->nu;
     if (nu < 0) nu = 0;
     if (nu >= 0.5) nu = 0.5 - FLT_EPSILON * 2;
@@ -217,13 +382,10 @@ static void vmat_import(vmat *m, const vxo_material *in, const vxo_robot *r) {
 static void lmat_make(lmat *l, const vmat *v1, const vmat *v2, int i1, int i2) {
     l->m1 = i1;
     l->m2 = i2;
-    float f1 = v1->sigma_fail, f2 = v2->sigma_fail, fail;
-    if (f1 == -1.0f) fail = f2;
-    else if (f2 == -1.0f) fail = f1;
-    else fail = f1 < f2 ? f1 : f2;
-    float E = 2.0f * v1->E * v2->E / (v1->E + v2->E);
+    curve_link(&l->cv, &v1->cv, &v2->cv);
+    float E = l->cv.E;
     l->E = E;
-    l->eps_fail = (fail == -1.0f) ? -1.0f : fail / E;
+    l->eps_fail = l->cv.eps_fail;
     l->cte = 0.5f * (v1->cte + v2->cte);
     float nu;
     if (v1->nu == 0 && v2->nu == 0) nu = 0;
@@ -268,6 +430,7 @@ typedef struct {
     vec pos2, a1v, a2v;
     vec fNeg, fPos, mNeg, mPos;
     float strain, maxStrain, area, tss;
+    float strainOffset; /* plastic offset of a non-linear material (VX3_Link::strainOffset) */
     double rest;
     int small, states;
     int gone; /* detached (gpu_update_detach): no longer updated, no longer any voxel's link */
@@ -462,11 +625,27 @@ void vxo_destroy(void *h) {
     free(S);
 }
 
-/* VX3_Material::stress, linear branch (VX3_Material.cu:90-101) */
-static float mat_stress(const lmat *m, float strain, float tss) {
-    if (m->eps_fail != -1.0f && strain > m->eps_fail) return 0.0f;
-    if (m->nu == 0.0f) return m->E * strain;
-    return m->eHat * ((1 - m->nu) * strain + m->nu * tss);
+/* VX3_Link::updateStrain (VX3_Link.cu:220-260): linear materials follow their law and
+ * track maxStrain; non-linear ones follow the curve on new ground (recording the
+ * strainOffset of the unloading line) and unload linearly below maxStrain */
+static float link_strain_update(link *L, const lmat *m, float eps) {
+    L->strain = eps;
+    if (m->cv.linear) {
+        if (eps > L->maxStrain) L->maxStrain = eps;
+        return curve_stress(&m->cv, m->nu, m->eHat, eps, L->tss, 0);
+    }
+    if (eps > L->maxStrain) {
+        L->maxStrain = eps;
+        float st = curve_stress(&m->cv, m->nu, m->eHat, eps, L->tss, 0);
+        if (m->nu != 0.0f)
+            L->strainOffset = L->maxStrain - curve_stress(&m->cv, m->nu, m->eHat, eps, 0.0f, 0) / (m->eHat * (1 - m->nu));
+        else
+            L->strainOffset = L->maxStrain - st / m->E;
+        return st;
+    }
+    float rel = eps - L->strainOffset;
+    if (m->nu != 0.0f) return curve_stress(&m->cv, m->nu, m->eHat, rel, L->tss, 1);
+    return m->E * rel;
 }
 
 /* VX3_Voxel::dampingMultiplier (VX3_Voxel.h:206-208) */
@@ -513,11 +692,9 @@ static void link_update(sim *S, link *L) {
     vec dPos2 = vscale(vsub(pos2, oldPos2), 0.5);
     vec dA1 = vscale(vsub(a1v, oldA1), 0.5);
     vec dA2 = vscale(vsub(a2v, oldA2), 0.5);
-    /* updateStrain (:220-260), linear materials */
+    /* updateStrain (:220-260) */
     float axialStrain = (float)(pos2.x / L->rest);
-    L->strain = axialStrain;
-    if (axialStrain > L->maxStrain) L->maxStrain = axialStrain;
-    float stress = mat_stress(m, axialStrain, L->tss);
+    float stress = link_strain_update(L, m, axialStrain);
     if (m->eps_fail != -1.0f && L->maxStrain > m->eps_fail) { /* isFailed */
         L->fNeg = L->fPos = L->mNeg = L->mPos = V(0, 0, 0);
         return;
@@ -971,9 +1148,24 @@ void vxo_link_mats(void *h, float *f16, int *lmat_of_link) {
         float *f = f16 + 16 * i;
         f[0] = m->E; f[1] = m->nu; f[2] = m->eHat; f[3] = m->a1; f[4] = m->a2; f[5] = m->b1; f[6] = m->b2; f[7] = m->b3;
         f[8] = m->sqA1; f[9] = m->sqA2xIp; f[10] = m->sqB1; f[11] = m->sqB2xFMp; f[12] = m->sqB3xIp;
-        f[13] = m->eps_fail; f[14] = 1.0f; f[15] = m->cte;
+        f[13] = m->eps_fail; f[14] = m->cv.linear ? 1.0f : 0.0f; f[15] = m->cte;
     }
     for (int i = 0; i < S->nl; i++) lmat_of_link[i] = S->l[i].mat;
+}
+
+void vxo_link_offsets(void *h, float *off) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nl; i++) off[i] = S->l[i].strainOffset;
+}
+
+int vxo_link_curve(void *h, int i, float *strain, float *stress, int cap) {
+    const curve *c = &((sim *)h)->lm[i].cv;  /* as the device copy holds it: one more 0 in front */
+    if (cap > 0) strain[0] = stress[0] = 0.0f;
+    for (int j = 0; j < c->n && j + 1 < cap; j++) {
+        strain[j + 1] = c->strain[j];
+        stress[j + 1] = c->stress[j];
+    }
+    return c->n + 1;
 }
 
 void vxo_surface(void *h, int *idx) {

@@ -19,12 +19,15 @@ extern "C" {
 /* One palette entry, values as read from the VXA <Material> element. */
 typedef struct vxo_material {
     double E, nu, rho, cte, mu_static, mu_kinetic;
-    double fail_stress;      /* used when model == 1 (MDL_LINEAR_FAIL) */
-    int model;               /* 0 = MDL_LINEAR, 1 = MDL_LINEAR_FAIL */
+    double fail_stress;      /* models 1 and 2 (-1: none) */
+    int model;               /* 0 MDL_LINEAR, 1 MDL_LINEAR_FAIL, 2 MDL_BILINEAR, 3 MDL_DATA */
     int fixed, is_measured;
     double thermal_on_after; /* TurnOnThermalExpansionAfterThisManySeconds */
     double cilia, cilia_on_after; /* Cilia, TurnOnCiliaAfterThisManySeconds */
     double remove_after;          /* RemoveFromSimulationAfterThisManySeconds (SecondaryExperiment) */
+    double plastic_mod, yield_stress; /* Plastic_Mod, Yield_Stress (model 2, MDL_BILINEAR) */
+    int n_data;                       /* model 3 (MDL_DATA): SSData points */
+    const double *strain_data, *stress_data;
 } vxo_material;
 
 /* A math-tree token (VX3_MathTreeToken, src/Utils/VX3_MathTree.h:29-36): op is the
@@ -68,6 +71,11 @@ void vxo_voxel_mats(void *h, float *f16, double *nomsize, int *fixed_measured);
 void vxo_link_mats(void *h, float *f16, int *lmat_of_link);
 int vxo_num_link_mats(void *h);
 void vxo_surface(void *h, int *idx);
+/* per link: the plastic strain offset; link material i's stress-strain points as the
+ * reference's device copy holds them (0, 0, then the model's points from (0,0) on; at
+ * most cap copied), returning their count */
+void vxo_link_offsets(void *h, float *off);
+int vxo_link_curve(void *h, int i, float *strain, float *stress, int cap);
 void vxo_last_contact(void *h, double *c3);
 void vxo_com(void *h, double *c3);
 double vxo_recommended_dt(void *h);

@@ -67,6 +67,7 @@ LMat link_material(const VMat &a, const VMat &b) {
     const float E = 2.0f * a.E * b.E / (a.E + b.E), L = (float)kL;
     l.E = E;
     l.eps_fail = -1.0f;
+    l.lin = 1;  // linear model: no stress-strain points
     l.eHat = E;
     l.a1 = E * L;
     l.a2 = E * L * L * L / 12.0f;

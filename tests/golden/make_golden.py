@@ -106,17 +106,51 @@ def cases():
     rem.secondary_experiment = True
     rem.cilia_base = 2e-2 * rng.standard_normal(rem.grid.shape + (3,))
     out["bern6_removal"] = (rem, 300, 100)
+    # bilinear (elastic-plastic) overhang clamped at the base (a Fixed material, floor off,
+    # so no stick/slip): gravity loads the root links past yield, the oscillation then
+    # unloads them along the offset line (VX3_Link::updateStrain)
+    plastic = [wl.Material(E=2e4, nu=0.0, rho=1e3, model=2, plastic_mod=4e3, yield_stress=8.0, fail_stress=-1.0),
+               wl.Material(E=2e4, nu=0.0, rho=1e3, fixed=1)]
+    clamp = grid.copy()
+    clamp[0, :, 0:2] = 2
+    out["bilinear_cantilever_plastic"] = (wl.Robot(grid=clamp, materials=plastic, volume_effects=False,
+                                                   z_offset=0, floor=False), 1500, 500)
+    # actuated body mixing a bilinear material with failure, a data-point curve and a
+    # linear material (merged link curves, springs in series), Poisson's ratio off
+    rng = np.random.default_rng(4)
+    dat = wl.Material(E=0, nu=0.0, cte=0.01, model=3, ss_strain=(0, 0.002, 0.006, 0.02, 0.05),
+                      ss_stress=(0, 200.0, 450.0, 700.0, 800.0))
+    bil = wl.Material(E=1e5, nu=0.0, cte=0.01, model=2, plastic_mod=3e4, yield_stress=100.0, fail_stress=900.0)
+    out["bern5_data_bilinear"] = (
+        wl.bernoulli_body(rng, (5, 4, 3), 0.9, [bil, dat, wl.Material(E=1e5, nu=0.0)], random_phase=True,
+                          temp_vary=True, temp_amplitude=8.0, temp_period=0.02, enable_expansion=1, z_offset=1,
+                          volume_effects=False), 400, 100)
+    # the same with Poisson's ratio on: the volumetric variant of the non-linear stress
+    rng = np.random.default_rng(5)
+    datnu = wl.Material(E=0, nu=0.3, cte=0.01, model=3, ss_strain=(0.002, 0.006, 0.02), ss_stress=(200.0, 450.0, 600.0))
+    bilnu = wl.Material(E=1e5, nu=0.35, cte=0.01, model=2, plastic_mod=2e4, yield_stress=150.0, fail_stress=-1.0)
+    out["bern4_data_bilinear_poisson"] = (
+        wl.bernoulli_body(rng, (4, 4, 4), 0.9, [datnu, bilnu, wl.Material(E=1e5, nu=0.3, cte=0.0)],
+                          random_phase=True, temp_vary=True, temp_amplitude=8.0, temp_period=0.02,
+                          enable_expansion=1, z_offset=1), 400, 100)
     return out
 
 
-def snapshot(s):
+def snapshot(s, plastic=False):
     v = s.voxels()
     lk = s.links()
     t = s.topology()
-    return dict(small=t["small"], states=t["states"], pos=v["pos"], orient=v["orient"], linmom=v["linmom"], angmom=v["angmom"], tempe=v["tempe"],
-                flags=v["flags"], strain=lk["strain"], maxstrain=lk["maxstrain"], rest=lk["rest"],
-                local9=lk["local9"], forces=lk["forces"], contact=s.last_contact(), com=s.com(),
-                time=np.array([s.time()]), dt=np.array([s.dt()], np.float32))
+    out = dict(small=t["small"], states=t["states"], pos=v["pos"], orient=v["orient"], linmom=v["linmom"], angmom=v["angmom"], tempe=v["tempe"],
+               flags=v["flags"], strain=lk["strain"], maxstrain=lk["maxstrain"], rest=lk["rest"],
+               local9=lk["local9"], forces=lk["forces"], contact=s.last_contact(), com=s.com(),
+               time=np.array([s.time()]), dt=np.array([s.dt()], np.float32))
+    if plastic:  # non-linear materials: the links' plastic strain offsets
+        out["soffset"] = s.link_offsets()
+    return out
+
+
+def nonlinear(r):
+    return any(m.mat_model() >= 2 for m in r.materials)
 
 
 def robot_record(r):
@@ -131,6 +165,12 @@ def robot_record(r):
                     enable_detach=r.enable_detach, secondary_experiment=r.secondary_experiment)
     rec = dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
                settings=np.array(json.dumps(settings)))
+    if nonlinear(r):  # material models beyond linear: MatModel and its parameters per palette entry
+        rec["models"] = np.array(json.dumps([dict(model=m.mat_model(), plastic_mod=m.plastic_mod,
+                                                  yield_stress=m.yield_stress,
+                                                  ss_strain=None if m.ss_strain is None else list(m.ss_strain),
+                                                  ss_stress=None if m.ss_stress is None else list(m.ss_stress))
+                                             for m in r.materials]))
     for name in ("cilia_base", "cilia_shift"):  # per cell of the padded lattice, 3 values each
         a = r.padded_cells(getattr(r, name))
         rec[name] = a.reshape(g.shape + (3,)) if a is not None else np.zeros(0)
@@ -151,12 +191,16 @@ def main(only=()):
         rec.update({"topo_" + k: v for k, v in topo.items()})
         rec.update({"mat_" + k: v for k, v in mats.items()})
         rec["recommended_dt0"] = np.array([s.recommended_dt()])
+        if nonlinear(robot):
+            curves = s.link_curves()
+            rec["link_curve_n"] = np.array([len(c) for c in curves], np.int32)
+            rec["link_curves"] = np.concatenate(curves) if curves else np.zeros((0, 2), np.float32)
         done, snaps = 0, []
         while done < steps:
             n = s.step(every)
             done += every
             snaps.append(done)
-            for k, v in snapshot(s).items():
+            for k, v in snapshot(s, nonlinear(robot)).items():
                 rec[f"s{done}_{k}"] = v
             rec[f"s{done}_surface"] = s.surface()
             if n < every:

@@ -26,6 +26,13 @@ def load(name):
                         cilia=float(m[9]) if len(m) > 9 else 0.0, cilia_on_after=float(m[10]) if len(m) > 10 else 0.0,
                         remove_after=float(m[11]) if len(m) > 11 else 0.0)
             for m in d["materials"]]
+    if "models" in d.files:  # MatModel 2/3 parameters per palette entry
+        for m, md in zip(mats, json.loads(str(d["models"]))):
+            m.model = md["model"]
+            m.plastic_mod = md["plastic_mod"]
+            m.yield_stress = md["yield_stress"]
+            m.ss_strain = None if md["ss_strain"] is None else tuple(md["ss_strain"])
+            m.ss_stress = None if md["ss_stress"] is None else tuple(md["ss_stress"])
     phase = d["phase"] if d["phase"].size else None
     robot = wl.Robot(grid=d["lattice"], materials=mats, phase=phase, z_offset=0, **s)
     for name in ("cilia_base", "cilia_shift"):

@@ -26,7 +26,9 @@ class VxoMaterial(ctypes.Structure):
                 ("cte", ctypes.c_double), ("mu_static", ctypes.c_double), ("mu_kinetic", ctypes.c_double),
                 ("fail_stress", ctypes.c_double), ("model", ctypes.c_int), ("fixed", ctypes.c_int),
                 ("is_measured", ctypes.c_int), ("thermal_on_after", ctypes.c_double),
-                ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double), ("remove_after", ctypes.c_double)]
+                ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double), ("remove_after", ctypes.c_double),
+                ("plastic_mod", ctypes.c_double), ("yield_stress", ctypes.c_double), ("n_data", ctypes.c_int),
+                ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p)]
 
 
 class VxoRobot(ctypes.Structure):
@@ -73,6 +75,8 @@ def _setup(lib, prefix):
         ("last_contact", None, [h, ctypes.c_void_p]),
         ("com", None, [h, ctypes.c_void_p]),
         ("recommended_dt", ctypes.c_double, [h]),
+        ("link_offsets", None, [h, ctypes.c_void_p]),
+        ("link_curve", ctypes.c_int, [h, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ]:
         f = getattr(lib, prefix + name)
         f.restype = res
@@ -162,6 +166,21 @@ class Sim:
         self._f("link_mats")(self.h, _P(lf), _P(lol))
         return dict(vmat=f, nomsize=ns, fixed_measured=fm, lmat=lf[:nlm], lmat_of_link=lol[:self.counts()[1]])
 
+    def link_offsets(self):
+        """Per link: the plastic strain offset of a non-linear material (0 otherwise)."""
+        off = np.zeros(max(self.counts()[1], 1), np.float32)
+        self._f("link_offsets")(self.h, _P(off))
+        return off[:self.counts()[1]]
+
+    def link_curves(self):
+        """Per link material: its stress-strain points as an (n, 2) float32 array."""
+        out = []
+        for i in range(self._f("num_link_mats")(self.h)):
+            e, s = np.zeros(128, np.float32), np.zeros(128, np.float32)
+            n = self._f("link_curve")(self.h, i, _P(e), _P(s), 128)
+            out.append(np.stack([e[:n], s[:n]], 1))
+        return out
+
     def surface(self):
         ns = self.counts()[2]
         idx = np.zeros(max(ns, 1), np.int32)
@@ -186,10 +205,14 @@ def robot_struct(robot):
     lattice = np.ascontiguousarray(g.reshape(-1).astype(np.uint8))
     phase = None if ph is None else np.ascontiguousarray(ph.reshape(-1).astype(np.float64))
     mats = (VxoMaterial * max(len(robot.materials), 1))()
+    ss_keep = []
     for i, m in enumerate(robot.materials):
+        n, e, s = m.ss_arrays()
+        ss_keep.append((e, s))
         mats[i] = VxoMaterial(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic,
-                              m.fail_stress, 0 if m.fail_stress == 0 else 1, m.fixed, m.is_measured, 0.0,
-                              m.cilia, m.cilia_on_after, m.remove_after)
+                              m.fail_stress, m.mat_model(), m.fixed, m.is_measured, 0.0,
+                              m.cilia, m.cilia_on_after, m.remove_after, m.plastic_mod, m.yield_stress,
+                              n, None if e is None else _P(e), None if s is None else _P(s))
     Z, Y, X = g.shape
     r = VxoRobot(X, Y, Z, _P(lattice), None if phase is None else _P(phase), len(robot.materials), mats,
                  robot.vox_size, robot.dt_frac, robot.grav_acc, int(robot.floor),
@@ -210,7 +233,7 @@ def robot_struct(robot):
                 setattr(r, name, _P(a))
     r.enable_detach = int(robot.enable_detach)
     r.secondary_experiment = int(robot.secondary_experiment)
-    return r, (lattice, phase, mats, progs, cil)
+    return r, (lattice, phase, mats, progs, cil, ss_keep)
 
 
 def _force_field_tokens(robot):

@@ -103,6 +103,38 @@ def test_runner_force_field_matches_oracle(tmp_path):
     assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size  # the field moved the robot
 
 
+def test_runner_material_models_match_oracle(tmp_path):
+    """MatModel 2 (bilinear, Plastic_Mod / Yield_Stress / Fail_Stress) and MatModel 3
+    (SSData points) read from the VXA by the runner: the report matches the oracle
+    running the same robot, and the plastic materials move it differently from linear
+    ones of the same initial modulus."""
+    vbuild.build()
+    exe = os.path.join(os.path.dirname(vbuild.LIB), "vx3g_sim")
+    rng = np.random.default_rng(12)
+    bil = wl.Material(E=1e5, nu=0.35, cte=0.01, model=2, plastic_mod=2e4, yield_stress=120.0, fail_stress=-1.0)
+    dat = wl.Material(E=0, nu=0.35, cte=0.01, model=3, ss_strain=(0, 0.002, 0.006, 0.02),
+                      ss_stress=(0, 200.0, 450.0, 600.0))
+    robot = wl.bernoulli_body(rng, (5, 4, 3), 0.85, [bil, dat, wl.Material(E=1e5, nu=0.35)], random_phase=True,
+                              temp_vary=True, temp_amplitude=10.0, temp_period=0.02, enable_expansion=1,
+                              stop_time=0.01, fitness_x=True)
+    (tmp_path / "base.vxa").write_text(wl.to_vxa(robot))
+    (tmp_path / "r.vxd").write_text("<VXD>\n</VXD>\n")
+    out = tmp_path / "report.xml"
+    r = subprocess.run([exe, "-i", str(tmp_path), "-o", str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    node = ET.parse(out).getroot().find("detail/r")
+    s, c0, _ = _oracle_until(robot, 0.01)
+    assert float(node.find("currentTime").text) == pytest.approx(s.time(), rel=1e-12)
+    com = [float(node.find(f"currentCenterOfMass/{k}").text) for k in "xyz"]
+    np.testing.assert_allclose(com, s.com(), rtol=0, atol=1e-6 * robot.vox_size)
+    assert np.count_nonzero(s.link_offsets()) > 0  # some links yielded
+    lin = wl.Robot(**{**robot.__dict__, "materials": [wl.Material(E=1e5, nu=0.35, cte=0.01),
+                                                      wl.Material(E=1e5, nu=0.35, cte=0.01),
+                                                      wl.Material(E=1e5, nu=0.35)]})
+    f, _, _ = _oracle_until(lin, 0.01)
+    assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size
+
+
 def test_runner_cilia_matches_oracle(tmp_path):
     """EnableCilia with Structure/BaseCiliaForce and ShiftCiliaForce rows and per-material
     Cilia / TurnOnCiliaAfterThisManySeconds, through the runner, against the oracle."""

@@ -272,6 +272,28 @@ def test_changing_surface_mixed_matches_fp64(name):
         abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
 
 
+@pytest.mark.parametrize("name", ["bilinear_cantilever_plastic", "bern5_data_bilinear", "bern4_data_bilinear_poisson"])
+def test_nonlinear_materials_mixed_matches_fp64(name):
+    """Bilinear and data-point stress-strain models with plastic unloading: the
+    mixed-precision kernels follow the FP64 ones (COM within 1e-5 relative, small-angle
+    states identical at the end of the golden horizon), and the adjoint refuses them."""
+    robot, d = golden_cases.load(name)
+    f = abi.Batch([robot], abi.PRECISION_FP64)
+    m = abi.Batch([robot], abi.PRECISION_MIXED)
+    n = int(d["snap_steps"][-1])
+    f.step(n)
+    m.step(n)
+    assert np.all(f.status() == 0) and np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - f.com(), axis=1) / np.linalg.norm(f.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
+    lf, lm = f.links(), m.links()
+    plastic = lf["maxstrain"] > 0
+    assert plastic.any()
+    np.testing.assert_allclose(lm["maxstrain"], lf["maxstrain"], rtol=0, atol=1e-5)
+    with pytest.raises(abi.Vx3gError, match="not implemented"):
+        abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
+
+
 def test_mixed_com_error_vs_fp64():
     rng = np.random.default_rng(21)
     mats = [wl.Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]

@@ -35,7 +35,8 @@ class Material(ctypes.Structure):
                 ("mu_static", ctypes.c_double), ("mu_kinetic", ctypes.c_double), ("fail_stress", ctypes.c_double),
                 ("model", ctypes.c_int), ("fixed", ctypes.c_int), ("is_measured", ctypes.c_int),
                 ("thermal_on_after", ctypes.c_double), ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double),
-                ("remove_after", ctypes.c_double)]
+                ("remove_after", ctypes.c_double), ("plastic_mod", ctypes.c_double), ("yield_stress", ctypes.c_double),
+                ("n_data", ctypes.c_int), ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p)]
 
 
 class RobotDesc(ctypes.Structure):
@@ -125,10 +126,14 @@ def robot_desc(robot):
     lattice = np.ascontiguousarray(g.reshape(-1).astype(np.uint8))
     phase = None if ph is None else np.ascontiguousarray(ph.reshape(-1).astype(np.float64))
     mats = (Material * len(robot.materials))()
+    ss_keep = []
     for i, m in enumerate(robot.materials):
+        n, e, s = m.ss_arrays()
+        ss_keep.append((e, s))
         mats[i] = Material(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress,
-                           0 if m.fail_stress == 0 else 1, int(m.fixed), int(m.is_measured), 0.0,
-                           float(m.cilia), float(m.cilia_on_after), float(m.remove_after))
+                           m.mat_model(), int(m.fixed), int(m.is_measured), 0.0,
+                           float(m.cilia), float(m.cilia_on_after), float(m.remove_after),
+                           float(m.plastic_mod), float(m.yield_stress), n, _P(e), _P(s))
     Z, Y, X = g.shape
     log10E = getattr(robot, "log10E", None)
     if log10E is not None:
@@ -157,7 +162,7 @@ def robot_desc(robot):
             if a is not None:
                 cil.append(a)
                 setattr(d, name, _P(a))
-    return d, (lattice, phase, mats, log10E, progs, cil)
+    return d, (lattice, phase, mats, log10E, progs, cil, ss_keep)
 
 
 class Batch:

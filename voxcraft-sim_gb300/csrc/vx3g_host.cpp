@@ -21,6 +21,7 @@
 #include "../../include/vx3g.h"
 #include "vx3g_adjoint.h"
 #include "vx3g_internal.h"
+#include "vx3g_material.h"
 
 using namespace vx3g;
 
@@ -44,15 +45,36 @@ struct HostVMat {
     float E, nu, rho, cte, mu_s, mu_k, z_int, z_glob, z_col, eHat, sigma_fail, grav_mult;
     float mass, mass_inv, sqrt_mass, mom, mom_inv, c2m, c2i;
     double nom;
+    MatModel model;  // stress-strain model (E and sigma_fail above are its values)
 };
+
+// the stress-strain model of a palette entry as CVX_Sim::CopyMat sets it (src/VXA/VX_Sim.cpp:390-409)
+MatModel material_model(const vx3g_material &in) {
+    MatModel m;
+    bool ok = false;
+    switch (in.model) {
+        case 0: ok = model_linear(m, (float)in.E, -1.0f); break;
+        case 1: ok = model_linear(m, (float)in.E, (float)in.fail_stress); break;
+        case 2: ok = model_bilinear(m, (float)in.E, (float)in.plastic_mod, (float)in.yield_stress, (float)in.fail_stress); break;
+        case 3: {
+            std::vector<float> e(in.n_data), s(in.n_data);
+            for (int i = 0; i < in.n_data; i++) e[i] = (float)in.strain_data[i], s[i] = (float)in.stress_data[i];
+            ok = model_data(m, in.n_data, e.data(), s.data());
+            break;
+        }
+    }
+    if (!ok) m = MatModel();  // the setter failed: the material keeps addMaterial's default model
+    return m;
+}
 
 float ehat(float E, float nu) { return E / ((1 - 2 * nu) * (1 + nu)); }
 
 // CVX_Sim::CopyMat + Import damping + EnableVolumeEffects + CVX_MaterialVoxel::updateDerived
 HostVMat import_material(const vx3g_material &in, const vx3g_robot_desc &r) {
     HostVMat m{};
-    m.E = (float)in.E;
-    m.sigma_fail = in.model == 1 ? (float)in.fail_stress : -1.0f;
+    m.model = material_model(in);
+    m.E = m.model.E;
+    m.sigma_fail = m.model.sigma_fail;
     float nu = (float)in.nu;
     if (nu < 0) nu = 0;
     if (nu >= 0.5) nu = 0.5 - FLT_EPSILON * 2;
@@ -107,15 +129,23 @@ VMat to_vmat(const HostVMat &m, const vx3g_material &in) {
     return v;
 }
 
-LMat combine(const HostVMat &v1, const HostVMat &v2) {
+LMat combine(const HostVMat &v1, const HostVMat &v2, std::vector<float2> &pts) {
     LMat l{};
-    float f1 = v1.sigma_fail, f2 = v2.sigma_fail, failS;
-    if (f1 == -1.0f) failS = f2;
-    else if (f2 == -1.0f) failS = f1;
-    else failS = f1 < f2 ? f1 : f2;
-    float E = 2.0f * v1.E * v2.E / (v1.E + v2.E);
+    const MatModel lm = model_link(v1.model, v2.model);
+    const float E = lm.E;
     l.E = E;
-    l.eps_fail = (failS == -1.0f) ? -1.0f : failS / E;
+    l.eps_fail = lm.eps_fail;
+    l.lin = lm.linear ? 1 : 0;
+    l.ssn = (int)lm.strain.size() + 1;
+    l.sso = 0;
+    if (!lm.linear) {
+        // the data points of the curve as the reference's device copy holds them:
+        // VX3_Material::syncVectors (VX3_Material.cu:463-481) puts one more (0,0) in front,
+        // which the stress function's segment tests then see
+        l.sso = (int)pts.size();
+        pts.push_back(make_float2(0.0f, 0.0f));
+        for (size_t i = 0; i < lm.strain.size(); i++) pts.push_back(make_float2(lm.strain[i], lm.stress[i]));
+    }
     float nu;
     if (v1.nu == 0 && v2.nu == 0) {
         nu = 0;
@@ -202,6 +232,7 @@ struct vx3g_ctx {
     bool any_detach = false;  // some robot has EnableDetach
     bool any_remove = false;  // some robot removes voxels (SecondaryExperiment)
     bool any_dyn = false;     // some robot's surface follows its link table (detach or removal)
+    bool any_nonlinear = false;  // some material has a non-linear stress-strain model
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -334,6 +365,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     std::vector<double4> cil_h;
     std::vector<double> cil_on_h;
     std::vector<double> rm_h;  // per voxel: removal time (+inf: never)
+    std::vector<float2> ss_h;  // stress-strain points of the non-linear link materials
     c->voff.assign(c->nr + 1, 0);
     c->loff.assign(c->nr + 1, 0);
 
@@ -350,11 +382,16 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         double cte_max = 0;
         for (int i = 0; i < R.n_materials; i++) {
             const vx3g_material &in = R.materials[i];
-            if (in.model != 0 && in.model != 1)
-                return fail(VX3G_ERR_UNSUPPORTED, "only linear material models (MatModel 0/1) are supported");
-            if (in.model == 1 && !(in.fail_stress > 0)) return fail(VX3G_ERR_INVALID, "fail_stress must be positive");
-            if (!(in.E > 0)) return fail(VX3G_ERR_INVALID, "Young's modulus must be positive");
+            if (in.model < 0 || in.model > 3)
+                return fail(VX3G_ERR_UNSUPPORTED, "material model (MatModel) must be 0, 1, 2 or 3");
+            if (in.model == 3 && (in.n_data < 0 || in.n_data > VX3G_MAX_MODEL_POINTS ||
+                                  (in.n_data > 0 && (!in.strain_data || !in.stress_data))))
+                return fail(VX3G_ERR_INVALID, "MatModel 3 needs 0.." + std::to_string(VX3G_MAX_MODEL_POINTS) +
+                                                  " stress-strain points and both arrays");
+            if (R.log10E && in.model > 1)
+                return fail(VX3G_ERR_UNSUPPORTED, "per-voxel moduli (log10E) need linear material models");
             hm[i] = import_material(in, R);
+            if (!hm[i].model.linear) c->any_nonlinear = true;
             if (!R.log10E) vmats.push_back(to_vmat(hm[i], in));
             cte_max = std::fmax(cte_max, std::fabs((double)hm[i].cte));
         }
@@ -422,7 +459,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
                 int lm;
                 if (R.log10E) {  // one link material per link
                     lm = (int)lmats.size() - lbase;
-                    lmats.push_back(orient(combine(hv[vp - v0], hv[vn - v0]), hv[vn - v0], hv[vp - v0],
+                    lmats.push_back(orient(combine(hv[vp - v0], hv[vn - v0], ss_h), hv[vn - v0], hv[vp - v0],
                                            R.materials[mn].fixed, R.materials[mp].fixed));
                 } else {
                     // the combined constants come from the pair's first use (vox1 = the new voxel);
@@ -431,7 +468,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
                     if (base < 0) {
                         base = (int)pair_vals.size();
                         pair_lmat[mn * R.n_materials + mp] = base;
-                        pair_vals.push_back(combine(hm[mp], hm[mn]));
+                        pair_vals.push_back(combine(hm[mp], hm[mn], ss_h));
                     }
                     int &ori = ori_lmat[mn * R.n_materials + mp];
                     if (ori < 0) {
@@ -591,6 +628,13 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     if ((rc = c->alloc(&ls, 9 * (size_t)d.nl * rsz)) || (rc = c->alloc(&sl, 6 * (size_t)d.nv * 6 * rsz))) return rc;
     d.lstate = ls;
     d.slots = sl;
+    d.soff = nullptr;
+    d.ss = nullptr;
+    if (!ss_h.empty()) {  // non-linear link materials: their curves and a plastic strain offset per link
+        float2 *dss;
+        if ((rc = c->upload(&dss, ss_h)) || (rc = c->alloc(&d.soff, d.nl))) return rc;
+        d.ss = dss;
+    }
     RobotP *drp;
     VMat *dvm;
     LMat *dlm;
@@ -1418,6 +1462,8 @@ int vx3g_record(vx3g_ctx *c, int n, int k) {
     if (c->ff_pos)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a force field that reads the voxel position is not implemented");
     if (c->any_cilia) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of cilia forces is not implemented");
+    if (c->any_nonlinear)
+        return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of non-linear material models is not implemented");
     if (c->any_detach || c->any_remove)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a changing link table (detach, removal) is not implemented");
     CU(cudaSetDevice(c->device));

@@ -59,6 +59,8 @@ struct LMat {  // one link material (global index), oriented: (negative end, pos
     float area, tss;  // transverse area / strain sum frozen at link creation
     float dmcN, dmcP; // the ends' dampingMultiplier numerators 2*sqrt(m)*zetaInternal (VMat.dmc)
     int fixN, fixP;   // the ends' materials are Fixed
+    int lin;          // 1: linear model (VX3_Material::linear); 0: data points d.ss[sso .. sso+ssn)
+    int ssn, sso;     // stress-strain points of a non-linear model: (0,0), then the model's from (0,0) on
 };
 
 struct RobotP {
@@ -123,6 +125,8 @@ struct Dev {
     uint2 *linfo;
     void *lstate;   // 9*NL of R, component-major
     float2 *strain;
+    float *soff;    // per link: strainOffset of a non-linear link material (VX3_Link.cu:231-258), or NULL
+    const float2 *ss;  // stress-strain points {strain, stress} of the non-linear link materials
     void *slots;    // 6*NV Slot<R>
     // robots
     const RobotP *rp;

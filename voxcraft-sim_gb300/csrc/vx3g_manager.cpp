@@ -164,6 +164,7 @@ struct RobotSpec {
     std::vector<double> phase;
     std::vector<double> cilia_base, cilia_shift;  // 3 per cell, or empty
     std::vector<vx3g_material> mats;
+    std::vector<std::vector<double>> ss_strain, ss_stress;  // SSData points per material (mats[i] points here)
     std::vector<int> mat_rgba;  // 4 ints per material
     vx3g_robot_desc desc{};
     const Node *stop = nullptr, *fitness = nullptr;
@@ -249,10 +250,32 @@ void read_spec(RobotSpec &S) {
             const Node *mech = m->child("Mechanical");
             vx3g_material M{};
             int model = mech ? vx3g::xml::get_int(mech, "MatModel", 0) : 0;
-            if (model != 0 && model != 1) throw std::runtime_error(S.filename + ": MatModel " + std::to_string(model) + " is not supported");
+            if (model < 0 || model > 3) throw std::runtime_error(S.filename + ": MatModel " + std::to_string(model) + " is not supported");
             M.model = model;
             M.E = vx3g::xml::get_double(mech, "Elastic_Mod", 0.0);
             M.fail_stress = vx3g::xml::get_double(mech, "Fail_Stress", 0.0);
+            M.plastic_mod = vx3g::xml::get_double(mech, "Plastic_Mod", 0.0);  // VX_Object.cpp:1439-1440
+            M.yield_stress = vx3g::xml::get_double(mech, "Yield_Stress", 0.0);
+            // <SSData><NumDataPts/><StrainData><Strain/>...</StrainData><StressData>...</StressData></SSData>
+            // (VX_Object.cpp:1397-1418): the first NumDataPts values of each list
+            std::vector<double> se, ss;
+            if (const Node *sd = mech ? mech->child("SSData") : nullptr) {
+                const int n = vx3g::xml::get_int(sd, "NumDataPts", 0);
+                auto values = [&](const char *list, const char *item, std::vector<double> &dst) {
+                    if (const Node *ln = sd->child(list))
+                        for (const Node *v : ln->all(item))
+                            if ((int)dst.size() < n) dst.push_back(std::atof(v->text.c_str()));
+                };
+                values("StrainData", "Strain", se);
+                values("StressData", "Stress", ss);
+                if ((int)se.size() != n || (int)ss.size() != n)
+                    throw std::runtime_error(S.filename + ": SSData holds fewer points than NumDataPts");
+                if (n > VX3G_MAX_MODEL_POINTS)
+                    throw std::runtime_error(S.filename + ": SSData holds more than " +
+                                             std::to_string(VX3G_MAX_MODEL_POINTS) + " points");
+            }
+            S.ss_strain.push_back(se);
+            S.ss_stress.push_back(ss);
             M.rho = vx3g::xml::get_double(mech, "Density", 0.0);
             M.nu = vx3g::xml::get_double(mech, "Poissons_Ratio", 0.0);
             M.cte = vx3g::xml::get_double(mech, "CTE", 0.0);
@@ -268,6 +291,11 @@ void read_spec(RobotSpec &S) {
             const Node *disp = m->child("Display");
             for (const char *c : {"Red", "Green", "Blue", "Alpha"})
                 S.mat_rgba.push_back((int)(vx3g::xml::get_double(disp, c, std::strcmp(c, "Alpha") ? 0.5 : 1.0) * 255));
+        }
+        for (size_t i = 0; i < S.mats.size(); i++) {  // the SSData arrays live in S
+            S.mats[i].n_data = (int)S.ss_strain[i].size();
+            S.mats[i].strain_data = S.ss_strain[i].empty() ? nullptr : S.ss_strain[i].data();
+            S.mats[i].stress_data = S.ss_stress[i].empty() ? nullptr : S.ss_stress[i].data();
         }
     }
     const Node *st = vxc->child("Structure");

@@ -50,19 +50,18 @@ __device__ __forceinline__ float df_diff3(float ah, float al, float bh, float bl
     return s2 + (e2 + (e + ((al - bl) - cl)));
 }
 
-// Rotation vector of a unit quaternion, v * 2*atan2(|v|, w)/|v|.  For the small
-// rotations most links carry (|v|/w < 0.01) the factor is (2/w) * atan(x)/x with
-// x = |v|/w, taken from the Maclaurin series of arctan, atan(x)/x = 1 - x^2/3 + x^4/5
-// - ..., whose first omitted term (x^6/7 < 1.5e-13) is far below FP32 rounding; this
-// needs neither the square root nor the arctangent.
+// ToRotationVector (src/VX3/VX3_Quat3D.h:347-359) of a unit quaternion (w, v) in FP32.
+// The reference takes 1 - w^2 as the squared sine of the half angle and, below
+// 2.4e-3 (rotations under about 0.098 rad), does not evaluate the rotation vector
+// 2*acos(w)/sin(theta/2) * v but the approximation 2*sqrt((2 - 2w)/(1 - w^2)) * v =
+// 2*sqrt(2/(1 + w)) * v, which is smaller by about theta^2/96 relative: 2.6e-5 at
+// 0.05 rad, far above FP32 rounding, in every link's bending and torsion terms.  The
+// same two branches are taken here, with 1 - w^2 formed as |v|^2 (no cancellation)
+// and acos(w)/sin as atan2(|v|, w)/|v|.
 __device__ __forceinline__ V3<float> rotvec_f(float w, V3<float> v) {
     const float s2 = v.x * v.x + v.y * v.y + v.z * v.z;
     if (!(s2 > 0.0f)) return V3<float>{0, 0, 0};
-    if (w > 0.0f && s2 < 1e-4f * (w * w)) {
-        const float iw = __frcp_rn(w);  // = 1.0f / w (both correctly rounded)
-        const float x2 = s2 * (iw * iw);
-        return scl(v, 2.0f * iw * (1.0f - x2 * (1.0f / 3.0f - x2 * 0.2f)));
-    }
+    if (s2 < 2.4e-3f) return scl(v, 2.0f * sqrtf(2.0f / (1.0f + w)));
     const float s = sqrtf(s2);
     return scl(v, 2.0f * atan2f(s, w) / s);
 }
@@ -268,17 +267,13 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     const V3<float> dA2 = scl(sub(a2v, oldA2), 0.5f);
     const float axialStrain = pos2.x / L;
     sm.x = axialStrain;
-    if (axialStrain > sm.y) sm.y = axialStrain;
+    const float stress = link_stress(d, m, l, axialStrain, &sm.y);  // updateStrain (VX3_Link.cu:220-260)
     d.strain[l] = sm;
     if (axialStrain > 100) atomicOr(&d.status[r], 1);
 
     Slot<float> *S = (Slot<float> *)d.slots;
     Slot<float> *sNeg = &S[(size_t)(2 * axis) * d.nv + e.x];
     Slot<float> *sPos = &S[(size_t)(2 * axis + 1) * d.nv + e.y];
-    float stress;
-    if (m.eps_fail != -1.0f && axialStrain > m.eps_fail) stress = 0.0f;
-    else if (m.nu == 0.0f) stress = m.E * axialStrain;
-    else stress = m.eHat * ((1 - m.nu) * axialStrain + m.nu * m.tss);
     uint32_t nfl = (fl & ~(LF_SMALL | LF_LVV)) | (small ? LF_SMALL : 0u);
     if (m.eps_fail != -1.0f && sm.y > m.eps_fail) {
         const V3<float> z{0, 0, 0};
@@ -332,11 +327,19 @@ __device__ __forceinline__ void base_size_df(const VMat &m, float te, float &hi,
 }
 
 // temperature at time t (gpu_update_temperature, VX3_VoxelyzeKernel.cu:625-650): the phase
-// 2*3.1415926f*(t/P + phase) reduced to cycles in FP64, the sine in FP32
+// 2*3.1415926f*(t/P + phase) reduced to cycles c in FP64 and split into c_hi + c_lo
+// (two floats); sin(2 pi c) = sin(2 pi c_hi) + 2 pi c_lo cos(2 pi c_hi), the second
+// term dropping (2 pi c_lo)^2 / 2 < 1e-13.  The FP32 sine alone would carry the
+// rounding of c (up to 3.7e-7 rad of phase); with the correction the temperature is
+// within about one FP32 rounding of the FP64 step's.
 __device__ __forceinline__ float temperature_f(const RobotP &rp, double phase, double t) {
     double c = (t * rp.inv_period + phase) * ((double)(2 * 3.1415926f) * (1.0 / 6.283185307179586));
     c -= floor(c);
-    float T = (float)rp.temp_amp * sinpif(2.0f * (float)c);
+    const float ch = (float)c;
+    const float cl = (float)(c - (double)ch);
+    float sn, cs;
+    sincospif(2.0f * ch, &sn, &cs);
+    float T = (float)rp.temp_amp * fmaf(6.28318531f * cl, cs, sn);
     if (!rp.expansion && T > 0) T = 0;
     return T;
 }

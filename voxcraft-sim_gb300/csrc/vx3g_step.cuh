@@ -216,6 +216,56 @@ __device__ inline V3<double> force_field(const Dev &d, const RobotP &rp, double 
                       rp.ff[2] >= 0 ? math_eval(d.ftok + rp.ff[2], x, y, z, t, nv) : 0.0};
 }
 
+// ------------------------------------------------------------- link material models
+// VX3_Material::stress (src/VX3/VX3_Material.cu:90-124) of link material m at strain eps:
+// zero past failure; the linear law for linear models, in compression and on the first
+// segment (or when forced); else the segment of the data points holding eps (the last
+// one extrapolated), with the volumetric variant when Poisson's ratio is on.  The data
+// points are read only on a non-linear segment.
+__device__ __forceinline__ float model_stress(const LMat &m, const float2 *pts, float eps, float tss, bool force_linear) {
+    if (m.eps_fail != -1.0f && eps > m.eps_fail) return 0.0f;
+    if (m.lin || force_linear || eps <= pts[1].x) {
+        if (m.nu == 0.0f) return m.E * eps;
+        return m.eHat * ((1 - m.nu) * eps + m.nu * tss);
+    }
+    for (int i = 2; i < m.ssn; i++) {
+        const float2 a = pts[i - 1], b = pts[i];
+        if (eps <= b.x || i == m.ssn - 1) {
+            const float perc = (eps - a.x) / (b.x - a.x);
+            const float basic = a.y + perc * (b.y - a.y);
+            if (m.nu == 0.0f) return basic;
+            const float modulus = (b.y - a.y) / (b.x - a.x);
+            const float mod_hat = modulus / ((1 - 2 * m.nu) * (1 + m.nu));
+            const float eff = basic / modulus;  // strain where the segment's line from 0 reaches the stress
+            const float eff_tss = tss * (eff / eps);
+            return mod_hat * ((1 - m.nu) * eff + m.nu * eff_tss);
+        }
+    }
+    return 0.0f;
+}
+
+// VX3_Link::updateStrain (src/VX3/VX3_Link.cu:220-260): the link's stress at axial strain
+// eps, with maxStrain (*max_strain) and, for non-linear materials, the plastic
+// strainOffset (d.soff[l]): on new ground the curve is followed and the offset of the
+// unloading line recorded; below the largest strain reached the material unloads
+// linearly from that offset.
+__device__ __forceinline__ float link_stress(const Dev &d, const LMat &m, int l, float eps, float *max_strain) {
+    if (m.lin) {
+        if (eps > *max_strain) *max_strain = eps;
+        return model_stress(m, nullptr, eps, m.tss, false);
+    }
+    const float2 *pts = d.ss + m.sso;
+    if (eps > *max_strain) {
+        *max_strain = eps;
+        const float st = model_stress(m, pts, eps, m.tss, false);
+        d.soff[l] = m.nu != 0.0f ? *max_strain - model_stress(m, pts, eps, 0.0f, false) / (m.eHat * (1 - m.nu))
+                                 : *max_strain - st / m.E;
+        return st;
+    }
+    const float rel = eps - d.soff[l];
+    return m.nu != 0.0f ? model_stress(m, pts, rel, m.tss, true) : m.E * rel;
+}
+
 // ------------------------------------------------------------- link pass
 template <class R> __device__ __forceinline__ void link_update(const Dev &d, int l) {
     const uint2 li = d.linfo[l];
@@ -275,18 +325,13 @@ template <class R> __device__ __forceinline__ void link_update(const Dev &d, int
     const float axialStrain = (float)(pos2.x / restR);
     float2 sm = d.strain[l];
     sm.x = axialStrain;
-    if (axialStrain > sm.y) sm.y = axialStrain;
+    const float stress = link_stress(d, m, l, axialStrain, &sm.y);
     d.strain[l] = sm;
     if (axialStrain > 100) atomicOr(&d.status[r], 1);  // divergence (VX3_VoxelyzeKernel.cu:271-281)
 
     Slot<R> *S = (Slot<R> *)d.slots;
     Slot<R> *sNeg = &S[(size_t)(2 * axis) * d.nv + e.x];
     Slot<R> *sPos = &S[(size_t)(2 * axis + 1) * d.nv + e.y];
-    // VX3_Material::stress linear branch (VX3_Material.cu:90-101)
-    float stress;
-    if (m.eps_fail != -1.0f && axialStrain > m.eps_fail) stress = 0.0f;
-    else if (m.nu == 0.0f) stress = m.E * axialStrain;
-    else stress = m.eHat * ((1 - m.nu) * axialStrain + m.nu * m.tss);
     uint32_t nfl = (fl & ~(LF_SMALL | LF_LVV)) | (small ? LF_SMALL : 0u);
     if (m.eps_fail != -1.0f && sm.y > m.eps_fail) {  // isFailed: forces zero (lvv unchanged)
         const V3<R> z{0, 0, 0};

@@ -37,6 +37,25 @@ class Material:
     cilia_on_after: float = 0.0  # TurnOnCiliaAfterThisManySeconds
     remove_after: float = 0.0  # RemoveFromSimulationAfterThisManySeconds (SecondaryExperiment; 0: never)
     name: str = "mat"
+    model: Optional[int] = None  # MatModel (0 linear, 1 linear+failure, 2 bilinear, 3 data points);
+                                 # None: 0 without fail_stress, 1 with
+    plastic_mod: float = 0.0   # Plastic_Mod (MatModel 2)
+    yield_stress: float = 0.0  # Yield_Stress (MatModel 2)
+    ss_strain: Optional[tuple] = None  # SSData strain points (MatModel 3), (0, 0) first as in a VXA
+    ss_stress: Optional[tuple] = None  # SSData stress points (MatModel 3)
+
+    def mat_model(self) -> int:
+        if self.model is not None:
+            return int(self.model)
+        return 0 if self.fail_stress == 0 else 1
+
+    def ss_arrays(self):
+        """(n, strain float64 array, stress float64 array) of the SSData points, or (0, None, None)."""
+        if self.mat_model() != 3 or self.ss_strain is None:
+            return 0, None, None
+        e = np.ascontiguousarray(self.ss_strain, np.float64)
+        s = np.ascontiguousarray(self.ss_stress, np.float64)
+        return len(e), e, s
 
 
 @dataclasses.dataclass
@@ -233,6 +252,16 @@ def to_vxd(r: Robot) -> str:
     return "<VXD>\n" + structure_xml(r, replace="VXA.VXC.Structure") + "\n</VXD>\n"
 
 
+def _ss_xml(m: Material) -> str:
+    """<SSData> of a MatModel 3 material (src/VXA/VX_Object.cpp:1397-1418)."""
+    n, e, s = m.ss_arrays()
+    if not n:
+        return ""
+    return (f"<SSData><NumDataPts>{n}</NumDataPts><StrainData>" + "".join(f"<Strain>{_fmt(x)}</Strain>" for x in e)
+            + "</StrainData><StressData>" + "".join(f"<Stress>{_fmt(x)}</Stress>" for x in s)
+            + "</StressData></SSData>")
+
+
 def to_vxa(r: Robot) -> str:
     """Serialise a Robot as a self-contained VXA document."""
     g, ph = r.padded()
@@ -281,8 +310,10 @@ def to_vxa(r: Robot) -> str:
             f'<Material ID="{i + 1}"><Name>{m.name}{i + 1}</Name>'
             "<Display><Red>0.5</Red><Green>0.5</Green><Blue>0.5</Blue><Alpha>1</Alpha></Display>"
             "<Mechanical>"
-            f"<MatModel>{0 if m.fail_stress == 0 else 1}</MatModel>"
+            f"<MatModel>{m.mat_model()}</MatModel>"
+            + _ss_xml(m) +
             f"<Elastic_Mod>{_fmt(m.E)}</Elastic_Mod><Fail_Stress>{_fmt(m.fail_stress)}</Fail_Stress>"
+            f"<Plastic_Mod>{_fmt(m.plastic_mod)}</Plastic_Mod><Yield_Stress>{_fmt(m.yield_stress)}</Yield_Stress>"
             f"<Density>{_fmt(m.rho)}</Density><Poissons_Ratio>{_fmt(m.nu)}</Poissons_Ratio>"
             f"<CTE>{_fmt(m.cte)}</CTE><MaterialTempPhase>0</MaterialTempPhase>"
             f"<Cilia>{_fmt(m.cilia)}</Cilia><TurnOnCiliaAfterThisManySeconds>{_fmt(m.cilia_on_after)}"
