@@ -99,6 +99,24 @@ typedef struct vx3g_math_token {
 } vx3g_math_token;
 #define VX3G_MAX_MATH_TOKENS 256
 
+/* One boundary-condition region of the VXA <Environment><Boundary_Conditions>
+ * (CVX_FRegion, src/old/VX_FRegion.cpp:165-219).  Every voxel the region touches
+ * gets an external (VX3_External): the fixed degrees of freedom held at their
+ * prescribed displacement, and an equal share of the region's force and torque
+ * (CVX_Sim::Import, src/VXA/VX_Sim.cpp:109-141). */
+typedef struct vx3g_bc_region {
+    int prim;            /* PrimType: 0 box, 1 cylinder, 2 sphere (3, a mesh, -> VX3G_ERR_UNSUPPORTED) */
+    int dof_fixed;       /* DofFixed: 1 X, 2 Y, 4 Z translation, 8 X, 16 Y, 32 Z rotation */
+    float x, y, z;       /* X, Y, Z: the region's corner (box, cylinder) or centre (sphere) in
+                            fractions of the workspace (the lattice's extent) */
+    float dx, dy, dz;    /* dX, dY, dZ: box size; cylinder length along its one non-zero axis */
+    float radius;        /* Radius (sphere, cylinder), in fractions of the workspace's largest side */
+    double force[3];     /* ForceX..Z (N), divided equally among the voxels it touches */
+    double torque[3];    /* TorqueX..Z (N m), likewise */
+    double displace[3];  /* DisplaceX..Z (m): translation of the fixed translational DOFs */
+    double ang_displace[3]; /* AngDisplaceX..Z (rad): rotation vector of the fixed rotational DOFs */
+} vx3g_bc_region;
+
 /* One simulation: the content of a merged VXA document. */
 typedef struct vx3g_robot_desc {
     int nx, ny, nz;                 /* X_Voxels, Y_Voxels, Z_Voxels */
@@ -140,6 +158,9 @@ typedef struct vx3g_robot_desc {
                                        candidates, and keeps counting toward the centre of mass; the
                                        initial-position reset of the same block is the caller's (it
                                        touches only the report) */
+    int n_bcs;                      /* Environment/Boundary_Conditions regions, applied in order */
+    const vx3g_bc_region *bcs;      /* (the lattice's cells are vox_size cubes: Lattice_Dim with all
+                                       dimension adjustments 1 and no line or layer offsets) */
 } vx3g_robot_desc;
 
 typedef struct vx3g_batch_desc {

@@ -411,6 +411,40 @@ static void lmat_make(lmat *l, const vmat *v1, const vmat *v2, int i1, int i2) {
     l->sqB3xIp = sqrtf(l->b3 * L * L / 6.0f);
 }
 
+/* ------------------------------------------------- boundary conditions */
+/* A voxel's external (VX3_External): fixed DOFs with translation and rotation,
+ * force and moment. */
+typedef struct {
+    int any, dof;
+    float f[3], m[3];
+    double t[3], r[3];
+    quat q;
+} vext;
+
+/* CP_Box / CP_Cylinder / CP_Sphere ::IsTouching(P, Dist, Envelope) (src/old/VX_FRegion.cpp:395-605),
+ * with Dist the half-cell vector: region coordinates in float, the rest in double */
+static int bc_touch(const vxo_bc_region *b, const double P[3], const double D[3], const double W[3]) {
+    if (b->prim == 0) {
+        float hx = b->x + b->dx, hy = b->y + b->dy, hz = b->z + b->dz;
+        double px = P[0] / W[0], py = P[1] / W[1], pz = P[2] / W[2];
+        double dx = D[0] / W[0], dy = D[1] / W[1], dz = D[2] / W[2];
+        return px + dx > b->x && px - dx < hx && py + dy > b->y && py - dy < hy && pz + dz > b->z && pz - dz < hz;
+    }
+    double wm = W[0] > W[1] ? W[0] : W[1];
+    if (W[2] > wm) wm = W[2];
+    double cx = b->x * W[0], cy = b->y * W[1], cz = b->z * W[2];
+    double rad = b->radius * wm;
+    if (b->prim == 2) {
+        double dist = sqrt(D[0] * D[0] + D[1] * D[1] + D[2] * D[2]);
+        return sqrt((P[0] - cx) * (P[0] - cx) + (P[1] - cy) * (P[1] - cy) + (P[2] - cz) * (P[2] - cz)) < rad + dist;
+    }
+    double sx = b->dx * W[0], sy = b->dy * W[1], sz = b->dz * W[2];
+    if (b->dx != 0) return P[0] > cx && P[0] < cx + sx && sqrt((P[1] - cy) * (P[1] - cy) + (P[2] - cz) * (P[2] - cz)) < rad;
+    if (b->dy != 0) return P[1] > cy && P[1] < cy + sy && sqrt((P[0] - cx) * (P[0] - cx) + (P[2] - cz) * (P[2] - cz)) < rad;
+    if (b->dz != 0) return P[2] > cz && P[2] < cz + sz && sqrt((P[0] - cx) * (P[0] - cx) + (P[1] - cy) * (P[1] - cy)) < rad;
+    return 0;
+}
+
 /* ---------------------------------------------------------------- state */
 enum { F_SURFACE = 1 << 1, F_FLOOR = 1 << 2, F_STATIC = 1 << 3 };
 enum { L_LVV = 1 };
@@ -452,6 +486,7 @@ typedef struct {
     vxo_math_token *ff[3]; /* force-field programs (copies) or NULL */
     vec *cilia_base;       /* per voxel: BaseCiliaForce + 0 * ShiftCiliaForce (the signal stays 0), or NULL */
     int *mat_removed;      /* per material: removeVoxels has removed it (VX3_MaterialVoxel::removed) */
+    vext *ext;             /* per voxel: boundary-condition externals, or NULL without regions */
 } sim;
 
 /* VX3_MathTree::eval (src/Utils/VX3_MathTree.h:50-191): tokens in order, each result
@@ -603,6 +638,48 @@ void *vxo_create(const vxo_robot *r) {
         }
     }
     free(vid);
+    /* boundary conditions (CVX_Sim::Import, src/VXA/VX_Sim.cpp:109-141): regions counted on
+     * the GetXYZ cell centres (1e-6 lattice units further in x and y), applied to each voxel
+     * touched at its position plus half a cell, in voxel then region order */
+    S->r.bcs = NULL;
+    if (r->n_bcs > 0) {
+        double vs = r->vox_size;
+        double W[3] = {vs * (double)nx, vs * (double)ny, vs * (double)nz}, H[3] = {0.5 * vs, 0.5 * vs, 0.5 * vs};
+        int *size = (int *)calloc((size_t)r->n_bcs, sizeof(int));
+        for (int j = 0; j < r->n_bcs; j++)
+            for (int i = 0; i < S->nv; i++) {
+                const voxel *v = &S->v[i];
+                double P[3] = {vs * ((0.5 + v->ix) + 1e-6), vs * ((0.5 + v->iy) + 1e-6), vs * (0.5 + v->iz)};
+                if (bc_touch(&r->bcs[j], P, H, W)) size[j]++;
+            }
+        S->ext = (vext *)calloc(S->nv ? S->nv : 1, sizeof(vext));
+        for (int i = 0; i < S->nv; i++) {
+            const voxel *v = &S->v[i];
+            vext *e = &S->ext[i];
+            e->q = qident();
+            double P[3] = {v->ix * vs + H[0], v->iy * vs + H[1], v->iz * vs + H[2]};
+            for (int j = 0; j < r->n_bcs; j++) {
+                const vxo_bc_region *b = &r->bcs[j];
+                if (!bc_touch(b, P, H, W)) continue;
+                e->any = 1;
+                for (int k = 0; k < 6; k++) { /* CVX_External::setDisplacement */
+                    if (!(b->dof_fixed & (1 << k))) continue;
+                    e->dof |= 1 << k;
+                    double d = k < 3 ? b->displace[k] : b->ang_displace[k - 3];
+                    if (d != 0.0f) { if (k < 3) e->t[k] = d; else e->r[k - 3] = d; }
+                }
+                double inv = 1.0 / (double)size[j];
+                for (int k = 0; k < 3; k++) { /* addForce(force() + Force/Size): float sums */
+                    float fa = (float)((double)e->f[k] + inv * b->force[k]);
+                    float ma = (float)((double)e->m[k] + inv * b->torque[k]);
+                    e->f[k] += fa;
+                    e->m[k] += ma;
+                }
+            }
+            if (e->r[0] != 0.0 || e->r[1] != 0.0 || e->r[2] != 0.0) e->q = q_from_rotvec(V(e->r[0], e->r[1], e->r[2]));
+        }
+        free(size);
+    }
     for (int i = 0; i < S->nl; i++) update_rest(S, &S->l[i]);
     S->surf = (int *)malloc(sizeof(int) * (S->nv ? S->nv : 1));
     S->last_contact = (double *)calloc(3 * (size_t)(S->nv ? S->nv : 1), sizeof(double));
@@ -621,7 +698,7 @@ void vxo_destroy(void *h) {
     sim *S = (sim *)h;
     if (!S) return;
     free(S->vm); free(S->lm); free(S->v); free(S->l); free(S->surf); free(S->last_contact);
-    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]); free(S->cilia_base); free(S->mat_removed);
+    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]); free(S->cilia_base); free(S->mat_removed); free(S->ext);
     free(S);
 }
 
@@ -757,6 +834,14 @@ static void voxel_update(sim *S, voxel *v, float dtf) {
     double dt = dtf;
     v->prevDt = (float)dt;
     if (dt == 0.0f) return;
+    const vext *ex = S->ext && S->ext[v - S->v].any ? &S->ext[v - S->v] : NULL;
+    if (ex && ex->dof == 0x3F) { /* isFixedAll (VX3_Voxel.cu:167-173) */
+        double s = m->nom_size;
+        v->pos = V(v->ix * s + ex->t[0], v->iy * s + ex->t[1], v->iz * s + ex->t[2]);
+        v->orient = ex->q;
+        v->linMom = v->angMom = V(0, 0, 0);
+        return;
+    }
     /* force() */
     vec F = V(0, 0, 0);
     for (int i = 0; i < 6; i++) {
@@ -765,6 +850,7 @@ static void voxel_update(sim *S, voxel *v, float dtf) {
         F = vadd(F, (i % 2 == 1) ? L->fPos : L->fNeg);
     }
     F = qrot(v->orient, F);
+    if (ex) F = vadd(F, V(ex->f[0], ex->f[1], ex->f[2])); /* external force (VX3_Voxel.cu:363-364) */
     vec vel = vscale(v->linMom, m->mass_inv);
     F = vsub(F, vscale(vel, m->z_glob * m->c2xSqMxExS));
     F.z += -m->mass * 9.80665f * m->grav_mult;
@@ -806,10 +892,29 @@ static void voxel_update(sim *S, voxel *v, float dtf) {
         M = vadd(M, (i % 2 == 1) ? L->mPos : L->mNeg);
     }
     M = qrot(v->orient, M);
+    if (ex) M = vadd(M, V(ex->m[0], ex->m[1], ex->m[2])); /* external moment (:393-394) */
     vec angVel = vscale(v->angMom, m->mom_inertia_inv);
     M = vsub(M, vscale(angVel, m->z_glob * m->c2xSqIxExSxSxS));
     v->angMom = vadd(v->angMom, vscale(M, dt));
     v->orient = qmul(q_from_rotvec(vscale(v->angMom, dt * m->mom_inertia_inv)), v->orient);
+    if (ex) { /* fixed DOFs (VX3_Voxel.cu:222-257) */
+        double s = m->nom_size;
+        if (ex->dof & 1) { v->pos.x = v->ix * s + ex->t[0]; v->linMom.x = 0; }
+        if (ex->dof & 2) { v->pos.y = v->iy * s + ex->t[1]; v->linMom.y = 0; }
+        if (ex->dof & 4) { v->pos.z = v->iz * s + ex->t[2]; v->linMom.z = 0; }
+        if (ex->dof & 0x38) {
+            if ((ex->dof & 0x38) == 0x38) {
+                v->orient = ex->q;
+                v->angMom = V(0, 0, 0);
+            } else {
+                vec rv = q_to_rotvec(v->orient);
+                if (ex->dof & 8) { rv.x = 0; v->angMom.x = 0; }
+                if (ex->dof & 16) { rv.y = 0; v->angMom.y = 0; }
+                if (ex->dof & 32) { rv.z = 0; v->angMom.z = 0; }
+                v->orient = q_from_rotvec(rv);
+            }
+        }
+    }
     if ((v->flags & F_FLOOR) && floor_pen(S, v) >= 0) {
         if (v->flags & F_STATIC) v->angMom = V(0, 0, 0);
     }

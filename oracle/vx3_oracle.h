@@ -37,6 +37,15 @@ typedef struct vxo_math_token {
     double value;
 } vxo_math_token;
 
+/* A boundary-condition region (CVX_FRegion): PrimType 0 box, 1 cylinder, 2 sphere;
+ * DofFixed bits 1,2,4 translation x,y,z and 8,16,32 rotation x,y,z; coordinates in
+ * fractions of the workspace (floats, as the reference keeps them). */
+typedef struct vxo_bc_region {
+    int prim, dof_fixed;
+    float x, y, z, dx, dy, dz, radius;
+    double force[3], torque[3], displace[3], ang_displace[3];
+} vxo_bc_region;
+
 /* One simulation (one merged VXA). */
 typedef struct vxo_robot {
     int nx, ny, nz;
@@ -54,6 +63,8 @@ typedef struct vxo_robot {
     const double *cilia_base, *cilia_shift; /* nx*ny*nz*3 Base/ShiftCiliaForce per cell, or NULL */
     int enable_detach;                    /* Simulator/AttachDetach/EnableDetach */
     int secondary_experiment;             /* Simulator/SecondaryExperiment: material removal */
+    int n_bcs;                            /* Environment/Boundary_Conditions regions */
+    const vxo_bc_region *bcs;
 } vxo_robot;
 
 void *vxo_create(const vxo_robot *r);

@@ -14,6 +14,7 @@ The reference produces no golden vectors of its own for this path, so these
 files are what pins the oracle and, through it, the GB300 kernels.
 """
 
+import dataclasses
 import json
 import os
 import sys
@@ -133,6 +134,28 @@ def cases():
         wl.bernoulli_body(rng, (4, 4, 4), 0.9, [datnu, bilnu, wl.Material(E=1e5, nu=0.3, cte=0.0)],
                           random_phase=True, temp_vary=True, temp_amplitude=8.0, temp_period=0.02,
                           enable_expansion=1, z_offset=1), 400, 100)
+    # boundary conditions: a cantilever clamped (all six DOFs) on its first layer with a
+    # load on its last, floor off
+    beam_bcs = [wl.BCRegion(prim=0, dof_fixed=63, x=0.0, y=0.0, z=0.0, dx=0.05, dy=1.0, dz=1.0),
+                wl.BCRegion(prim=0, dof_fixed=0, x=0.95, y=0.0, z=0.0, dx=0.05, dy=1.0, dz=1.0, force=(0.0, 0.0, -0.02))]
+    out["beam10_clamped_bcs"] = (wl.Robot(grid=np.ones((2, 2, 10), np.uint8), materials=[wl.Material(E=1e5, nu=0.35)],
+                                          floor=False, bcs=beam_bcs), 600, 200)
+    # partial DOFs on an actuated body on the floor: X/Y translation (with a displacement)
+    # and the Z rotation held on one face, a sphere region with a force and a torque, a
+    # cylinder fixing the X rotation, a box fixing Z translation and Y rotation; regions
+    # overlap (the reference's force accumulation doubles earlier shares)
+    rng = np.random.default_rng(21)
+    bmats = [wl.Material(E=2e5, nu=0.35, cte=0.01), wl.Material(E=1e5, nu=0.35)]
+    part = wl.bernoulli_body(rng, (6, 5, 4), 0.9, bmats, random_phase=True, temp_vary=True, temp_amplitude=15.0,
+                             temp_period=0.05, z_offset=0)
+    part.bcs = [wl.BCRegion(prim=0, dof_fixed=1 | 2 | 32, x=0.0, y=0.0, z=0.0, dx=0.2, dy=1.0, dz=1.0,
+                            displace=(0.001, 0.0, 0.0), ang_displace=(0.0, 0.0, 0.05)),
+                wl.BCRegion(prim=2, dof_fixed=0, x=0.7, y=0.5, z=0.6, radius=0.2, torque=(1e-4, 0.0, 2e-4),
+                            force=(0.0, 0.01, 0.0)),
+                wl.BCRegion(prim=1, dof_fixed=8, x=0.0, y=0.5, z=0.5, dx=1.0, radius=0.15, force=(0.0, 0.0, 0.005)),
+                wl.BCRegion(prim=0, dof_fixed=4 | 16, x=0.5, y=0.0, z=0.0, dx=0.5, dy=0.5, dz=0.3,
+                            displace=(0.0, 0.0, -0.0005), force=(0.003, 0.0, 0.0))]
+    out["bern6_partial_bcs"] = (part, 400, 100)
     return out
 
 
@@ -165,6 +188,8 @@ def robot_record(r):
                     enable_detach=r.enable_detach, secondary_experiment=r.secondary_experiment)
     rec = dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
                settings=np.array(json.dumps(settings)))
+    if r.bcs:  # boundary-condition regions
+        rec["bcs"] = np.array(json.dumps([dataclasses.asdict(b) for b in r.bcs]))
     if nonlinear(r):  # material models beyond linear: MatModel and its parameters per palette entry
         rec["models"] = np.array(json.dumps([dict(model=m.mat_model(), plastic_mod=m.plastic_mod,
                                                   yield_stress=m.yield_stress,

@@ -35,6 +35,9 @@ def load(name):
             m.ss_stress = None if md["ss_stress"] is None else tuple(md["ss_stress"])
     phase = d["phase"] if d["phase"].size else None
     robot = wl.Robot(grid=d["lattice"], materials=mats, phase=phase, z_offset=0, **s)
+    if "bcs" in d.files:  # boundary-condition regions
+        robot.bcs = [wl.BCRegion(**{k: tuple(v) if isinstance(v, list) else v for k, v in b.items()})
+                     for b in json.loads(str(d["bcs"]))]
     for name in ("cilia_base", "cilia_shift"):
         if name in d.files and d[name].size:
             setattr(robot, name, d[name])

@@ -31,6 +31,13 @@ class VxoMaterial(ctypes.Structure):
                 ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p)]
 
 
+class VxoBC(ctypes.Structure):
+    _fields_ = [("prim", ctypes.c_int), ("dof_fixed", ctypes.c_int), ("x", ctypes.c_float), ("y", ctypes.c_float),
+                ("z", ctypes.c_float), ("dx", ctypes.c_float), ("dy", ctypes.c_float), ("dz", ctypes.c_float),
+                ("radius", ctypes.c_float), ("force", ctypes.c_double * 3), ("torque", ctypes.c_double * 3),
+                ("displace", ctypes.c_double * 3), ("ang_displace", ctypes.c_double * 3)]
+
+
 class VxoRobot(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
                 ("lattice", ctypes.c_void_p), ("phase", ctypes.c_void_p),
@@ -43,7 +50,8 @@ class VxoRobot(ctypes.Structure):
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
                 ("force_field", ctypes.c_void_p * 3),
                 ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
-                ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int)]
+                ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int),
+                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(VxoBC))]
 
 
 def build_oracle():
@@ -233,7 +241,13 @@ def robot_struct(robot):
                 setattr(r, name, _P(a))
     r.enable_detach = int(robot.enable_detach)
     r.secondary_experiment = int(robot.secondary_experiment)
-    return r, (lattice, phase, mats, progs, cil, ss_keep)
+    bcs = None
+    if robot.bcs:
+        from vx3g.abi import bc_array
+        bcs = bc_array(VxoBC, robot.bcs)
+        r.n_bcs = len(robot.bcs)
+        r.bcs = bcs
+    return r, (lattice, phase, mats, progs, cil, ss_keep, bcs)
 
 
 def _force_field_tokens(robot):

@@ -135,6 +135,31 @@ def test_runner_material_models_match_oracle(tmp_path):
     assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size
 
 
+def test_runner_boundary_conditions_match_oracle(tmp_path):
+    """<Environment><Boundary_Conditions> read by the runner: a clamped, loaded
+    cantilever and an actuated body with partial DOF fixes, against the oracle."""
+    import golden_cases
+    vbuild.build()
+    exe = os.path.join(os.path.dirname(vbuild.LIB), "vx3g_sim")
+    for name in ("beam10_clamped_bcs", "bern6_partial_bcs"):
+        robot, _ = golden_cases.load(name)
+        robot.stop_time = 0.01
+        d = tmp_path / name
+        d.mkdir()
+        (d / "base.vxa").write_text(wl.to_vxa(robot))
+        (d / "r.vxd").write_text("<VXD>\n</VXD>\n")
+        out = d / "report.xml"
+        r = subprocess.run([exe, "-i", str(d), "-o", str(out)], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        node = ET.parse(out).getroot().find("detail/r")
+        s, _, _ = _oracle_until(robot, 0.01)
+        com = [float(node.find(f"currentCenterOfMass/{k}").text) for k in "xyz"]
+        np.testing.assert_allclose(com, s.com(), rtol=0, atol=1e-6 * robot.vox_size)
+        free = wl.Robot(**{**robot.__dict__, "bcs": None})
+        f, _, _ = _oracle_until(free, 0.01)
+        assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size, name  # the regions acted
+
+
 def test_runner_cilia_matches_oracle(tmp_path):
     """EnableCilia with Structure/BaseCiliaForce and ShiftCiliaForce rows and per-material
     Cilia / TurnOnCiliaAfterThisManySeconds, through the runner, against the oracle."""

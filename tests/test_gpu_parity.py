@@ -294,6 +294,34 @@ def test_nonlinear_materials_mixed_matches_fp64(name):
         abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
 
 
+@pytest.mark.parametrize("name", ["beam10_clamped_bcs", "bern6_partial_bcs"])
+def test_boundary_conditions_mixed_matches_fp64(name):
+    """Boundary-condition externals (fully clamped voxels, fixed translations with a
+    displacement, all and partial rotation fixes, region forces and torques): the
+    mixed-precision kernels follow the FP64 ones (COM within 1e-5 relative), the
+    fully fixed voxels sit exactly at their prescribed pose in both, and the adjoint
+    refuses them."""
+    robot, d = golden_cases.load(name)
+    f = abi.Batch([robot], abi.PRECISION_FP64)
+    m = abi.Batch([robot], abi.PRECISION_MIXED)
+    n = int(d["snap_steps"][-1])
+    p0 = f.state()["pos"]
+    f.step(n)
+    m.step(n)
+    assert np.all(f.status() == 0) and np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - f.com(), axis=1) / np.linalg.norm(f.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
+    if name == "beam10_clamped_bcs":
+        clamp = f.topology()["ijk"][:, 0] == 0
+        for b, tol in ((f, 0.0), (m, 1e-12)):  # mixed: a double as an FP32 hi/lo pair (~48 bits)
+            st = b.state()
+            assert np.max(np.abs(st["pos"][clamp] - p0[clamp])) <= tol
+            assert np.max(np.abs(st["orient"][clamp] - np.array([1.0, 0, 0, 0]))) <= tol
+            assert np.all(st["linmom"][clamp] == 0)
+    with pytest.raises(abi.Vx3gError, match="not implemented"):
+        abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
+
+
 def test_mixed_com_error_vs_fp64():
     rng = np.random.default_rng(21)
     mats = [wl.Material(E=float(10 ** rng.uniform(5, 7)), nu=0.35, cte=0.01) for _ in range(4)]

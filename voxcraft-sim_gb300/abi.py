@@ -39,6 +39,23 @@ class Material(ctypes.Structure):
                 ("n_data", ctypes.c_int), ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p)]
 
 
+class BCRegion(ctypes.Structure):
+    _fields_ = [("prim", ctypes.c_int), ("dof_fixed", ctypes.c_int), ("x", ctypes.c_float), ("y", ctypes.c_float),
+                ("z", ctypes.c_float), ("dx", ctypes.c_float), ("dy", ctypes.c_float), ("dz", ctypes.c_float),
+                ("radius", ctypes.c_float), ("force", ctypes.c_double * 3), ("torque", ctypes.c_double * 3),
+                ("displace", ctypes.c_double * 3), ("ang_displace", ctypes.c_double * 3)]
+
+
+def bc_array(cls, bcs):
+    """ctypes array of `cls` (BCRegion or the oracle's struct of the same layout) from workloads.BCRegion."""
+    arr = (cls * max(len(bcs), 1))()
+    for i, b in enumerate(bcs):
+        arr[i] = cls(int(b.prim), int(b.dof_fixed), b.x, b.y, b.z, b.dx, b.dy, b.dz, b.radius,
+                     (ctypes.c_double * 3)(*b.force), (ctypes.c_double * 3)(*b.torque),
+                     (ctypes.c_double * 3)(*b.displace), (ctypes.c_double * 3)(*b.ang_displace))
+    return arr
+
+
 class RobotDesc(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
                 ("lattice", ctypes.c_void_p), ("phase", ctypes.c_void_p),
@@ -51,7 +68,8 @@ class RobotDesc(ctypes.Structure):
                 ("bond_damping", ctypes.c_double), ("col_damping", ctypes.c_double), ("slow_damping", ctypes.c_double),
                 ("log10E", ctypes.c_void_p), ("force_field", ctypes.c_void_p * 3),
                 ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
-                ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int)]
+                ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int),
+                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(BCRegion))]
 
 
 class BatchDesc(ctypes.Structure):
@@ -162,7 +180,12 @@ def robot_desc(robot):
             if a is not None:
                 cil.append(a)
                 setattr(d, name, _P(a))
-    return d, (lattice, phase, mats, log10E, progs, cil, ss_keep)
+    bcs = None
+    if robot.bcs:
+        bcs = bc_array(BCRegion, robot.bcs)
+        d.n_bcs = len(robot.bcs)
+        d.bcs = bcs
+    return d, (lattice, phase, mats, log10E, progs, cil, ss_keep, bcs)
 
 
 class Batch:

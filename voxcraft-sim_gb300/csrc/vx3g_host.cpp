@@ -21,6 +21,7 @@
 #include "../../include/vx3g.h"
 #include "vx3g_adjoint.h"
 #include "vx3g_internal.h"
+#include "vx3g_bc.h"
 #include "vx3g_material.h"
 
 using namespace vx3g;
@@ -233,6 +234,7 @@ struct vx3g_ctx {
     bool any_remove = false;  // some robot removes voxels (SecondaryExperiment)
     bool any_dyn = false;     // some robot's surface follows its link table (detach or removal)
     bool any_nonlinear = false;  // some material has a non-linear stress-strain model
+    bool any_bcs = false;        // some voxel has a boundary-condition external
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -366,6 +368,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     std::vector<double> cil_on_h;
     std::vector<double> rm_h;  // per voxel: removal time (+inf: never)
     std::vector<float2> ss_h;  // stress-strain points of the non-linear link materials
+    std::vector<ExtBC> ext_h;  // boundary-condition externals
+    std::vector<int> vext_h;   // per voxel: index into ext_h or -1
     c->voff.assign(c->nr + 1, 0);
     c->loff.assign(c->nr + 1, 0);
 
@@ -519,6 +523,36 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             }
         }
         c->any_remove |= rp.remove != 0;
+        // Environment/Boundary_Conditions: the externals of the voxels the regions touch
+        vext_h.resize(pos.size(), -1);
+        rp.bcs = 0;
+        if (R.n_bcs < 0 || (R.n_bcs > 0 && !R.bcs)) return fail(VX3G_ERR_INVALID, "n_bcs needs the regions");
+        for (int j = 0; j < R.n_bcs; j++) {
+            if (R.bcs[j].prim == 3)
+                return fail(VX3G_ERR_UNSUPPORTED, "mesh boundary-condition regions (PrimType 3) are not supported");
+            if (R.bcs[j].prim < 0 || R.bcs[j].prim > 3) return fail(VX3G_ERR_INVALID, "unknown PrimType");
+        }
+        if (R.n_bcs > 0) {
+            std::vector<int> ix(nvr), iy(nvr), iz(nvr);
+            for (int k = 0; k < nvr; k++) {
+                const short4 l = c->ijk[v0 + k];
+                ix[k] = l.x, iy[k] = l.y, iz[k] = l.z;
+            }
+            const std::vector<VoxelExt> ex = bc_externals(R, ix, iy, iz);
+            for (int k = 0; k < nvr; k++) {
+                if (!ex[k].any) continue;
+                const VoxelExt &e = ex[k];
+                ExtBC b{};
+                b.t = make_double4(e.t[0], e.t[1], e.t[2], 0.0);
+                b.q = make_double4(e.q[0], e.q[1], e.q[2], e.q[3]);
+                for (int k = 0; k < 3; k++) b.f[k] = e.f[k], b.m[k] = e.m[k];
+                b.dof = e.dof;
+                vext_h[v0 + k] = (int)ext_h.size();
+                ext_h.push_back(b);
+                rp.bcs = 1;
+            }
+        }
+        c->any_bcs |= rp.bcs != 0;
         rp.dyn = rp.detach || rp.remove ? 1 : 0;
         c->any_dyn |= rp.dyn != 0;
         rp.ff_pos = 0;
@@ -628,6 +662,21 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     if ((rc = c->alloc(&ls, 9 * (size_t)d.nl * rsz)) || (rc = c->alloc(&sl, 6 * (size_t)d.nv * 6 * rsz))) return rc;
     d.lstate = ls;
     d.slots = sl;
+    d.ext = nullptr;
+    d.vext = nullptr;
+    d.xrot = nullptr;
+    d.nxrot = 0;
+    if (c->any_bcs) {
+        ExtBC *dext;
+        if ((rc = c->upload(&dext, ext_h)) || (rc = c->upload(&d.vext, vext_h))) return rc;
+        d.ext = dext;
+        std::vector<int> xrot;  // voxels with some but not all rotational DOFs fixed
+        for (size_t v = 0; v < vext_h.size(); v++)
+            if (vext_h[v] >= 0 && (ext_h[vext_h[v]].dof & EXT_R) && (ext_h[vext_h[v]].dof & EXT_R) != EXT_R)
+                xrot.push_back((int)v);
+        if (!xrot.empty() && (rc = c->upload(&d.xrot, xrot))) return rc;
+        d.nxrot = (int)xrot.size();
+    }
     d.soff = nullptr;
     d.ss = nullptr;
     if (!ss_h.empty()) {  // non-linear link materials: their curves and a plastic strain offset per link
@@ -720,7 +769,10 @@ void enqueue_voxels(vx3g_ctx *c, int parity) {
     launch_extra_forces(c->d, parity, c->stream);  // robots with a force field or cilia only
     launch_detach(c->d, c->stream);                // EnableDetach robots only (after the collision pass)
     if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(c->d, parity, c->stream);
-    else launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, !c->any_detach);  // detach writes voxel info
+    else {
+        launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, !c->any_detach);  // detach writes voxel info
+        launch_ext_rot_mixed(c->d, c->stream);     // partial rotation fixes, if any voxel has one
+    }
     launch_remove(c->d, parity, c->stream);        // SecondaryExperiment robots only (end of the step)
 }
 
@@ -747,6 +799,7 @@ cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
     launch_extra_forces(c->d, parity, c->stream);
     launch_detach(c->d, c->stream);
     launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, false);
+    launch_ext_rot_mixed(c->d, c->stream);
     launch_remove(c->d, parity, c->stream);
     return cudaSuccess;
 }
@@ -1464,6 +1517,7 @@ int vx3g_record(vx3g_ctx *c, int n, int k) {
     if (c->any_cilia) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of cilia forces is not implemented");
     if (c->any_nonlinear)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of non-linear material models is not implemented");
+    if (c->any_bcs) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of boundary conditions is not implemented");
     if (c->any_detach || c->any_remove)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a changing link table (detach, removal) is not implemented");
     CU(cudaSetDevice(c->device));

@@ -78,7 +78,20 @@ struct RobotP {
     int detach = 0;            // 1: EnableDetach (failed links leave)
     int remove = 0;            // 1: SecondaryExperiment with a material that leaves (k_remove)
     int dyn = 0;               // detach || remove: the surface follows the link table
+    int bcs = 0;               // 1: some voxel has a boundary-condition external (Dev::vext)
 };
+
+// a voxel's boundary-condition external (VX3_External): fixed DOFs with their prescribed
+// translation and rotation, applied force and moment
+struct ExtBC {
+    double4 t;   // extTranslation {x, y, z, -}
+    double4 q;   // _extRotationQ {w, x, y, z}
+    float f[3];  // extForce
+    float m[3];  // extMoment
+    int dof;     // fixed DOFs: bits 0-2 translation x, y, z; 3-5 rotation x, y, z
+    int pad;
+};
+enum : int { EXT_T = 0x7, EXT_R = 0x38, EXT_ALL = 0x3F };
 
 // grid of one robot on the large-robot list path (bounding box in cells of cutoff + skin)
 struct GridP {
@@ -171,6 +184,10 @@ struct Dev {
     int any_dyn;          // some robot's surface follows its link table (detach or removal)
     unsigned char *vgone; // per voxel: removed (removeVoxels), or NULL when no robot removes voxels
     double *rm_at;        // per voxel: the time after which it is removed (+inf: never), or NULL
+    const ExtBC *ext;  // boundary-condition externals, or NULL when no robot has any
+    int *vext;         // per voxel: its index in ext, or -1 (NULL when no robot has any)
+    int *xrot;         // voxels with some but not all rotations fixed (mixed precision: k_ext_rot_mixed)
+    int nxrot;
     double *com_part;  // [NR][com_tiles][4] partial sums of the centre of mass
     int com_tiles;     // tiles of kComTile voxels of the largest robot
     int nv, nl, nr, ns;
@@ -201,6 +218,8 @@ void launch_links_mixed(const Dev &d, cudaStream_t s, int shape = 0, bool pdl = 
 // pdl = false when the kernel before it wrote voxel info (detach): no early start
 void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape = 0, bool pdl = true);
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
+// partial rotation fixes of boundary-condition voxels after the mixed-precision voxel pass
+void launch_ext_rot_mixed(const Dev &d, cudaStream_t s);
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s);
 void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 // surface-voxel collision of one step: displacement check and list rebuild (one

@@ -169,6 +169,7 @@ struct RobotSpec {
     vx3g_robot_desc desc{};
     const Node *stop = nullptr, *fitness = nullptr;
     std::vector<vx3g_math_token> ff[3];  // force-field programs (desc.force_field points here)
+    std::vector<vx3g_bc_region> bcs;     // Environment/Boundary_Conditions (desc.bcs points here)
     std::unique_ptr<Node> doc;
     int record_step = 0, record_voxel = 1, record_link = 0, save_all = 0;
     double reinit_after = 0.0;  // ReinitializeInitialPositionAfterThisManySeconds (SecondaryExperiment)
@@ -239,11 +240,49 @@ void read_spec(RobotSpec &S) {
         d.vary_temp = vx3g::xml::get_bool(root, "VXA.Environment.Thermal.VaryTempEnabled", false);
         d.temp_period = vx3g::xml::get_double(root, "VXA.Environment.Thermal.TempPeriod", 0.1);
     }
+    // Environment/Boundary_Conditions: NumBCs FRegion elements (CVX_Environment::ReadXML,
+    // src/old/VX_Environment.cpp:101-117; CVX_FRegion::ReadXML, src/old/VX_FRegion.cpp:165-219)
+    if (const Node *bc = vx3g::xml::find(root, "VXA.Environment.Boundary_Conditions")) {
+        const int n = vx3g::xml::get_int(bc, "NumBCs", 0);
+        const std::vector<const Node *> regs = bc->all("FRegion");
+        if ((int)regs.size() < n) throw std::runtime_error(S.filename + ": fewer FRegion elements than NumBCs");
+        for (int i = 0; i < n; i++) {
+            const Node *f = regs[i];
+            vx3g_bc_region b{};
+            double prim;
+            if (!vx3g::xml::get_double(f, "PrimType", &prim)) throw std::runtime_error(S.filename + ": FRegion without PrimType");
+            b.prim = (int)prim;
+            const char *geo[7] = {"X", "Y", "Z", "dX", "dY", "dZ", "Radius"};
+            float *dst[7] = {&b.x, &b.y, &b.z, &b.dx, &b.dy, &b.dz, &b.radius};
+            for (int k = 0; k < 7; k++) *dst[k] = (float)vx3g::xml::get_double(f, geo[k], 0.0);
+            double dof;
+            if (vx3g::xml::get_double(f, "DofFixed", &dof)) b.dof_fixed = (int)dof & 0x3F;
+            else b.dof_fixed = vx3g::xml::get_bool(f, "Fixed", false) ? 0x3F : 0;  // older files: a binary Fixed
+            const char *ax = "XYZ";
+            for (int k = 0; k < 3; k++) {
+                const std::string a(1, ax[k]);
+                b.force[k] = vx3g::xml::get_double(f, "Force" + a, 0.0);
+                b.torque[k] = vx3g::xml::get_double(f, "Torque" + a, 0.0);
+                b.displace[k] = vx3g::xml::get_double(f, "Displace" + a, 0.0);
+                b.ang_displace[k] = vx3g::xml::get_double(f, "AngDisplace" + a, 0.0);
+            }
+            S.bcs.push_back(b);
+        }
+    }
     // VXC
     const Node *vxc = vxa->child("VXC");
     if (!vxc) throw std::runtime_error(S.filename + ": no <VXC> element");
     double dim = vx3g::xml::get_double(vxc, "Lattice.Lattice_Dim", 0.001);
     d.vox_size = dim * vx3g::xml::get_double(vxc, "Lattice.X_Dim_Adj", 1.0);
+    if (!S.bcs.empty()) {  // regions are placed on a cubic lattice without offsets
+        for (const char *k : {"Lattice.X_Dim_Adj", "Lattice.Y_Dim_Adj", "Lattice.Z_Dim_Adj"})
+            if (vx3g::xml::get_double(vxc, k, 1.0) != 1.0)
+                throw std::runtime_error(S.filename + ": boundary conditions need lattice dimension adjustments of 1");
+        for (const char *k : {"Lattice.X_Line_Offset", "Lattice.Y_Line_Offset", "Lattice.X_Layer_Offset",
+                              "Lattice.Y_Layer_Offset"})
+            if (vx3g::xml::get_double(vxc, k, 0.0) != 0.0)
+                throw std::runtime_error(S.filename + ": boundary conditions need a lattice without line or layer offsets");
+    }
     const Node *pal = vxc->child("Palette");
     if (pal) {
         for (const Node *m : pal->all("Material")) {
@@ -369,6 +408,8 @@ void read_spec(RobotSpec &S) {
     d.phase = S.phase.data();
     d.n_materials = (int)S.mats.size();
     d.materials = S.mats.data();
+    d.n_bcs = (int)S.bcs.size();
+    d.bcs = S.bcs.empty() ? nullptr : S.bcs.data();
 }
 
 void check(int rc, const char *what) {

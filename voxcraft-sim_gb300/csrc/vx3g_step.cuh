@@ -439,6 +439,28 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
         return;
     }
 
+    // boundary-condition external (VX3_External), if any
+    const int xi = rp.bcs ? d.vext[v] : -1;
+    ExtBC ex{};
+    if (xi >= 0) ex = d.ext[xi];
+    const int dof = ex.dof;
+    if (dof == EXT_ALL) {  // isFixedAll (VX3_Voxel.cu:167-173): at its prescribed pose, motion halted
+        const short4 l = d.ijk[v];
+        p.x = l.x * m.nom_size + ex.t.x;
+        p.y = l.y * m.nom_size + ex.t.y;
+        p.z = l.z * m.nom_size + ex.t.z;
+        d.quat[v] = ex.q;
+        d.linmom[v] = make_double4(0, 0, 0, 0);
+        d.angmom[v] = make_double4(0, 0, 0, 0);
+        if (actuated) {
+            float te = tcur[v];
+            p.w = temperature_base_size<EXACT>(rp, m, d.phase[v], tn, p.w, &te);
+            tnext[v] = te;
+        }
+        d.pos[v] = p;
+        return;
+    }
+
     // link force/moment sums in direction order 0..5 (VX3_Voxel::force/moment, VX3_Voxel.cu:350-397)
     V3<R> Fs{0, 0, 0}, Ms{0, 0, 0};
     const Slot<R> *S = (const Slot<R> *)d.slots;
@@ -462,6 +484,7 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
     if constexpr (EXACT) {
         const Q4<double> o{q.x, q.y, q.z, q.w};
         V3<double> F = qrot(o, Fs);
+        if (xi >= 0) F = add(F, V3<double>{ex.f[0], ex.f[1], ex.f[2]});  // external force (:363-364)
         const V3<double> vel = scl(lmv, m.mass_inv);
         F = sub(F, scl(vel, m.c_glob));
         F.z += m.grav_force;
@@ -513,9 +536,28 @@ template <class R> __device__ __forceinline__ void voxel_update(const Dev &d, in
         }
         p.x += tr.x; p.y += tr.y; p.z += tr.z;
         V3<double> M = qrot(o, Ms);
+        if (xi >= 0) M = add(M, V3<double>{ex.m[0], ex.m[1], ex.m[2]});  // external moment (:393-394)
         M = sub(M, scl(scl(amv, m.mom_inv), m.c_glob_rot));
         amv = add(amv, scl(M, dt));
-        const Q4<double> on = qmul(from_rotvec(scl(amv, dt * m.mom_inv)), o);
+        Q4<double> on = qmul(from_rotvec(scl(amv, dt * m.mom_inv)), o);
+        if (dof) {  // fixed DOFs (VX3_Voxel.cu:222-257)
+            const short4 l = d.ijk[v];
+            if (dof & 1) { p.x = l.x * m.nom_size + ex.t.x; lmv.x = 0; }
+            if (dof & 2) { p.y = l.y * m.nom_size + ex.t.y; lmv.y = 0; }
+            if (dof & 4) { p.z = l.z * m.nom_size + ex.t.z; lmv.z = 0; }
+            if (dof & EXT_R) {
+                if ((dof & EXT_R) == EXT_R) {  // all rotations: the prescribed orientation
+                    on = Q4<double>{ex.q.x, ex.q.y, ex.q.z, ex.q.w};
+                    amv = V3<double>{0, 0, 0};
+                } else {  // some: zero those components of the rotation vector
+                    V3<double> rv = to_rotvec(on);
+                    if (dof & 8) { rv.x = 0; amv.x = 0; }
+                    if (dof & 16) { rv.y = 0; amv.y = 0; }
+                    if (dof & 32) { rv.z = 0; amv.z = 0; }
+                    on = from_rotvec(rv);
+                }
+            }
+        }
         d.quat[v] = make_double4(on.w, on.x, on.y, on.z);
     } else {
         const Q4<float> o{(float)q.x, (float)q.y, (float)q.z, (float)q.w};

@@ -59,6 +59,26 @@ class Material:
 
 
 @dataclasses.dataclass
+class BCRegion:
+    """An <Environment><Boundary_Conditions> region (FRegion): every voxel it touches has
+    the fixed DOFs held at their displacement and a share of the force and torque.
+    Coordinates are fractions of the workspace (the lattice's extent)."""
+    prim: int = 0              # PrimType: 0 box, 1 cylinder, 2 sphere
+    dof_fixed: int = 0         # DofFixed: 1 X, 2 Y, 4 Z translation; 8 X, 16 Y, 32 Z rotation
+    x: float = 0.0
+    y: float = 0.0
+    z: float = 0.0
+    dx: float = 0.0
+    dy: float = 0.0
+    dz: float = 0.0
+    radius: float = 0.0
+    force: tuple = (0.0, 0.0, 0.0)
+    torque: tuple = (0.0, 0.0, 0.0)
+    displace: tuple = (0.0, 0.0, 0.0)
+    ang_displace: tuple = (0.0, 0.0, 0.0)
+
+
+@dataclasses.dataclass
 class Robot:
     """One simulation: lattice (z, y, x) of palette indices and its settings."""
     grid: np.ndarray                      # int8/uint8 [Z, Y, X], 0 = empty
@@ -92,6 +112,7 @@ class Robot:
     stop_formula: Optional[tuple] = None  # or any StopConditionFormula math tree (see math_tokens)
     fitness_x: bool = False               # FitnessFunction "x" (COM displacement along x)
     record_step: int = 0                  # RecordHistory/RecordStepSize
+    bcs: Optional[list] = None            # Environment/Boundary_Conditions: BCRegion list
 
     def occupied(self) -> np.ndarray:
         return self.grid > 0
@@ -262,6 +283,23 @@ def _ss_xml(m: Material) -> str:
             + "</StressData></SSData>")
 
 
+def _bcs_xml(r: Robot) -> str:
+    """<Boundary_Conditions> (src/old/VX_Environment.cpp:101-117, VX_FRegion.cpp:165-219)."""
+    if not r.bcs:
+        return ""
+    out = [f"<Boundary_Conditions><NumBCs>{len(r.bcs)}</NumBCs>"]
+    for b in r.bcs:
+        vals = [("PrimType", b.prim), ("X", b.x), ("Y", b.y), ("Z", b.z), ("dX", b.dx), ("dY", b.dy), ("dZ", b.dz),
+                ("Radius", b.radius), ("DofFixed", b.dof_fixed)]
+        vals += [(f"Force{a}", v) for a, v in zip("XYZ", b.force)] + [(f"Torque{a}", v) for a, v in zip("XYZ", b.torque)]
+        vals += [(f"Displace{a}", v) for a, v in zip("XYZ", b.displace)]
+        vals += [(f"AngDisplace{a}", v) for a, v in zip("XYZ", b.ang_displace)]
+        out.append("<FRegion>" + "".join(f"<{k}>{_fmt(v) if isinstance(v, float) else v}</{k}>" for k, v in vals)
+                   + "</FRegion>")
+    out.append("</Boundary_Conditions>")
+    return "".join(out)
+
+
 def to_vxa(r: Robot) -> str:
     """Serialise a Robot as a self-contained VXA document."""
     g, ph = r.padded()
@@ -295,6 +333,7 @@ def to_vxa(r: Robot) -> str:
               "<RecordLink>0</RecordLink></RecordHistory>"] if r.record_step else []),
            "</Simulator>",
            "<Environment>",
+           _bcs_xml(r),
            f"<Gravity><GravEnabled>{int(r.gravity)}</GravEnabled><GravAcc>{_fmt(r.grav_acc)}</GravAcc>"
            f"<FloorEnabled>{int(r.floor)}</FloorEnabled></Gravity>",
            "<Thermal><TempEnabled>0</TempEnabled>"
