@@ -6,17 +6,26 @@
 The default line also carries the adjoint's backward/forward time ratio on the
 differentiable 12x12x6 robot ("adjoint"; --no-adjoint leaves it out).
 
-A bench "step" is one CUDA-graph chunk of --chunk (default 100) physics time
-steps over the whole batch; the default 200 timed chunks cover the 20,000 steps
-of the single-body configuration (after 500 warm-up steps).  Timed steps are bracketed by CUDA events on the
-library's stream; the L2 cache is flushed (512 MB overwrite) before every timed
-chunk.  The default workload is the single large body (64^3 Bernoulli(0.6),
-collisions + floor, mixed precision).  Under torchrun each rank runs its own
-replica of the workload on its own GPU (robots are independent; no collective).
+A bench "step" is --chunk (default 1000) physics time steps of the whole batch,
+replayed as CUDA graphs of --graph-chunk (100) steps.  The timed run starts a fresh
+context at physics step 0, so the default K (the configuration's steps / chunk: 20
+for the single large body) covers the configuration's whole run; the W warm-up
+bench steps run on a context of their own, which also tunes the launch shapes.
+Timed steps are bracketed by CUDA events on the library's stream; the L2 cache is
+flushed (512 MB overwrite) before every timed bench step.  The default workload is
+the single large body (64^3 Bernoulli(0.6), collisions + floor, mixed precision).
+Under torchrun each rank runs its own replica of the workload on its own GPU
+(robots are independent; no collective).
 
-"e2e" replays the same window (same warm-up, then the same K chunks of the same
-trajectory) on a fresh batch through the C ABI with the voxel state in pinned
-host memory: each chunk uploads the state, steps, reads the state and the COM back.
+The mixed-precision line also carries the metric's comparison: the FP64 step over
+the same window ("fp64_value", "mixed_over_fp64"), the relative centre-of-mass error
+of the mixed run against it ("com_rel_err", at 2000 steps and at the end of the
+window), and the plain FP64 single-simulation rate of the 10^3 block
+("c1_fp64_value").
+
+"e2e" replays the same window on a fresh context through the C ABI with the voxel
+state in pinned host memory: every bench step uploads the state, steps, reads the
+state and the COM back.
 """
 
 import argparse
@@ -24,6 +33,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -313,23 +323,51 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# physics steps of each workload's configuration (the window one bench run covers)
+CONFIG_STEPS = {"c1": 10000, "c2": 20000, "c3": 10000, "c5": 4000}
+
+
+def timed_run(robots, prec, dev, K, C, G, cache, flush=True, com_at=()):
+    """A fresh context of the workload from physics step 0: launch shapes from the tuning
+    cache, step graphs captured beforehand, then K bench steps of C physics steps each,
+    each between CUDA events on the library's stream (after a 512 MB L2 overwrite).
+    Returns (per-step ms, context, {physics step: COM} for the steps in com_at)."""
+    b = abi.Batch(robots, prec, device=dev, graph_chunk=G)
+    b.autotune(0, cache)
+    b.prepare_graphs()
+    b.synchronize()
+    ms, coms = [], {}
+    for k in range(K):
+        if flush:
+            b.flush_l2()
+        ms.append(b.time_steps(C))
+        if (k + 1) * C in com_at:
+            coms[(k + 1) * C] = b.com()
+    return ms, b, coms
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)  # 200 chunks of 100: the 64^3 body's 20,000-step run
+    ap.add_argument("--steps", type=int, default=None,
+                    help="bench steps (default: the configuration's physics steps / --chunk, e.g. 20 for c2)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="vx3g", choices=["vx3g", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--chunk", type=int, default=100)
+    ap.add_argument("--chunk", type=int, default=1000, help="physics steps per bench step")
+    ap.add_argument("--graph-chunk", type=int, default=100, help="physics steps per CUDA graph")
     ap.add_argument("--ref-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 run of the same window")
     ap.add_argument("--tune-cache", default=None, help="JSON cache of tuned launch shapes (read and appended)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every step's kernels one by one instead of replaying CUDA graphs "
                          "(each launch then its own record in a per-kernel profiler)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = max(1, CONFIG_STEPS[args.workload] // args.chunk)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -339,40 +377,43 @@ def main():
     desc, builder = WORKLOADS[args.workload]
     robots = builder()
     prec = abi.PRECISION_MIXED if args.precision == "mixed" else abi.PRECISION_FP64
-    b = abi.Batch(robots, prec, device=dev, graph_chunk=-1 if args.no_graphs else args.chunk)
-    actuated = any(r.temp_vary for r in robots)
-    surf = b.surface()
-    ns_coll = 0
-    for i, r in enumerate(robots):
-        if r.enable_collision:
-            ns_coll += int(np.count_nonzero((surf >= b.voxel_offset[i]) & (surf < b.voxel_offset[i + 1])))
     W, K, C = args.warmup, args.steps, args.chunk
-    # warm-up: W-1 chunks of real steps while the launch shapes are tuned, then one
-    # chunk through the (re)built step graph
-    b.autotune(max(16, (W - 1) * C), args.tune_cache)
-    b.step(C)
-    b.synchronize()
+    G = -1 if args.no_graphs else args.graph_chunk
+    cache = args.tune_cache or os.path.join(tempfile.mkdtemp(prefix="vx3g_tune_"), "shapes.json")
+    actuated = any(r.temp_vary for r in robots)
+
+    # warm-up on a context of its own: W bench steps, the first ones tuning the launch
+    # shapes (written to the cache the timed contexts read), the clocks coming up
+    bw = abi.Batch(robots, prec, device=dev, graph_chunk=G)
+    tune = min(W * C, 2000)
+    bw.autotune(tune, cache)
+    if W * C > tune:
+        bw.step(W * C - tune)
+    bw.synchronize()
+    bw.close()
     if dist:
         dist.barrier()
-    per_chunk = []
+    com_at = {k * C for k in range(1, K + 1) if k * C in (2000, K * C)}
     with ClockSampler(dev) as clk:
-        for _ in range(K):
-            b.flush_l2()
-            per_chunk.append(b.time_steps(C))
+        per_chunk, b, com_mx = timed_run(robots, prec, dev, K, C, G, cache, com_at=com_at)
     b.synchronize()
     if dist:
         dist.barrier()
     total_ms = barrier_and_max(float(np.sum(per_chunk)), world)
     status = b.status()
-    vox_steps = b.nv * C * K * world
+    nv, nl = b.nv, b.nl
+    vox_steps = nv * C * K * world
     value = vox_steps / (total_ms / 1e3)
+    surf = b.surface()
+    ns_coll = 0
+    for i, r in enumerate(robots):
+        if r.enable_collision:
+            ns_coll += int(np.count_nonzero((surf >= b.voxel_offset[i]) & (surf < b.voxel_offset[i + 1])))
 
-    # per-pass device times (after the measured run); the dominant kernel is the
-    # single kernel with the largest time: the link pass, the voxel pass or the
-    # contact evaluation (the collision pass's other kernels are the small check and
-    # the rebuild, which runs only in some steps)
+    # per-pass device times (after the measured run); the dominant kernel is the single
+    # kernel with the largest time: the link pass, the voxel pass or the contact evaluation
     passes = b.time_passes(20)
-    ab = algorithmic_bytes(b.nv, b.nl, ns_coll, actuated)
+    ab = algorithmic_bytes(nv, nl, ns_coll, actuated)
     kernel_ms = {"k_links_mixed" if prec else "k_links": passes["links"],
                  "k_voxels_mixed" if prec else "k_voxels": passes["voxels"]}
     if ns_coll:
@@ -388,13 +429,33 @@ def main():
     shapes = [int(x) for x in b.launch_shapes()]
     b.close()
 
-    # e2e through the C ABI with host buffers: a fresh batch of the same robots runs
-    # the same warm-up steps and then the same K chunks of the same trajectory, the
-    # voxel state living in pinned host memory: every chunk uploads it, steps, reads
-    # it back and reads the COM
-    b2 = abi.Batch(robots, prec, device=dev, graph_chunk=-1 if args.no_graphs else args.chunk)
-    b2.autotune(max(16, (W - 1) * C), args.tune_cache)
-    b2.step(C)
+    # the metric's comparison: the FP64 step over the same window, and the mixed run's
+    # relative COM error against it (end of the window, and at 2000 steps)
+    fp64 = None
+    if prec == abi.PRECISION_MIXED and not args.no_fp64:
+        ms64, b64, com64 = timed_run(robots, abi.PRECISION_FP64, dev, K, C, G, cache, com_at=com_at)
+        t64 = barrier_and_max(float(np.sum(ms64)), world)
+        b64.close()
+        rel = lambda a, c: np.linalg.norm(a - c, axis=1) / np.linalg.norm(c, axis=1)  # noqa: E731
+        errs = {s: rel(com_mx[s], com64[s]) for s in sorted(com64)}
+        fp64 = {"fp64_value": vox_steps / (t64 / 1e3), "fp64_ms_per_step": t64 / K,
+                "mixed_over_fp64": (vox_steps / (total_ms / 1e3)) / (vox_steps / (t64 / 1e3)),
+                "com_rel_err": {f"step_{s}": {"max": float(e.max()), "median": float(np.median(e)),
+                                              "robots_le_1e-5": float(np.mean(e <= 1e-5))}
+                                for s, e in errs.items()}}
+        # the plain FP64 single-simulation step (the 10^3 block), the >= 3x denominator
+        c1 = workloads.c1_block_drop()
+        ms1, b1, _ = timed_run(c1, abi.PRECISION_FP64, dev, 2, 1000, G, cache, flush=False)
+        fp64["c1_fp64_value"] = b1.nv * 1000 / (ms1[1] / 1e3)
+        fp64["mixed_over_c1_fp64"] = value / fp64["c1_fp64_value"]
+        b1.close()
+
+    # e2e through the C ABI with host buffers: a fresh context of the same robots runs the
+    # same K bench steps of the same trajectory from step 0, the voxel state living in
+    # pinned host memory: every bench step uploads it, steps, reads it back and reads the COM
+    b2 = abi.Batch(robots, prec, device=dev, graph_chunk=G)
+    b2.autotune(0, cache)
+    b2.prepare_graphs()
     host = pinned_copy(b2.state())
     b2.synchronize()
     if dist:
@@ -415,11 +476,13 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 link forces + f64 integration" if prec else "f64", "data": "synthetic (seeded generator)",
-        "config": {"workload": desc, "robots": len(robots), "voxels": b.nv, "links": b.nl,
+        "config": {"workload": desc, "robots": len(robots), "voxels": nv, "links": nl,
                    "collision_surface_voxels": ns_coll, "precision": args.precision,
-                   "physics_steps_per_bench_step": C, "cuda_graphs": not args.no_graphs,
+                   "physics_steps_per_bench_step": C, "window": f"physics steps 0-{K * C} of a fresh context "
+                   f"(the configuration runs {CONFIG_STEPS[args.workload]})",
+                   "cuda_graphs": not args.no_graphs, "graph_chunk": G,
                    "launch_shapes": {"links": shapes[:2], "voxels": shapes[2:]},
-                   "l2": "512 MB overwrite before every timed chunk", "parallelism": f"replicas x{world}"},
+                   "l2": "512 MB overwrite before every timed bench step", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "kernel_ms": kernel_ms, "pass_ms": passes, "algorithmic_bytes_per_launch": ab,
@@ -430,6 +493,8 @@ def main():
         "clocks": clk.summary(),
         "robot_status_nonzero": int(np.count_nonzero(status)),
     }
+    if fp64:
+        line.update(fp64)
     if rank == 0 and args.workload == "c2" and not args.no_adjoint:
         line["adjoint"] = measure_adjoint(dev)
     if rank == 0 and args.workload == "c5" and not args.no_adjoint:

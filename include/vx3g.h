@@ -186,6 +186,10 @@ const char *vx3g_last_error(void);
  * stream; robots that diverged stay frozen).  Full chunks run as CUDA graphs. */
 int vx3g_step(vx3g_ctx *ctx, int n_steps);
 int vx3g_synchronize(vx3g_ctx *ctx);
+/* Captures and instantiates the CUDA graphs vx3g_step replays (both step parities)
+ * without running them, so that the first vx3g_step of a latency-sensitive loop does
+ * not pay for the capture.  Optional; no counterpart in the reference. */
+int vx3g_prepare_graphs(vx3g_ctx *ctx);
 /* The context's CUDA stream (a cudaStream_t), for event timing by the caller. */
 void *vx3g_stream(vx3g_ctx *ctx);
 

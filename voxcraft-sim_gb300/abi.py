@@ -26,7 +26,7 @@ EXPORTS = [
     "vx3g_get_topology", "vx3g_get_surface", "vx3g_com", "vx3g_dt", "vx3g_time", "vx3g_status",
     "vx3g_steps_taken", "vx3g_time_steps", "vx3g_flush_l2", "vx3g_time_passes", "vx3g_stop_robot",
     "vx3g_record", "vx3g_backward", "vx3g_recommended_dt_noalloc", "vx3g_autotune", "vx3g_launch_shapes",
-    "vx3g_debug_barrier",
+    "vx3g_debug_barrier", "vx3g_prepare_graphs",
 ]
 
 
@@ -121,6 +121,7 @@ def load(path: str = LIB_PATH):
     lib.vx3g_launch_shapes.argtypes = [vp, vp]
     lib.vx3g_backward.argtypes = [vp, dp, dp, dp]
     lib.vx3g_debug_barrier.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
+    lib.vx3g_prepare_graphs.argtypes = [vp]
     _lib = lib
     return lib
 
@@ -228,6 +229,10 @@ class Batch:
 
     def step(self, n: int):
         _check(self.lib.vx3g_step(self.h, int(n)), "vx3g_step")
+
+    def prepare_graphs(self):
+        """Capture the step graphs now (vx3g_prepare_graphs), outside any timed region."""
+        _check(self.lib.vx3g_prepare_graphs(self.h), "vx3g_prepare_graphs")
 
     def synchronize(self):
         _check(self.lib.vx3g_synchronize(self.h), "vx3g_synchronize")

@@ -664,18 +664,17 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     d.slots = sl;
     d.ext = nullptr;
     d.vext = nullptr;
-    d.xrot = nullptr;
-    d.nxrot = 0;
+    d.xbc = nullptr;
+    d.nxbc = 0;
     if (c->any_bcs) {
         ExtBC *dext;
         if ((rc = c->upload(&dext, ext_h)) || (rc = c->upload(&d.vext, vext_h))) return rc;
         d.ext = dext;
-        std::vector<int> xrot;  // voxels with some but not all rotational DOFs fixed
+        std::vector<int> xbc;  // the voxels with an external
         for (size_t v = 0; v < vext_h.size(); v++)
-            if (vext_h[v] >= 0 && (ext_h[vext_h[v]].dof & EXT_R) && (ext_h[vext_h[v]].dof & EXT_R) != EXT_R)
-                xrot.push_back((int)v);
-        if (!xrot.empty() && (rc = c->upload(&d.xrot, xrot))) return rc;
-        d.nxrot = (int)xrot.size();
+            if (vext_h[v] >= 0) xbc.push_back((int)v);
+        if ((rc = c->upload(&d.xbc, xbc))) return rc;
+        d.nxbc = (int)xbc.size();
     }
     d.soff = nullptr;
     d.ss = nullptr;
@@ -771,7 +770,7 @@ void enqueue_voxels(vx3g_ctx *c, int parity) {
     if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(c->d, parity, c->stream);
     else {
         launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, !c->any_detach);  // detach writes voxel info
-        launch_ext_rot_mixed(c->d, c->stream);     // partial rotation fixes, if any voxel has one
+        launch_voxels_bc_mixed(c->d, parity, c->stream);  // voxels with a boundary condition, if any
     }
     launch_remove(c->d, parity, c->stream);        // SecondaryExperiment robots only (end of the step)
 }
@@ -799,7 +798,7 @@ cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
     launch_extra_forces(c->d, parity, c->stream);
     launch_detach(c->d, c->stream);
     launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, false);
-    launch_ext_rot_mixed(c->d, c->stream);
+    launch_voxels_bc_mixed(c->d, parity, c->stream);
     launch_remove(c->d, parity, c->stream);
     return cudaSuccess;
 }
@@ -872,6 +871,16 @@ int vx3g_step(vx3g_ctx *c, int n) {
         }
     }
     CU(cudaGetLastError());
+    return VX3G_OK;
+}
+
+int vx3g_prepare_graphs(vx3g_ctx *c) {
+    if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    if (c->chunk == INT32_MAX) return VX3G_OK;  // graphs off
+    CU(cudaSetDevice(c->device));
+    cudaGraphExec_t g;
+    for (int parity = 0; parity < 2; parity++)
+        if (int rc = get_graph(c, parity, &g)) return rc;
     return VX3G_OK;
 }
 

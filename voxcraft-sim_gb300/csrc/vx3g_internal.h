@@ -186,8 +186,8 @@ struct Dev {
     double *rm_at;        // per voxel: the time after which it is removed (+inf: never), or NULL
     const ExtBC *ext;  // boundary-condition externals, or NULL when no robot has any
     int *vext;         // per voxel: its index in ext, or -1 (NULL when no robot has any)
-    int *xrot;         // voxels with some but not all rotations fixed (mixed precision: k_ext_rot_mixed)
-    int nxrot;
+    int *xbc;          // the voxels with an external, in voxel order (mixed precision: k_voxels_bc_mixed)
+    int nxbc;
     double *com_part;  // [NR][com_tiles][4] partial sums of the centre of mass
     int com_tiles;     // tiles of kComTile voxels of the largest robot
     int nv, nl, nr, ns;
@@ -218,8 +218,9 @@ void launch_links_mixed(const Dev &d, cudaStream_t s, int shape = 0, bool pdl = 
 // pdl = false when the kernel before it wrote voxel info (detach): no early start
 void launch_voxels_mixed(const Dev &d, int parity, cudaStream_t s, int shape = 0, bool pdl = true);
 void launch_init_temperature(const Dev &d, int mixed, cudaStream_t s);
-// partial rotation fixes of boundary-condition voxels after the mixed-precision voxel pass
-void launch_ext_rot_mixed(const Dev &d, cudaStream_t s);
+// the mixed-precision voxel pass of the voxels with a boundary-condition external (after
+// the main pass, which skips them)
+void launch_voxels_bc_mixed(const Dev &d, int parity, cudaStream_t s);
 void launch_init_temperature_mixed(const Dev &d, cudaStream_t s);
 void launch_dt(const Dev &d, double *maxfreq2_scratch, cudaStream_t s);
 // surface-voxel collision of one step: displacement check and list rebuild (one

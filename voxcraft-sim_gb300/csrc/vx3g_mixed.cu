@@ -365,7 +365,11 @@ __device__ __forceinline__ void set_df(float &hi, float &lo, double x) {
     lo = (float)(x - (double)hi);
 }
 
-__device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parity) {
+// BC = false: every voxel without a boundary-condition external (the main pass, which
+// compiles without the external code).  BC = true: the voxels with one (Dev::xbc), after
+// the main pass, with the external force and moment, the fixed DOFs and the fixed-all
+// pose (VX3_Voxel.cu:167-173, 222-257, 363-364, 393-394).
+template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parity) {
     // the voxel's own state is loaded together with its info word, before any branch
     // (latency-bound kernel: one dependent level fewer)
     const uint2 vi = d.vinfo[v];
@@ -383,17 +387,18 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
     const double Tcur = d.T[(size_t)parity * d.nr + r];
     const int st = d.status[r];
     const float dtf = d.dt[r];
-    if (v == rp.voff) d.T[(size_t)(parity ^ 1) * d.nr + r] = (st == 0) ? Tcur + dtf : Tcur;
+    if (!BC && v == rp.voff) d.T[(size_t)(parity ^ 1) * d.nr + r] = (st == 0) ? Tcur + dtf : Tcur;
     if (st != 0) return;
     uint32_t fl = vi.y;
     if (fl & VF_FIXED) return;
+    if (!BC && rp.bcs && d.vext[v] >= 0) return;  // stepped by the BC pass
     const VMat m = d.vmat[fl >> 8];
     const bool actuated = rp.vary_temp && rp.temp_period > 0;
     float *tcur = d.tempe + (size_t)parity * d.nv, *tnext = d.tempe + (size_t)(parity ^ 1) * d.nv;
     const double tn = Tcur + dtf;
-    const int xi = rp.bcs ? d.vext[v] : -1;  // boundary-condition external, if any
-    const int dof = xi >= 0 ? d.ext[xi].dof : 0;
-    if (dtf != 0.0f && dof == EXT_ALL) {  // isFixedAll (VX3_Voxel.cu:167-173)
+    const int xi = BC ? d.vext[v] : -1;  // boundary-condition external
+    const int dof = BC ? d.ext[xi].dof : 0;
+    if (BC && dtf != 0.0f && dof == EXT_ALL) {  // isFixedAll (VX3_Voxel.cu:167-173)
         const ExtBC &e = d.ext[xi];
         const short4 l = d.ijk[v];
         set_df(pH.x, pL.x, l.x * m.nom_size + e.t.x);
@@ -425,7 +430,7 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
         const bool floorOn = rp.floor != 0;
         const Q4<float> o{qH.x, qH.y, qH.z, qH.w};
         V3<float> F = qrot(o, Fs);
-        if (xi >= 0) F = add(F, V3<float>{d.ext[xi].f[0], d.ext[xi].f[1], d.ext[xi].f[2]});  // external force
+        if (BC) F = add(F, V3<float>{d.ext[xi].f[0], d.ext[xi].f[1], d.ext[xi].f[2]});  // external force
         const V3<float> vel{(lH.x + lL.x) * m.mass_inv, (lH.y + lL.y) * m.mass_inv, (lH.z + lL.z) * m.mass_inv};
         F = sub(F, scl(vel, m.c_glob));
         F.z += m.grav_force;
@@ -479,7 +484,7 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
         df_add(pH.y, pL.y, tr.y);
         df_add(pH.z, pL.z, tr.z);
         V3<float> M = qrot(o, Ms);
-        if (xi >= 0) M = add(M, V3<float>{d.ext[xi].m[0], d.ext[xi].m[1], d.ext[xi].m[2]});  // external moment
+        if (BC) M = add(M, V3<float>{d.ext[xi].m[0], d.ext[xi].m[1], d.ext[xi].m[2]});  // external moment
         const V3<float> avel{(aH.x + aL.x) * m.mom_inv, (aH.y + aL.y) * m.mom_inv, (aH.z + aL.z) * m.mom_inv};
         M = sub(M, scl(avel, m.c_glob_rot));
         df_add(aH.x, aL.x, M.x * dtf);
@@ -505,7 +510,7 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
         df_add(qH.y, qL.y, delta.x);
         df_add(qH.z, qL.z, delta.y);
         df_add(qH.w, qL.w, delta.z);
-        if (dof) {  // fixed DOFs (VX3_Voxel.cu:222-257); a partial rotation fix follows in k_ext_rot_mixed
+        if (BC && dof) {  // fixed DOFs (VX3_Voxel.cu:222-257), in FP64 on the hi/lo pairs
             const ExtBC &e = d.ext[xi];
             if (dof & EXT_T) {
                 const short4 l = d.ijk[v];
@@ -513,12 +518,23 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
                 if (dof & 2) { set_df(pH.y, pL.y, l.y * m.nom_size + e.t.y); lH.y = lL.y = 0; }
                 if (dof & 4) { set_df(pH.z, pL.z, l.z * m.nom_size + e.t.z); lH.z = lL.z = 0; }
             }
-            if ((dof & EXT_R) == EXT_R) {
+            if ((dof & EXT_R) == EXT_R) {  // all rotations: the prescribed orientation
                 set_df(qH.x, qL.x, e.q.x);
                 set_df(qH.y, qL.y, e.q.y);
                 set_df(qH.z, qL.z, e.q.z);
                 set_df(qH.w, qL.w, e.q.w);
                 aH.x = aH.y = aH.z = aL.x = aL.y = aL.z = 0;
+            } else if (dof & EXT_R) {  // some: those rotation-vector components zeroed
+                V3<double> rv = to_rotvec(Q4<double>{(double)qH.x + qL.x, (double)qH.y + qL.y, (double)qH.z + qL.z,
+                                                     (double)qH.w + qL.w});
+                if (dof & 8) { rv.x = 0; aH.x = aL.x = 0; }
+                if (dof & 16) { rv.y = 0; aH.y = aL.y = 0; }
+                if (dof & 32) { rv.z = 0; aH.z = aL.z = 0; }
+                const Q4<double> q = from_rotvec(rv);
+                set_df(qH.x, qL.x, q.w);
+                set_df(qH.y, qL.y, q.x);
+                set_df(qH.z, qL.z, q.y);
+                set_df(qH.w, qL.w, q.z);
             }
         }
         const float pen2 = 0.5f * ((pH.w - m.nom_hi) + (pL.w - m.nom_lo)) - (pH.z + pL.z);
@@ -542,40 +558,14 @@ __device__ __forceinline__ void voxels_mixed_body(const Dev &d, int v, int parit
     P[2 * v + 1] = pL;
 }
 
-// Partial rotation fixes (VX3_Voxel.cu:242-256): some but not all rotational DOFs
-// fixed.  After the voxel pass, for the listed voxels that stepped: the orientation's
-// rotation vector (ToRotationVector) with the fixed components zeroed becomes the
-// orientation again (FromRotationVector), and those angular-momentum components are
-// zeroed; FP64 on the hi/lo pairs.  The static-friction zeroing of the voxel pass
-// touches only angular momentum, so doing this afterwards changes nothing else.
-__global__ void k_ext_rot_mixed(Dev d) {
+// the voxels with a boundary-condition external, after the main voxel pass
+__global__ void __launch_bounds__(128) k_voxels_bc_mixed(Dev d, int parity) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.nxrot) return;
-    const int v = d.xrot[i];
-    const uint2 vi = d.vinfo[v];
-    if (d.status[vi.x] != 0 || (vi.y & VF_FIXED) || d.dt[vi.x] == 0.0f) return;
-    const int dof = d.ext[d.vext[v]].dof;
-    float4 *Qa = reinterpret_cast<float4 *>(d.quat);
-    float4 *AM = reinterpret_cast<float4 *>(d.angmom);
-    float4 qH = Qa[2 * v], qL = Qa[2 * v + 1], aH = AM[2 * v], aL = AM[2 * v + 1];
-    V3<double> rv = to_rotvec(Q4<double>{(double)qH.x + qL.x, (double)qH.y + qL.y, (double)qH.z + qL.z,
-                                         (double)qH.w + qL.w});
-    if (dof & 8) { rv.x = 0; aH.x = aL.x = 0; }
-    if (dof & 16) { rv.y = 0; aH.y = aL.y = 0; }
-    if (dof & 32) { rv.z = 0; aH.z = aL.z = 0; }
-    const Q4<double> q = from_rotvec(rv);
-    set_df(qH.x, qL.x, q.w);
-    set_df(qH.y, qL.y, q.x);
-    set_df(qH.z, qL.z, q.y);
-    set_df(qH.w, qL.w, q.z);
-    Qa[2 * v] = qH;
-    Qa[2 * v + 1] = qL;
-    AM[2 * v] = aH;
-    AM[2 * v + 1] = aL;
+    if (i < d.nxbc) voxels_mixed_body<true>(d, d.xbc[i], parity);
 }
 
-void launch_ext_rot_mixed(const Dev &d, cudaStream_t s) {
-    if (d.nxrot) k_ext_rot_mixed<<<(d.nxrot + 127) / 128, 128, 0, s>>>(d);
+void launch_voxels_bc_mixed(const Dev &d, int parity, cudaStream_t s) {
+    if (d.nxbc) k_voxels_bc_mixed<<<(d.nxbc + 127) / 128, 128, 0, s>>>(d, parity);
 }
 
 // Launch-shape variants (threads per block, minimum resident blocks): the same body,
@@ -588,7 +578,7 @@ template <int TPB, int MINB> __global__ void __launch_bounds__(TPB, MINB) k_link
 }
 template <int TPB, int MINB> __global__ void __launch_bounds__(TPB, MINB) k_voxels_mixed(Dev d, int parity) {
     const int v = blockIdx.x * TPB + threadIdx.x;
-    if (v < d.nv) voxels_mixed_body(d, v, parity);
+    if (v < d.nv) voxels_mixed_body<false>(d, v, parity);
 }
 
 const LaunchShape kLinkShapes[kMixedShapes] = {{256, 1}, {256, 4}, {128, 9}, {128, 10}, {64, 20}, {256, 5}};
