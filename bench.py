@@ -145,6 +145,16 @@ def barrier_and_max(value, world):
     return float(t.item())
 
 
+def allreduce_sum(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def init_dist(world):
     if world > 1:
         import torch.distributed as dist
@@ -362,6 +372,9 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 run of the same window")
     ap.add_argument("--tune-cache", default=None, help="JSON cache of tuned launch shapes (read and appended)")
+    ap.add_argument("--shard", action="store_true",
+                    help="split the population across the ranks (robots [r*R/W, (r+1)*R/W) on rank r) "
+                         "instead of one replica per rank")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every step's kernels one by one instead of replaying CUDA graphs "
                          "(each launch then its own record in a per-kernel profiler)")
@@ -376,6 +389,12 @@ def main():
     dev = local
     desc, builder = WORKLOADS[args.workload]
     robots = builder()
+    n_total = len(robots)
+    if args.shard:  # this rank's contiguous range of the population; no data crosses ranks
+        lo, hi = workloads.shard(len(robots), rank, world)
+        robots = robots[lo:hi]
+        if not robots:
+            raise SystemExit(f"rank {rank}: no robots in its shard ({n_total} robots over {world} ranks)")
     prec = abi.PRECISION_MIXED if args.precision == "mixed" else abi.PRECISION_FP64
     W, K, C = args.warmup, args.steps, args.chunk
     G = -1 if args.no_graphs else args.graph_chunk
@@ -402,7 +421,9 @@ def main():
     total_ms = barrier_and_max(float(np.sum(per_chunk)), world)
     status = b.status()
     nv, nl = b.nv, b.nl
-    vox_steps = nv * C * K * world
+    # units all ranks processed: replicas each step the whole workload; shards their ranges
+    nv_job = allreduce_sum(float(nv), world) if args.shard else nv * world
+    vox_steps = nv_job * C * K
     value = vox_steps / (total_ms / 1e3)
     surf = b.surface()
     ns_coll = 0
@@ -469,24 +490,27 @@ def main():
     e2e_s = barrier_and_max(time.perf_counter() - t0, world)
     h2d = sum(a.nbytes for a in host.values())
     d2h = h2d + com.nbytes
-    e2e_value = b2.nv * C * K * world / e2e_s
+    e2e_value = nv_job * C * K / e2e_s
     b2.close()
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-        "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "strong" if args.shard else "weak",
+        "vs_baseline": None,
         "dtype": "f32 link forces + f64 integration" if prec else "f64", "data": "synthetic (seeded generator)",
-        "config": {"workload": desc, "robots": len(robots), "voxels": nv, "links": nl,
+        "config": {"workload": desc, "robots": n_total, "robots_on_rank0": len(robots), "voxels": nv, "links": nl,
                    "collision_surface_voxels": ns_coll, "precision": args.precision,
                    "physics_steps_per_bench_step": C, "window": f"physics steps 0-{K * C} of a fresh context "
                    f"(the configuration runs {CONFIG_STEPS[args.workload]})",
                    "cuda_graphs": not args.no_graphs, "graph_chunk": G,
                    "launch_shapes": {"links": shapes[:2], "voxels": shapes[2:]},
-                   "l2": "512 MB overwrite before every timed bench step", "parallelism": f"replicas x{world}"},
+                   "l2": "512 MB overwrite before every timed bench step",
+                   "parallelism": f"robot shards x{world} of {n_total} robots" if args.shard else f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "kernel_ms": kernel_ms, "pass_ms": passes, "algorithmic_bytes_per_launch": ab,
-                     "whole_step_algorithmic_gbs": (ab["links"] + ab["voxels"] + ab["collision"]) * C * K * world
+                     # this GPU's algorithmic bytes over the job time, against one GPU's peak
+                     "whole_step_algorithmic_gbs": (ab["links"] + ab["voxels"] + ab["collision"]) * C * K
                      / (total_ms / 1e3) / 1e9},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": kernels_per_step * C * K,

@@ -54,8 +54,10 @@ class VX3_SimulationManager {
                           std::filesystem::path in_input_dir, int in_num_of_devices);
     ~VX3_SimulationManager();
 
-    // Runs every sub-batch to its stop conditions; fills and sorts h_results.
-    // Throws std::runtime_error with the library's message on failure.
+    // Runs every sub-batch to its stop conditions, all at once: one host thread per
+    // sub-batch, each driving its own device (sub-batch i on device i, or devices[i]);
+    // fills and sorts h_results.  Throws std::runtime_error with the library's message
+    // on failure (the first failing sub-batch's, after all have finished).
     void start();
 
     std::vector<std::vector<std::filesystem::path>> sub_batches;
@@ -68,6 +70,10 @@ class VX3_SimulationManager {
     int precision = 0;           // VX3G_PRECISION_FP64 or VX3G_PRECISION_MIXED
     long max_steps = 1000000;    // CUDA_Simulation's loop bound
     FILE *history = stdout;      // history text sink when RecordStepSize > 0
+    std::vector<int> devices;    // device of each sub-batch (empty: sub-batch i on device i)
+
+  private:
+    std::vector<VX3_SimulationResult> run_sub_batch(int index, int device, const void *base_doc);
 };
 
 // Writes the vx3_node_worker report (src/Executables/vx3_node_worker.cu:98-141).

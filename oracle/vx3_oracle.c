@@ -482,7 +482,8 @@ typedef struct {
     double t, optimal_dt;
     float dt;
     int surface_stale, diverged;
-    int threads; /* > 1: timing mode, loops run under OpenMP */
+    int threads; /* > 1: loops run under OpenMP */
+    int exact;   /* with threads > 1: contact sums in the serial loop's order (else timing mode) */
     vxo_math_token *ff[3]; /* force-field programs (copies) or NULL */
     vec *cilia_base;       /* per voxel: BaseCiliaForce + 0 * ShiftCiliaForce (the signal stays 0), or NULL */
     int *mat_removed;      /* per material: removeVoxels has removed it (VX3_MaterialVoxel::removed) */
@@ -960,18 +961,21 @@ static int is_linked(const sim *S, int a, int b) {
 
 /* handle_collision_attachment (collision half) + VX3_Collision
  * (VX3_VoxelyzeKernel.cu:682-727, VX3_Collision.cu:3-31) */
-static void collide(sim *S, voxel *v1, voxel *v2, int i1, int i2) {
+/* the contact force of one surface pair (voxel1 = v1, the later in surface order), or 0
+ * where the reference's handle_collision_attachment leaves the pair before adding one
+ * (VX3_VoxelyzeKernel.cu:682-727, VX3_Collision.cu:3-31) */
+static int pair_force(const sim *S, const voxel *v1, const voxel *v2, int i1, int i2, double bsa1, double bsa2,
+                      vec *out) {
     const vmat *m1 = &S->vm[v1->mat], *m2 = &S->vm[v2->mat];
-    if (m1->fixed && m2->fixed) return;
+    if (m1->fixed && m2->fixed) return 0;
     vec diff = vsub(v1->pos, v2->pos);
-    double bsa1 = base_size_avg(S, v1), bsa2 = base_size_avg(S, v2);
     double wd = (bsa1 + bsa2) * 0.625;
-    if (diff.x > wd || diff.x < -wd) return;
-    if (diff.y > wd || diff.y < -wd) return;
-    if (diff.z > wd || diff.z < -wd) return;
-    if (vlen(diff) > wd) return;
-    if (is_linked(S, i1, i2)) return;
-    if (!S->r.enable_collision) return;
+    if (diff.x > wd || diff.x < -wd) return 0;
+    if (diff.y > wd || diff.y < -wd) return 0;
+    if (diff.z > wd || diff.z < -wd) return 0;
+    if (vlen(diff) > wd) return 0;
+    if (is_linked(S, i1, i2)) return 0;
+    if (!S->r.enable_collision) return 0;
     float k1 = (float)(2 * m1->E * m1->nom_size), k2 = (float)(2 * m2->E * m2->nom_size);
     double pstiff = 2.0f / (1.0f / k1 + 1.0f / k2);
     double dampC = 0.5f * (m1->z_col * m1->c2xSqMxExS + m2->z_col * m2->c2xSqMxExS);
@@ -984,8 +988,36 @@ static void collide(sim *S, voxel *v1, voxel *v2, int i1, int i2) {
         double rv = vdot(vscale(v1->linMom, m1->mass_inv), u) - vdot(vscale(v2->linMom, m2->mass_inv), u);
         f = vscale(u, pstiff * rel + dampC * rv);
     }
+    *out = f;
+    return 1;
+}
+
+static void collide(sim *S, voxel *v1, voxel *v2, int i1, int i2) {
+    vec f;
+    if (!pair_force(S, v1, v2, i1, i2, base_size_avg(S, v1), base_size_avg(S, v2), &f)) return;
     v1->contact = vadd(v1->contact, f);
     v2->contact = vadd(v2->contact, vneg(f));
+}
+
+/* The serial pair loop adds to the contact of surface voxel k first its pairs (k, b),
+ * b < k ascending, as voxel1, then the pairs (a, k), a > k ascending, as voxel2.  Each
+ * voxel gathers its own sum in that order here, so rows run in parallel with the serial
+ * loop's result bit for bit (every pair's force is evaluated once from each side). */
+static void collide_gather_threaded(sim *S) {
+    double *bsa = (double *)malloc(sizeof(double) * (S->ns ? S->ns : 1));
+    for (int k = 0; k < S->ns; k++) bsa[k] = base_size_avg(S, &S->v[S->surf[k]]);
+#pragma omp parallel for schedule(dynamic, 32)
+    for (int k = 0; k < S->ns; k++) {
+        const int ik = S->surf[k];
+        voxel *vk = &S->v[ik];
+        vec acc = vk->contact, f;
+        for (int b = 0; b < k; b++)
+            if (pair_force(S, vk, &S->v[S->surf[b]], ik, S->surf[b], bsa[k], bsa[b], &f)) acc = vadd(acc, f);
+        for (int a = k + 1; a < S->ns; a++)
+            if (pair_force(S, &S->v[S->surf[a]], vk, S->surf[a], ik, bsa[a], bsa[k], &f)) acc = vadd(acc, vneg(f));
+        vk->contact = acc;
+    }
+    free(bsa);
 }
 
 /* The same all-pairs loop with rows spread over threads (timing mode only:
@@ -1041,8 +1073,30 @@ static void remove_voxels(sim *S) {
 static int do_step(sim *S) {
     const vxo_robot *r = &S->r;
     /* gpu_update_temperature (:625-650) + setTemperature (VX3_Voxel.cu:107-113) */
-    if (r->vary_temp && r->temp_period > 0) {
-#pragma omp parallel for if (S->threads > 1) schedule(static)
+    if (r->vary_temp && r->temp_period > 0 && S->threads > 1) {
+        /* threaded: every temperature first, then every rest length (the values the serial
+         * loop leaves, each link's later end seeing both new temperatures) */
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < S->nv; i++) {
+            voxel *v = &S->v[i];
+            const vmat *m = &S->vm[v->mat];
+            if (v->removed || m->thermal_on_after > S->t || m->fixed) continue;
+            double T = r->temp_amplitude * sin(2 * 3.1415926f * (S->t / r->temp_period + v->phase));
+            if (!r->enable_expansion && T > 0) T = 0;
+            v->tempe = (float)T;
+        }
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < S->nl; i++) {
+            const link *L = &S->l[i];
+            const voxel *a = &S->v[L->neg], *b = &S->v[L->pos];
+            const vmat *ma = &S->vm[a->mat], *mb = &S->vm[b->mat];
+            int ua = !(a->removed || ma->thermal_on_after > S->t || ma->fixed);
+            int ub = !(b->removed || mb->thermal_on_after > S->t || mb->fixed);
+            int attached = 0;
+            for (int d = 0; d < 6; d++) attached |= (ua && a->links[d] == i) || (ub && b->links[d] == i);
+            if (attached) update_rest(S, &S->l[i]);
+        }
+    } else if (r->vary_temp && r->temp_period > 0) {
         for (int i = 0; i < S->nv; i++) {
             voxel *v = &S->v[i];
             const vmat *m = &S->vm[v->mat];
@@ -1084,7 +1138,8 @@ static int do_step(sim *S) {
     }
     /* gpu_update_attach (:833-843): pairs first > second in surface order */
     if (r->enable_collision) {
-        if (S->threads > 1) collide_rows_threaded(S, 0, S->ns);
+        if (S->threads > 1 && S->exact) collide_gather_threaded(S);
+        else if (S->threads > 1) collide_rows_threaded(S, 0, S->ns);
         else
             for (int a = 0; a < S->ns; a++)
                 for (int b = 0; b < a; b++) collide(S, &S->v[S->surf[a]], &S->v[S->surf[b]], S->surf[a], S->surf[b]);
@@ -1135,9 +1190,15 @@ int vxo_step(void *h, int n) {
 void vxo_set_threads(void *h, int n) {
     sim *S = (sim *)h;
     S->threads = n > 1 ? n : 1;
+    S->exact = 0;
 #ifdef _OPENMP
     if (n > 1) omp_set_num_threads(n);
 #endif
+}
+
+void vxo_set_exact_threads(void *h, int n) {
+    vxo_set_threads(h, n);
+    ((sim *)h)->exact = 1;
 }
 
 /* Seconds spent by the all-pairs collision loop over surface rows [begin, end)

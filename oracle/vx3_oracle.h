@@ -92,6 +92,9 @@ void vxo_com(void *h, double *c3);
 double vxo_recommended_dt(void *h);
 /* timing helpers for the CPU baseline (not used for parity) */
 void vxo_set_threads(void *h, int n);
+/* n threads with results bit-identical to the serial step (contact forces gathered per
+ * voxel in the serial loop's order); for large parity cases */
+void vxo_set_exact_threads(void *h, int n);
 double vxo_time_collision_rows(void *h, int begin, int end);
 int vxo_step_no_collision(void *h, int n);
 

@@ -120,6 +120,12 @@ class Sim:
         f.restype, f.argtypes = None, [ctypes.c_void_p, ctypes.c_int]
         f(self.h, n)
 
+    def set_exact_threads(self, n):
+        """Run the C restatement on n threads with results identical to the serial step."""
+        f = self.lib.vxo_set_exact_threads
+        f.restype, f.argtypes = None, [ctypes.c_void_p, ctypes.c_int]
+        f(self.h, n)
+
     def time_collision_rows(self, begin, end):
         f = self.lib.vxo_time_collision_rows
         f.restype, f.argtypes = ctypes.c_double, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]

@@ -160,6 +160,32 @@ def test_runner_boundary_conditions_match_oracle(tmp_path):
         assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size, name  # the regions acted
 
 
+def test_runner_sub_batches_run_concurrently(tmp_path):
+    """VX3_SimulationManager::start runs every sub-batch at once, one host thread and
+    context per device: four robots dealt round-robin into two sub-batches, both on
+    device 0 (one GPU here), give exactly the results of the single sub-batch run --
+    robots are independent, and a robot's result does not depend on its batch."""
+    vbuild.build()
+    exe = os.path.join(os.path.dirname(vbuild.LIB), "vx3g_sim")
+    rng = np.random.default_rng(31)
+    mats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=3e5, nu=0.35, cte=0.0)]
+    robots = [wl.bernoulli_body(rng, tuple(int(x) for x in rng.integers(4, 7, size=3)), 0.8, mats, random_phase=True,
+                                temp_vary=True, temp_amplitude=39.0, stop_time=0.02, fitness_x=True,
+                                enable_collision=bool(i % 2)) for i in range(4)]
+    (tmp_path / "base.vxa").write_text(wl.to_vxa(robots[0]))
+    for i, r in enumerate(robots):
+        (tmp_path / f"r{i}.vxd").write_text(wl.to_vxd(r))
+    reports = {}
+    for tag, extra in (("one", ["--devices", "1"]), ("two", ["--devices", "2", "--device-map", "0,0"])):
+        out = tmp_path / f"{tag}.xml"
+        p = subprocess.run([exe, "-i", str(tmp_path), "-o", str(out)] + extra, capture_output=True, text=True,
+                           timeout=600)
+        assert p.returncode == 0, p.stderr
+        reports[tag] = {n.tag: {c.tag: c.text for c in n if len(c) == 0} for n in ET.parse(out).getroot().find("detail")}
+    assert sorted(reports["one"]) == [f"r{i}" for i in range(4)]
+    assert reports["one"] == reports["two"]
+
+
 def test_runner_cilia_matches_oracle(tmp_path):
     """EnableCilia with Structure/BaseCiliaForce and ShiftCiliaForce rows and per-material
     Cilia / TurnOnCiliaAfterThisManySeconds, through the runner, against the oracle."""

@@ -11,6 +11,9 @@
 #include "../../include/vx3_simulation_manager.h"
 
 #include <algorithm>
+#include <exception>
+#include <mutex>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -496,11 +499,18 @@ VX3_SimulationManager::VX3_SimulationManager(std::vector<std::vector<fs::path>> 
 
 VX3_SimulationManager::~VX3_SimulationManager() {}
 
-void VX3_SimulationManager::start() {
-    auto base_doc = vx3g::xml::parse_file(base.string());
-    for (int dev = 0; dev < num_of_devices && dev < (int)sub_batches.size(); dev++) {
-        auto &files = sub_batches[dev];
-        if (files.empty()) continue;
+// One device's sub-batch: read (base VXA + each VXD), simulated as one vx3g batch until
+// every robot's stop condition holds, collected into result records.  Runs on its own
+// host thread (one per device); the history text of concurrent sub-batches is written
+// under one lock, a record at a time.
+static std::mutex g_history_lock;
+
+std::vector<VX3_SimulationResult> VX3_SimulationManager::run_sub_batch(int index, int dev, const void *base_doc_p) {
+    const Node *base_doc = static_cast<const Node *>(base_doc_p);
+    std::vector<VX3_SimulationResult> h_results;
+    {
+        auto &files = sub_batches[index];
+        if (files.empty()) return h_results;
         std::vector<std::unique_ptr<RobotSpec>> specs;
         for (auto &f : files) {
             auto S = std::make_unique<RobotSpec>();
@@ -632,7 +642,10 @@ void VX3_SimulationManager::start() {
                 check(vx3g_time(ctx, t.data()), "vx3g_time");
                 const long j = loop + chunk - 1;
                 for (int r = 0; r < R; r++)
-                    if (stride[r] && !done[r] && j % stride[r] == 0) print_history(this->history, ctx, r, *specs[r], j, t[r], voff, loff);
+                    if (stride[r] && !done[r] && j % stride[r] == 0) {
+                        std::lock_guard<std::mutex> g(g_history_lock);
+                        print_history(this->history, ctx, r, *specs[r], j, t[r], voff, loff);
+                    }
             }
             loop += chunk;
         }
@@ -689,6 +702,34 @@ void VX3_SimulationManager::start() {
         }
         vx3g_destroy(ctx);
     }
+    return h_results;
+}
+
+// All sub-batches at once, one host thread (and so one CUDA context stream) per device,
+// as the reference launches every device's kernel before its one synchronisation
+// (VX3_SimulationManager.cu:138-155); the results are merged in sub-batch order and sorted.
+void VX3_SimulationManager::start() {
+    auto base_doc = vx3g::xml::parse_file(base.string());
+    const int n = std::min(num_of_devices, (int)sub_batches.size());
+    if (!devices.empty() && (int)devices.size() < n)
+        throw std::runtime_error("devices: one device per sub-batch is needed");
+    std::vector<std::vector<VX3_SimulationResult>> per(n);
+    std::vector<std::exception_ptr> errs(n);
+    std::vector<std::thread> threads;
+    for (int i = 0; i < n; i++) {
+        const int dev = devices.empty() ? i : devices[i];
+        threads.emplace_back([this, i, dev, &per, &errs, &base_doc] {
+            try {
+                per[i] = run_sub_batch(i, dev, base_doc.get());
+            } catch (...) {
+                errs[i] = std::current_exception();
+            }
+        });
+    }
+    for (auto &t : threads) t.join();
+    for (auto &e : errs)
+        if (e) std::rethrow_exception(e);
+    for (auto &v : per) h_results.insert(h_results.end(), v.begin(), v.end());
     std::sort(h_results.begin(), h_results.end(), VX3_SimulationResult::compareFitnessScore);
 }
 

@@ -368,6 +368,19 @@ def to_vxa(r: Robot) -> str:
     return "\n".join(out)
 
 
+# ------------------------------------------------------------------ sharding
+def shard(n_robots: int, rank: int, world: int):
+    """The contiguous robot range [lo, hi) that rank `rank` of `world` simulates when a
+    population is split across GPUs: robots are independent (no inter-robot forces), so
+    each rank steps its range as a batch of its own and no data crosses ranks.  The
+    ranges cover 0..n_robots-1 exactly once, in order, sizes differing by at most one."""
+    if world <= 0 or not 0 <= rank < world:
+        raise ValueError("rank must lie in [0, world)")
+    base, extra = divmod(n_robots, world)
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
+
+
 # ------------------------------------------------------------------ named workloads
 def c1_block_drop() -> List[Robot]:
     """Plain FP64 reference method: 10x10x10 solid block (E=1e6 Pa, Poisson 0.35,
