@@ -209,7 +209,8 @@ int vx3g_get_voxel_aux(vx3g_ctx *ctx, float *tempe, int32_t *flags, double *cont
 /* Link state in the reference's link order: strain, maxStrain (float),
  * local9 = pos2, angle1v, angle2v (9 doubles), forces12 = forceNeg, forcePos,
  * momentNeg, momentPos (12 doubles), small = small-angle flag (bit 0) | 2 once the
- * link has left the lattice (detached or removed: no voxel's link any more). */
+ * link has left the lattice (detached or removed: no voxel's link any more) | 4 while
+ * its local velocity is valid (LOCAL_VELOCITY_VALID: the damping terms apply). */
 int vx3g_get_links(vx3g_ctx *ctx, float *strain, float *max_strain, double *local9, double *forces12,
                    int32_t *small);
 /* Topology: voxel lattice indices (3 ints), voxel palette index (0-based),

@@ -1004,20 +1004,36 @@ static void collide(sim *S, voxel *v1, voxel *v2, int i1, int i2) {
  * voxel gathers its own sum in that order here, so rows run in parallel with the serial
  * loop's result bit for bit (every pair's force is evaluated once from each side). */
 static void collide_gather_threaded(sim *S) {
-    double *bsa = (double *)malloc(sizeof(double) * (S->ns ? S->ns : 1));
-    for (int k = 0; k < S->ns; k++) bsa[k] = base_size_avg(S, &S->v[S->surf[k]]);
+    /* surface positions and base sizes, compact, for the box test that rejects most pairs
+     * (the same doubles and comparisons as pair_force, which repeats them for the rest) */
+    const int ns = S->ns;
+    double *c = (double *)malloc(sizeof(double) * 4 * (ns ? ns : 1));
+    for (int k = 0; k < ns; k++) {
+        const voxel *v = &S->v[S->surf[k]];
+        c[4 * k] = v->pos.x; c[4 * k + 1] = v->pos.y; c[4 * k + 2] = v->pos.z;
+        c[4 * k + 3] = base_size_avg(S, v);
+    }
 #pragma omp parallel for schedule(dynamic, 32)
-    for (int k = 0; k < S->ns; k++) {
+    for (int k = 0; k < ns; k++) {
         const int ik = S->surf[k];
         voxel *vk = &S->v[ik];
+        const double *ck = c + 4 * k;
         vec acc = vk->contact, f;
-        for (int b = 0; b < k; b++)
-            if (pair_force(S, vk, &S->v[S->surf[b]], ik, S->surf[b], bsa[k], bsa[b], &f)) acc = vadd(acc, f);
-        for (int a = k + 1; a < S->ns; a++)
-            if (pair_force(S, &S->v[S->surf[a]], vk, S->surf[a], ik, bsa[a], bsa[k], &f)) acc = vadd(acc, vneg(f));
+        for (int b = 0; b < k; b++) {  /* (k, b): k is voxel1 */
+            const double *cb = c + 4 * b;
+            double wd = (ck[3] + cb[3]) * 0.625, dx = ck[0] - cb[0], dy = ck[1] - cb[1], dz = ck[2] - cb[2];
+            if (dx > wd || dx < -wd || dy > wd || dy < -wd || dz > wd || dz < -wd) continue;
+            if (pair_force(S, vk, &S->v[S->surf[b]], ik, S->surf[b], ck[3], cb[3], &f)) acc = vadd(acc, f);
+        }
+        for (int a = k + 1; a < ns; a++) {  /* (a, k): k is voxel2 */
+            const double *ca = c + 4 * a;
+            double wd = (ca[3] + ck[3]) * 0.625, dx = ca[0] - ck[0], dy = ca[1] - ck[1], dz = ca[2] - ck[2];
+            if (dx > wd || dx < -wd || dy > wd || dy < -wd || dz > wd || dz < -wd) continue;
+            if (pair_force(S, &S->v[S->surf[a]], vk, S->surf[a], ik, ca[3], ck[3], &f)) acc = vadd(acc, vneg(f));
+        }
         vk->contact = acc;
     }
-    free(bsa);
+    free(c);
 }
 
 /* The same all-pairs loop with rows spread over threads (timing mode only:
@@ -1255,6 +1271,55 @@ void vxo_set_voxels(void *h, const double *pos, const double *orient, const doub
         v->orient = Q(orient[4 * i], orient[4 * i + 1], orient[4 * i + 2], orient[4 * i + 3]);
         v->linMom = V(linmom[3 * i], linmom[3 * i + 1], linmom[3 * i + 2]);
         v->angMom = V(angmom[3 * i], angmom[3 * i + 1], angmom[3 * i + 2]);
+    }
+}
+
+/* The rest of a run's state, to continue another implementation's run: time,
+ * per voxel the temperature of the last step and the static-friction flag, per link
+ * pos2/angle1v/angle2v, strain, maxStrain and flags (bit 0 smallAngle, bit 2
+ * LOCAL_VELOCITY_VALID).  The time step stays the one recommended for the created
+ * (unstrained) robot, as in a run from the start; voxels that stepped have it as
+ * previousDt; rest lengths follow the temperatures. */
+void vxo_set_run_state(void *h, double t, const float *tempe, const int *static_flag, const double *local9,
+                       const float *strain, const float *maxstrain, const int *link_flags) {
+    sim *S = (sim *)h;
+    if (!S->optimal_dt) {
+        /* as the first step takes it: after the temperatures of time 0 (do_step) */
+        const vxo_robot *r = &S->r;
+        if (r->vary_temp && r->temp_period > 0)
+            for (int i = 0; i < S->nv; i++) {
+                voxel *v = &S->v[i];
+                const vmat *m = &S->vm[v->mat];
+                if (v->removed || m->thermal_on_after > 0.0 || m->fixed) continue;
+                double T = r->temp_amplitude * sin(2 * 3.1415926f * (0.0 / r->temp_period + v->phase));
+                if (!r->enable_expansion && T > 0) T = 0;
+                v->tempe = (float)T;
+            }
+        for (int i = 0; i < S->nl; i++) update_rest(S, &S->l[i]);
+        S->optimal_dt = vxo_recommended_dt(S);
+    }
+    if (S->optimal_dt < 1e-10) S->optimal_dt = 1e-10;
+    float dt = S->r.dt_frac * S->optimal_dt;
+    S->dt = dt;
+    S->t = t;
+    for (int i = 0; i < S->nv; i++) {
+        voxel *v = &S->v[i];
+        v->tempe = tempe[i];
+        v->flags = static_flag[i] ? (v->flags | F_STATIC) : (v->flags & ~F_STATIC);
+        v->prevDt = S->vm[v->mat].fixed ? 0.0f : dt;
+        v->contact = V(0, 0, 0);
+    }
+    for (int i = 0; i < S->nl; i++) {
+        link *L = &S->l[i];
+        const double *q = local9 + 9 * (size_t)i;
+        L->pos2 = V(q[0], q[1], q[2]);
+        L->a1v = V(q[3], q[4], q[5]);
+        L->a2v = V(q[6], q[7], q[8]);
+        L->strain = strain[i];
+        L->maxStrain = maxstrain[i];
+        L->small = link_flags[i] & 1;
+        L->states = (link_flags[i] & 4) ? (L->states | L_LVV) : (L->states & ~L_LVV);
+        update_rest(S, L);
     }
 }
 

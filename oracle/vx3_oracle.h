@@ -75,6 +75,10 @@ double vxo_time(void *h);
 float vxo_dt(void *h);
 void vxo_voxels(void *h, double *pos, double *orient, double *linmom, double *angmom, float *tempe, int *flags);
 void vxo_set_voxels(void *h, const double *pos, const double *orient, const double *linmom, const double *angmom);
+/* the rest of a run's state (time, temperatures, static friction, link state) to continue
+ * a run taken elsewhere: link_flags bit 0 smallAngle, bit 2 LOCAL_VELOCITY_VALID */
+void vxo_set_run_state(void *h, double t, const float *tempe, const int *static_flag, const double *local9,
+                       const float *strain, const float *maxstrain, const int *link_flags);
 void vxo_topology(void *h, int *mat, int *ijk, int *slots);
 void vxo_link_topology(void *h, int *negpos, int *axis, int *small, int *states);
 void vxo_links(void *h, float *strain, float *maxstrain, double *rest, double *local9, double *forces12);

@@ -120,6 +120,20 @@ class Sim:
         f.restype, f.argtypes = None, [ctypes.c_void_p, ctypes.c_int]
         f(self.h, n)
 
+    def set_state(self, pos, orient, linmom, angmom, t, tempe, static_flag, local9, strain, maxstrain, link_flags):
+        """Continue a run taken elsewhere: voxel state, time, temperatures, static friction,
+        link state (link_flags bit 0 smallAngle, bit 2 LOCAL_VELOCITY_VALID)."""
+        c = lambda a, t_: np.ascontiguousarray(a, t_)  # noqa: E731
+        arrs = [c(pos, np.float64), c(orient, np.float64), c(linmom, np.float64), c(angmom, np.float64)]
+        f = self.lib.vxo_set_voxels
+        f.restype, f.argtypes = None, [ctypes.c_void_p] * 5
+        f(self.h, *[_P(a) for a in arrs])
+        more = [c(tempe, np.float32), c(static_flag, np.int32), c(local9, np.float64), c(strain, np.float32),
+                c(maxstrain, np.float32), c(link_flags, np.int32)]
+        g = self.lib.vxo_set_run_state
+        g.restype, g.argtypes = None, [ctypes.c_void_p, ctypes.c_double] + [ctypes.c_void_p] * 6
+        g(self.h, float(t), *[_P(a) for a in more])
+
     def set_exact_threads(self, n):
         """Run the C restatement on n threads with results identical to the serial step."""
         f = self.lib.vxo_set_exact_threads

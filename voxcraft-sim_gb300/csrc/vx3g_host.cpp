@@ -1047,7 +1047,7 @@ int vx3g_get_links(vx3g_ctx *c, float *strain, float *max_strain, double *local9
     for (size_t l = 0; l < nl; l++) {
         if (strain) strain[l] = sm[l].x;
         if (max_strain) max_strain[l] = sm[l].y;
-        if (small) small[l] = ((li[l].y & LF_SMALL) ? 1 : 0) | ((li[l].y & LF_GONE) ? 2 : 0);
+        if (small) small[l] = ((li[l].y & LF_SMALL) ? 1 : 0) | ((li[l].y & LF_GONE) ? 2 : 0) | ((li[l].y & LF_LVV) ? 4 : 0);
         if (local9)
             for (int k = 0; k < 9; k++) local9[9 * l + k] = rd(ls, (size_t)k * nl + l);
         if (forces12) {
