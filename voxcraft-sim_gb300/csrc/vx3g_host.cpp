@@ -745,6 +745,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         (rc = c->alloc(&d.hblock, hs / 1024)) || (rc = c->alloc(&d.lwork, (size_t)d.nr)) || (rc = c->upload(&d.cpk, cpk)) ||
         (rc = c->alloc(&d.lwork_ctr, 1)))
         return rc;
+    d.crec = nullptr;
+    if (d.mixed && d.ns && (rc = c->alloc(&d.crec, 3 * (size_t)d.nv))) return rc;
     CU(init_collision(d));
     if (d.mixed && d.ns) {
         CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));

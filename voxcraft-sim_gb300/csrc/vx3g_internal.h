@@ -153,6 +153,11 @@ struct Dev {
     int *csurf;     // collision surface list (global voxel index), NS entries
     int4 *ccell;    // x: the bucket of a collision-surface voxel in the large-robot grid (-1: not binned)
     float4 *cposf;  // FP32 position per collision-surface voxel, written by the displacement check
+    // mixed precision: per voxel, the contact record of the collision-surface voxels for this
+    // step, written by the displacement check: [3v] {position hi x, y, z; base size},
+    // [3v+1] {position lo x, y, z; penetrationStiffness}, [3v+2] {velocity (linMom hi / m);
+    // collision damping} -- one contiguous read per contact candidate (NULL in FP64)
+    float4 *crec;
     unsigned *cpk;  // per collision-surface voxel: packed lattice word (kPackMask, kPackFixed; shared-memory path)
     float4 *cref;   // position at the last list build (w: squared displacement that forces a rebuild)
     int *nbr;       // candidate lists, slot-major [kNbrCap][NS]: partner voxel indices, ascending

@@ -118,35 +118,32 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
     const int n = d.nnb[s];
     const int *lst = d.nbr + s;  // slot-major: entry k at lst[k*ns]
     const size_t ns = (size_t)d.ns;
-    const float4 *P = reinterpret_cast<const float4 *>(d.pos);
-    const float4 *LM = reinterpret_cast<const float4 *>(d.linmom);
+    const float4 *R = d.crec;  // contact records of this step (written by the displacement check)
     V3<float> acc{0, 0, 0};
     if (n) {
-        const float4 pvH = P[2 * v], pvL = P[2 * v + 1];
-        const float bv = pvH.w + pvL.w;  // baseSizeAverage = baseSize (isotropic)
-        const VMat &mv = d.vmat[vi.y >> 8];
+        const float4 pvH = R[3 * v], pvL = R[3 * v + 1], wv = R[3 * v + 2];
+        const float bv = pvH.w;  // baseSizeAverage = baseSize (isotropic)
         for (int k = 0; k < n; k++) {
             const int u = lst[k * ns];  // partner voxel, ascending
-            const float4 puH = P[2 * u], puL = P[2 * u + 1];
+            const float4 puH = R[3 * u], puL = R[3 * u + 1];
             // offset from the later surface voxel (voxel1) to the earlier one (voxel2)
             const float sg = u < v ? 1.0f : -1.0f;
             const float ox = sg * df_diff(puH.x, puL.x, pvH.x, pvL.x);
             const float oy = sg * df_diff(puH.y, puL.y, pvH.y, pvL.y);
             const float oz = sg * df_diff(puH.z, puL.z, pvH.z, pvL.z);
-            const float bu = puH.w + puL.w;
+            const float bu = puH.w;
             const float wd = (bv + bu) * 0.625f;
             const float dist = sqrtf(ox * ox + oy * oy + oz * oz);
             if (!(dist <= wd)) continue;
             const float rel = wd - dist;
             if (!(rel > 0)) continue;
-            const VMat &mu = d.vmat[d.vinfo[u].y >> 8];
-            const float pstiff = 2.0f / (1.0f / mv.pstiff + 1.0f / mu.pstiff);
-            const float dampC = 0.5f * (mv.c_col + mu.c_col);
+            const float4 wu = R[3 * u + 2];
+            const float pstiff = 2.0f / (1.0f / pvL.w + 1.0f / puL.w);
+            const float dampC = 0.5f * (wv.w + wu.w);
             const float inv = 1.0f / dist;
             const float ux = ox * inv, uy = oy * inv, uz = oz * inv;
-            const float4 lvH = LM[2 * v], luH = LM[2 * u];
-            const float w1x = lvH.x * mv.mass_inv, w1y = lvH.y * mv.mass_inv, w1z = lvH.z * mv.mass_inv;
-            const float w2x = luH.x * mu.mass_inv, w2y = luH.y * mu.mass_inv, w2z = luH.z * mu.mass_inv;
+            const float w1x = wv.x, w1y = wv.y, w1z = wv.z;
+            const float w2x = wu.x, w2y = wu.y, w2z = wu.z;
             // voxel1 = the later one: rv = w1.u - w2.u with (1, 2) = (v, u) when u < v, else (u, v)
             const float rv = sg * ((w1x * ux + w1y * uy + w1z * uz) - (w2x * ux + w2y * uy + w2z * uz));
             const float f = pstiff * rel + dampC * rv;
