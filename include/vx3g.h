@@ -79,6 +79,11 @@ typedef struct vx3g_material {
     int n_data;              /* model 3: SSData NumDataPts (a leading (0,0) point is skipped), at most
                                 VX3G_MAX_MODEL_POINTS */
     const double *strain_data, *stress_data; /* model 3: SSData StrainData / StressData values */
+    int is_pacemaker;         /* isPaceMaker: with enable_signals, emits a signal of 100 every pacemaker_period s */
+    double pacemaker_period;  /* PaceMakerPeriod (s) */
+    double signal_value_decay; /* signalValueDecay: a received signal is passed on scaled by this (VXA default 0.9) */
+    double signal_time_delay; /* signalTimeDelay (s): delay before a voxel passes a signal on (VXA default 0.03) */
+    double inactive_period;   /* inactivePeriod (s): refractory time after a signal (VXA default 0.03) */
 } vx3g_material;
 #define VX3G_MAX_MODEL_POINTS 32
 
@@ -161,6 +166,12 @@ typedef struct vx3g_robot_desc {
     int n_bcs;                      /* Environment/Boundary_Conditions regions, applied in order */
     const vx3g_bc_region *bcs;      /* (the lattice's cells are vox_size cubes: Lattice_Dim with all
                                        dimension adjustments 1 and no line or layer offsets) */
+    int enable_signals;             /* Simulator/EnableSignals: pacemaker voxels emit signals that spread
+                                       along links, decaying; a voxel's signal scales its ShiftCiliaForce
+                                       (VX3_Voxel.cu:271-348, VX3_VoxelyzeKernel.cu:857).  The reference
+                                       lets each voxel thread write its neighbours' signal state without
+                                       synchronisation; here voxels take their turns in voxel order, the
+                                       order of a serial loop over the voxel pass */
 } vx3g_robot_desc;
 
 typedef struct vx3g_batch_desc {
@@ -217,6 +228,8 @@ int vx3g_get_links(vx3g_ctx *ctx, float *strain, float *max_strain, double *loca
  * link ends (neg, pos voxel indices, packed global), link axis (0 x, 1 y, 2 z). */
 int vx3g_get_topology(vx3g_ctx *ctx, int32_t *voxel_ijk, int32_t *voxel_mat, int32_t *link_ends,
                       int32_t *link_axis);
+/* Per voxel: its localSignal (VX3_Voxel::localSignal; 0 in robots without signals). */
+int vx3g_get_signals(vx3g_ctx *ctx, double *local_signal);
 /* Surface voxels (fewer than six links, not removed), global voxel indices in voxel
  * order; with enable_detach or secondary_experiment the set follows the link table
  * (vx3g_counts gives its current size). */

@@ -106,6 +106,10 @@ void build_kernel(RefSim &S) {
         VX3_Voxel tmp(Vx.voxel(i), k);
         memcpy((void *)(k->d_voxels + i), (void *)&tmp, sizeof(VX3_Voxel));
         tmp.ext = NULL; // ownership moved to the array copy
+        // the constructor leaves the pending signal uninitialised (VX3_Voxel.cu:10-14); a
+        // voxel starts with none here, as the other signal members start at 0 (VX3_Voxel.h:306-309)
+        k->d_voxels[i].d_signal.value = 0.0;
+        k->d_voxels[i].d_signal.activeTime = 0.0;
     }
     k->DtFrac = S.sim.DtFrac;
     k->TempEnabled = S.sim.pEnv->IsTempEnabled();
@@ -389,6 +393,13 @@ void vx3ref_set_cilia(void *h, int enable) { ((RefSim *)h)->k->EnableCilia = ena
 void vx3ref_set_detach(void *h, int enable) { ((RefSim *)h)->k->enableDetach = enable != 0; }
 // VXA.Simulator.SecondaryExperiment (VX3_SimulationManager.cu:364)
 void vx3ref_set_secondary(void *h, int enable) { ((RefSim *)h)->k->SecondaryExperiment = enable; }
+// VXA.Simulator.EnableSignals (VX3_SimulationManager.cu:361)
+void vx3ref_set_signals(void *h, int enable) { ((RefSim *)h)->k->EnableSignals = enable; }
+// per voxel: localSignal
+void vx3ref_signals(void *h, double *out) {
+    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    for (int i = 0; i < k->num_d_voxels; i++) out[i] = k->d_voxels[i].localSignal;
+}
 
 void vx3ref_destroy(void *h) { /* the reference frees nothing reliably either; leak in tests */ (void)h; }
 

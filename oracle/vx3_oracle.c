@@ -301,6 +301,8 @@ typedef struct {
     double thermal_on_after;
     double cilia, cilia_on_after; /* Cilia, TurnOnCiliaAfterThisManySeconds (VX_Object.cpp:1429,1437) */
     double remove_after;          /* RemoveFromSimulationAfterThisManySeconds (VX_Object.cpp:1427) */
+    int pacemaker;                /* isPaceMaker */
+    double pace_period, sig_decay, sig_delay, inactive; /* PaceMakerPeriod, signalValueDecay, signalTimeDelay, inactivePeriod */
 } vmat;
 
 typedef struct {
@@ -336,6 +338,11 @@ static void vmat_import(vmat *m, const vxo_material *in, const vxo_robot *r) {
     memset(m, 0, sizeof(*m));
     m->cilia = in->cilia;
     m->cilia_on_after = in->cilia_on_after;
+    m->pacemaker = in->is_pacemaker;
+    m->pace_period = in->pacemaker_period;
+    m->sig_decay = in->signal_value_decay;
+    m->sig_delay = in->signal_time_delay;
+    m->inactive = in->inactive_period;
     m->remove_after = in->remove_after;
     /* the model as CVX_Sim::CopyMat sets it (VX_Sim.cpp:390-409) */
     int ok = 0;
@@ -457,6 +464,10 @@ typedef struct {
     int flags;
     int removed; /* removeVoxels (SecondaryExperiment): no longer stepped, linked or collided */
     double phase;
+    /* signals (VX3_Voxel.h:304-309): localSignal, localSignaldt, packmakerNextPulse,
+     * inactiveUntil, the pending signal d_signal {value, activeTime}; all 0 at the start */
+    double sig_local, sig_local_dt, pace_next, inactive_until, sig_value, sig_active;
+    int stepped; /* reached the end of timeStep this step (signals run only there) */
 } voxel;
 
 typedef struct {
@@ -485,7 +496,8 @@ typedef struct {
     int threads; /* > 1: loops run under OpenMP */
     int exact;   /* with threads > 1: contact sums in the serial loop's order (else timing mode) */
     vxo_math_token *ff[3]; /* force-field programs (copies) or NULL */
-    vec *cilia_base;       /* per voxel: BaseCiliaForce + 0 * ShiftCiliaForce (the signal stays 0), or NULL */
+    vec *cilia_base;       /* per voxel: BaseCiliaForce, or NULL */
+    vec *cilia_shift;      /* per voxel: ShiftCiliaForce (scaled by localSignal), or NULL */
     int *mat_removed;      /* per material: removeVoxels has removed it (VX3_MaterialVoxel::removed) */
     vext *ext;             /* per voxel: boundary-condition externals, or NULL without regions */
 } sim;
@@ -630,12 +642,14 @@ void *vxo_create(const vxo_robot *r) {
     }
     if (r->enable_cilia) { /* VX_Sim.cpp:102-105: per-voxel cilia vectors in voxel order */
         S->cilia_base = (vec *)calloc(S->nv ? S->nv : 1, sizeof(vec));
+        S->cilia_shift = (vec *)calloc(S->nv ? S->nv : 1, sizeof(vec));
         for (int c = 0; c < ncell; c++) {
             if (vid[c] < 0) continue;
             vec b = V(0, 0, 0), sh = V(0, 0, 0);
             if (r->cilia_base) b = V(r->cilia_base[3 * c], r->cilia_base[3 * c + 1], r->cilia_base[3 * c + 2]);
             if (r->cilia_shift) sh = V(r->cilia_shift[3 * c], r->cilia_shift[3 * c + 1], r->cilia_shift[3 * c + 2]);
-            S->cilia_base[vid[c]] = vadd(b, vscale(sh, 0.0)); /* base + localSignal * shift, signal 0 */
+            S->cilia_base[vid[c]] = b;
+            S->cilia_shift[vid[c]] = sh;
         }
     }
     free(vid);
@@ -699,7 +713,7 @@ void vxo_destroy(void *h) {
     sim *S = (sim *)h;
     if (!S) return;
     free(S->vm); free(S->lm); free(S->v); free(S->l); free(S->surf); free(S->last_contact);
-    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]); free(S->cilia_base); free(S->mat_removed); free(S->ext);
+    free(S->ff[0]); free(S->ff[1]); free(S->ff[2]); free(S->cilia_base); free(S->cilia_shift); free(S->mat_removed); free(S->ext);
     free(S);
 }
 
@@ -834,6 +848,7 @@ static void voxel_update(sim *S, voxel *v, float dtf) {
     const vmat *m = &S->vm[v->mat];
     double dt = dtf;
     v->prevDt = (float)dt;
+    v->stepped = 0;
     if (dt == 0.0f) return;
     const vext *ex = S->ext && S->ext[v - S->v].any ? &S->ext[v - S->v] : NULL;
     if (ex && ex->dof == 0x3F) { /* isFixedAll (VX3_Voxel.cu:167-173) */
@@ -861,7 +876,7 @@ static void voxel_update(sim *S, voxel *v, float dtf) {
          * (VX3_VoxelyzeKernel.cu:846-859) for surface voxels, before the voxel pass */
         vec cf = V(0, 0, 0);
         if (S->cilia_base && !(v->flags & F_SURFACE) && m->cilia != 0 && !(m->cilia_on_after > S->t))
-            cf = qrot(v->orient, S->cilia_base[v - S->v]);
+            cf = qrot(v->orient, vadd(S->cilia_base[v - S->v], vscale(S->cilia_shift[v - S->v], v->sig_local)));
         F = vadd(F, vscale(cf, m->cilia));
     }
     /* force field (VX3_Voxel.cu:178-184; constant 0 unless the VXA gives one) */
@@ -918,6 +933,52 @@ static void voxel_update(sim *S, voxel *v, float dtf) {
     }
     if ((v->flags & F_FLOOR) && floor_pen(S, v) >= 0) {
         if (v->flags & F_STATIC) v->angMom = V(0, 0, 0);
+    }
+    v->stepped = 1;
+}
+
+/* ------------------------------------------------------------------ signals */
+/* VX3_Voxel::receiveSignal (VX3_Voxel.cu:301-322): the receiving voxel's material */
+static void sig_receive(sim *S, voxel *v, double value, double active_time, int force) {
+    const vmat *m = &S->vm[v->mat];
+    if (!force && v->inactive_until > active_time) return;
+    if (value < 0.1) return;
+    v->inactive_until = active_time + m->inactive;
+    v->sig_local = value;
+    v->sig_value = value * m->sig_decay;
+    if (v->sig_value < 0.1) v->sig_value = 0;
+    v->sig_active = active_time;
+}
+
+/* the end of VX3_Voxel::timeStep with EnableSignals (VX3_Voxel.cu:271-276): propagateSignal
+ * (:323-348; to the voxel at the other end of each link, in direction order), packMaker
+ * (:291-299), localSignalDecay (:279-289).  They change only signal state, which the step's
+ * physics does not read, so running them for every voxel in voxel order after the voxel
+ * pass is the serial loop's result. */
+static void voxel_signals(sim *S, voxel *v) {
+    const vmat *m = &S->vm[v->mat];
+    const double t = S->t;
+    if (!(v->sig_active > t) && !(v->sig_value < 0.1)) {
+        for (int d = 0; d < 6; d++) {
+            if (v->links[d] < 0) continue;
+            const link *L = &S->l[v->links[d]];
+            voxel *o = &S->v[(&S->v[L->neg] == v) ? L->pos : L->neg];
+            sig_receive(S, o, v->sig_value, t + m->sig_delay, 0);
+        }
+        v->sig_value = 0;
+        v->sig_active = 0;
+        v->inactive_until = t + 2 * m->sig_delay + m->inactive;
+    }
+    if (m->pacemaker && !(v->pace_next > t)) {
+        sig_receive(S, v, 100, t, 1);
+        v->pace_next = t + m->pace_period;
+    }
+    if (!(v->sig_local_dt > t)) {
+        if (v->sig_local < 0.1) v->sig_local = 0;
+        else {
+            v->sig_local = v->sig_local * 0.9;
+            v->sig_local_dt = t + 0.01;
+        }
     }
 }
 
@@ -1188,9 +1249,17 @@ static int do_step(sim *S) {
         if (S->vm[S->v[i].mat].fixed) continue;
         voxel_update(S, &S->v[i], dt);
     }
+    if (r->enable_signals)  /* in voxel order, after the voxel pass (see voxel_signals) */
+        for (int i = 0; i < S->nv; i++)
+            if (S->v[i].stepped && !S->v[i].removed && !S->vm[S->v[i].mat].fixed) voxel_signals(S, &S->v[i]);
     if (r->secondary_experiment) remove_voxels(S);
     S->t += dt;
     return 1;
+}
+
+void vxo_signals(void *h, double *out) {
+    sim *S = (sim *)h;
+    for (int i = 0; i < S->nv; i++) out[i] = S->v[i].sig_local;
 }
 
 int vxo_step(void *h, int n) {

@@ -28,6 +28,8 @@ typedef struct vxo_material {
     double plastic_mod, yield_stress; /* Plastic_Mod, Yield_Stress (model 2, MDL_BILINEAR) */
     int n_data;                       /* model 3 (MDL_DATA): SSData points */
     const double *strain_data, *stress_data;
+    int is_pacemaker;                 /* isPaceMaker */
+    double pacemaker_period, signal_value_decay, signal_time_delay, inactive_period;
 } vxo_material;
 
 /* A math-tree token (VX3_MathTreeToken, src/Utils/VX3_MathTree.h:29-36): op is the
@@ -65,6 +67,7 @@ typedef struct vxo_robot {
     int secondary_experiment;             /* Simulator/SecondaryExperiment: material removal */
     int n_bcs;                            /* Environment/Boundary_Conditions regions */
     const vxo_bc_region *bcs;
+    int enable_signals;                   /* Simulator/EnableSignals */
 } vxo_robot;
 
 void *vxo_create(const vxo_robot *r);
@@ -90,6 +93,8 @@ void vxo_surface(void *h, int *idx);
  * reference's device copy holds them (0, 0, then the model's points from (0,0) on; at
  * most cap copied), returning their count */
 void vxo_link_offsets(void *h, float *off);
+/* per voxel: localSignal */
+void vxo_signals(void *h, double *local_signal);
 int vxo_link_curve(void *h, int i, float *strain, float *stress, int cap);
 void vxo_last_contact(void *h, double *c3);
 void vxo_com(void *h, double *c3);

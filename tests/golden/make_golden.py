@@ -156,10 +156,25 @@ def cases():
                 wl.BCRegion(prim=0, dof_fixed=4 | 16, x=0.5, y=0.0, z=0.0, dx=0.5, dy=0.5, dz=0.3,
                             displace=(0.0, 0.0, -0.0005), force=(0.003, 0.0, 0.0))]
     out["bern6_partial_bcs"] = (part, 400, 100)
+    # EnableSignals: pacemaker voxels fire every 2 ms, signals spread along links with short
+    # delays and decay; each voxel's signal scales its ShiftCiliaForce; self-collision on
+    rng = np.random.default_rng(17)
+    smats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0, signal_time_delay=0.0004, inactive_period=0.0006),
+             wl.Material(E=3e5, nu=0.35, is_pacemaker=1, pacemaker_period=0.002, signal_time_delay=0.0003,
+                         inactive_period=0.0005, signal_value_decay=0.95, cilia=0.5),
+             wl.Material(E=5e5, nu=0.35, cilia=-0.8, signal_time_delay=0.0002, inactive_period=0.0004,
+                         signal_value_decay=0.85)]
+    sig = wl.bernoulli_body(rng, (6, 5, 4), 0.85, smats, random_phase=True, temp_vary=True, temp_amplitude=15.0,
+                            z_offset=1, enable_collision=True)
+    sig.enable_cilia = True
+    sig.enable_signals = True
+    sig.cilia_base = 1e-2 * rng.standard_normal(sig.grid.shape + (3,))
+    sig.cilia_shift = 2e-4 * rng.standard_normal(sig.grid.shape + (3,))
+    out["bern6_signals_cilia"] = (sig, 400, 100)
     return out
 
 
-def snapshot(s, plastic=False):
+def snapshot(s, plastic=False, signals=False):
     v = s.voxels()
     lk = s.links()
     t = s.topology()
@@ -169,6 +184,8 @@ def snapshot(s, plastic=False):
                time=np.array([s.time()]), dt=np.array([s.dt()], np.float32))
     if plastic:  # non-linear materials: the links' plastic strain offsets
         out["soffset"] = s.link_offsets()
+    if signals:  # EnableSignals: every voxel's localSignal
+        out["signal"] = s.signals()
     return out
 
 
@@ -185,9 +202,13 @@ def robot_record(r):
                     temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,
                     temp_base=r.temp_base, enable_expansion=r.enable_expansion, enable_collision=r.enable_collision,
                     volume_effects=r.volume_effects, force_field=r.force_field, enable_cilia=r.enable_cilia,
-                    enable_detach=r.enable_detach, secondary_experiment=r.secondary_experiment)
+                    enable_detach=r.enable_detach, secondary_experiment=r.secondary_experiment,
+                    enable_signals=r.enable_signals)
     rec = dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
                settings=np.array(json.dumps(settings)))
+    if r.enable_signals:  # signal parameters per palette entry
+        rec["signal_mats"] = np.array([[m.is_pacemaker, m.pacemaker_period, m.signal_value_decay, m.signal_time_delay,
+                                        m.inactive_period] for m in r.materials], np.float64)
     if r.bcs:  # boundary-condition regions
         rec["bcs"] = np.array(json.dumps([dataclasses.asdict(b) for b in r.bcs]))
     if nonlinear(r):  # material models beyond linear: MatModel and its parameters per palette entry
@@ -225,7 +246,7 @@ def main(only=()):
             n = s.step(every)
             done += every
             snaps.append(done)
-            for k, v in snapshot(s, nonlinear(robot)).items():
+            for k, v in snapshot(s, nonlinear(robot), robot.enable_signals).items():
                 rec[f"s{done}_{k}"] = v
             rec[f"s{done}_surface"] = s.surface()
             if n < every:

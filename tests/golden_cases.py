@@ -33,6 +33,10 @@ def load(name):
             m.yield_stress = md["yield_stress"]
             m.ss_strain = None if md["ss_strain"] is None else tuple(md["ss_strain"])
             m.ss_stress = None if md["ss_stress"] is None else tuple(md["ss_stress"])
+    if "signal_mats" in d.files:  # isPaceMaker, PaceMakerPeriod, signalValueDecay, signalTimeDelay, inactivePeriod
+        for m, row in zip(mats, d["signal_mats"]):
+            m.is_pacemaker, m.pacemaker_period, m.signal_value_decay, m.signal_time_delay, m.inactive_period = (
+                int(row[0]), float(row[1]), float(row[2]), float(row[3]), float(row[4]))
     phase = d["phase"] if d["phase"].size else None
     robot = wl.Robot(grid=d["lattice"], materials=mats, phase=phase, z_offset=0, **s)
     if "bcs" in d.files:  # boundary-condition regions

@@ -28,7 +28,10 @@ class VxoMaterial(ctypes.Structure):
                 ("is_measured", ctypes.c_int), ("thermal_on_after", ctypes.c_double),
                 ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double), ("remove_after", ctypes.c_double),
                 ("plastic_mod", ctypes.c_double), ("yield_stress", ctypes.c_double), ("n_data", ctypes.c_int),
-                ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p)]
+                ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p),
+                ("is_pacemaker", ctypes.c_int), ("pacemaker_period", ctypes.c_double),
+                ("signal_value_decay", ctypes.c_double), ("signal_time_delay", ctypes.c_double),
+                ("inactive_period", ctypes.c_double)]
 
 
 class VxoBC(ctypes.Structure):
@@ -51,7 +54,7 @@ class VxoRobot(ctypes.Structure):
                 ("force_field", ctypes.c_void_p * 3),
                 ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
                 ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int),
-                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(VxoBC))]
+                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(VxoBC)), ("enable_signals", ctypes.c_int)]
 
 
 def build_oracle():
@@ -194,6 +197,14 @@ class Sim:
         self._f("link_mats")(self.h, _P(lf), _P(lol))
         return dict(vmat=f, nomsize=ns, fixed_measured=fm, lmat=lf[:nlm], lmat_of_link=lol[:self.counts()[1]])
 
+    def signals(self):
+        """Per voxel: localSignal."""
+        out = np.zeros(max(self.counts()[0], 1))
+        f = getattr(self.lib, self.p + "signals")
+        f.restype, f.argtypes = None, [ctypes.c_void_p, ctypes.c_void_p]
+        f(self.h, _P(out))
+        return out[:self.counts()[0]]
+
     def link_offsets(self):
         """Per link: the plastic strain offset of a non-linear material (0 otherwise)."""
         off = np.zeros(max(self.counts()[1], 1), np.float32)
@@ -240,7 +251,9 @@ def robot_struct(robot):
         mats[i] = VxoMaterial(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic,
                               m.fail_stress, m.mat_model(), m.fixed, m.is_measured, 0.0,
                               m.cilia, m.cilia_on_after, m.remove_after, m.plastic_mod, m.yield_stress,
-                              n, None if e is None else _P(e), None if s is None else _P(s))
+                              n, None if e is None else _P(e), None if s is None else _P(s),
+                              int(m.is_pacemaker), m.pacemaker_period, m.signal_value_decay, m.signal_time_delay,
+                              m.inactive_period)
     Z, Y, X = g.shape
     r = VxoRobot(X, Y, Z, _P(lattice), None if phase is None else _P(phase), len(robot.materials), mats,
                  robot.vox_size, robot.dt_frac, robot.grav_acc, int(robot.floor),
@@ -261,6 +274,7 @@ def robot_struct(robot):
                 setattr(r, name, _P(a))
     r.enable_detach = int(robot.enable_detach)
     r.secondary_experiment = int(robot.secondary_experiment)
+    r.enable_signals = int(robot.enable_signals)
     bcs = None
     if robot.bcs:
         from vx3g.abi import bc_array
@@ -310,4 +324,7 @@ def ref_sim(robot) -> Sim:
     lib.vx3ref_set_secondary.restype = None
     lib.vx3ref_set_secondary.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.vx3ref_set_secondary(h, int(robot.secondary_experiment))
+    lib.vx3ref_set_signals.restype = None
+    lib.vx3ref_set_signals.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.vx3ref_set_signals(h, int(robot.enable_signals))
     return Sim(lib, "vx3ref_", h, progs)

@@ -160,6 +160,28 @@ def test_runner_boundary_conditions_match_oracle(tmp_path):
         assert np.abs(f.com() - s.com()).max() > 1e-4 * robot.vox_size, name  # the regions acted
 
 
+def test_runner_signals_match_oracle(tmp_path):
+    """Simulator/EnableSignals with pacemaker materials and ShiftCiliaForce rows read by
+    the runner from the VXA: the report matches the oracle running the same robot, and
+    the signals moved it."""
+    import golden_cases
+    vbuild.build()
+    exe = os.path.join(os.path.dirname(vbuild.LIB), "vx3g_sim")
+    robot, _ = golden_cases.load("bern6_signals_cilia")
+    robot.stop_time = 0.008
+    (tmp_path / "base.vxa").write_text(wl.to_vxa(robot))
+    (tmp_path / "r.vxd").write_text("<VXD>\n</VXD>\n")
+    out = tmp_path / "report.xml"
+    r = subprocess.run([exe, "-i", str(tmp_path), "-o", str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    node = ET.parse(out).getroot().find("detail/r")
+    s, _, _ = _oracle_until(robot, 0.008)
+    com = [float(node.find(f"currentCenterOfMass/{k}").text) for k in "xyz"]
+    np.testing.assert_allclose(com, s.com(), rtol=0, atol=1e-6 * robot.vox_size)
+    quiet, _, _ = _oracle_until(wl.Robot(**{**robot.__dict__, "enable_signals": False}), 0.008)
+    assert np.abs(quiet.com() - s.com()).max() > 1e-4 * robot.vox_size
+
+
 def test_runner_sub_batches_run_concurrently(tmp_path):
     """VX3_SimulationManager::start runs every sub-batch at once, one host thread and
     context per device: four robots dealt round-robin into two sub-batches, both on

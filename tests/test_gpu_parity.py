@@ -51,6 +51,8 @@ def test_fp64_against_reference_golden(name):
         np.testing.assert_allclose(lk["strain"], d[f"s{snap}_strain"], rtol=0, atol=1e-6)
         np.testing.assert_allclose(b.time()[0], d[f"s{snap}_time"][0], rtol=1e-12)
         assert np.float32(b.dt()[0]) == d[f"s{snap}_dt"][0]
+        if f"s{snap}_signal" in d.files:  # EnableSignals: localSignal per voxel
+            np.testing.assert_allclose(b.signals(), d[f"s{snap}_signal"], rtol=1e-12, atol=0)
     assert np.all(b.status() == 0)
 
 
@@ -290,6 +292,23 @@ def test_nonlinear_materials_mixed_matches_fp64(name):
     plastic = lf["maxstrain"] > 0
     assert plastic.any()
     np.testing.assert_allclose(lm["maxstrain"], lf["maxstrain"], rtol=0, atol=1e-5)
+    with pytest.raises(abi.Vx3gError, match="not implemented"):
+        abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
+
+
+def test_signals_mixed_matches_fp64():
+    """EnableSignals with shifting cilia: the mixed-precision context carries the same
+    signals (they depend on time, links and materials only) and follows the FP64 COM
+    within 1e-5 relative; the adjoint refuses signals."""
+    robot, d = golden_cases.load("bern6_signals_cilia")
+    f = abi.Batch([robot], abi.PRECISION_FP64)
+    m = abi.Batch([robot], abi.PRECISION_MIXED)
+    f.step(400)
+    m.step(400)
+    assert np.array_equal(f.signals(), m.signals())
+    assert np.count_nonzero(f.signals()) > 0
+    rel = np.linalg.norm(m.com() - f.com(), axis=1) / np.linalg.norm(f.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
     with pytest.raises(abi.Vx3gError, match="not implemented"):
         abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
 

@@ -49,6 +49,8 @@ def test_trajectory_bit_exact(name):
         # dampingMultiplier divides by a previousDt of 0; the fixed voxel never reads it)
         if f"s{snap}_soffset" in d.files:
             got["soffset"] = s.link_offsets()
+        if f"s{snap}_signal" in d.files:
+            got["signal"] = s.signals()
         for k, a in got.items():
             b = d[f"s{snap}_{k}"]
             assert np.array_equal(a, b, equal_nan=True), f"{name} step {snap}: {k} differs (max {np.max(np.abs(a - b)) if a.shape == b.shape else 'shape'})"

@@ -26,7 +26,7 @@ EXPORTS = [
     "vx3g_get_topology", "vx3g_get_surface", "vx3g_com", "vx3g_dt", "vx3g_time", "vx3g_status",
     "vx3g_steps_taken", "vx3g_time_steps", "vx3g_flush_l2", "vx3g_time_passes", "vx3g_stop_robot",
     "vx3g_record", "vx3g_backward", "vx3g_recommended_dt_noalloc", "vx3g_autotune", "vx3g_launch_shapes",
-    "vx3g_debug_barrier", "vx3g_prepare_graphs",
+    "vx3g_debug_barrier", "vx3g_prepare_graphs", "vx3g_get_signals",
 ]
 
 
@@ -36,7 +36,10 @@ class Material(ctypes.Structure):
                 ("model", ctypes.c_int), ("fixed", ctypes.c_int), ("is_measured", ctypes.c_int),
                 ("thermal_on_after", ctypes.c_double), ("cilia", ctypes.c_double), ("cilia_on_after", ctypes.c_double),
                 ("remove_after", ctypes.c_double), ("plastic_mod", ctypes.c_double), ("yield_stress", ctypes.c_double),
-                ("n_data", ctypes.c_int), ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p)]
+                ("n_data", ctypes.c_int), ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p),
+                ("is_pacemaker", ctypes.c_int), ("pacemaker_period", ctypes.c_double),
+                ("signal_value_decay", ctypes.c_double), ("signal_time_delay", ctypes.c_double),
+                ("inactive_period", ctypes.c_double)]
 
 
 class BCRegion(ctypes.Structure):
@@ -69,7 +72,7 @@ class RobotDesc(ctypes.Structure):
                 ("log10E", ctypes.c_void_p), ("force_field", ctypes.c_void_p * 3),
                 ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
                 ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int),
-                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(BCRegion))]
+                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(BCRegion)), ("enable_signals", ctypes.c_int)]
 
 
 class BatchDesc(ctypes.Structure):
@@ -122,6 +125,7 @@ def load(path: str = LIB_PATH):
     lib.vx3g_backward.argtypes = [vp, dp, dp, dp]
     lib.vx3g_debug_barrier.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
     lib.vx3g_prepare_graphs.argtypes = [vp]
+    lib.vx3g_get_signals.argtypes = [vp, dp]
     _lib = lib
     return lib
 
@@ -152,7 +156,9 @@ def robot_desc(robot):
         mats[i] = Material(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress,
                            m.mat_model(), int(m.fixed), int(m.is_measured), 0.0,
                            float(m.cilia), float(m.cilia_on_after), float(m.remove_after),
-                           float(m.plastic_mod), float(m.yield_stress), n, _P(e), _P(s))
+                           float(m.plastic_mod), float(m.yield_stress), n, _P(e), _P(s),
+                           int(m.is_pacemaker), float(m.pacemaker_period), float(m.signal_value_decay),
+                           float(m.signal_time_delay), float(m.inactive_period))
     Z, Y, X = g.shape
     log10E = getattr(robot, "log10E", None)
     if log10E is not None:
@@ -181,6 +187,7 @@ def robot_desc(robot):
             if a is not None:
                 cil.append(a)
                 setattr(d, name, _P(a))
+    d.enable_signals = int(robot.enable_signals)
     bcs = None
     if robot.bcs:
         bcs = bc_array(BCRegion, robot.bcs)
@@ -277,6 +284,12 @@ class Batch:
         _check(self.lib.vx3g_get_links(self.h, _P(strain), _P(maxs), _P(local9), _P(forces), _P(small)),
                "vx3g_get_links")
         return dict(strain=strain, maxstrain=maxs, local9=local9, forces=forces, small=small)
+
+    def signals(self):
+        """Per voxel: localSignal (0 in robots without signals)."""
+        out = np.zeros(self.nv)
+        _check(self.lib.vx3g_get_signals(self.h, _P(out)), "vx3g_get_signals")
+        return out
 
     def topology(self):
         ijk = np.zeros((self.nv, 3), np.int32)

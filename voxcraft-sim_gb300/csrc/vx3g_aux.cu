@@ -164,7 +164,13 @@ __global__ void k_extra_forces(Dev d, int parity) {
         const bool surface = (d.vinfo[v].y & VF_LINKMASK) != VF_LINKMASK;
         if (surface && !(d.cil_on[v] > t)) {
             const double4 q = load_state(d, d.quat, v);
-            cf = qrot(Q4<double>{q.x, q.y, q.z, q.w}, V3<double>{c.x, c.y, c.z});
+            V3<double> b{c.x, c.y, c.z};  // baseCiliaForce + localSignal * shiftCiliaForce
+            if (rp.signals) {
+                const double sl = d.sig[6 * (size_t)v];
+                const double4 sh = d.cils[v];
+                b = V3<double>{c.x + sl * sh.x, c.y + sl * sh.y, c.z + sl * sh.z};
+            }
+            cf = qrot(Q4<double>{q.x, q.y, q.z, q.w}, b);
         }
         d.cfv[v] = make_double4(cf.x * c.w, cf.y * c.w, cf.z * c.w, 0.0);
     }
@@ -177,6 +183,98 @@ __global__ void k_extra_forces(Dev d, int parity) {
 
 void launch_extra_forces(const Dev &d, int parity, cudaStream_t s) {
     if ((d.ffv || d.cfv) && d.nv) k_extra_forces<<<(d.nv + 255) / 256, 256, 0, s>>>(d, parity);
+}
+
+// ---------------------------------------------------------------- signals
+// The end of VX3_Voxel::timeStep with EnableSignals (VX3_Voxel.cu:271-348): propagateSignal
+// (the pending signal, once due, passed to the voxel across each link in direction order,
+// each receiver taking it unless refractory), packMaker, localSignalDecay.  A voxel writes
+// its neighbours' signal state, so the voxels of a robot take their turns in voxel order, as
+// a serial loop over the voxel pass does: one warp per robot walks its voxels 32 at a time;
+// a group in which no voxel passes a signal on touches only each voxel's own state and runs
+// in parallel, a group with one runs voxel by voxel on lane 0.  The physics of the step does
+// not read signal state, so this runs after the voxel pass.
+__device__ __forceinline__ void sig_receive(const Dev &d, int v, double value, double at, bool force) {
+    double *S = d.sig + 6 * (size_t)v;
+    const VMat &m = d.vmat[d.vinfo[v].y >> 8];
+    if (!force && S[3] > at) return;
+    if (value < 0.1) return;
+    S[3] = at + m.inactive;  // inactiveUntil
+    S[0] = value;            // localSignal
+    double sv = value * m.sig_decay;
+    if (sv < 0.1) sv = 0;
+    S[4] = sv;
+    S[5] = at;
+}
+
+// the voxel reached the end of timeStep this step (stepped, not fixed in all DOFs)
+__device__ __forceinline__ bool sig_turn(const Dev &d, const RobotP &rp, int v) {
+    if (d.vinfo[v].y & VF_FIXED) return false;  // material Fixed, or removed
+    if (rp.bcs && d.vext[v] >= 0 && d.ext[d.vext[v]].dof == EXT_ALL) return false;
+    return true;
+}
+
+__device__ __forceinline__ bool sig_sends(const Dev &d, int v, double t) {
+    const double *S = d.sig + 6 * (size_t)v;
+    return !(S[5] > t) && !(S[4] < 0.1);
+}
+
+__device__ void sig_own(const Dev &d, int v, double t) {  // packMaker, localSignalDecay
+    double *S = d.sig + 6 * (size_t)v;
+    const VMat &m = d.vmat[d.vinfo[v].y >> 8];
+    if (m.pacemaker && !(S[2] > t)) {
+        sig_receive(d, v, 100, t, true);
+        S[2] = t + m.pace_period;
+    }
+    if (!(S[1] > t)) {
+        if (S[0] < 0.1) S[0] = 0;
+        else {
+            S[0] = S[0] * 0.9;
+            S[1] = t + 0.01;
+        }
+    }
+}
+
+__device__ void sig_send(const Dev &d, int v, double t) {  // propagateSignal
+    double *S = d.sig + 6 * (size_t)v;
+    const uint2 vi = d.vinfo[v];
+    const VMat &m = d.vmat[vi.y >> 8];
+    for (int dir = 0; dir < 6; dir++) {
+        const int u = d.vnb[6 * (size_t)v + dir];
+        if (u >= 0 && ((vi.y >> dir) & 1u)) sig_receive(d, u, S[4], t + m.sig_delay, false);
+    }
+    S[4] = 0;
+    S[5] = 0;
+    S[3] = t + 2 * m.sig_delay + m.inactive;
+}
+
+__global__ void k_signals(Dev d, int parity) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= d.nsigrob) return;
+    const int r = d.sigrob[w];
+    const RobotP &rp = d.rp[r];
+    if (d.status[r] != 0 || d.dt[r] == 0.0f) return;
+    const double t = d.T[(size_t)parity * d.nr + r];
+    const int end = rp.voff + rp.nv;
+    for (int base = rp.voff; base < end; base += 32) {
+        const int v = base + lane;
+        const bool mine = v < end && sig_turn(d, rp, v);
+        const unsigned sends = __ballot_sync(0xffffffffu, mine && sig_sends(d, v, t));
+        if (!sends) {
+            if (mine) sig_own(d, v, t);
+        } else if (lane == 0) {
+            for (int u = base; u < min(base + 32, end); u++) {
+                if (!sig_turn(d, rp, u)) continue;
+                if (sig_sends(d, u, t)) sig_send(d, u, t);
+                sig_own(d, u, t);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+void launch_signals(const Dev &d, int parity, cudaStream_t s) {
+    if (d.nsigrob) k_signals<<<(d.nsigrob + 3) / 4, 128, 0, s>>>(d, parity);
 }
 
 // ---------------------------------------------------------------- detach

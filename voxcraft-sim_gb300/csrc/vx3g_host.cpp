@@ -127,6 +127,11 @@ VMat to_vmat(const HostVMat &m, const vx3g_material &in) {
     v.is_measured = in.is_measured ? 1 : 0;
     v.nom_size = m.nom;
     v.thermal_on_after = in.thermal_on_after;
+    v.pacemaker = in.is_pacemaker ? 1 : 0;
+    v.pace_period = in.pacemaker_period;
+    v.sig_decay = in.signal_value_decay;
+    v.sig_delay = in.signal_time_delay;
+    v.inactive = in.inactive_period;
     return v;
 }
 
@@ -235,6 +240,7 @@ struct vx3g_ctx {
     bool any_dyn = false;     // some robot's surface follows its link table (detach or removal)
     bool any_nonlinear = false;  // some material has a non-linear stress-strain model
     bool any_bcs = false;        // some voxel has a boundary-condition external
+    bool any_signals = false;    // some robot has EnableSignals
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -364,8 +370,9 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     std::vector<uint2> vinfo, linfo;
     std::vector<int> csurf;
     std::vector<MathTok> ftok;
-    std::vector<double4> cil_h;
+    std::vector<double4> cil_h, cils_h;  // BaseCiliaForce (w: Cilia), ShiftCiliaForce
     std::vector<double> cil_on_h;
+    std::vector<int> vnb_h, sigrob_h;    // signals: the voxel across each link, robots with signals
     std::vector<double> rm_h;  // per voxel: removal time (+inf: never)
     std::vector<float2> ss_h;  // stress-strain points of the non-linear link materials
     std::vector<ExtBC> ext_h;  // boundary-condition externals
@@ -614,14 +621,28 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
                     if (R.cilia_base) b[j] = R.cilia_base[3 * cell + j];
                     if (R.cilia_shift) sh[j] = R.cilia_shift[3 * cell + j];
                 }
-                const double sig = 0.0;  // localSignal: signals are not simulated
-                cil_h[v] = make_double4(b[0] + sig * sh[0], b[1] + sig * sh[1], b[2] + sig * sh[2], M.cilia);
+                cil_h[v] = make_double4(b[0], b[1], b[2], M.cilia);  // + localSignal * shift on the device
+                if (R.enable_signals) {
+                    cils_h.resize(pos.size(), make_double4(0, 0, 0, 0));
+                    cils_h[v] = make_double4(sh[0], sh[1], sh[2], 0.0);
+                }
                 if (M.cilia != 0) {
                     cil_on_h[v] = M.cilia_on_after;
                     rp.cilia = 1;
                 }
             }
             c->any_cilia |= rp.cilia != 0;
+        }
+        // signals: the voxel across each direction's link (links of the lattice, in creation)
+        rp.signals = R.enable_signals ? 1 : 0;
+        if (rp.signals) {
+            vnb_h.resize(6 * pos.size(), -1);
+            for (int l = c->loff[r]; l < (int)c->ends.size(); l++) {
+                const int a = (int)c->laxis[l];
+                vnb_h[6 * (size_t)c->ends[l].x + 2 * a] = c->ends[l].y;      // negative end: toward +axis
+                vnb_h[6 * (size_t)c->ends[l].y + 2 * a + 1] = c->ends[l].x;  // positive end: toward -axis
+            }
+            sigrob_h.push_back(r);
         }
         // lists in shared memory when the robot fits (lattice coordinates below 512, packed in 10 bits each)
         int cmax = 0;
@@ -698,6 +719,22 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     d.cil = nullptr;
     d.cil_on = nullptr;
     d.cfv = nullptr;
+    d.cils = nullptr;
+    d.sig = nullptr;
+    d.vnb = nullptr;
+    d.sigrob = nullptr;
+    d.nsigrob = (int)sigrob_h.size();
+    if (d.nsigrob) {
+        vnb_h.resize(6 * pos.size(), -1);
+        if ((rc = c->alloc(&d.sig, 6 * pos.size())) || (rc = c->upload(&d.vnb, vnb_h)) ||
+            (rc = c->upload(&d.sigrob, sigrob_h)))
+            return rc;
+        if (!cils_h.empty()) {
+            cils_h.resize(pos.size(), make_double4(0, 0, 0, 0));
+            if ((rc = c->upload(&d.cils, cils_h))) return rc;
+        }
+    }
+    c->any_signals = d.nsigrob > 0;
     if (c->any_cilia &&
         ((rc = c->upload(&d.cil, cil_h)) || (rc = c->upload(&d.cil_on, cil_on_h)) || (rc = c->alloc(&d.cfv, d.nv))))
         return rc;
@@ -774,6 +811,7 @@ void enqueue_voxels(vx3g_ctx *c, int parity) {
         launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, !c->any_detach);  // detach writes voxel info
         launch_voxels_bc_mixed(c->d, parity, c->stream);  // voxels with a boundary condition, if any
     }
+    launch_signals(c->d, parity, c->stream);       // EnableSignals robots only (the end of timeStep)
     launch_remove(c->d, parity, c->stream);        // SecondaryExperiment robots only (end of the step)
 }
 
@@ -801,6 +839,7 @@ cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
     launch_detach(c->d, c->stream);
     launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, false);
     launch_voxels_bc_mixed(c->d, parity, c->stream);
+    launch_signals(c->d, parity, c->stream);
     launch_remove(c->d, parity, c->stream);
     return cudaSuccess;
 }
@@ -1063,6 +1102,21 @@ int vx3g_get_links(vx3g_ctx *c, float *strain, float *max_strain, double *local9
             }
         }
     }
+    return VX3G_OK;
+}
+
+int vx3g_get_signals(vx3g_ctx *c, double *local) {
+    if (!c || !local) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_get_signals");
+    const size_t n = c->d.nv;
+    if (!c->d.sig) {
+        std::fill(local, local + n, 0.0);
+        return VX3G_OK;
+    }
+    std::vector<double> h;
+    int rc;
+    if ((rc = download(c, h, c->d.sig, 6 * n))) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; i++) local[i] = h[6 * i];
     return VX3G_OK;
 }
 
@@ -1529,6 +1583,7 @@ int vx3g_record(vx3g_ctx *c, int n, int k) {
     if (c->any_nonlinear)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of non-linear material models is not implemented");
     if (c->any_bcs) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of boundary conditions is not implemented");
+    if (c->any_signals) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of signals is not implemented");
     if (c->any_detach || c->any_remove)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a changing link table (detach, removal) is not implemented");
     CU(cudaSetDevice(c->device));

@@ -50,6 +50,8 @@ struct VMat {  // one voxel material (global index), constants as the reference 
     int fixed, is_measured;
     double nom_size;
     double thermal_on_after;
+    int pacemaker;     // isPaceMaker
+    double pace_period, sig_decay, sig_delay, inactive;  // PaceMakerPeriod, signalValueDecay, signalTimeDelay, inactivePeriod
 };
 
 struct LMat {  // one link material (global index), oriented: (negative end, positive end) materials
@@ -79,6 +81,7 @@ struct RobotP {
     int remove = 0;            // 1: SecondaryExperiment with a material that leaves (k_remove)
     int dyn = 0;               // detach || remove: the surface follows the link table
     int bcs = 0;               // 1: some voxel has a boundary-condition external (Dev::vext)
+    int signals = 0;           // 1: EnableSignals (k_signals; the cilia force reads the signal)
 };
 
 // a voxel's boundary-condition external (VX3_External): fixed DOFs with their prescribed
@@ -183,6 +186,14 @@ struct Dev {
     double4 *cil;         // per voxel: BaseCiliaForce + 0 * ShiftCiliaForce, material Cilia (robots with cilia)
     double *cil_on;       // per voxel: the time cilia switch on (+inf: never; interior or Cilia 0)
     double4 *cfv;         // per voxel: this step's CiliaForce * Cilia (robots with cilia), or NULL
+    double4 *cils;        // per voxel: ShiftCiliaForce (robots with cilia and signals), or NULL
+    // signals: per voxel {localSignal, localSignaldt, packmakerNextPulse, inactiveUntil, pending
+    // value, pending activeTime} (VX3_Voxel.h:304-309), and the voxel across each direction's
+    // link (-1: none); robots with signals: sigrob[nsigrob]
+    double *sig;
+    int *vnb;
+    int *sigrob;
+    int nsigrob;
     int *srf;             // [NR] a link of the robot detached or a voxel left this step: rebuild its lists next step
     int any_detach;       // some robot has EnableDetach
     int any_remove;       // some robot removes voxels (k_remove)
@@ -239,6 +250,8 @@ void launch_extra_forces(const Dev &d, int parity, cudaStream_t s);
 void launch_detach(const Dev &d, cudaStream_t s);
 // removeVoxels (VX3_VoxelyzeKernel.cu:365-397) at the end of the step of the given parity
 void launch_remove(const Dev &d, int parity, cudaStream_t s);
+// the signals of the step of the given parity (the end of VX3_Voxel::timeStep), after the voxel pass
+void launch_signals(const Dev &d, int parity, cudaStream_t s);
 // one-time setup of the collision kernels (shared-memory size, grid); fills d.cgrid
 cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);

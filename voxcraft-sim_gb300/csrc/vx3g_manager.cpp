@@ -199,8 +199,7 @@ void read_spec(RobotSpec &S) {
     if (vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableAttach", false))
         throw std::runtime_error(S.filename + ": runtime attachment is not supported");
     d.enable_detach = vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableDetach", false);  // :330
-    if (vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0))
-        throw std::runtime_error(S.filename + ": signals are not supported");
+    d.enable_signals = vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0);  // :361
     // SecondaryExperiment (VX3_SimulationManager.cu:364-365): material removal on the device,
     // the initial-position reset here
     d.secondary_experiment = vx3g::xml::get_int(root, "VXA.Simulator.SecondaryExperiment", 0);
@@ -329,6 +328,14 @@ void read_spec(RobotSpec &S) {
             M.cilia = vx3g::xml::get_double(mech, "Cilia", 0.0);  // VX_Object.cpp:1429, 1437
             M.cilia_on_after = vx3g::xml::get_double(mech, "TurnOnCiliaAfterThisManySeconds", 0.0);
             M.remove_after = vx3g::xml::get_double(mech, "RemoveFromSimulationAfterThisManySeconds", 0.0);  // :1427
+            // signals (VX_Object.cpp:1420-1424)
+            M.is_pacemaker = vx3g::xml::get_int(mech, "isPaceMaker", 0);
+            M.pacemaker_period = vx3g::xml::get_double(mech, "PaceMakerPeriod", 0.0);
+            M.signal_value_decay = vx3g::xml::get_double(mech, "signalValueDecay", 0.9);
+            M.signal_time_delay = vx3g::xml::get_double(mech, "signalTimeDelay", 0.03);
+            M.inactive_period = vx3g::xml::get_double(mech, "inactivePeriod", 0.03);
+            if (vx3g::xml::get_int(mech, "isTarget", 0))  // collisions with targets count hits and signal
+                throw std::runtime_error(S.filename + ": target materials (isTarget) are not supported");
             S.mats.push_back(M);
             const Node *disp = m->child("Display");
             for (const char *c : {"Red", "Green", "Blue", "Alpha"})
@@ -426,6 +433,8 @@ void print_history(FILE *out, vx3g_ctx *ctx, int robot, const RobotSpec &S, long
     check(vx3g_counts(ctx, &nv, &nl, &ns), "vx3g_counts");
     std::vector<double> pos(3 * (size_t)nv), orient(4 * (size_t)nv);
     std::vector<float> tempe(nv), strain(nl), maxs(nl);
+    std::vector<double> signal(nv);
+    check(vx3g_get_signals(ctx, signal.data()), "vx3g_get_signals");
     std::vector<int32_t> ends(2 * (size_t)nl), axis(nl), vmat(nv), surf(ns), lflag(nl);
     check(vx3g_get_state(ctx, pos.data(), orient.data(), nullptr, nullptr), "vx3g_get_state");
     check(vx3g_get_voxel_aux(ctx, tempe.data(), nullptr, nullptr), "vx3g_get_voxel_aux");
@@ -473,7 +482,7 @@ void print_history(FILE *out, vx3g_ctx *ctx, int robot, const RobotSpec &S, long
             fprintf(out, "%.1f,%.1f,%.1f,%.1f,%.1f,%.1f,", corner[0][0] * vs, corner[0][1] * vs, corner[0][2] * vs,
                     corner[1][0] * vs, corner[1][1] * vs, corner[1][2] * vs);
             fprintf(out, "%d,", vmat[s] + 1);
-            fprintf(out, "%.1f,", 0.0);
+            fprintf(out, "%.1f,", signal[s]);  // localSignal, for colouring (:88)
             fprintf(out, ";");
         }
         fprintf(out, "<<<>>>");

@@ -43,6 +43,11 @@ class Material:
     yield_stress: float = 0.0  # Yield_Stress (MatModel 2)
     ss_strain: Optional[tuple] = None  # SSData strain points (MatModel 3), (0, 0) first as in a VXA
     ss_stress: Optional[tuple] = None  # SSData stress points (MatModel 3)
+    is_pacemaker: int = 0              # isPaceMaker: emits a signal every pacemaker_period seconds
+    pacemaker_period: float = 0.0      # PaceMakerPeriod
+    signal_value_decay: float = 0.9    # signalValueDecay
+    signal_time_delay: float = 0.03    # signalTimeDelay
+    inactive_period: float = 0.03      # inactivePeriod
 
     def mat_model(self) -> int:
         if self.model is not None:
@@ -113,6 +118,7 @@ class Robot:
     fitness_x: bool = False               # FitnessFunction "x" (COM displacement along x)
     record_step: int = 0                  # RecordHistory/RecordStepSize
     bcs: Optional[list] = None            # Environment/Boundary_Conditions: BCRegion list
+    enable_signals: bool = False          # Simulator/EnableSignals
 
     def occupied(self) -> np.ndarray:
         return self.grid > 0
@@ -318,6 +324,7 @@ def to_vxa(r: Robot) -> str:
            f"<EnableAttach>0</EnableAttach><EnableDetach>{int(r.enable_detach)}</EnableDetach></AttachDetach>",
            f"<EnableExpansion>{int(r.enable_expansion)}</EnableExpansion>",
            *([f"<EnableCilia>1</EnableCilia>"] if r.enable_cilia else []),
+           *([f"<EnableSignals>1</EnableSignals>"] if r.enable_signals else []),
            *([f"<SecondaryExperiment>1</SecondaryExperiment><ReinitializeInitialPositionAfterThisManySeconds>"
               f"{_fmt(r.reinit_after)}</ReinitializeInitialPositionAfterThisManySeconds>"]
              if r.secondary_experiment else []),
@@ -360,6 +367,10 @@ def to_vxa(r: Robot) -> str:
             f"<RemoveFromSimulationAfterThisManySeconds>{_fmt(m.remove_after)}</RemoveFromSimulationAfterThisManySeconds>"
             f"<uStatic>{_fmt(m.mu_static)}</uStatic><uDynamic>{_fmt(m.mu_kinetic)}</uDynamic>"
             f"<Fixed>{int(m.fixed)}</Fixed><isMeasured>{int(m.is_measured)}</isMeasured>"
+            f"<isPaceMaker>{int(m.is_pacemaker)}</isPaceMaker><PaceMakerPeriod>{_fmt(m.pacemaker_period)}</PaceMakerPeriod>"
+            f"<signalValueDecay>{_fmt(m.signal_value_decay)}</signalValueDecay>"
+            f"<signalTimeDelay>{_fmt(m.signal_time_delay)}</signalTimeDelay>"
+            f"<inactivePeriod>{_fmt(m.inactive_period)}</inactivePeriod>"
             "</Mechanical></Material>")
     out.append("</Palette>")
     out.append(structure_xml(r))
