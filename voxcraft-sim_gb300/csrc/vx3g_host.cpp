@@ -651,6 +651,13 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             cmax = std::max(cmax, (int)std::max(q.x, std::max(q.y, q.z)));
         }
         rp.lchunks = rp.ns > 0 && rp.ns <= kLocalListMax && cmax < 512 ? (rp.ns + kLocalListChunk - 1) / kLocalListChunk : 0;
+        // Verlet skin: a robot rebuilt on the global hashed grid (a whole large body at a time)
+        // keeps a wider skin than one rebuilt in shared memory, trading longer candidate lists
+        // for fewer rebuilds (measured on the 64^3 body and the 256-robot batch)
+        if (rp.ns > 0 && !rp.lchunks) {
+            rp.skin = 0.4 * R.vox_size;
+            rp.inv_list_cell = 1.0 / (rp.cell_size + rp.skin);
+        }
     }
     c->voff[c->nr] = (int)pos.size();
     c->loff[c->nr] = (int)c->ends.size();
