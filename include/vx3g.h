@@ -44,6 +44,8 @@ extern "C" {
 #define VX3G_ROBOT_DIVERGED 1          /* a link strain exceeded 100; the robot stops stepping */
 #define VX3G_ROBOT_CONTACT_OVERFLOW 2  /* more contact candidates than one voxel can hold */
 #define VX3G_ROBOT_STOPPED 4           /* stopped by the caller (vx3g_stop_robot) */
+#define VX3G_ROBOT_LINK_CAPACITY 8     /* attachment wanted a runtime link beyond the robot's reserve
+                                          (links that detached keep their slots); the robot stops */
 
 /* ---- precision of the step ---------------------------------------------- */
 #define VX3G_PRECISION_FP64 0   /* the reference's arithmetic: FP64 vectors, FP32 scalars where it uses float */
@@ -84,6 +86,9 @@ typedef struct vx3g_material {
     double signal_value_decay; /* signalValueDecay: a received signal is passed on scaled by this (VXA default 0.9) */
     double signal_time_delay; /* signalTimeDelay (s): delay before a voxel passes a signal on (VXA default 0.03) */
     double inactive_period;   /* inactivePeriod (s): refractory time after a signal (VXA default 0.03) */
+    int sticky;               /* Sticky: with enable_attach, touching voxels of this material link up.  A
+                                 sticky material of an attaching robot must be linear (model 0/1) with
+                                 Poisson's ratio 0 (or volume effects off), else VX3G_ERR_UNSUPPORTED */
 } vx3g_material;
 #define VX3G_MAX_MODEL_POINTS 32
 
@@ -172,6 +177,22 @@ typedef struct vx3g_robot_desc {
                                        lets each voxel thread write its neighbours' signal state without
                                        synchronisation; here voxels take their turns in voxel order, the
                                        order of a serial loop over the voxel pass */
+    int enable_attach;              /* Simulator/AttachDetach/EnableAttach: two voxels of one Sticky material
+                                       that come within the contact envelope, both allowed by the attach
+                                       conditions, unfixed and more than five links apart, get a new link
+                                       along the dominant axis of their offset in the first one's frame
+                                       when both faces are free (handle_collision_attachment,
+                                       VX3_VoxelyzeKernel.cu:729-830).  The reference runs all pairs of
+                                       a step at once; here they take their turns in the order of its
+                                       serial loop over surface pairs.  Needs enable_collision. */
+    int safety_guard;               /* Simulator/AttachDetach/SafetyGuard (VXA default 500): a new link's
+                                       forces and moments are scaled by 0.01 for its first this many
+                                       updates (VX3_Link.cu:206-213) */
+    const vx3g_math_token *attach_condition[5]; /* AttachCondition/Condition_0..4 programs or NULL: a
+                                       voxel may attach while every given program is > 0 at its
+                                       position after its last step (x, y, z), t (that step's start
+                                       time), num_voxel; an absent condition holds (the reference reads
+                                       an unset value there) */
 } vx3g_robot_desc;
 
 typedef struct vx3g_batch_desc {
@@ -217,7 +238,8 @@ int vx3g_set_state(vx3g_ctx *ctx, const double *pos, const double *orient, const
 /* tempe: float per voxel; flags: reference voxel bool-state bits (FLOOR_ENABLED 4,
  * FLOOR_STATIC_FRICTION 8); contact: 3 doubles per voxel (last step's contact force). */
 int vx3g_get_voxel_aux(vx3g_ctx *ctx, float *tempe, int32_t *flags, double *contact);
-/* Link state in the reference's link order: strain, maxStrain (float),
+/* Link state in the reference's link order (each robot's lattice links, then its runtime
+ * links in creation order, then its unused reserve, reported as gone): strain, maxStrain (float),
  * local9 = pos2, angle1v, angle2v (9 doubles), forces12 = forceNeg, forcePos,
  * momentNeg, momentPos (12 doubles), small = small-angle flag (bit 0) | 2 once the
  * link has left the lattice (detached or removed: no voxel's link any more) | 4 while
@@ -225,7 +247,8 @@ int vx3g_get_voxel_aux(vx3g_ctx *ctx, float *tempe, int32_t *flags, double *cont
 int vx3g_get_links(vx3g_ctx *ctx, float *strain, float *max_strain, double *local9, double *forces12,
                    int32_t *small);
 /* Topology: voxel lattice indices (3 ints), voxel palette index (0-based),
- * link ends (neg, pos voxel indices, packed global), link axis (0 x, 1 y, 2 z). */
+ * link ends (neg, pos voxel indices, packed global; -1 for an unused reserve slot),
+ * link axis (0 x, 1 y, 2 z). */
 int vx3g_get_topology(vx3g_ctx *ctx, int32_t *voxel_ijk, int32_t *voxel_mat, int32_t *link_ends,
                       int32_t *link_axis);
 /* Per voxel: its localSignal (VX3_Voxel::localSignal; 0 in robots without signals). */
@@ -234,6 +257,9 @@ int vx3g_get_signals(vx3g_ctx *ctx, double *local_signal);
  * order; with enable_detach or secondary_experiment the set follows the link table
  * (vx3g_counts gives its current size). */
 int vx3g_get_surface(vx3g_ctx *ctx, int32_t *surface);
+/* Per robot: links in use, the lattice's plus those made by attachment so far (each
+ * robot's link range of vx3g_offsets holds these first, then its unused reserve). */
+int vx3g_links_in_use(vx3g_ctx *ctx, int32_t *n_links /* per robot */);
 
 int vx3g_com(vx3g_ctx *ctx, double *com /* 3 per robot */);
 int vx3g_dt(vx3g_ctx *ctx, double *dt /* per robot: the float step, widened */);

@@ -13,21 +13,29 @@
 //  * doTimeStep's child-kernel sequence, run as serial loops
 //    (src/VX3/VX3_VoxelyzeKernel.cu:237-359, kernels at :566-650, :682-727, :833-843)
 //  * recommendedTimeStep (:184-217), regenerateSurfaceVoxels (:495-513),
-//    updateCurrentCenterOfMass (:477-493), is_neighbor (:651-680)
+//    updateCurrentCenterOfMass (:477-493), is_neighbor (:651-680),
+//    combinedMaterial (:515-528), the attachment half of handle_collision_attachment
+//    (:729-830) and the attach conditions of gpu_update_voxels (:606-621)
 //  * the VXA read of src/VX3/VX3_SimulationManager.cu:298-308
 // Every physics function called below (VX3_Link::updateForces,
 // VX3_Voxel::timeStep, VX3_Collision::updateContactForce, ...) is the
 // reference's own code.
 //
-// Deviation (documented): the reference probes ONE random link per step for
+// Deviations (documented): the reference probes ONE random link per step for
 // strain > 100 (VX3_VoxelyzeKernel.cu:271-281); this driver checks every link,
-// which is what the GB300 kernels do as well.
+// which is what the GB300 kernels do as well.  The reference runs every surface pair
+// of a step at once, so which of two competing attachments wins (and the order of
+// contact sums) depends on thread timing; this driver runs the pairs in the serial
+// loop's order, first ascending, second ascending below it.  An AttachCondition the
+// VXA does not give leaves the reference reading an unset value (VX3_MathTree::eval
+// returns values[0] of an empty program); here an absent condition holds.
 
 #include "VX3_VoxelyzeKernel.cuh"
 #include "VX3_MemoryCleaner.h"
 #include "VX_Sim.h"
 #include "XML_Rip.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <map>
 #include <string>
@@ -38,10 +46,20 @@ bool VX3_MemoryCleaner_running = false;
 boost::mutex MemoryCleaner_mutex;
 std::vector<void *> MemoryCleaner_toBeFreedCUDAPointer;
 
-// Runtime link creation (attach) is out of scope; the reference's device-side
-// VX3_Link constructor references this member, so it must resolve.  It is
-// never reached because attach is disabled in every oracle run.
-VX3_MaterialLink *VX3_VoxelyzeKernel::combinedMaterial(VX3_MaterialVoxel *, VX3_MaterialVoxel *) { return NULL; }
+// d_v_linkMats of each kernel object: the link materials of the lattice, then those
+// made at runtime (VX3_VoxelyzeKernel.cuh:91-93)
+static std::map<VX3_VoxelyzeKernel *, std::vector<VX3_MaterialLink *>> g_link_mats;
+
+// VX3_VoxelyzeKernel.cu:515-528: the link material of a voxel-material pair, made with the
+// reference's device constructor on first use
+VX3_MaterialLink *VX3_VoxelyzeKernel::combinedMaterial(VX3_MaterialVoxel *mat1, VX3_MaterialVoxel *mat2) {
+    std::vector<VX3_MaterialLink *> &v = g_link_mats[this];
+    for (VX3_MaterialLink *m : v)
+        if ((m->vox1Mat == mat1 && m->vox2Mat == mat2) || (m->vox1Mat == mat2 && m->vox2Mat == mat1)) return m;
+    VX3_MaterialLink *m = new VX3_MaterialLink(mat1, mat2);
+    v.push_back(m);
+    return m;
+}
 
 namespace {
 
@@ -52,6 +70,8 @@ struct RefSim {
     VX3_VoxelyzeKernel *k = nullptr;
     std::vector<VX3_Voxel *> surface;        // d_surface_voxels
     std::vector<double> last_contact;        // contact force per voxel captured before the voxel pass
+    std::vector<VX3_Link *> new_links;       // links made at runtime (the tail of d_v_links), in creation order
+    bool cond_set[5] = {false, false, false, false, false};  // AttachCondition/Condition_k given
     float last_dt = 0.0f;
     int steps_done = 0;
     bool diverged = false;
@@ -87,6 +107,8 @@ void build_kernel(RefSim &S) {
         VcudaMemcpy(k->d_linkMats + i, &tmp, sizeof(VX3_MaterialLink), VcudaMemcpyHostToDevice);
         k->h_linkMats.push_back(lmats[i]);
     }
+    std::vector<VX3_MaterialLink *> &known = g_link_mats[k];
+    for (int i = 0; i < k->num_d_linkMats; i++) known.push_back(k->d_linkMats + i);
 
     k->num_d_voxels = Vx.voxelCount();
     VcudaMalloc((void **)&k->d_voxels, (k->num_d_voxels ? k->num_d_voxels : 1) * sizeof(VX3_Voxel));
@@ -172,8 +194,8 @@ bool is_neighbor(VX3_Voxel *voxel1, VX3_Voxel *voxel2, VX3_Link *incoming_link, 
     return false;
 }
 
-// collision half of handle_collision_attachment (VX3_VoxelyzeKernel.cu:682-727)
-void collide_pair(VX3_Voxel *voxel1, VX3_Voxel *voxel2, VX3_VoxelyzeKernel *k) {
+// handle_collision_attachment (VX3_VoxelyzeKernel.cu:682-830), collision then attachment
+void collide_pair(RefSim &S, VX3_Voxel *voxel1, VX3_Voxel *voxel2, VX3_VoxelyzeKernel *k) {
     if (voxel1->mat->fixed && voxel2->mat->fixed) return;
     VX3_Vec3D<double> diff = voxel1->pos - voxel2->pos;
     double watchDistance = (voxel1->baseSizeAverage() + voxel2->baseSizeAverage()) * COLLISION_ENVELOPE_RADIUS;
@@ -182,14 +204,61 @@ void collide_pair(VX3_Voxel *voxel1, VX3_Voxel *voxel2, VX3_VoxelyzeKernel *k) {
     if (diff.z > watchDistance || diff.z < -watchDistance) return;
     if (diff.Length() > watchDistance) return;
     if (is_neighbor(voxel1, voxel2, NULL, 1)) return;
+    VX3_Vec3D<> c1, c2;
     if (k->EnableCollision) {
         VX3_Collision collision(voxel1, voxel2);
         collision.updateContactForce();
-        VX3_Vec3D<> c1 = collision.contactForce(voxel1);
-        VX3_Vec3D<> c2 = collision.contactForce(voxel2);
+        c1 = collision.contactForce(voxel1);
+        c2 = collision.contactForce(voxel2);
         voxel1->contactForce += c1;
         voxel2->contactForce += c2;
     }
+    if (!k->enableAttach) return;
+    // the attachment half (:729-830)
+    if (!voxel1->enableAttach || !voxel2->enableAttach) return;
+    if (voxel1->mat->fixed || voxel2->mat->fixed) return;
+    if (voxel1->mat != voxel2->mat) return;
+    if (!voxel1->mat->sticky) return;
+    if (is_neighbor(voxel1, voxel2, NULL, 5)) return;
+    linkDirection dir1, dir2;
+    linkAxis axis;
+    VX3_Vec3D<double> e = voxel1->position() - voxel2->position();
+    VX3_Vec3D<double> ea = voxel1->orientation().RotateVec3DInv(-e);
+    VX3_Vec3D<double> f = ea.Abs();
+    bool reverse = false;
+    if (f.x >= f.y && f.x >= f.z) {
+        axis = X_AXIS;
+        if (ea.x < 0) dir1 = X_NEG, dir2 = X_POS, reverse = true;
+        else dir1 = X_POS, dir2 = X_NEG;
+    } else if (f.y >= f.x && f.y >= f.z) {
+        axis = Y_AXIS;
+        if (ea.y < 0) dir1 = Y_NEG, dir2 = Y_POS, reverse = true;
+        else dir1 = Y_POS, dir2 = Y_NEG;
+    } else {
+        axis = Z_AXIS;
+        if (ea.z < 0) dir1 = Z_NEG, dir2 = Z_POS, reverse = true;
+        else dir1 = Z_POS, dir2 = Z_NEG;
+    }
+    if (voxel1->links[dir1] != NULL || voxel2->links[dir2] != NULL) return;
+    VX3_Link *pL = reverse ? new VX3_Link(voxel1, dir1, voxel2, dir2, axis, k)
+                           : new VX3_Link(voxel2, dir2, voxel1, dir1, axis, k);
+    pL->isNewLink = k->SafetyGuard;
+    S.new_links.push_back(pL);
+    k->isSurfaceChanged = true;
+    voxel1->contactForce -= c1;
+    voxel2->contactForce -= c2;
+}
+
+// every link of the kernel: the lattice's (d_links), then the runtime ones
+int link_count(const RefSim &S) { return S.k->num_d_links + (int)S.new_links.size(); }
+VX3_Link *link_at(const RefSim &S, int i) {
+    return i < S.k->num_d_links ? S.k->d_links + i : S.new_links[(size_t)(i - S.k->num_d_links)];
+}
+int link_index(const RefSim &S, const VX3_Link *L) {
+    if (L >= S.k->d_links && L < S.k->d_links + S.k->num_d_links) return (int)(L - S.k->d_links);
+    for (size_t j = 0; j < S.new_links.size(); j++)
+        if (S.new_links[j] == L) return S.k->num_d_links + (int)j;
+    return -1;
 }
 
 // removeVoxels (VX3_VoxelyzeKernel.cu:365-397), restated over the kernel's arrays: once a
@@ -248,10 +317,10 @@ bool do_time_step(RefSim &S) {
     dt = k->DtFrac * k->OptimalDt;
     S.last_dt = dt;
 
-    // gpu_update_links (:566-581)
+    // gpu_update_links (:566-581) over d_v_links
     bool diverged = false;
-    for (int i = 0; i < k->num_d_links; i++) {
-        VX3_Link *t = k->d_links + i;
+    for (int i = 0; i < link_count(S); i++) {
+        VX3_Link *t = link_at(S, i);
         if (t->removed) continue;
         if (t->pVPos->mat->fixed && t->pVNeg->mat->fixed) continue;
         if (t->isDetached) continue;
@@ -272,7 +341,7 @@ bool do_time_step(RefSim &S) {
                 VX3_Voxel *voxel1 = S.surface[first];
                 VX3_Voxel *voxel2 = S.surface[second];
                 if (voxel1->removed || voxel2->removed) continue;
-                collide_pair(voxel1, voxel2, k);
+                collide_pair(S, voxel1, voxel2, k);
             }
     }
     S.last_contact.assign((size_t)k->num_d_voxels * 3, 0.0);
@@ -284,8 +353,8 @@ bool do_time_step(RefSim &S) {
 
     // updateDetach / gpu_update_detach (:292-294, :946-967), after the collision pass
     if (k->enableDetach) {
-        for (int i = 0; i < k->num_d_links; i++) {
-            VX3_Link *t = &k->d_links[i];
+        for (int i = 0; i < link_count(S); i++) {
+            VX3_Link *t = link_at(S, i);
             if (t->removed || t->isDetached) continue;
             if (t->isFailed()) {
                 t->isDetached = true;
@@ -314,6 +383,15 @@ bool do_time_step(RefSim &S) {
         if (t->removed) continue;
         if (t->mat->fixed) continue;
         t->timeStep(dt, k->currentTime, k);
+        if (k->enableAttach) {  // update sticky status (:606-621); an absent condition holds
+            bool ok = true;
+            for (int c = 0; c < 5 && ok; c++)
+                if (S.cond_set[c] && !(VX3_MathTree::eval(t->pos.x, t->pos.y, t->pos.z, k->collisionCount, k->currentTime,
+                                                          k->recentAngle, k->targetCloseness, k->numClosePairs,
+                                                          k->num_d_voxels, k->AttachCondition[c]) > 0))
+                    ok = false;
+            t->enableAttach = ok;
+        }
     }
     // SecondaryExperiment (:335-349): material removal at the end of the step, before the
     // time advances (the initial-position reset there is the caller's bookkeeping)
@@ -393,6 +471,22 @@ void vx3ref_set_cilia(void *h, int enable) { ((RefSim *)h)->k->EnableCilia = ena
 void vx3ref_set_detach(void *h, int enable) { ((RefSim *)h)->k->enableDetach = enable != 0; }
 // VXA.Simulator.SecondaryExperiment (VX3_SimulationManager.cu:364)
 void vx3ref_set_secondary(void *h, int enable) { ((RefSim *)h)->k->SecondaryExperiment = enable; }
+// VXA.Simulator.AttachDetach.EnableAttach and SafetyGuard (VX3_SimulationManager.cu:329,333)
+void vx3ref_set_attach(void *h, int enable, int safety_guard) {
+    ((RefSim *)h)->k->enableAttach = enable != 0;
+    ((RefSim *)h)->k->SafetyGuard = safety_guard;
+}
+// AttachCondition/Condition_k (VX3_SimulationManager.cu:334-343), tokens laid out as for
+// vx3ref_set_force_field
+int vx3ref_set_attach_condition(void *h, int k, const void *tokens, int n) {
+    struct Tok { int op, reserved; double value; };
+    RefSim *S = (RefSim *)h;
+    if (k < 0 || k > 4 || n < 1 || n > 1024) return -1;
+    const Tok *t = (const Tok *)tokens;
+    for (int i = 0; i < n; i++) S->k->AttachCondition[k][i].set((VX3_MathTreeOperator)t[i].op, t[i].value);
+    S->cond_set[k] = true;
+    return 0;
+}
 // VXA.Simulator.EnableSignals (VX3_SimulationManager.cu:361)
 void vx3ref_set_signals(void *h, int enable) { ((RefSim *)h)->k->EnableSignals = enable; }
 // per voxel: localSignal
@@ -406,7 +500,7 @@ void vx3ref_destroy(void *h) { /* the reference frees nothing reliably either; l
 void vx3ref_counts(void *h, int *nv, int *nl, int *nsurf) {
     RefSim *S = (RefSim *)h;
     *nv = S->k->num_d_voxels;
-    *nl = S->k->num_d_links;
+    *nl = link_count(*S);
     *nsurf = (int)S->surface.size();
 }
 
@@ -445,20 +539,22 @@ void vx3ref_voxels(void *h, double *pos, double *orient, double *linmom, double 
 
 // per voxel: material index (into the voxel material list), lattice indices, 6 link slots (-1 if none)
 void vx3ref_topology(void *h, int *mat, int *ijk, int *slots) {
-    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
+    RefSim *S = (RefSim *)h;
+    VX3_VoxelyzeKernel *k = S->k;
     for (int i = 0; i < k->num_d_voxels; i++) {
         VX3_Voxel &v = k->d_voxels[i];
         mat[i] = (int)(v.mat - k->d_voxelMats);
         ijk[3 * i] = v.ix; ijk[3 * i + 1] = v.iy; ijk[3 * i + 2] = v.iz;
-        for (int d = 0; d < 6; d++) slots[6 * i + d] = v.links[d] ? (int)(v.links[d] - k->d_links) : -1;
+        for (int d = 0; d < 6; d++) slots[6 * i + d] = v.links[d] ? link_index(*S, v.links[d]) : -1;
     }
 }
 
 // per link: neg, pos voxel index, axis, small-angle flag, bool states
 void vx3ref_link_topology(void *h, int *negpos, int *axis, int *small, int *states) {
-    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
-    for (int i = 0; i < k->num_d_links; i++) {
-        VX3_Link &L = k->d_links[i];
+    RefSim *S = (RefSim *)h;
+    VX3_VoxelyzeKernel *k = S->k;
+    for (int i = 0; i < link_count(*S); i++) {
+        VX3_Link &L = *link_at(*S, i);
         negpos[2 * i] = vidx(k, L.pVNeg);
         negpos[2 * i + 1] = vidx(k, L.pVPos);
         axis[i] = (int)L.axis;
@@ -469,9 +565,9 @@ void vx3ref_link_topology(void *h, int *negpos, int *axis, int *small, int *stat
 
 // per link: strain, maxStrain, restLength, pos2/angle1v/angle2v (9), forceNeg/forcePos/momentNeg/momentPos (12)
 void vx3ref_links(void *h, float *strain, float *maxstrain, double *rest, double *local9, double *forces12) {
-    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
-    for (int i = 0; i < k->num_d_links; i++) {
-        VX3_Link &L = k->d_links[i];
+    RefSim *S = (RefSim *)h;
+    for (int i = 0; i < link_count(*S); i++) {
+        VX3_Link &L = *link_at(*S, i);
         strain[i] = L.strain;
         maxstrain[i] = L.maxStrain;
         rest[i] = L.currentRestLength;
@@ -504,30 +600,34 @@ void vx3ref_voxel_mats(void *h, float *f16, double *nomsize, int *fixed_measured
     }
 }
 int vx3ref_num_voxel_mats(void *h) { return ((RefSim *)h)->k->num_d_voxelMats; }
-int vx3ref_num_link_mats(void *h) { return ((RefSim *)h)->k->num_d_linkMats; }
+int vx3ref_num_link_mats(void *h) { return (int)g_link_mats[((RefSim *)h)->k].size(); }
 
 // link mats: 16 floats each: E, nu, eHat, a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp, epsilonFail, linear, alphaCTE
 void vx3ref_link_mats(void *h, float *f16, int *lmat_of_link) {
-    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
-    for (int i = 0; i < k->num_d_linkMats; i++) {
-        VX3_MaterialLink &m = k->d_linkMats[i];
+    RefSim *S = (RefSim *)h;
+    const std::vector<VX3_MaterialLink *> &all = g_link_mats[S->k];
+    for (size_t i = 0; i < all.size(); i++) {
+        VX3_MaterialLink &m = *all[i];
         float *f = f16 + 16 * i;
         f[0] = m.E; f[1] = m.nu; f[2] = m._eHat; f[3] = m._a1; f[4] = m._a2; f[5] = m._b1; f[6] = m._b2; f[7] = m._b3;
         f[8] = m._sqA1; f[9] = m._sqA2xIp; f[10] = m._sqB1; f[11] = m._sqB2xFMp; f[12] = m._sqB3xIp;
         f[13] = m.epsilonFail; f[14] = m.linear ? 1.0f : 0.0f; f[15] = m.alphaCTE;
     }
-    for (int i = 0; i < k->num_d_links; i++) lmat_of_link[i] = (int)(k->d_links[i].mat - k->d_linkMats);
+    for (int i = 0; i < link_count(*S); i++) {
+        VX3_MaterialLink *m = link_at(*S, i)->mat;
+        lmat_of_link[i] = (int)(std::find(all.begin(), all.end(), m) - all.begin());
+    }
 }
 
 // per link: the plastic strain offset (VX3_Link::strainOffset) of non-linear materials
 void vx3ref_link_offsets(void *h, float *off) {
-    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
-    for (int i = 0; i < k->num_d_links; i++) off[i] = k->d_links[i].strainOffset;
+    RefSim *S = (RefSim *)h;
+    for (int i = 0; i < link_count(*S); i++) off[i] = link_at(*S, i)->strainOffset;
 }
 
 // stress-strain points of link material i ((0,0) first); returns their count, copies at most cap
 int vx3ref_link_curve(void *h, int i, float *strain, float *stress, int cap) {
-    VX3_MaterialLink &m = ((RefSim *)h)->k->d_linkMats[i];
+    VX3_MaterialLink &m = *g_link_mats[((RefSim *)h)->k][(size_t)i];
     const int n = (int)m.d_strainData.size();
     for (int j = 0; j < n && j < cap; j++) {
         strain[j] = m.d_strainData[j];
@@ -538,10 +638,10 @@ int vx3ref_link_curve(void *h, int i, float *strain, float *stress, int cap) {
 
 // link transverse info frozen at init: area, strainSum
 void vx3ref_link_transverse(void *h, float *area, float *ssum) {
-    VX3_VoxelyzeKernel *k = ((RefSim *)h)->k;
-    for (int i = 0; i < k->num_d_links; i++) {
-        area[i] = k->d_links[i].currentTransverseArea;
-        ssum[i] = k->d_links[i].currentTransverseStrainSum;
+    RefSim *S = (RefSim *)h;
+    for (int i = 0; i < link_count(*S); i++) {
+        area[i] = link_at(*S, i)->currentTransverseArea;
+        ssum[i] = link_at(*S, i)->currentTransverseStrainSum;
     }
 }
 

@@ -6,11 +6,13 @@
  * written so that C's usual conversions reproduce the reference's mix of
  * float and double exactly (build with -ffp-contract=off).
  *
- * Scope: linear materials (MatModel 0/1); the link table changes only by detach
- * and by material removal (no attachment); no boundary-condition regions, no
- * signals (cilia with the signal at 0);
- * force field: the robot's x/y/z math-tree programs (constant 0 when absent, the
- * reference default, VX3_ForceField.h:10-20), target-tracking variables 0.
+ * Scope: material models 0-3 (linear, linear with failure, bilinear, data points);
+ * boundary-condition regions; signals and cilia; the link table changes by detach,
+ * by material removal and by attachment (runtime links between touching Sticky
+ * voxels of one material whose Poisson's ratio is 0, in the serial pair loop's
+ * order); force field and attach conditions: math-tree programs (force field 0
+ * when absent, the reference default, VX3_ForceField.h:10-20; an absent attach
+ * condition holds), target-tracking variables 0.
  */
 #include "vx3_oracle.h"
 
@@ -303,6 +305,7 @@ typedef struct {
     double remove_after;          /* RemoveFromSimulationAfterThisManySeconds (VX_Object.cpp:1427) */
     int pacemaker;                /* isPaceMaker */
     double pace_period, sig_decay, sig_delay, inactive; /* PaceMakerPeriod, signalValueDecay, signalTimeDelay, inactivePeriod */
+    int sticky;                   /* Sticky (VX_Object.cpp:1436) */
 } vmat;
 
 typedef struct {
@@ -344,6 +347,7 @@ static void vmat_import(vmat *m, const vxo_material *in, const vxo_robot *r) {
     m->sig_delay = in->signal_time_delay;
     m->inactive = in->inactive_period;
     m->remove_after = in->remove_after;
+    m->sticky = in->sticky != 0;
     /* the model as CVX_Sim::CopyMat sets it (VX_Sim.cpp:390-409) */
     int ok = 0;
     if (in->model == 0) ok = curve_linear(&m->cv, (float)in->E, -1.0f);
@@ -468,6 +472,7 @@ typedef struct {
      * inactiveUntil, the pending signal d_signal {value, activeTime}; all 0 at the start */
     double sig_local, sig_local_dt, pace_next, inactive_until, sig_value, sig_active;
     int stepped; /* reached the end of timeStep this step (signals run only there) */
+    int attach_ok; /* VX3_Voxel::enableAttach: the attach conditions held after its last step (true at first) */
 } voxel;
 
 typedef struct {
@@ -479,11 +484,13 @@ typedef struct {
     double rest;
     int small, states;
     int gone; /* detached (gpu_update_detach): no longer updated, no longer any voxel's link */
+    int is_new; /* VX3_Link::isNewLink: updates left whose forces are scaled by 0.01 (runtime links) */
 } link;
 
 typedef struct {
     vxo_robot r;
     int nv, nl, nvm, nlm, ns;
+    int nl0, lcap;            /* links of the lattice (recommendedTimeStep reads only those); capacity */
     vmat *vm;
     lmat *lm;
     voxel *v;
@@ -500,6 +507,7 @@ typedef struct {
     vec *cilia_shift;      /* per voxel: ShiftCiliaForce (scaled by localSignal), or NULL */
     int *mat_removed;      /* per material: removeVoxels has removed it (VX3_MaterialVoxel::removed) */
     vext *ext;             /* per voxel: boundary-condition externals, or NULL without regions */
+    vxo_math_token *acond[5]; /* attach-condition programs (copies) or NULL */
 } sim;
 
 /* VX3_MathTree::eval (src/Utils/VX3_MathTree.h:50-191): tokens in order, each result
@@ -584,6 +592,14 @@ void *vxo_create(const vxo_robot *r) {
         S->ff[k] = (vxo_math_token *)calloc((size_t)n + 1, sizeof(vxo_math_token));
         memcpy(S->ff[k], r->force_field[k], sizeof(vxo_math_token) * (size_t)n);
     }
+    for (int k = 0; k < 5; k++) {
+        S->r.attach_cond[k] = NULL;
+        if (!r->attach_cond[k]) continue;
+        int n = 0;
+        while (n < VXO_MAX_TOKENS - 1 && r->attach_cond[k][n].op != 0) n++;
+        S->acond[k] = (vxo_math_token *)calloc((size_t)n + 1, sizeof(vxo_math_token));
+        memcpy(S->acond[k], r->attach_cond[k], sizeof(vxo_math_token) * (size_t)n);
+    }
     int nx = r->nx, ny = r->ny, nz = r->nz, ncell = nx * ny * nz;
     S->nvm = r->n_materials;
     S->vm = (vmat *)calloc(S->nvm ? S->nvm : 1, sizeof(vmat));
@@ -594,7 +610,8 @@ void *vxo_create(const vxo_robot *r) {
     S->nv = 0;
     for (int c = 0; c < ncell; c++) vid[c] = r->lattice[c] > 0 ? S->nv++ : -1;
     S->v = (voxel *)calloc(S->nv ? S->nv : 1, sizeof(voxel));
-    S->l = (link *)calloc(3 * (size_t)(S->nv ? S->nv : 1), sizeof(link));
+    S->lcap = 3 * (S->nv ? S->nv : 1);
+    S->l = (link *)calloc((size_t)S->lcap, sizeof(link));
     S->lm = (lmat *)calloc((size_t)S->nvm * S->nvm + 1, sizeof(lmat));
     S->nl = 0;
     S->nlm = 0;
@@ -611,6 +628,7 @@ void *vxo_create(const vxo_robot *r) {
         v->tempe = 0.0f;
         v->prevDt = 0.0f;
         v->phase = r->phase ? r->phase[c] : 0.0;
+        v->attach_ok = 1; /* VX3_Voxel.h:302 */
         for (int d = 0; d < 6; d++) v->links[d] = -1;
         int nb[3] = {x > 0 ? vid[c - 1] : -1, y > 0 ? vid[c - nx] : -1, z > 0 ? vid[c - nx * ny] : -1};
         for (int a = 0; a < 3; a++) {
@@ -696,6 +714,7 @@ void *vxo_create(const vxo_robot *r) {
         free(size);
     }
     for (int i = 0; i < S->nl; i++) update_rest(S, &S->l[i]);
+    S->nl0 = S->nl;
     S->surf = (int *)malloc(sizeof(int) * (S->nv ? S->nv : 1));
     S->last_contact = (double *)calloc(3 * (size_t)(S->nv ? S->nv : 1), sizeof(double));
     S->surface_stale = 1;
@@ -714,6 +733,7 @@ void vxo_destroy(void *h) {
     if (!S) return;
     free(S->vm); free(S->lm); free(S->v); free(S->l); free(S->surf); free(S->last_contact);
     free(S->ff[0]); free(S->ff[1]); free(S->ff[2]); free(S->cilia_base); free(S->cilia_shift); free(S->mat_removed); free(S->ext);
+    for (int k = 0; k < 5; k++) free(S->acond[k]);
     free(S);
 }
 
@@ -819,6 +839,13 @@ static void link_update(sim *S, link *L) {
     L->fPos = to_axis_original(L->axis, fPos);
     L->mNeg = to_axis_original(L->axis, mNeg);
     L->mPos = to_axis_original(L->axis, mPos);
+    if (L->is_new) { /* a runtime link's first SafetyGuard updates (VX3_Link.cu:206-213) */
+        L->fNeg = vscale(L->fNeg, 0.01);
+        L->fPos = vscale(L->fPos, 0.01);
+        L->mNeg = vscale(L->mNeg, 0.01);
+        L->mPos = vscale(L->mPos, 0.01);
+        L->is_new -= 1;
+    }
 }
 
 /* VX3_Voxel::floorForce (VX3_Voxel.cu:399-426) */
@@ -986,7 +1013,7 @@ static void voxel_signals(sim *S, voxel *v) {
 double vxo_recommended_dt(void *h) {
     sim *S = (sim *)h;
     double MaxFreq2 = 0.0f;
-    for (int i = 0; i < S->nl; i++) {
+    for (int i = 0; i < S->nl0; i++) { /* the lattice's links (num_d_links), not runtime ones */
         link *L = &S->l[i];
         const lmat *m = &S->lm[L->mat];
         double m1 = S->vm[S->v[L->neg].mat].mass, m2 = S->vm[S->v[L->pos].mat].mass;
@@ -1022,9 +1049,10 @@ static int is_linked(const sim *S, int a, int b) {
 
 /* handle_collision_attachment (collision half) + VX3_Collision
  * (VX3_VoxelyzeKernel.cu:682-727, VX3_Collision.cu:3-31) */
-/* the contact force of one surface pair (voxel1 = v1, the later in surface order), or 0
- * where the reference's handle_collision_attachment leaves the pair before adding one
- * (VX3_VoxelyzeKernel.cu:682-727, VX3_Collision.cu:3-31) */
+/* the contact force of one surface pair (voxel1 = v1, the later in surface order): 1 with
+ * the force in *out; 0 where the reference's handle_collision_attachment leaves the pair
+ * before any contact (VX3_VoxelyzeKernel.cu:682-727, VX3_Collision.cu:3-31); 2 where it
+ * passes the pair on to the attachment half without a contact (EnableCollision off) */
 static int pair_force(const sim *S, const voxel *v1, const voxel *v2, int i1, int i2, double bsa1, double bsa2,
                       vec *out) {
     const vmat *m1 = &S->vm[v1->mat], *m2 = &S->vm[v2->mat];
@@ -1036,7 +1064,7 @@ static int pair_force(const sim *S, const voxel *v1, const voxel *v2, int i1, in
     if (diff.z > wd || diff.z < -wd) return 0;
     if (vlen(diff) > wd) return 0;
     if (is_linked(S, i1, i2)) return 0;
-    if (!S->r.enable_collision) return 0;
+    if (!S->r.enable_collision) return 2;
     float k1 = (float)(2 * m1->E * m1->nom_size), k2 = (float)(2 * m2->E * m2->nom_size);
     double pstiff = 2.0f / (1.0f / k1 + 1.0f / k2);
     double dampC = 0.5f * (m1->z_col * m1->c2xSqMxExS + m2->z_col * m2->c2xSqMxExS);
@@ -1053,11 +1081,91 @@ static int pair_force(const sim *S, const voxel *v1, const voxel *v2, int i1, in
     return 1;
 }
 
+static void attach_pair(sim *S, int i1, int i2, int had_contact, vec f);
+
 static void collide(sim *S, voxel *v1, voxel *v2, int i1, int i2) {
-    vec f;
-    if (!pair_force(S, v1, v2, i1, i2, base_size_avg(S, v1), base_size_avg(S, v2), &f)) return;
-    v1->contact = vadd(v1->contact, f);
-    v2->contact = vadd(v2->contact, vneg(f));
+    vec f = V(0, 0, 0);
+    const int rc = pair_force(S, v1, v2, i1, i2, base_size_avg(S, v1), base_size_avg(S, v2), &f);
+    if (!rc) return;
+    if (rc == 1) {
+        v1->contact = vadd(v1->contact, f);
+        v2->contact = vadd(v2->contact, vneg(f));
+    }
+    if (S->r.enable_attach) attach_pair(S, i1, i2, rc == 1, f);
+}
+
+/* is_neighbor (VX3_VoxelyzeKernel.cu:651-680): b within `depth` links of a, never going
+ * straight back over the link just taken */
+static int within_links(const sim *S, int a, int b, int incoming, int depth) {
+    if (a == b) return 1;
+    if (depth <= 0) return 0;
+    for (int d = 0; d < 6; d++) {
+        const int li = S->v[a].links[d];
+        if (li < 0 || li == incoming) continue;
+        const link *L = &S->l[li];
+        if (within_links(S, L->neg == a ? L->pos : L->neg, b, li, depth - 1)) return 1;
+    }
+    return 0;
+}
+
+/* VX3_VoxelyzeKernel::combinedMaterial (:515-528) for two voxels of one material m: the
+ * link material of the pair (m, m), made on first use */
+static int lmat_same(sim *S, int m) {
+    for (int k = 0; k < S->nlm; k++)
+        if (S->lm[k].m1 == m && S->lm[k].m2 == m) return k;
+    lmat_make(&S->lm[S->nlm], &S->vm[m], &S->vm[m], m, m);
+    return S->nlm++;
+}
+
+/* the attachment half of handle_collision_attachment (VX3_VoxelyzeKernel.cu:729-830), for a
+ * pair that passed the envelope and direct-neighbour tests: two enableAttach voxels of one
+ * Sticky, unfixed material more than five links apart get a new link along the dominant
+ * axis of voxel2's offset in voxel1's frame, if both of those faces are free; the pair's
+ * contact of this step is taken back.  The new link is the device constructor's
+ * (VX3_Link.cu:31-56) after reset() (:58-70): zero state, small-angle, no valid local
+ * velocity, rest length from both base sizes, transverse area of two unstrained faces
+ * (the material's Poisson's ratio is 0), isNewLink = SafetyGuard. */
+static void attach_pair(sim *S, int i1, int i2, int had_contact, vec f) {
+    voxel *v1 = &S->v[i1], *v2 = &S->v[i2];
+    if (!v1->attach_ok || !v2->attach_ok) return;
+    const vmat *m1 = &S->vm[v1->mat];
+    if (m1->fixed || S->vm[v2->mat].fixed) return;
+    if (v1->mat != v2->mat) return;
+    if (!m1->sticky) return;
+    if (within_links(S, i1, i2, -1, 5)) return;
+    const vec ea = qrotinv(v1->orient, vneg(vsub(v1->pos, v2->pos)));
+    const vec fa = V(fabs(ea.x), fabs(ea.y), fabs(ea.z));
+    int axis, rev;
+    if (fa.x >= fa.y && fa.x >= fa.z) axis = 0, rev = ea.x < 0;
+    else if (fa.y >= fa.x && fa.y >= fa.z) axis = 1, rev = ea.y < 0;
+    else axis = 2, rev = ea.z < 0;
+    const int d1 = 2 * axis + (rev ? 1 : 0), d2 = 2 * axis + (rev ? 0 : 1);
+    if (v1->links[d1] >= 0 || v2->links[d2] >= 0) return;
+    if (S->nl == S->lcap) {
+        S->lcap *= 2;
+        S->l = (link *)realloc(S->l, sizeof(link) * (size_t)S->lcap);
+    }
+    link *L = &S->l[S->nl];
+    memset(L, 0, sizeof(*L));
+    L->neg = rev ? i2 : i1; /* the voxel on the axis' negative side */
+    L->pos = rev ? i1 : i2;
+    L->axis = axis;
+    L->mat = lmat_same(S, v1->mat);
+    L->small = 1;
+    L->states = 0;
+    update_rest(S, L);
+    const float sz = (float)m1->nom_size;
+    L->area = 0.5f * (sz * sz + sz * sz);
+    L->tss = 0.0f;
+    L->is_new = S->r.safety_guard;
+    v1->links[d1] = S->nl;
+    v2->links[d2] = S->nl;
+    S->nl++;
+    S->surface_stale = 1;
+    if (had_contact) {
+        v1->contact = vsub(v1->contact, f);
+        v2->contact = vsub(v2->contact, vneg(f));
+    }
 }
 
 /* The serial pair loop adds to the contact of surface voxel k first its pairs (k, b),
@@ -1213,8 +1321,12 @@ static int do_step(sim *S) {
             if (!interior && !S->v[i].removed) S->surf[S->ns++] = i;
         }
     }
-    /* gpu_update_attach (:833-843): pairs first > second in surface order */
-    if (r->enable_collision) {
+    /* gpu_update_attach (:833-843): pairs first > second in surface order; with
+     * attachment the serial loop itself (links made by earlier pairs count for later ones) */
+    if (r->enable_attach) {
+        for (int a = 0; a < S->ns; a++)
+            for (int b = 0; b < a; b++) collide(S, &S->v[S->surf[a]], &S->v[S->surf[b]], S->surf[a], S->surf[b]);
+    } else if (r->enable_collision) {
         if (S->threads > 1 && S->exact) collide_gather_threaded(S);
         else if (S->threads > 1) collide_rows_threaded(S, 0, S->ns);
         else
@@ -1249,6 +1361,15 @@ static int do_step(sim *S) {
         if (S->vm[S->v[i].mat].fixed) continue;
         voxel_update(S, &S->v[i], dt);
     }
+    if (r->enable_attach) /* gpu_update_voxels (:606-621): enableAttach after the voxel's step */
+        for (int i = 0; i < S->nv; i++) {
+            voxel *v = &S->v[i];
+            if (v->removed || S->vm[v->mat].fixed) continue;
+            int ok = 1;
+            for (int k = 0; k < 5 && ok; k++)
+                if (S->acond[k] && !(math_eval(S->acond[k], v->pos.x, v->pos.y, v->pos.z, S->t, S->nv) > 0)) ok = 0;
+            v->attach_ok = ok;
+        }
     if (r->enable_signals)  /* in voxel order, after the voxel pass (see voxel_signals) */
         for (int i = 0; i < S->nv; i++)
             if (S->v[i].stepped && !S->v[i].removed && !S->vm[S->v[i].mat].fixed) voxel_signals(S, &S->v[i]);

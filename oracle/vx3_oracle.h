@@ -30,6 +30,7 @@ typedef struct vxo_material {
     const double *strain_data, *stress_data;
     int is_pacemaker;                 /* isPaceMaker */
     double pacemaker_period, signal_value_decay, signal_time_delay, inactive_period;
+    int sticky;                       /* Sticky: runtime links with touching voxels of this material */
 } vxo_material;
 
 /* A math-tree token (VX3_MathTreeToken, src/Utils/VX3_MathTree.h:29-36): op is the
@@ -68,6 +69,9 @@ typedef struct vxo_robot {
     int n_bcs;                            /* Environment/Boundary_Conditions regions */
     const vxo_bc_region *bcs;
     int enable_signals;                   /* Simulator/EnableSignals */
+    int enable_attach;                    /* Simulator/AttachDetach/EnableAttach */
+    int safety_guard;                     /* Simulator/AttachDetach/SafetyGuard (the reference's default is 500) */
+    const vxo_math_token *attach_cond[5]; /* AttachCondition/Condition_0..4 programs, or NULL (no condition) */
 } vxo_robot;
 
 void *vxo_create(const vxo_robot *r);

@@ -171,10 +171,56 @@ def cases():
     sig.cilia_base = 1e-2 * rng.standard_normal(sig.grid.shape + (3,))
     sig.cilia_shift = 2e-4 * rng.standard_normal(sig.grid.shape + (3,))
     out["bern6_signals_cilia"] = (sig, 400, 100)
+    # EnableAttach: sticky pieces dropped on a sticky plate link up where they land (Z axis),
+    # each far (over five links) from the other; a piece of another sticky material and a
+    # non-sticky piece only collide; the first condition holds attachment off for 4 ms and
+    # SafetyGuard 60 ends the new links' force scaling within the run
+    att = np.zeros((5, 3, 11), np.uint8)
+    att[0, :, :] = 1
+    att[2:4, 1, 0:2] = 1
+    att[2:4, 1, 4:6] = 1
+    att[2:4, 1, 8] = 2
+    att[2, 0:2, 10] = 3
+    amats = [wl.Material(E=1e5, nu=0.0, sticky=1, mu_static=0.5, mu_kinetic=0.3),
+             wl.Material(E=2e5, nu=0.0, sticky=1), wl.Material(E=1e5, nu=0.0)]
+    out["sticky_drop_attach"] = (wl.Robot(grid=att, materials=amats, volume_effects=False, enable_collision=True,
+                                          enable_attach=True, safety_guard=60,
+                                          attach_conditions=[("mtGREATERTHAN", ("mtVAR", "t"), ("mtCONST", 0.004))]),
+                                 800, 200)
+    # three bimorph U shapes (each arm an expanding outer layer on a passive inner one, so the
+    # arms bend together as the temperature rises) facing x, y and z: their tips touch and
+    # link along all three axes, ten links at five-link spacing (floor off; no stick/slip,
+    # so the run is not chaotic: a 1e-12 m nudge stays below 1e-9 m over the run)
+    arm, w = 8, 5
+    L = arm + 1
+    u = np.zeros((L, 2 * w + 3, w + L + 2), np.uint8)
+    u[0, 0, 0:w] = 2
+    u[1:L, 0, 0] = 1
+    u[1:L, 0, 1] = 2
+    u[1:L, 0, w - 1] = 1
+    u[1:L, 0, w - 2] = 2
+    y0, x0 = 2, w + 2
+    u[0, y0:y0 + w, 3] = 2
+    u[1:L, y0, 3] = 1
+    u[1:L, y0 + 1, 3] = 2
+    u[1:L, y0 + w - 1, 3] = 1
+    u[1:L, y0 + w - 2, 3] = 2
+    u[0:w, y0, x0] = 2
+    u[0, y0, x0:x0 + L] = 1
+    u[1, y0, x0 + 1:x0 + L] = 2
+    u[w - 1, y0, x0:x0 + L] = 1
+    u[w - 2, y0, x0 + 1:x0 + L] = 2
+    umats = [wl.Material(E=1e5, nu=0.0, sticky=1, cte=0.01), wl.Material(E=1e5, nu=0.0, sticky=1, cte=0.0)]
+    out["bimorph_u3_attach"] = (wl.Robot(grid=u, materials=umats, volume_effects=False, enable_collision=True,
+                                         enable_attach=True, temp_vary=True, temp_amplitude=20.0, temp_period=0.05,
+                                         enable_expansion=1, floor=False, safety_guard=40, phase=np.zeros(u.shape),
+                                         attach_conditions=[("mtGREATERTHAN", ("mtVAR", "t"), ("mtCONST", 0.002)),
+                                                            None, ("mtLESSTHAN", ("mtVAR", "z"), ("mtCONST", 1.0))]),
+                                1600, 400)
     return out
 
 
-def snapshot(s, plastic=False, signals=False):
+def snapshot(s, plastic=False, signals=False, attach=0):
     v = s.voxels()
     lk = s.links()
     t = s.topology()
@@ -186,6 +232,9 @@ def snapshot(s, plastic=False, signals=False):
         out["soffset"] = s.link_offsets()
     if signals:  # EnableSignals: every voxel's localSignal
         out["signal"] = s.signals()
+    if attach:  # EnableAttach (attach = the palette size): the link table as it stands, runtime links appended
+        out["negpos"], out["axis"], out["slots"] = t["negpos"], t["axis"], t["slots"]
+        out["lmat_of_link"] = s.materials(attach)["lmat_of_link"]
     return out
 
 
@@ -196,14 +245,15 @@ def nonlinear(r):
 def robot_record(r):
     g, ph = r.padded()
     mats = np.array([[m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress, m.fixed, m.is_measured,
-                      m.cilia, m.cilia_on_after, m.remove_after] for m in r.materials], np.float64)
+                      m.cilia, m.cilia_on_after, m.remove_after, m.sticky] for m in r.materials], np.float64)
     settings = dict(vox_size=r.vox_size, dt_frac=r.dt_frac, bond_damping=r.bond_damping, col_damping=r.col_damping,
                     slow_damping=r.slow_damping, gravity=r.gravity, grav_acc=r.grav_acc, floor=r.floor,
                     temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,
                     temp_base=r.temp_base, enable_expansion=r.enable_expansion, enable_collision=r.enable_collision,
                     volume_effects=r.volume_effects, force_field=r.force_field, enable_cilia=r.enable_cilia,
                     enable_detach=r.enable_detach, secondary_experiment=r.secondary_experiment,
-                    enable_signals=r.enable_signals)
+                    enable_signals=r.enable_signals, enable_attach=r.enable_attach, safety_guard=r.safety_guard,
+                    attach_conditions=r.attach_conditions)
     rec = dict(lattice=g, phase=(ph if ph is not None else np.zeros(0)), materials=mats,
                settings=np.array(json.dumps(settings)))
     if r.enable_signals:  # signal parameters per palette entry
@@ -246,7 +296,8 @@ def main(only=()):
             n = s.step(every)
             done += every
             snaps.append(done)
-            for k, v in snapshot(s, nonlinear(robot), robot.enable_signals).items():
+            for k, v in snapshot(s, nonlinear(robot), robot.enable_signals,
+                                 len(robot.materials) if robot.enable_attach else 0).items():
                 rec[f"s{done}_{k}"] = v
             rec[f"s{done}_surface"] = s.surface()
             if n < every:

@@ -18,13 +18,14 @@ def names():
 def load(name):
     d = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
     s = json.loads(str(d["settings"]))
-    if s.get("force_field") is not None:  # math trees were stored as nested JSON lists
-        tup = lambda n: tuple(tup(c) if isinstance(c, list) else c for c in n)  # noqa: E731
-        s["force_field"] = [None if t is None else tup(t) for t in s["force_field"]]
+    tup = lambda n: tuple(tup(c) if isinstance(c, list) else c for c in n)  # noqa: E731
+    for key in ("force_field", "attach_conditions"):  # math trees were stored as nested JSON lists
+        if s.get(key) is not None:
+            s[key] = [None if t is None else tup(t) for t in s[key]]
     mats = [wl.Material(E=m[0], nu=m[1], rho=m[2], cte=m[3], mu_static=m[4], mu_kinetic=m[5], fail_stress=m[6],
                         fixed=int(m[7]), is_measured=int(m[8]),
                         cilia=float(m[9]) if len(m) > 9 else 0.0, cilia_on_after=float(m[10]) if len(m) > 10 else 0.0,
-                        remove_after=float(m[11]) if len(m) > 11 else 0.0)
+                        remove_after=float(m[11]) if len(m) > 11 else 0.0, sticky=int(m[12]) if len(m) > 12 else 0)
             for m in d["materials"]]
     if "models" in d.files:  # MatModel 2/3 parameters per palette entry
         for m, md in zip(mats, json.loads(str(d["models"]))):

@@ -31,7 +31,7 @@ class VxoMaterial(ctypes.Structure):
                 ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p),
                 ("is_pacemaker", ctypes.c_int), ("pacemaker_period", ctypes.c_double),
                 ("signal_value_decay", ctypes.c_double), ("signal_time_delay", ctypes.c_double),
-                ("inactive_period", ctypes.c_double)]
+                ("inactive_period", ctypes.c_double), ("sticky", ctypes.c_int)]
 
 
 class VxoBC(ctypes.Structure):
@@ -54,7 +54,8 @@ class VxoRobot(ctypes.Structure):
                 ("force_field", ctypes.c_void_p * 3),
                 ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
                 ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int),
-                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(VxoBC)), ("enable_signals", ctypes.c_int)]
+                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(VxoBC)), ("enable_signals", ctypes.c_int),
+                ("enable_attach", ctypes.c_int), ("safety_guard", ctypes.c_int), ("attach_cond", ctypes.c_void_p * 5)]
 
 
 def build_oracle():
@@ -253,7 +254,7 @@ def robot_struct(robot):
                               m.cilia, m.cilia_on_after, m.remove_after, m.plastic_mod, m.yield_stress,
                               n, None if e is None else _P(e), None if s is None else _P(s),
                               int(m.is_pacemaker), m.pacemaker_period, m.signal_value_decay, m.signal_time_delay,
-                              m.inactive_period)
+                              m.inactive_period, int(m.sticky))
     Z, Y, X = g.shape
     r = VxoRobot(X, Y, Z, _P(lattice), None if phase is None else _P(phase), len(robot.materials), mats,
                  robot.vox_size, robot.dt_frac, robot.grav_acc, int(robot.floor),
@@ -275,19 +276,33 @@ def robot_struct(robot):
     r.enable_detach = int(robot.enable_detach)
     r.secondary_experiment = int(robot.secondary_experiment)
     r.enable_signals = int(robot.enable_signals)
+    r.enable_attach = int(robot.enable_attach)
+    r.safety_guard = int(robot.safety_guard)
+    conds = _attach_tokens(robot)
+    for k, t in enumerate(conds):
+        if t is not None:
+            r.attach_cond[k] = _P(t)
     bcs = None
     if robot.bcs:
         from vx3g.abi import bc_array
         bcs = bc_array(VxoBC, robot.bcs)
         r.n_bcs = len(robot.bcs)
         r.bcs = bcs
-    return r, (lattice, phase, mats, progs, cil, ss_keep, bcs)
+    return r, (lattice, phase, mats, progs, cil, ss_keep, bcs, conds)
 
 
 def _force_field_tokens(robot):
     from vx3g.workloads import math_tokens
     ff = getattr(robot, "force_field", None) or [None] * 3
     return [None if t is None else np.ascontiguousarray(math_tokens(t)) for t in ff]
+
+
+def _attach_tokens(robot):
+    """The five AttachCondition programs (None where absent)."""
+    from vx3g.workloads import math_tokens
+    conds = list(getattr(robot, "attach_conditions", None) or [])
+    conds += [None] * (5 - len(conds))
+    return [None if t is None else np.ascontiguousarray(math_tokens(t)) for t in conds[:5]]
 
 
 def oracle_sim(robot) -> Sim:
@@ -327,4 +342,13 @@ def ref_sim(robot) -> Sim:
     lib.vx3ref_set_signals.restype = None
     lib.vx3ref_set_signals.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.vx3ref_set_signals(h, int(robot.enable_signals))
-    return Sim(lib, "vx3ref_", h, progs)
+    lib.vx3ref_set_attach.restype = None
+    lib.vx3ref_set_attach.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    lib.vx3ref_set_attach(h, int(robot.enable_attach), int(robot.safety_guard))
+    lib.vx3ref_set_attach_condition.restype = ctypes.c_int
+    lib.vx3ref_set_attach_condition.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    conds = _attach_tokens(robot)
+    for k, t in enumerate(conds):
+        if t is not None:
+            assert lib.vx3ref_set_attach_condition(h, k, _P(t), len(t)) == 0
+    return Sim(lib, "vx3ref_", h, (progs, conds))

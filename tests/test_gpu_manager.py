@@ -182,6 +182,30 @@ def test_runner_signals_match_oracle(tmp_path):
     assert np.abs(quiet.com() - s.com()).max() > 1e-4 * robot.vox_size
 
 
+def test_runner_attachment_matches_oracle(tmp_path):
+    """Simulator/AttachDetach/EnableAttach with SafetyGuard, an AttachCondition program and
+    Sticky materials read by the runner from the VXA: the pieces dropped on the plate link
+    up and the report matches the oracle running the same robot; without attachment the
+    robot ends elsewhere."""
+    import golden_cases
+    vbuild.build()
+    exe = os.path.join(os.path.dirname(vbuild.LIB), "vx3g_sim")
+    robot, _ = golden_cases.load("sticky_drop_attach")
+    robot.stop_time = 0.06
+    (tmp_path / "base.vxa").write_text(wl.to_vxa(robot))
+    (tmp_path / "r.vxd").write_text("<VXD>\n</VXD>\n")
+    out = tmp_path / "report.xml"
+    r = subprocess.run([exe, "-i", str(tmp_path), "-o", str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    node = ET.parse(out).getroot().find("detail/r")
+    s, _, _ = _oracle_until(robot, 0.06)
+    assert s.counts()[1] > ob.oracle_sim(robot).counts()[1]  # links were made
+    com = [float(node.find(f"currentCenterOfMass/{k}").text) for k in "xyz"]
+    np.testing.assert_allclose(com, s.com(), rtol=0, atol=1e-6 * robot.vox_size)
+    loose, _, _ = _oracle_until(wl.Robot(**{**robot.__dict__, "enable_attach": False}), 0.06)
+    assert np.abs(loose.com() - s.com()).max() > 1e-4 * robot.vox_size
+
+
 def test_runner_sub_batches_run_concurrently(tmp_path):
     """VX3_SimulationManager::start runs every sub-batch at once, one host thread and
     context per device: four robots dealt round-robin into two sub-batches, both on

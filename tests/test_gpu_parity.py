@@ -32,17 +32,27 @@ def test_fp64_against_reference_golden(name):
     robot, d = golden_cases.load(name)
     b = abi.Batch([robot], abi.PRECISION_FP64)
     t = b.topology()
-    for k in ("ijk", "negpos", "axis", "mat"):
+    n = int(b.links_in_use()[0])  # the link range holds a reserve for runtime links after these
+    for k in ("ijk", "mat"):
         assert np.array_equal(t[k], d["topo_" + k]), k
+    for k in ("negpos", "axis"):
+        assert np.array_equal(t[k][:n], d["topo_" + k]), k
     done = 0
     for snap in d["snap_steps"]:
         snap = int(snap)
         b.step(snap - done)
         done = snap
         st, aux, lk = b.state(), b.voxel_aux(), b.links()
+        n = int(b.links_in_use()[0])
+        lk = {k: v[:n] for k, v in lk.items()}
+        if f"s{snap}_negpos" in d.files:  # attachment: the same runtime links, in order, on the same faces
+            t = b.topology()
+            assert np.array_equal(t["negpos"][:n], d[f"s{snap}_negpos"])
+            assert np.array_equal(t["axis"][:n], d[f"s{snap}_axis"])
         dpos = np.max(np.abs(st["pos"] - d[f"s{snap}_pos"]))
         assert dpos <= POS_TOL * robot.vox_size, f"{name}@{snap}: pos error {dpos:.3e}"
-        assert np.max(np.abs(st["orient"] - d[f"s{snap}_orient"])) < 1e-9
+        dq = np.max(np.abs(st["orient"] - d[f"s{snap}_orient"]))
+        assert dq < 1e-9, f"{name}@{snap}: orientation error {dq:.3e} (links in use {n})"
         assert np.array_equal(b.surface(), d[f"s{snap}_surface"])
         assert np.array_equal(lk["small"] & 1, d[f"s{snap}_small"])
         assert np.array_equal(aux["flags"] & 8, d[f"s{snap}_flags"] & 8)  # static friction
@@ -311,6 +321,115 @@ def test_signals_mixed_matches_fp64():
     assert np.all(rel <= 1e-5), rel
     with pytest.raises(abi.Vx3gError, match="not implemented"):
         abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
+
+
+def _com_links(robot, precision, steps, nudge=0.0, seed=1):
+    b = abi.Batch([robot], precision)
+    if nudge:
+        st = b.state()
+        st["pos"] += nudge * np.random.default_rng(seed).choice([-1.0, 1.0], size=st["pos"].shape)
+        b.set_state(**st)
+    b.step(steps)
+    assert np.all(b.status() == 0)
+    n = int(b.links_in_use()[0])
+    return b.com(), b.topology()["negpos"][:n]
+
+
+@pytest.mark.parametrize("name", ["sticky_drop_attach", "bimorph_u3_attach"])
+def test_attach_mixed_matches_fp64(name):
+    """EnableAttach in mixed precision against FP64.  The bending U shapes are not chaotic:
+    the mixed kernels make the FP64 (and the reference's) runtime links and follow the FP64
+    COM within 1e-5 relative.  The pieces dropped on a plate on the floor are: a 1e-9 m
+    nudge of the FP64 start moves the COM by 1.5e-5 to 1.4e-4 relative (by the nudge's
+    signs) through stick/slip at landing, so there the mixed error must stay within three
+    times the largest spread of four nudged FP64 runs (and the links made are the FP64
+    run's wherever the nudged FP64 runs make them too).  The adjoint refuses attachment."""
+    robot, d = golden_cases.load(name)
+    steps = int(d["snap_steps"][-1])
+    c64, l64 = _com_links(robot, abi.PRECISION_FP64, steps)
+    cmx, lmx = _com_links(robot, abi.PRECISION_MIXED, steps)
+    assert len(l64) == len(d[f"s{steps}_negpos"]) > len(d["topo_negpos"])
+    rel = float(np.linalg.norm(cmx - c64) / np.linalg.norm(c64))
+    if name == "bimorph_u3_attach":
+        assert np.array_equal(lmx, l64)
+        assert rel <= 1e-5, rel
+    else:
+        floor, same = 0.0, True
+        for seed in range(4):
+            cnd, lnd = _com_links(robot, abi.PRECISION_FP64, steps, nudge=1e-9, seed=seed)
+            floor = max(floor, float(np.linalg.norm(cnd - c64) / np.linalg.norm(c64)))
+            same = same and np.array_equal(lnd, l64)
+        if same:
+            assert np.array_equal(lmx, l64)
+        assert rel <= max(1e-5, 3 * floor), (rel, floor)
+    with pytest.raises(abi.Vx3gError, match="not implemented"):
+        abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
+
+
+def _sticky_scene(rng, nx, pieces, attach=True):
+    """A sticky plate nx long on the floor with `pieces` random sticky blocks dropped on it
+    from two cells up, some of a second sticky material, some not sticky; attach conditions
+    on time and height."""
+    g = np.zeros((6, 4, nx), np.uint8)
+    g[0, :, :] = 1
+    for k in range(pieces):
+        x = int(rng.integers(0, nx - 2))
+        h = int(rng.integers(1, 3))
+        mat = 2 if k % 5 == 4 else 3 if k % 7 == 6 else 1
+        g[2:2 + h, int(rng.integers(0, 3)), x:x + int(rng.integers(1, 3))] = mat
+    mats = [wl.Material(E=1e5, nu=0.0, sticky=1, mu_static=0.5, mu_kinetic=0.3),
+            wl.Material(E=2e5, nu=0.0, sticky=1), wl.Material(E=1e5, nu=0.0)]
+    return wl.Robot(grid=g, materials=mats, volume_effects=False, enable_collision=True, enable_attach=attach,
+                    safety_guard=int(rng.integers(20, 200)),
+                    attach_conditions=[("mtGREATERTHAN", ("mtVAR", "t"), ("mtCONST", 0.003)),
+                                       ("mtLESSTHAN", ("mtVAR", "z"), ("mtCONST", 0.05))])
+
+
+def test_attach_batch_matches_oracle():
+    """Attaching robots mixed with others in one batch, on both list builds (a robot longer
+    than 512 cells is rebuilt on the global hashed grid): per robot the FP64 kernels make the
+    oracle's runtime links in the oracle's order and keep its trajectory."""
+    rng = np.random.default_rng(31)
+    robots = [_sticky_scene(rng, 14, 6), wl.solid_block(3), _sticky_scene(rng, 520, 60),
+              golden_cases.load("bimorph_u3_attach")[0], _sticky_scene(rng, 20, 8, attach=False)]
+    b = abi.Batch(robots, abi.PRECISION_FP64)
+    steps = 500
+    b.step(steps)
+    st, t, use = b.state(), b.topology(), b.links_in_use()
+    made = 0
+    for i, r in enumerate(robots):
+        o = ob.oracle_sim(r)
+        n0 = o.counts()[1]
+        o.step(steps)
+        ot = o.topology()
+        lo = b.link_offset[i]
+        assert use[i] == o.counts()[1], i
+        assert np.array_equal(t["negpos"][lo:lo + use[i]], ot["negpos"] + b.voxel_offset[i]), i
+        assert np.array_equal(t["axis"][lo:lo + use[i]], ot["axis"]), i
+        err = np.max(np.abs(_robot_slice(b, i, st["pos"]) - o.voxels()["pos"]))
+        assert err <= POS_TOL * r.vox_size, (i, err)
+        made += int(use[i]) - n0
+    assert made >= 10, made
+    assert np.all(b.status() == 0)
+
+
+def test_attach_inputs_are_checked():
+    """Attachment needs collisions, and a Sticky material must be linear with Poisson's
+    ratio 0 (the runtime link's transverse area is the unstrained one)."""
+    for bad in ("collision", "poisson", "bilinear"):
+        r = golden_cases.load("sticky_drop_attach")[0]
+        if bad == "collision":
+            r.enable_collision = False
+        elif bad == "poisson":
+            r.volume_effects = True
+            r.materials[0].nu = 0.3
+        else:
+            m = r.materials[0]
+            m.model, m.plastic_mod, m.yield_stress, m.fail_stress = 2, 2e4, 50.0, -1.0
+        with pytest.raises(abi.Vx3gError, match="attach|Sticky"):
+            abi.Batch([r], abi.PRECISION_FP64)
+    robot, d = golden_cases.load("sticky_drop_attach")
+    assert abi.Batch([robot], abi.PRECISION_FP64).links_in_use()[0] == len(d["topo_negpos"])
 
 
 @pytest.mark.parametrize("name", ["beam10_clamped_bcs", "bern6_partial_bcs"])

@@ -3,7 +3,8 @@
 Golden vectors come from the reference sources compiled on the host
 (tests/golden/make_golden.py).  The restatement must reproduce them bit for
 bit: same topology and ordering, same derived material constants, and the
-same voxel/link state after every snapshot interval.
+same voxel/link state after every snapshot interval (with attachment: the same
+runtime links, in the same order, on the same faces).
 """
 
 import numpy as np
@@ -51,6 +52,9 @@ def test_trajectory_bit_exact(name):
             got["soffset"] = s.link_offsets()
         if f"s{snap}_signal" in d.files:
             got["signal"] = s.signals()
+        if f"s{snap}_negpos" in d.files:  # attachment: the link table with its runtime links
+            got.update(negpos=t["negpos"], axis=t["axis"], slots=t["slots"],
+                       lmat_of_link=s.materials(len(robot.materials))["lmat_of_link"])
         for k, a in got.items():
             b = d[f"s{snap}_{k}"]
             assert np.array_equal(a, b, equal_nan=True), f"{name} step {snap}: {k} differs (max {np.max(np.abs(a - b)) if a.shape == b.shape else 'shape'})"

@@ -39,7 +39,7 @@ class Material(ctypes.Structure):
                 ("n_data", ctypes.c_int), ("strain_data", ctypes.c_void_p), ("stress_data", ctypes.c_void_p),
                 ("is_pacemaker", ctypes.c_int), ("pacemaker_period", ctypes.c_double),
                 ("signal_value_decay", ctypes.c_double), ("signal_time_delay", ctypes.c_double),
-                ("inactive_period", ctypes.c_double)]
+                ("inactive_period", ctypes.c_double), ("sticky", ctypes.c_int)]
 
 
 class BCRegion(ctypes.Structure):
@@ -72,7 +72,9 @@ class RobotDesc(ctypes.Structure):
                 ("log10E", ctypes.c_void_p), ("force_field", ctypes.c_void_p * 3),
                 ("enable_cilia", ctypes.c_int), ("cilia_base", ctypes.c_void_p), ("cilia_shift", ctypes.c_void_p),
                 ("enable_detach", ctypes.c_int), ("secondary_experiment", ctypes.c_int),
-                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(BCRegion)), ("enable_signals", ctypes.c_int)]
+                ("n_bcs", ctypes.c_int), ("bcs", ctypes.POINTER(BCRegion)), ("enable_signals", ctypes.c_int),
+                ("enable_attach", ctypes.c_int), ("safety_guard", ctypes.c_int),
+                ("attach_condition", ctypes.c_void_p * 5)]
 
 
 class BatchDesc(ctypes.Structure):
@@ -126,6 +128,7 @@ def load(path: str = LIB_PATH):
     lib.vx3g_debug_barrier.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
     lib.vx3g_prepare_graphs.argtypes = [vp]
     lib.vx3g_get_signals.argtypes = [vp, dp]
+    lib.vx3g_links_in_use.argtypes = [vp, dp]
     _lib = lib
     return lib
 
@@ -158,7 +161,7 @@ def robot_desc(robot):
                            float(m.cilia), float(m.cilia_on_after), float(m.remove_after),
                            float(m.plastic_mod), float(m.yield_stress), n, _P(e), _P(s),
                            int(m.is_pacemaker), float(m.pacemaker_period), float(m.signal_value_decay),
-                           float(m.signal_time_delay), float(m.inactive_period))
+                           float(m.signal_time_delay), float(m.inactive_period), int(m.sticky))
     Z, Y, X = g.shape
     log10E = getattr(robot, "log10E", None)
     if log10E is not None:
@@ -188,6 +191,12 @@ def robot_desc(robot):
                 cil.append(a)
                 setattr(d, name, _P(a))
     d.enable_signals = int(robot.enable_signals)
+    d.enable_attach = int(robot.enable_attach)
+    d.safety_guard = int(robot.safety_guard)
+    for k, tree in enumerate((getattr(robot, "attach_conditions", None) or [])[:5]):
+        if tree is not None:
+            progs.append(np.ascontiguousarray(wl.math_tokens(tree)))
+            d.attach_condition[k] = _P(progs[-1])
     bcs = None
     if robot.bcs:
         bcs = bc_array(BCRegion, robot.bcs)
@@ -284,6 +293,13 @@ class Batch:
         _check(self.lib.vx3g_get_links(self.h, _P(strain), _P(maxs), _P(local9), _P(forces), _P(small)),
                "vx3g_get_links")
         return dict(strain=strain, maxstrain=maxs, local9=local9, forces=forces, small=small)
+
+    def links_in_use(self):
+        """Per robot: its lattice's links plus those attachment has made (the first entries
+        of its link range; the rest of the range is unused reserve)."""
+        out = np.zeros(self.n_robots, np.int32)
+        _check(self.lib.vx3g_links_in_use(self.h, _P(out)), "vx3g_links_in_use")
+        return out
 
     def signals(self):
         """Per voxel: localSignal (0 in robots without signals)."""

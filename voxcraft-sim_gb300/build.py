@@ -24,6 +24,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = [
     ("vx3g_fp64.cu", ["--fmad=false"]),
     ("vx3g_aux.cu", ["--fmad=false"]),
+    ("vx3g_attach.cu", ["--fmad=false"]),
     ("vx3g_mixed.cu", []),
     ("vx3g_adjoint.cu", ["--fmad=false"]),
     ("vx3g_host.cpp", []),

@@ -39,6 +39,7 @@ __global__ void k_dt_links(Dev d, unsigned long long *mx) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= d.nl) return;
     const uint2 li = d.linfo[l];
+    if (li.y & LF_RUNTIME) return;  // the reference's loop covers the lattice's links (d_links) only
     const LMat &m = d.lmat[li.y >> 8];
     const int2 e = d.ends[l];
     const double m1 = d.vmat[d.vinfo[e.x].y >> 8].mass, m2 = d.vmat[d.vinfo[e.y].y >> 8].mass;
@@ -701,9 +702,14 @@ __device__ void grid_list(const Dev &d, int *cand) {
                                         acc = cu.x == c.x + dx && cu.y == y && cu.z == z && (int)d.vinfo[u].x == r;
                                     }
                                     // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them
+                                    // (a runtime link may join any two voxels: the face partners say)
                                     const int ddx = ik.x - ij.x, ddy = ik.y - ij.y, ddz = ik.z - ij.z;
-                                    if (abs(ddx) + abs(ddy) + abs(ddz) == 1 && ((vi.y >> link_bit(ddx, ddy, ddz)) & 1u))
+                                    if (rp.attach) {
+                                        if (linked_to(d, v, u)) acc = false;
+                                    } else if (abs(ddx) + abs(ddy) + abs(ddz) == 1 &&
+                                               ((vi.y >> link_bit(ddx, ddy, ddz)) & 1u)) {
                                         acc = false;
+                                    }
                                     if ((ij.w & 1) && (ik.w & 1)) acc = false;  // both fixed
                                 }
                                 if (acc) {
@@ -978,9 +984,12 @@ __device__ __forceinline__ void coll_list_robots(const Dev &d, unsigned char *ls
                             const int ad = abs(dl);
                             const bool face = ad == 1 || ad == (1 << 10) || ad == (1 << 20);
                             const int bit = (ad == 1 ? 0 : ad == (1 << 10) ? 2 : 4) + (dl > 0 ? 1 : 0);
-                            const bool linked = face && ((imask >> bit) & 1u);
-                            bool acc = ex * ex + ey * ey + ez * ez <= cut2 && t != i && !linked &&
+                            bool linked = face && ((imask >> bit) & 1u);
+                            bool acc = ex * ex + ey * ey + ez * ez <= cut2 && t != i &&
                                        !(ki & kt & kPackFixed) && !(kt & kPackInterior);
+                            // a runtime link may join any two voxels: the face partners say
+                            if (acc && rp.attach) linked = linked_to(d, d.csurf[s0 + i], d.csurf[s0 + t]);
+                            acc = acc && !linked;
                             if (!g.dense) {
                                 const int3 ct = local_cell(pt, g);
                                 acc = acc && ct.x == c.x + dx && ct.y == y && ct.z == z;  // same bucket, other cell
@@ -1175,6 +1184,10 @@ __global__ void k_coll_eval(Dev d) {
     const int n = d.nnb[s];
     const int *lst = d.nbr + s;  // slot-major: entry k at lst[k*ns]
     const size_t ns = (size_t)d.ns;
+    // attachment linked some pairs this step: their contact is added, then taken back
+    // (VX3_VoxelyzeKernel.cu:824-826); a listed pair with a link was linked this step
+    // (a link makes its robot rebuild its lists in the next step)
+    const bool att = d.narob && d.rp[r].attach && d.acnt[r] > 0;
     V3<double> acc{0, 0, 0};
     if (n) {
         const float4 pf = pos_f(d, v);
@@ -1203,8 +1216,10 @@ __global__ void k_coll_eval(Dev d) {
             if (diff.y > wd || diff.y < -wd) continue;
             if (diff.z > wd || diff.z < -wd) continue;
             if (len(diff) > wd) continue;
-            if (u < v) acc = add(acc, pair_force(d, v, u, bsa, bu));    // v.contactForce += force
-            else acc = add(acc, neg(pair_force(d, u, v, bu, bsa)));      // v.contactForce += -force
+            // v.contactForce += force (v is voxel1) or += -force (v is voxel2)
+            const V3<double> f = u < v ? pair_force(d, v, u, bsa, bu) : neg(pair_force(d, u, v, bu, bsa));
+            acc = add(acc, f);
+            if (att && linked_to(d, v, u)) acc = sub(acc, f);
         }
     }
     d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
@@ -1239,6 +1254,7 @@ cudaError_t launch_collision(const Dev &d, cudaStream_t s) {
     if (!d.ns) return cudaSuccess;
     const cudaError_t e = launch_coll_prepare(d, s);
     if (e != cudaSuccess) return e;
+    launch_attach(d, s);  // robots with EnableAttach: links made in the pair order, before the contacts
     launch_coll_eval(d, s);
     return cudaGetLastError();
 }

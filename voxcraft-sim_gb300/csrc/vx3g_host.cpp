@@ -132,6 +132,7 @@ VMat to_vmat(const HostVMat &m, const vx3g_material &in) {
     v.sig_decay = in.signal_value_decay;
     v.sig_delay = in.signal_time_delay;
     v.inactive = in.inactive_period;
+    v.alm = -1;  // set for Sticky materials of robots with EnableAttach
     return v;
 }
 
@@ -241,6 +242,8 @@ struct vx3g_ctx {
     bool any_nonlinear = false;  // some material has a non-linear stress-strain model
     bool any_bcs = false;        // some voxel has a boundary-condition external
     bool any_signals = false;    // some robot has EnableSignals
+    bool any_attach = false;     // some robot has EnableAttach (runtime links)
+    bool any_acond = false;      // some robot has an attach condition
     std::vector<double> mass_tot;  // per robot: mass of the measured voxels (the COM's weights)
     bool any_collision = false;
     // recorded run (vx3g_record) and the adjoint's buffers (vx3g_backward)
@@ -373,6 +376,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     std::vector<double4> cil_h, cils_h;  // BaseCiliaForce (w: Cilia), ShiftCiliaForce
     std::vector<double> cil_on_h;
     std::vector<int> vnb_h, sigrob_h;    // signals: the voxel across each link, robots with signals
+    std::vector<int> arob_h;             // robots with EnableAttach
     std::vector<double> rm_h;  // per voxel: removal time (+inf: never)
     std::vector<float2> ss_h;  // stress-strain points of the non-linear link materials
     std::vector<ExtBC> ext_h;  // boundary-condition externals
@@ -600,8 +604,9 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             const bool interior = (vinfo[v].y & VF_LINKMASK) == VF_LINKMASK;
             if (!interior) c->surface.push_back(v);
             // detach or removal: any voxel may become a surface voxel, so all take part
-            // (interior ones are skipped while their six links hold, removed ones for good)
-            if ((!interior || rp.dyn) && R.enable_collision) csurf.push_back(v);
+            // (interior ones are skipped while their six links hold, removed ones for good);
+            // attachment alone only turns surface voxels into interior ones
+            if ((!interior || rp.detach || rp.remove) && R.enable_collision) csurf.push_back(v);
         }
         rp.ns = (int)csurf.size() - rp.soff;
         // cilia (gpu_update_cilia_force, VX3_VoxelyzeKernel.cu:846-859): surface voxels of a
@@ -633,16 +638,79 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
             }
             c->any_cilia |= rp.cilia != 0;
         }
-        // signals: the voxel across each direction's link (links of the lattice, in creation)
+        // signals (the partner across each face: vnb, below)
         rp.signals = R.enable_signals ? 1 : 0;
-        if (rp.signals) {
+        if (rp.signals) sigrob_h.push_back(r);
+        // EnableAttach: Sticky materials get the link material of their runtime links (the pair
+        // (m, m), VX3_VoxelyzeKernel::combinedMaterial), the robot a reserve of links after its
+        // lattice's, each face's partner voxel is kept (vnb), and the surface follows the link table
+        rp.attach = 0;
+        if (R.enable_attach) {
+            if (!R.enable_collision)
+                return fail(VX3G_ERR_UNSUPPORTED, "robot " + std::to_string(r) + ": enable_attach needs enable_collision");
+            for (int k = 0; k < 5; k++) {  // AttachCondition/Condition_k programs
+                rp.acond[k] = -1;
+                if (!R.attach_condition[k]) continue;
+                int len = 0, rc;
+                bool reads_pos = false;
+                std::string why;
+                if ((rc = check_math_program(R.attach_condition[k], &len, &reads_pos, &why)))
+                    return fail(rc, "robot " + std::to_string(r) + ": attach_condition[" + std::to_string(k) + "]: " + why);
+                rp.acond[k] = (int)ftok.size();
+                for (int i = 0; i < len; i++)
+                    ftok.push_back(MathTok{R.attach_condition[k][i].op, 0, R.attach_condition[k][i].value});
+                c->any_acond = true;
+            }
+            int sticky_lm = -1;
+            for (int i = 0; i < R.n_materials; i++) {
+                const vx3g_material &M = R.materials[i];
+                if (!M.sticky || R.log10E) continue;  // per-voxel moduli: no two voxels share a material
+                if (!hm[i].model.linear || hm[i].nu != 0)
+                    return fail(VX3G_ERR_UNSUPPORTED, "robot " + std::to_string(r) + ": a Sticky material must be linear "
+                                "(MatModel 0/1) with Poisson's ratio 0 for attachment");
+                int &ori = ori_lmat[i * R.n_materials + i];
+                if (ori < 0) {
+                    ori = (int)lmats.size() - lbase;
+                    LMat l = combine(hm[i], hm[i], ss_h);
+                    l.dmcN = l.dmcP = 2 * hm[i].sqrt_mass * hm[i].z_int;
+                    l.fixN = l.fixP = M.fixed ? 1 : 0;
+                    lmats.push_back(l);
+                }
+                vmats[vbase + i].alm = lbase + ori;
+                if (sticky_lm < 0) sticky_lm = lbase + ori;
+            }
+            // reserve: a runtime link takes a free face of two Sticky voxels; twice the free faces
+            // leave room for faces freed again by detach
+            long long faces = 0;
+            for (int k = 0; k < nvr && sticky_lm >= 0; k++) {
+                const int v = v0 + k;
+                const vx3g_material &M = R.materials[c->vmat_local[v]];
+                if (!M.sticky || M.fixed || R.log10E) continue;
+                faces += 6 - __builtin_popcount(vinfo[v].y & VF_LINKMASK);
+            }
+            rp.ares = (int)c->ends.size();
+            rp.acap = faces ? (int)std::min<long long>(faces + 16, INT32_MAX / 4) : 0;
+            for (int k = 0; k < rp.acap; k++) {  // unused slots: gone, ends on a voxel of the robot
+                c->ends.push_back(make_int2(v0, v0));
+                c->laxis.push_back(0u);
+                linfo.push_back(make_uint2((unsigned)r, LF_GONE | LF_RUNTIME | LF_SMALL | ((uint32_t)sticky_lm << 8)));
+            }
+            rp.nl = (int)c->ends.size() - rp.loff;
+            rp.guard = R.safety_guard;
+            rp.attach = 1;
+            rp.dyn = 1;
+            c->any_dyn = true;
+            c->any_attach = true;
+            arob_h.push_back(r);
+        }
+        if (rp.signals || rp.attach) {  // the voxel across each face's link (lattice links)
             vnb_h.resize(6 * pos.size(), -1);
-            for (int l = c->loff[r]; l < (int)c->ends.size(); l++) {
+            for (int l = c->loff[r]; l < rp.loff + rp.nl; l++) {
+                if (linfo[l].y & LF_RUNTIME) continue;
                 const int a = (int)c->laxis[l];
                 vnb_h[6 * (size_t)c->ends[l].x + 2 * a] = c->ends[l].y;      // negative end: toward +axis
                 vnb_h[6 * (size_t)c->ends[l].y + 2 * a + 1] = c->ends[l].x;  // positive end: toward -axis
             }
-            sigrob_h.push_back(r);
         }
         // lists in shared memory when the robot fits (lattice coordinates below 512, packed in 10 bits each)
         int cmax = 0;
@@ -714,6 +782,11 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     RobotP *drp;
     VMat *dvm;
     LMat *dlm;
+    int words = 0;  // attachment: each robot's words of the collision-surface bitmap
+    for (int r : arob_h) {
+        rps[r].abit = words;
+        words += (rps[r].ns + 31) / 32;
+    }
     if ((rc = c->upload(&drp, rps)) || (rc = c->upload(&dvm, vmats)) || (rc = c->upload(&dlm, lmats))) return rc;
     d.rp = drp;
     d.vmat = dvm;
@@ -731,17 +804,33 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     d.vnb = nullptr;
     d.sigrob = nullptr;
     d.nsigrob = (int)sigrob_h.size();
-    if (d.nsigrob) {
+    if (d.nsigrob || !arob_h.empty()) {
         vnb_h.resize(6 * pos.size(), -1);
-        if ((rc = c->alloc(&d.sig, 6 * pos.size())) || (rc = c->upload(&d.vnb, vnb_h)) ||
-            (rc = c->upload(&d.sigrob, sigrob_h)))
-            return rc;
+        if ((rc = c->upload(&d.vnb, vnb_h))) return rc;
+    }
+    if (d.nsigrob) {
+        if ((rc = c->alloc(&d.sig, 6 * pos.size())) || (rc = c->upload(&d.sigrob, sigrob_h))) return rc;
         if (!cils_h.empty()) {
             cils_h.resize(pos.size(), make_double4(0, 0, 0, 0));
             if ((rc = c->upload(&d.cils, cils_h))) return rc;
         }
     }
     c->any_signals = d.nsigrob > 0;
+    // attachment: enableAttach (true at first, VX3_Voxel.h:302), isNewLink, the scan's marks
+    d.vatt = nullptr;
+    d.lnew = nullptr;
+    d.amask = nullptr;
+    d.abits = nullptr;
+    d.aflag = d.anum = d.acnt = nullptr;
+    d.arob = nullptr;
+    d.narob = (int)arob_h.size();
+    d.any_acond = c->any_acond ? 1 : 0;
+    if (d.narob) {
+        if ((rc = c->upload(&d.vatt, std::vector<unsigned char>(pos.size(), 1))) || (rc = c->alloc(&d.lnew, d.nl)) ||
+            (rc = c->alloc(&d.amask, d.ns)) || (rc = c->alloc(&d.abits, words)) || (rc = c->alloc(&d.aflag, d.nr)) ||
+            (rc = c->alloc(&d.anum, d.nr)) || (rc = c->alloc(&d.acnt, d.nr)) || (rc = c->upload(&d.arob, arob_h)))
+            return rc;
+    }
     if (c->any_cilia &&
         ((rc = c->upload(&d.cil, cil_h)) || (rc = c->upload(&d.cil_on, cil_on_h)) || (rc = c->alloc(&d.cfv, d.nv))))
         return rc;
@@ -792,7 +881,9 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
     d.crec = nullptr;
     if (d.mixed && d.ns && (rc = c->alloc(&d.crec, 3 * (size_t)d.nv))) return rc;
     CU(init_collision(d));
-    if (d.mixed && d.ns) {
+    // the contact evaluation beside the link pass, except with attachment (its links are made
+    // between the check and the evaluation and must not race the link pass's reads)
+    if (d.mixed && d.ns && !c->any_attach) {
         CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
         CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
         CU(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
@@ -810,14 +901,15 @@ void enqueue_links(vx3g_ctx *c) {
     if (c->precision == VX3G_PRECISION_FP64) launch_links_fp64(c->d, c->stream);
     else launch_links_mixed(c->d, c->stream, c->shape_links, !c->any_remove);  // removal writes link info
 }
-void enqueue_voxels(vx3g_ctx *c, int parity) {
-    launch_extra_forces(c->d, parity, c->stream);  // robots with a force field or cilia only
+void enqueue_voxels(vx3g_ctx *c, int parity, bool extra = true) {
+    if (extra) launch_extra_forces(c->d, parity, c->stream);  // robots with a force field or cilia only
     launch_detach(c->d, c->stream);                // EnableDetach robots only (after the collision pass)
     if (c->precision == VX3G_PRECISION_FP64) launch_voxels_fp64(c->d, parity, c->stream);
     else {
         launch_voxels_mixed(c->d, parity, c->stream, c->shape_voxels, !c->any_detach);  // detach writes voxel info
         launch_voxels_bc_mixed(c->d, parity, c->stream);  // voxels with a boundary condition, if any
     }
+    launch_attach_cond(c->d, parity, c->stream);   // robots with attach conditions: enableAttach
     launch_signals(c->d, parity, c->stream);       // EnableSignals robots only (the end of timeStep)
     launch_remove(c->d, parity, c->stream);        // SecondaryExperiment robots only (end of the step)
 }
@@ -825,8 +917,11 @@ void enqueue_voxels(vx3g_ctx *c, int parity) {
 cudaError_t enqueue_step(vx3g_ctx *c, int parity) {
     if (!c->overlap) {
         enqueue_links(c);
+        // with attachment the cilia force is taken before any link is made: from the surface the
+        // step started with, which the reference's cilia pass walks (VX3_VoxelyzeKernel.cu:296-303)
+        if (c->any_attach) launch_extra_forces(c->d, parity, c->stream);
         const cudaError_t e = launch_collision(c->d, c->stream);
-        enqueue_voxels(c, parity);
+        enqueue_voxels(c, parity, !c->any_attach);
         return e;
     }
     // the check / list rebuild, then the contact evaluation on the side stream beside the
@@ -960,6 +1055,43 @@ static int current_surface(vx3g_ctx *c, std::vector<int> &out) {
     return VX3G_OK;
 }
 
+// The link table as it stands: the host copy of the lattice's links, or, with attachment,
+// the device's (runtime links made so far, unused reserve slots with ends -1).
+static int current_links(vx3g_ctx *c, std::vector<int2> &ends, std::vector<uint32_t> &axis) {
+    if (!c->any_attach) {
+        ends = c->ends;
+        axis = c->laxis;
+        return VX3G_OK;
+    }
+    std::vector<uint2> li;
+    std::vector<int> made;
+    std::vector<RobotP> rps;
+    int rc;
+    if ((rc = download(c, ends, c->d.ends, c->d.nl)) || (rc = download(c, li, c->d.linfo, c->d.nl)) ||
+        (rc = download(c, made, c->d.anum, c->nr)) || (rc = download(c, rps, c->d.rp, c->nr)))
+        return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    axis.resize(ends.size());
+    for (size_t l = 0; l < ends.size(); l++) {
+        axis[l] = li[l].y & LF_AXIS;
+        const RobotP &q = rps[li[l].x];
+        if ((li[l].y & LF_RUNTIME) && (int)l >= q.ares + made[li[l].x]) ends[l] = make_int2(-1, -1);
+    }
+    return VX3G_OK;
+}
+
+int vx3g_links_in_use(vx3g_ctx *c, int32_t *n) {
+    if (!c || !n) return fail(VX3G_ERR_INVALID, "bad arguments to vx3g_links_in_use");
+    std::vector<int> made(c->nr, 0);
+    std::vector<RobotP> rps;
+    int rc;
+    if ((rc = download(c, rps, c->d.rp, c->nr))) return rc;
+    if (c->any_attach && (rc = download(c, made, c->d.anum, c->nr))) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    for (int r = 0; r < c->nr; r++) n[r] = (rps[r].attach ? rps[r].ares - rps[r].loff : rps[r].nl) + made[r];
+    return VX3G_OK;
+}
+
 int vx3g_counts(vx3g_ctx *c, int *nv, int *nl, int *ns) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
     if (nv) *nv = c->d.nv;
@@ -1077,6 +1209,12 @@ int vx3g_get_voxel_aux(vx3g_ctx *c, float *tempe, int32_t *flags, double *contac
 int vx3g_get_links(vx3g_ctx *c, float *strain, float *max_strain, double *local9, double *forces12, int32_t *small) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
     const size_t nl = c->d.nl, nv = c->d.nv;
+    std::vector<int2> lends;
+    std::vector<uint32_t> laxis;
+    if (forces12) {
+        int rc = current_links(c, lends, laxis);
+        if (rc) return rc;
+    }
     const bool fp64 = c->precision == VX3G_PRECISION_FP64;
     const size_t rsz = fp64 ? 8 : 4;
     std::vector<float2> sm;
@@ -1098,9 +1236,11 @@ int vx3g_get_links(vx3g_ctx *c, float *strain, float *max_strain, double *local9
         if (small) small[l] = ((li[l].y & LF_SMALL) ? 1 : 0) | ((li[l].y & LF_GONE) ? 2 : 0) | ((li[l].y & LF_LVV) ? 4 : 0);
         if (local9)
             for (int k = 0; k < 9; k++) local9[9 * l + k] = rd(ls, (size_t)k * nl + l);
-        if (forces12) {
-            const int a = (int)c->laxis[l];
-            const size_t sn = ((size_t)(2 * a) * nv + c->ends[l].x) * 6, sp = ((size_t)(2 * a + 1) * nv + c->ends[l].y) * 6;
+        if (forces12 && lends[l].x < 0) {  // an unused reserve slot
+            std::fill(forces12 + 12 * l, forces12 + 12 * l + 12, 0.0);
+        } else if (forces12) {
+            const int a = (int)laxis[l];
+            const size_t sn = ((size_t)(2 * a) * nv + lends[l].x) * 6, sp = ((size_t)(2 * a + 1) * nv + lends[l].y) * 6;
             for (int k = 0; k < 3; k++) {
                 forces12[12 * l + k] = rd(sl, sn + k);         // forceNeg
                 forces12[12 * l + 3 + k] = rd(sl, sp + k);     // forcePos
@@ -1129,13 +1269,19 @@ int vx3g_get_signals(vx3g_ctx *c, double *local) {
 
 int vx3g_get_topology(vx3g_ctx *c, int32_t *ijk, int32_t *vmat, int32_t *ends, int32_t *axis) {
     if (!c) return fail(VX3G_ERR_INVALID, "null context");
+    std::vector<int2> lends;
+    std::vector<uint32_t> laxis;
+    if (ends || axis) {
+        int rc = current_links(c, lends, laxis);
+        if (rc) return rc;
+    }
     for (size_t i = 0; i < (size_t)c->d.nv; i++) {
         if (ijk) { ijk[3 * i] = c->ijk[i].x; ijk[3 * i + 1] = c->ijk[i].y; ijk[3 * i + 2] = c->ijk[i].z; }
         if (vmat) vmat[i] = c->vmat_local[i];
     }
     for (size_t l = 0; l < (size_t)c->d.nl; l++) {
-        if (ends) { ends[2 * l] = c->ends[l].x; ends[2 * l + 1] = c->ends[l].y; }
-        if (axis) axis[l] = (int32_t)c->laxis[l];
+        if (ends) { ends[2 * l] = lends[l].x; ends[2 * l + 1] = lends[l].y; }
+        if (axis) axis[l] = (int32_t)laxis[l];
     }
     return VX3G_OK;
 }
@@ -1591,6 +1737,7 @@ int vx3g_record(vx3g_ctx *c, int n, int k) {
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of non-linear material models is not implemented");
     if (c->any_bcs) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of boundary conditions is not implemented");
     if (c->any_signals) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of signals is not implemented");
+    if (c->any_attach) return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of attachment is not implemented");
     if (c->any_detach || c->any_remove)
         return fail(VX3G_ERR_UNSUPPORTED, "the adjoint of a changing link table (detach, removal) is not implemented");
     CU(cudaSetDevice(c->device));

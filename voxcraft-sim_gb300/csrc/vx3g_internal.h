@@ -34,7 +34,11 @@ enum : uint32_t {
     LF_LVV = 1u << 3,         // LOCAL_VELOCITY_VALID
     LF_BOTH_FIXED = 1u << 4,  // both ends fixed: gpu_update_links skips the link
     LF_GONE = 1u << 5,        // detached (gpu_update_detach): no longer updated, no voxel's link
+    LF_RUNTIME = 1u << 6,     // made by attachment, or a reserve slot for one (GONE until made)
 };
+
+// robot status bit (VX3G_ROBOT_LINK_CAPACITY): attachment found the robot's link reserve used up
+constexpr int kStatusLinkCapacity = 8;
 
 struct VMat {  // one voxel material (global index), constants as the reference derives them
     float mass, mass_inv, mom_inv;
@@ -52,6 +56,8 @@ struct VMat {  // one voxel material (global index), constants as the reference 
     double thermal_on_after;
     int pacemaker;     // isPaceMaker
     double pace_period, sig_decay, sig_delay, inactive;  // PaceMakerPeriod, signalValueDecay, signalTimeDelay, inactivePeriod
+    int alm;           // Sticky material of a robot with EnableAttach: the link material of its runtime
+                       // links (VX3_VoxelyzeKernel::combinedMaterial of the pair); -1 otherwise
 };
 
 struct LMat {  // one link material (global index), oriented: (negative end, positive end) materials
@@ -82,6 +88,11 @@ struct RobotP {
     int dyn = 0;               // detach || remove: the surface follows the link table
     int bcs = 0;               // 1: some voxel has a boundary-condition external (Dev::vext)
     int signals = 0;           // 1: EnableSignals (k_signals; the cilia force reads the signal)
+    int attach = 0;            // 1: EnableAttach (k_attach_scan / k_attach_commit)
+    int acond[5] = {-1, -1, -1, -1, -1};  // attach-condition programs: token offset in Dev::ftok, or -1
+    int guard = 0;             // SafetyGuard: a runtime link's first updates scaled by 0.01
+    int ares = 0, acap = 0;    // the robot's reserve of runtime links: first link index, size
+    int abit = 0;              // first word of its collision-surface bitmap (Dev::abits)
 };
 
 // a voxel's boundary-condition external (VX3_External): fixed DOFs with their prescribed
@@ -204,6 +215,19 @@ struct Dev {
     int *vext;         // per voxel: its index in ext, or -1 (NULL when no robot has any)
     int *xbc;          // the voxels with an external, in voxel order (mixed precision: k_voxels_bc_mixed)
     int nxbc;
+    // attachment (robots with EnableAttach): per voxel enableAttach (VX3_Voxel.h:302); per link
+    // isNewLink (VX3_Link.h:240, runtime links only); per collision-surface voxel the candidate
+    // list entries that passed the parallel tests this step (bit k: entry k), with a bitmap of
+    // those voxels per robot; per robot: a pair passed this step, runtime links made so far,
+    // links made this step; the robots with EnableAttach
+    unsigned char *vatt;
+    int *lnew;
+    unsigned long long *amask;
+    unsigned *abits;
+    int *aflag, *anum, *acnt;
+    int *arob;
+    int narob;
+    int any_acond;     // some robot has an attach condition (k_attach_cond after the voxel pass)
     double *com_part;  // [NR][com_tiles][4] partial sums of the centre of mass
     int com_tiles;     // tiles of kComTile voxels of the largest robot
     int nv, nl, nr, ns;
@@ -252,6 +276,11 @@ void launch_detach(const Dev &d, cudaStream_t s);
 void launch_remove(const Dev &d, int parity, cudaStream_t s);
 // the signals of the step of the given parity (the end of VX3_Voxel::timeStep), after the voxel pass
 void launch_signals(const Dev &d, int parity, cudaStream_t s);
+// attachment (robots with EnableAttach), between the contact-list check and the contact
+// evaluation: the parallel pair tests, then the links made in the serial pair order
+void launch_attach(const Dev &d, cudaStream_t s);
+// enableAttach of every stepped voxel of robots with attach conditions, after the voxel pass
+void launch_attach_cond(const Dev &d, int parity, cudaStream_t s);
 // one-time setup of the collision kernels (shared-memory size, grid); fills d.cgrid
 cudaError_t init_collision(Dev &d);
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s);

@@ -172,6 +172,7 @@ struct RobotSpec {
     vx3g_robot_desc desc{};
     const Node *stop = nullptr, *fitness = nullptr;
     std::vector<vx3g_math_token> ff[3];  // force-field programs (desc.force_field points here)
+    std::vector<vx3g_math_token> ac[5];  // attach-condition programs (desc.attach_condition points here)
     std::vector<vx3g_bc_region> bcs;     // Environment/Boundary_Conditions (desc.bcs points here)
     std::unique_ptr<Node> doc;
     int record_step = 0, record_voxel = 1, record_link = 0, save_all = 0;
@@ -196,8 +197,16 @@ void read_spec(RobotSpec &S) {
     }
     d.volume_effects = vx3g::xml::get_bool(root, "VXA.Simulator.Features.VolumeEffectsEnabled", false);
     d.enable_collision = vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableCollision", true);
-    if (vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableAttach", false))
-        throw std::runtime_error(S.filename + ": runtime attachment is not supported");
+    // EnableAttach, SafetyGuard and AttachCondition/Condition_0..4 (VX3_SimulationManager.cu:329-343)
+    d.enable_attach = vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableAttach", false);
+    d.safety_guard = vx3g::xml::get_int(root, "VXA.Simulator.AttachDetach.SafetyGuard", 500);
+    for (int k = 0; k < 5; k++) {
+        const std::string key = "VXA.Simulator.AttachDetach.AttachCondition.Condition_" + std::to_string(k);
+        const Node *holder = vx3g::xml::find(root, key);
+        if (!holder || !formula_root(holder)) continue;
+        S.ac[k] = math_program(holder, S.filename + ": " + key);
+        d.attach_condition[k] = S.ac[k].data();
+    }
     d.enable_detach = vx3g::xml::get_bool(root, "VXA.Simulator.AttachDetach.EnableDetach", false);  // :330
     d.enable_signals = vx3g::xml::get_int(root, "VXA.Simulator.EnableSignals", 0);  // :361
     // SecondaryExperiment (VX3_SimulationManager.cu:364-365): material removal on the device,
@@ -323,6 +332,7 @@ void read_spec(RobotSpec &S) {
             M.mu_static = vx3g::xml::get_double(mech, "uStatic", 0.0);
             M.mu_kinetic = vx3g::xml::get_double(mech, "uDynamic", 0.0);
             M.fixed = vx3g::xml::get_int(mech, "Fixed", 0);
+            M.sticky = vx3g::xml::get_int(mech, "Sticky", 0);  // VX_Object.cpp:1436
             M.is_measured = vx3g::xml::get_int(mech, "isMeasured", 1);
             M.thermal_on_after = vx3g::xml::get_double(mech, "TurnOnThermalExpansionAfterThisManySeconds", 0.0);
             M.cilia = vx3g::xml::get_double(mech, "Cilia", 0.0);  // VX_Object.cpp:1429, 1437

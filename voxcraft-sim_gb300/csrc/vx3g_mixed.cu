@@ -100,7 +100,9 @@ __device__ __forceinline__ Q4<float> from_angle_to_posx_f(Q4<float> q, V3<float>
 // listed pairs, in FP32: the pair offset is taken from the hi/lo pairs (one rounding
 // of an exact difference), the envelope test and the force in FP32, contacts summed
 // in ascending partner order as the FP64 pass does.
-__global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
+// ATTACH: the batch has robots with EnableAttach (their pairs linked this step have their
+// contact added, then taken back); the other instance carries none of that code
+template <bool ATTACH> __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0) {  // the rebuild (if any) is done; the next check starts clear
         *d.cflag = 0;
@@ -119,6 +121,8 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
     const int *lst = d.nbr + s;  // slot-major: entry k at lst[k*ns]
     const size_t ns = (size_t)d.ns;
     const float4 *R = d.crec;  // contact records of this step (written by the displacement check)
+    // pairs linked by this step's attachment: contact added, then taken back
+    const bool att = ATTACH && d.rp[r].attach && d.acnt[r] > 0;
     V3<float> acc{0, 0, 0};
     if (n) {
         const float4 pvH = R[3 * v], pvL = R[3 * v + 1], wv = R[3 * v + 2];
@@ -148,6 +152,13 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
             const float rv = sg * ((w1x * ux + w1y * uy + w1z * uz) - (w2x * ux + w2y * uy + w2z * uz));
             const float f = pstiff * rel + dampC * rv;
             // v.contactForce += force (v is voxel1) or -= force (v is voxel2); force along u
+            if (ATTACH && att && linked_to(d, v, u)) {  // (acc + c) - c
+                const float cx = sg * ux * f, cy = sg * uy * f, cz = sg * uz * f;
+                acc.x = (acc.x + cx) - cx;
+                acc.y = (acc.y + cy) - cy;
+                acc.z = (acc.z + cz) - cz;
+                continue;
+            }
             acc.x += sg * ux * f;
             acc.y += sg * uy * f;
             acc.z += sg * uz * f;
@@ -157,7 +168,9 @@ __global__ void __launch_bounds__(256) k_coll_eval_mixed(Dev d) {
 }
 
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s) {
-    if (d.ns) k_coll_eval_mixed<<<(d.ns + 255) / 256, 256, 0, s>>>(d);
+    if (!d.ns) return;
+    if (d.narob) k_coll_eval_mixed<true><<<(d.ns + 255) / 256, 256, 0, s>>>(d);
+    else k_coll_eval_mixed<false><<<(d.ns + 255) / 256, 256, 0, s>>>(d);
 }
 
 // ------------------------------------------------------------- programmatic dependent launch
@@ -312,6 +325,7 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     mPos = qrotinv(angle2, mPos);
     store_slot(sNeg, to_axis_original(axis, fNeg), to_axis_original(axis, mNeg));
     store_slot(sPos, to_axis_original(axis, fPos), to_axis_original(axis, mPos));
+    if (fl & LF_RUNTIME) new_link_scale(d, l, sNeg, sPos);
     if (nfl != fl) d.linfo[l].y = nfl;
 }
 

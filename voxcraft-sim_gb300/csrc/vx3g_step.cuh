@@ -208,6 +208,15 @@ __device__ inline double math_eval(const MathTok *tok, double x, double y, doubl
     return 0.0;
 }
 
+// v has a link to u (is_neighbor depth 1, VX3_VoxelyzeKernel.cu:651-680) in the current link
+// table: robots whose links can be made at runtime keep each face's partner in Dev::vnb
+__device__ __forceinline__ bool linked_to(const Dev &d, int v, int u) {
+    const uint32_t m = d.vinfo[v].y & VF_LINKMASK;
+    for (int k = 0; k < 6; k++)
+        if (((m >> k) & 1u) && d.vnb[6 * (size_t)v + k] == u) return true;
+    return false;
+}
+
 // the force field of robot rp at position (x, y, z) and time t (VX3_Voxel.cu:178-184)
 __device__ inline V3<double> force_field(const Dev &d, const RobotP &rp, double x, double y, double z, double t) {
     const double nv = (double)rp.nv;
@@ -267,6 +276,22 @@ __device__ __forceinline__ float link_stress(const Dev &d, const LMat &m, int l,
 }
 
 // ------------------------------------------------------------- link pass
+// isNewLink (VX3_Link.cu:206-213): a runtime link's forces and moments, just stored, are
+// scaled by 0.01 for its first SafetyGuard updates (the product of the stored value is the
+// product the reference forms before storing).  The slots are read back through volatile
+// pointers, so the common path's values need not stay live across this rare branch.
+template <class R> __device__ __forceinline__ void new_link_scale(const Dev &d, int l, Slot<R> *sNeg, Slot<R> *sPos) {
+    const int n = d.lnew[l];
+    if (n == 0) return;
+    const R k = (R)0.01;
+    volatile R *a = reinterpret_cast<volatile R *>(sNeg), *b = reinterpret_cast<volatile R *>(sPos);
+    for (int c = 0; c < 6; c++) {
+        a[c] = a[c] * k;
+        b[c] = b[c] * k;
+    }
+    d.lnew[l] = n - 1;
+}
+
 template <class R> __device__ __forceinline__ void link_update(const Dev &d, int l) {
     const uint2 li = d.linfo[l];
     const int r = (int)li.x;
@@ -376,6 +401,7 @@ template <class R> __device__ __forceinline__ void link_update(const Dev &d, int
     mPos = qrotinv(angle2, mPos);
     store_slot(sNeg, to_axis_original(axis, fNeg), to_axis_original(axis, mNeg));
     store_slot(sPos, to_axis_original(axis, fPos), to_axis_original(axis, mPos));
+    if (fl & LF_RUNTIME) new_link_scale(d, l, sNeg, sPos);
     if (nfl != fl) d.linfo[l].y = nfl;
 }
 

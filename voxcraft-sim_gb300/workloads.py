@@ -48,6 +48,7 @@ class Material:
     signal_value_decay: float = 0.9    # signalValueDecay
     signal_time_delay: float = 0.03    # signalTimeDelay
     inactive_period: float = 0.03      # inactivePeriod
+    sticky: int = 0                    # Sticky: with EnableAttach, touching voxels of this material link up
 
     def mat_model(self) -> int:
         if self.model is not None:
@@ -119,6 +120,11 @@ class Robot:
     record_step: int = 0                  # RecordHistory/RecordStepSize
     bcs: Optional[list] = None            # Environment/Boundary_Conditions: BCRegion list
     enable_signals: bool = False          # Simulator/EnableSignals
+    enable_attach: bool = False           # Simulator/AttachDetach/EnableAttach (runtime links between Sticky voxels)
+    safety_guard: int = 500               # Simulator/AttachDetach/SafetyGuard: a new link's forces are scaled
+                                          # by 0.01 for its first this many updates
+    attach_conditions: Optional[list] = None  # AttachDetach/AttachCondition/Condition_0..4: up to five math
+                                              # trees (None entries absent); a voxel may attach while all > 0
 
     def occupied(self) -> np.ndarray:
         return self.grid > 0
@@ -321,7 +327,12 @@ def to_vxa(r: Robot) -> str:
            "</Damping>",
            f"<Features><VolumeEffectsEnabled>{int(r.volume_effects)}</VolumeEffectsEnabled></Features>",
            f"<AttachDetach><EnableCollision>{int(r.enable_collision)}</EnableCollision>"
-           f"<EnableAttach>0</EnableAttach><EnableDetach>{int(r.enable_detach)}</EnableDetach></AttachDetach>",
+           f"<EnableAttach>{int(r.enable_attach)}</EnableAttach><EnableDetach>{int(r.enable_detach)}</EnableDetach>"
+           + (f"<SafetyGuard>{int(r.safety_guard)}</SafetyGuard>" if r.enable_attach else "")
+           + ("<AttachCondition>" + "".join(f"<Condition_{i}>{math_tree_xml(t)}</Condition_{i}>"
+                                            for i, t in enumerate(r.attach_conditions) if t is not None)
+              + "</AttachCondition>" if r.enable_attach and r.attach_conditions else "")
+           + "</AttachDetach>",
            f"<EnableExpansion>{int(r.enable_expansion)}</EnableExpansion>",
            *([f"<EnableCilia>1</EnableCilia>"] if r.enable_cilia else []),
            *([f"<EnableSignals>1</EnableSignals>"] if r.enable_signals else []),
@@ -366,7 +377,7 @@ def to_vxa(r: Robot) -> str:
             "</TurnOnCiliaAfterThisManySeconds>"
             f"<RemoveFromSimulationAfterThisManySeconds>{_fmt(m.remove_after)}</RemoveFromSimulationAfterThisManySeconds>"
             f"<uStatic>{_fmt(m.mu_static)}</uStatic><uDynamic>{_fmt(m.mu_kinetic)}</uDynamic>"
-            f"<Fixed>{int(m.fixed)}</Fixed><isMeasured>{int(m.is_measured)}</isMeasured>"
+            f"<Fixed>{int(m.fixed)}</Fixed><Sticky>{int(m.sticky)}</Sticky><isMeasured>{int(m.is_measured)}</isMeasured>"
             f"<isPaceMaker>{int(m.is_pacemaker)}</isPaceMaker><PaceMakerPeriod>{_fmt(m.pacemaker_period)}</PaceMakerPeriod>"
             f"<signalValueDecay>{_fmt(m.signal_value_decay)}</signalValueDecay>"
             f"<signalTimeDelay>{_fmt(m.signal_time_delay)}</signalTimeDelay>"
