@@ -356,6 +356,32 @@ def timed_run(robots, prec, dev, K, C, G, cache, flush=True, com_at=()):
     return ms, b, coms
 
 
+def profile_window(args):
+    """The workload stepped to physics step START in CUDA graphs (launch shapes tuned
+    first), then N steps with every kernel launched on its own, bracketed by the driver's
+    profiler start and stop, so that a profiler started with collection off records only
+    the kernels of those N steps (for a window deep into a run, e.g. C2's contact-heavy
+    middle, without intercepting the launches before it)."""
+    import ctypes
+    start, n = args.profile_window
+    robots = WORKLOADS[args.workload][1]()
+    prec = abi.PRECISION_MIXED if args.precision == "mixed" else abi.PRECISION_FP64
+    cache = args.tune_cache or os.path.join(tempfile.mkdtemp(prefix="vx3g_tune_"), "shapes.json")
+    b = abi.Batch(robots, prec, device=0, graph_chunk=args.graph_chunk)
+    b.autotune(min(start, 2000), cache)
+    b.step(start - min(start, 2000))
+    b.synchronize()
+    cuda = ctypes.CDLL("libcuda.so.1")  # the context vx3g made current on this thread
+    if cuda.cuProfilerStart() != 0:
+        raise SystemExit("cuProfilerStart failed")
+    for _ in range(n):
+        b.step(1)  # a single step: its kernels launched one by one
+    b.synchronize()
+    cuda.cuProfilerStop()
+    print(json.dumps({"profile_window": [start, n], "workload": args.workload, "precision": args.precision,
+                      "steps_taken": int(b.steps_taken()), "status": [int(x) for x in b.status()]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -378,11 +404,16 @@ def main():
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every step's kernels one by one instead of replaying CUDA graphs "
                          "(each launch then its own record in a per-kernel profiler)")
+    ap.add_argument("--profile-window", type=int, nargs=2, metavar=("START", "N"), default=None,
+                    help="for ncu --profile-from-start off: run START physics steps in CUDA graphs, then N "
+                         "steps launched one by one between cuProfilerStart and cuProfilerStop; no bench line")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = max(1, CONFIG_STEPS[args.workload] // args.chunk)
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_window:
+        return profile_window(args)
 
     rank, world, local = dist_env()
     dist = init_dist(world)

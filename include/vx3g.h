@@ -157,7 +157,7 @@ typedef struct vx3g_robot_desc {
     int enable_cilia;               /* Simulator/EnableCilia: gpu_update_cilia_force (VX3_VoxelyzeKernel.cu:846-859) */
     const double *cilia_base;       /* nx*ny*nz*3 Structure/BaseCiliaForce vectors (per cell) or NULL for 0 */
     const double *cilia_shift;      /* nx*ny*nz*3 Structure/ShiftCiliaForce vectors or NULL; scaled by the
-                                       voxel's signal, which stays 0 (signals are not supported) */
+                                       voxel's localSignal (0 unless enable_signals) */
     int enable_detach;              /* Simulator/AttachDetach/EnableDetach: a failed link leaves both voxels'
                                        link tables after the collision pass (gpu_update_detach,
                                        VX3_VoxelyzeKernel.cu:946-967); the surface, the contact
