@@ -532,74 +532,123 @@ __device__ __forceinline__ int grid_bucket(const Dev &d, const GridP &g, int3 c,
     return dense ? g.base + (c.z * g.gy + c.y) * g.gx + c.x : (int)cell_hash(c.x, c.y, c.z, r, d.hsize - 1);
 }
 
-// (a) bounding boxes of the due robots' surface voxels; called by every thread of the
-// grid for the same s sequence (warp-uniform), a warp whose voxels are one robot's
-// reduces first so that the atomics are one per warp, not per voxel
-__device__ __forceinline__ void grid_box(const Dev &d, int s) {
-    int v = 0, r = -1;
-    bool valid = s < d.ns && grid_voxel(d, s, &v, &r) && (d.vinfo[v].y & VF_LINKMASK) != VF_LINKMASK &&
-                 !(d.vgone && d.vgone[v]);
-    unsigned k[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
-    if (valid) {
-        const float4 p = d.cposf[s];
-        k[0] = k[3] = fkey(p.x);
-        k[1] = k[4] = fkey(p.y);
-        k[2] = k[5] = fkey(p.z);
-    }
-    const unsigned any = __ballot_sync(0xffffffffu, valid);
-    if (!any) return;
-    const int r0 = __shfl_sync(0xffffffffu, r, __ffs(any) - 1);
-    if (__all_sync(0xffffffffu, !valid || r == r0)) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            k[0] = min(k[0], __shfl_xor_sync(0xffffffffu, k[0], o));
-            k[1] = min(k[1], __shfl_xor_sync(0xffffffffu, k[1], o));
-            k[2] = min(k[2], __shfl_xor_sync(0xffffffffu, k[2], o));
-            k[3] = max(k[3], __shfl_xor_sync(0xffffffffu, k[3], o));
-            k[4] = max(k[4], __shfl_xor_sync(0xffffffffu, k[4], o));
-            k[5] = max(k[5], __shfl_xor_sync(0xffffffffu, k[5], o));
-        }
-        if ((threadIdx.x & 31) != 0) return;
-        r = r0;
-    } else if (!valid) {
-        return;
-    }
+// (a) bounding boxes of the due robots' surface voxels.  Each thread keeps a running box
+// of its voxels while they belong to one robot; warps, then the CTA, reduce the boxes of
+// one robot before the atomics, so a single large body costs a few atomics per CTA (the
+// per-warp atomics on six words serialised to ~20 us for a 64^3 body)
+__device__ __forceinline__ void box_atomics(const Dev &d, int r, const unsigned k[6]) {
     unsigned *b = d.gbox + 6 * (size_t)r;
     atomicMin(b + 0, k[0]), atomicMin(b + 1, k[1]), atomicMin(b + 2, k[2]);
     atomicMax(b + 3, k[3]), atomicMax(b + 4, k[4]), atomicMax(b + 5, k[5]);
 }
 
-// (b) one thread: grid of every due robot, dense if all fit the bucket table
+__device__ void grid_boxes(const Dev &d, int gt, int gs) {
+    __shared__ int wr[kLocalListThreads / 32];
+    __shared__ unsigned wk[kLocalListThreads / 32][6];
+    unsigned k[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+    int rc = -1;
+    for (int s = gt; s < d.ns; s += gs) {
+        int v, r;
+        if (!grid_voxel(d, s, &v, &r) || (d.vinfo[v].y & VF_LINKMASK) == VF_LINKMASK || (d.vgone && d.vgone[v]))
+            continue;
+        if (rc >= 0 && r != rc) {  // the thread's voxels changed robot: flush the box so far
+            box_atomics(d, rc, k);
+            k[0] = k[1] = k[2] = 0xffffffffu;
+            k[3] = k[4] = k[5] = 0u;
+        }
+        rc = r;
+        const float4 p = d.cposf[s];
+        k[0] = min(k[0], fkey(p.x)), k[1] = min(k[1], fkey(p.y)), k[2] = min(k[2], fkey(p.z));
+        k[3] = max(k[3], fkey(p.x)), k[4] = max(k[4], fkey(p.y)), k[5] = max(k[5], fkey(p.z));
+    }
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const unsigned any = __ballot_sync(0xffffffffu, rc >= 0);
+    int wrob = -1;
+    if (any) {
+        const int r0 = __shfl_sync(0xffffffffu, rc, __ffs(any) - 1);
+        if (__all_sync(0xffffffffu, rc < 0 || rc == r0)) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                k[0] = min(k[0], __shfl_xor_sync(0xffffffffu, k[0], o));
+                k[1] = min(k[1], __shfl_xor_sync(0xffffffffu, k[1], o));
+                k[2] = min(k[2], __shfl_xor_sync(0xffffffffu, k[2], o));
+                k[3] = max(k[3], __shfl_xor_sync(0xffffffffu, k[3], o));
+                k[4] = max(k[4], __shfl_xor_sync(0xffffffffu, k[4], o));
+                k[5] = max(k[5], __shfl_xor_sync(0xffffffffu, k[5], o));
+            }
+            wrob = r0;
+        } else if (rc >= 0) {
+            box_atomics(d, rc, k);  // robots mixed within the warp: one flush per thread
+        }
+    }
+    if (lane == 0) {
+        wr[wp] = wrob;
+        for (int c = 0; c < 6; c++) wk[wp][c] = k[c];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // merge the warps' boxes of one robot, flushing when the robot changes
+        int br = -1;
+        unsigned bk[6];
+        for (int w = 0; w < kLocalListThreads / 32; w++) {
+            if (wr[w] < 0) continue;
+            if (br >= 0 && wr[w] != br) box_atomics(d, br, bk);
+            if (wr[w] != br) {
+                br = wr[w];
+                for (int c = 0; c < 6; c++) bk[c] = wk[w][c];
+            } else {
+                for (int c = 0; c < 3; c++) bk[c] = min(bk[c], wk[w][c]);
+                for (int c = 3; c < 6; c++) bk[c] = max(bk[c], wk[w][c]);
+            }
+        }
+        if (br >= 0) box_atomics(d, br, bk);
+    }
+    __syncthreads();
+}
+
+// (b) one thread: grid of every due robot, cells of the list cutoff: dense if every due
+// robot's box fits the bucket table, else hashed.  gmode[0] = the reach in cells of a
+// dense grid's neighbourhood (1), 0 hashed.  (Cells of half the cutoff with a reach of 2
+// scan 58% of the candidates, but leave one or two voxels per cell to share a staged
+// neighbourhood: the 64^3 body's lists took 243 us instead of 126 us.)
 __device__ void grid_params(const Dev &d) {
+    int reach = 1;
     long long total = 0;
-    bool fits = true;
-    for (int r = 0; r < d.nr; r++) {
+    for (; reach >= 0; reach--) {  // 1: dense, 0: hashed
+        total = 0;
+        bool fits = true;
+        for (int r = 0; r < d.nr; r++) {
+            const RobotP &rp = d.rp[r];
+            if (rp.lchunks || !rp.ns || !d.cflag[1 + r]) continue;
+            const unsigned *b = d.gbox + 6 * (size_t)r;
+            GridP g;
+            g.ic = (float)rp.inv_list_cell;
+            g.mnx = fkey_inv(b[0]), g.mny = fkey_inv(b[1]), g.mnz = fkey_inv(b[2]);
+            const float ex = (fkey_inv(b[3]) - g.mnx) * g.ic, ey = (fkey_inv(b[4]) - g.mny) * g.ic,
+                        ez = (fkey_inv(b[5]) - g.mnz) * g.ic;
+            g.gx = g.gy = g.gz = 1;
+            g.base = 0;
+            if (ex >= 0.0f && ey >= 0.0f && ez >= 0.0f && ex < 65536.0f && ey < 65536.0f && ez < 65536.0f) {
+                g.gx = (int)ex + 1, g.gy = (int)ey + 1, g.gz = (int)ez + 1;
+                const long long cells = (long long)g.gx * g.gy * g.gz;
+                g.base = (int)min(total, (long long)INT_MAX);
+                total += cells;
+            } else {
+                if (!(ex >= 0.0f && ey >= 0.0f && ez >= 0.0f)) g.mnx = g.mny = g.mnz = 0.0f;  // no finite box
+                fits = false;
+            }
+            d.ggrid[r] = g;
+        }
+        if (reach == 0 || (fits && total <= d.hsize)) break;
+    }
+    for (int r = 0; r < d.nr; r++) {  // the boxes are ready for the next rebuild
         const RobotP &rp = d.rp[r];
         if (rp.lchunks || !rp.ns || !d.cflag[1 + r]) continue;
         unsigned *b = d.gbox + 6 * (size_t)r;
-        GridP g;
-        g.ic = (float)rp.inv_list_cell;
-        g.mnx = fkey_inv(b[0]), g.mny = fkey_inv(b[1]), g.mnz = fkey_inv(b[2]);
-        const float ex = (fkey_inv(b[3]) - g.mnx) * g.ic, ey = (fkey_inv(b[4]) - g.mny) * g.ic,
-                    ez = (fkey_inv(b[5]) - g.mnz) * g.ic;
-        g.gx = g.gy = g.gz = 1;
-        if (ex >= 0.0f && ey >= 0.0f && ez >= 0.0f && ex < 65536.0f && ey < 65536.0f && ez < 65536.0f) {
-            g.gx = (int)ex + 1, g.gy = (int)ey + 1, g.gz = (int)ez + 1;
-            const long long cells = (long long)g.gx * g.gy * g.gz;
-            g.base = (int)min(total, (long long)INT_MAX);
-            total += cells;
-        } else {
-            if (!(ex >= 0.0f && ey >= 0.0f && ez >= 0.0f)) g.mnx = g.mny = g.mnz = 0.0f;  // no finite box
-            fits = false;
-        }
-        d.ggrid[r] = g;
-        b[0] = b[1] = b[2] = 0xffffffffu;  // ready for the next rebuild
+        b[0] = b[1] = b[2] = 0xffffffffu;
         b[3] = b[4] = b[5] = 0u;
     }
-    if (total > d.hsize) fits = false;
-    const int used = fits ? (int)((total + 1023) / 1024 * 1024) : d.hsize;
-    d.gmode[0] = fits ? 1 : 0;
-    d.gmode[1] = used;
+    d.gmode[0] = reach;
+    d.gmode[1] = reach ? (int)((total + 1023) / 1024 * 1024) : d.hsize;
 }
 
 // (c) count the due surface voxels per bucket
@@ -637,135 +686,242 @@ __device__ __forceinline__ void grid_scatter(const Dev &d, int s) {
     d.ssurf[slot] = s;
 }
 
-// (e) the lists, three lanes per voxel in cell order; cand: kNbrCap ints per thread
-__device__ void grid_list(const Dev &d, int *cand) {
-    constexpr int T = kLocalListThreads;
-    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
-    const int trio = lane / 3, q = lane - 3 * trio, tb = lane - q;
-    const bool dense = d.gmode[0] != 0;
-    const int used = d.gmode[1];
-    const int nbin = min(d.hstart[used - 1] + d.hcount[used - 1], d.ns);  // voxels binned
+// (e) the lists of the binned voxels, a kernel of its own after k_coll_prepare.
+// Dense grid: every warp takes an equal contiguous range of the binned voxels (cell
+// order) and works through it cell by cell.  Every voxel of a cell has the same 3 x 3 x 3
+// neighbourhood -- nine runs of three buckets in the binned order -- so the warp streams
+// the candidates through its lanes 32 at a time (one independent load each) and, in each
+// round, tests each of its voxels of the cell against them: one round trip to memory per
+// 32 candidates serves all of them.  The voxels and their partner lists sit in shared
+// memory (32 voxels at a time); the partners found are compacted by ballot and written
+// out in ascending voxel order, each at its rank.  A hashed grid (a bucket may hold
+// several cells) is listed voxel by voxel with the same tests, each candidate's cell
+// compared.  The 64^3 body's lists at step 4,700: 126 us (three lanes per voxel with
+// sorted sub-lists in shared memory, inside the cooperative kernel at 16 warps per SM
+// with a third of the lanes active: 190 us; one warp per voxel: 152 us; a warp per cell
+// with each CTA a contiguous range of buckets: 380 us, the occupied cells of a folded
+// body falling to few CTAs; staging only the candidates near a cell's voxels: 165 us).
+constexpr int kGridListThreads = 128;
+constexpr int kGridListWarps = kGridListThreads / 32;
+
+struct ListScratch {
+    int found[32][kNbrCap];  // the partners of the cell's voxels (32 at a time), in the order found
+    int nfound[32];
+    float4 pv[32];           // those voxels: FP32 position, voxel index in w
+    short4 ij[32];           // lattice coordinates, w = fixed
+    uint32_t viy[32];        // link bits
+    int s[32];               // collision-surface index
+    int lst[kNbrCap];        // one voxel's partners (voxel indices) for the per-voxel path
+};
+
+// the partner tests of one pair (voxel v: position pv, lattice word ij, link bits vi_y,
+// robot parameters rp) for a candidate u at pu / ik within the cutoff
+__device__ __forceinline__ bool list_pair(const Dev &d, bool attach, int v, float4 pv, short4 ij, uint32_t vi_y,
+                                          float cut2, int u, float4 pu, short4 ik) {
+    const float ex = pu.x - pv.x, ey = pu.y - pv.y, ez = pu.z - pv.z;
+    if (!(u != v && ex * ex + ey * ey + ez * ez <= cut2)) return false;
+    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them
+    // (a runtime link may join any two voxels: the face partners say)
+    const int ddx = ik.x - ij.x, ddy = ik.y - ij.y, ddz = ik.z - ij.z;
+    if (attach) {
+        if (linked_to(d, v, u)) return false;
+    } else if (abs(ddx) + abs(ddy) + abs(ddz) == 1 && ((vi_y >> link_bit(ddx, ddy, ddz)) & 1u)) {
+        return false;
+    }
+    return !((ij.w & 1) && (ik.w & 1));  // not both fixed
+}
+
+// the found partners (n of them, the first kNbrCap kept in L) written in ascending order
+__device__ __forceinline__ void list_write(const Dev &d, int lane, int s, int r, float4 pv, float skin, int n,
+                                           const int *L) {
+    __syncwarp();
+    const int nc = min(n, kNbrCap);
     const size_t ns = (size_t)d.ns;
-    const int per_pass = gridDim.x * (T / 32) * 10;  // voxels per pass of the grid
-    for (int base = 0; base < nbin; base += per_pass) {  // uniform over the grid
-        const int k = base + (blockIdx.x * (T / 32) + wp) * 10 + trio;
-        const bool valid = lane < 30 && k < nbin;
-        int *my = cand + tid;  // this thread's sub-list, entry j at my[j*T]
-        int nc = 0, v = 0, s = 0;
-        float4 pv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (valid) {
-            s = d.ssurf[k];
-            pv = d.spos[k];
-            v = __float_as_int(pv.w);
-            const short4 ij = d.sij[k];
-            const uint2 vi = d.vinfo[v];
-            const int r = (int)vi.x;
-            const RobotP &rp = d.rp[r];
-            const GridP g = d.ggrid[r];
-            const int3 c = grid_cell(g, pv, dense);
-            // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
-            const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
-            const int z = c.z + q - 1;
-            if (!dense || (z >= 0 && z < g.gz)) {
-                for (int dy = -1; dy <= 1; dy++) {
-                    const int y = c.y + dy;
-                    if (dense && (y < 0 || y >= g.gy)) continue;
-                    for (int dx = -1; dx <= (dense ? -1 : 1); dx++) {
-                        int b, e;
-                        if (dense) {
-                            const int rw = g.base + (z * g.gy + y) * g.gx;
-                            b = d.hstart[rw + max(c.x - 1, 0)];
-                            e = d.hfill[rw + min(c.x + 1, g.gx - 1)];  // the bucket's end after the scatter
-                        } else {
-                            const int h = (int)cell_hash(c.x + dx, y, z, r, d.hsize - 1);
-                            b = d.hstart[h];
-                            e = d.hfill[h];
-                        }
-                        e = min(e, nbin);
-                        // four candidates' positions are loaded before any is tested, so
-                        // four gathers are in flight (the appends keep candidate order)
-                        for (int j0 = b; j0 < e; j0 += 4) {
-                            float4 pq[4];
+    for (int a = lane; a < nc; a += 32) {  // entries are distinct voxel indices: ranks are a permutation
+        const int x = L[a];
+        int rank = 0;
+        for (int i = 0; i < nc; i++) rank += L[i] < x ? 1 : 0;
+        d.nbr[s + (size_t)rank * ns] = x;
+    }
+    if (lane == 0) {
+        d.nnb[s] = nc;
+        if (n > kNbrCap) atomicOr(&d.status[r], 2);
+        const float lim = 0.49f * skin;  // rebuild when a voxel has moved farther than this
+        d.cref[s] = make_float4(pv.x, pv.y, pv.z, lim * lim);
+    }
+    __syncwarp();
+}
+
+// one binned voxel k, its candidates read from global memory, 32 at a time
+__device__ void list_voxel(const Dev &d, int k, int nbin, bool dense, int lane, int *L) {
+    const int s = d.ssurf[k];
+    const float4 pv = d.spos[k];
+    const int v = __float_as_int(pv.w);
+    const short4 ij = d.sij[k];
+    const uint2 vi = d.vinfo[v];
+    const int r = (int)vi.x;
+    const RobotP &rp = d.rp[r];
+    const GridP g = d.ggrid[r];
+    const int3 c = grid_cell(g, pv, dense);
+    // 1e-3 relative margin: FP32 positions up to ~100 m from the origin lose no true pair
+    const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
+    const bool attach = rp.attach != 0;
+    const int R = dense ? d.gmode[0] : 1, w = 2 * R + 1;  // reach in cells
+    const int nruns = dense ? w * w : 27;
+    // run `lane`: [rb, rb + rl) of the binned order; hashed grid: its cell (cx, cy, cz)
+    int rb = 0, rl = 0, cx = 0, cy = 0, cz = 0;
+    if (lane < nruns) {
+        int e = 0;
+        if (dense) {
+            const int z = c.z + lane / w - R, y = c.y + lane % w - R;
+            if (z >= 0 && z < g.gz && y >= 0 && y < g.gy) {
+                const int rw = g.base + (z * g.gy + y) * g.gx;
+                rb = d.hstart[rw + max(c.x - R, 0)];
+                e = d.hfill[rw + min(c.x + R, g.gx - 1)];  // the bucket's end after the scatter
+            }
+        } else {
+            cz = c.z + lane / 9 - 1, cy = c.y + (lane / 3) % 3 - 1, cx = c.x + lane % 3 - 1;
+            const int h = (int)cell_hash(cx, cy, cz, r, d.hsize - 1);
+            rb = d.hstart[h];
+            e = d.hfill[h];
+        }
+        rl = max(min(e, nbin) - rb, 0);
+    }
+    int ro = rl;  // inclusive, then exclusive prefix of the run lengths
 #pragma unroll
-                            for (int t = 0; t < 4; t++) pq[t] = j0 + t < e ? d.spos[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, ro, o);
+        if (lane >= o) ro += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, ro, 31);
+    ro -= rl;
+    int n = 0;  // partners found so far (the same in every lane)
+    for (int t0 = 0; t0 < total; t0 += 32) {
+        const int t = t0 + lane;
+        int run = 0;  // the last run starting at or before t (empty runs share the next one's start)
+        for (int i = 1; i < nruns; i++) run += __shfl_sync(0xffffffffu, ro, i) <= t ? 1 : 0;
+        const int jb = __shfl_sync(0xffffffffu, rb, run), jo = __shfl_sync(0xffffffffu, ro, run);
+        const int ex_x = __shfl_sync(0xffffffffu, cx, run), ex_y = __shfl_sync(0xffffffffu, cy, run),
+                  ex_z = __shfl_sync(0xffffffffu, cz, run);
+        bool acc = false;
+        int u = 0;
+        if (t < total) {
+            const int j = jb + (t - jo);
+            const float4 pu = d.spos[j];
+            const short4 ik = d.sij[j];
+            u = __float_as_int(pu.w);
+            acc = list_pair(d, attach, v, pv, ij, vi.y, cut2, u, pu, ik);
+            if (acc && !dense) {  // another cell in the same bucket, or another robot
+                const int3 cu = grid_cell(g, pu, false);
+                acc = cu.x == ex_x && cu.y == ex_y && cu.z == ex_z && (int)d.vinfo[u].x == r;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, acc);
+        if (acc) {
+            const int p = n + __popc(m & ((1u << lane) - 1u));
+            if (p < kNbrCap) L[p] = u;
+        }
+        n += __popc(m);
+    }
+    list_write(d, lane, s, r, pv, (float)rp.skin, n, L);
+}
+
+__global__ void __launch_bounds__(kGridListThreads) k_grid_list(Dev d) {
+    __shared__ ListScratch scratch[kGridListWarps];
+    if (!*(volatile int *)d.cflag) return;   // no robot is due this step
+    if (*(volatile int *)d.err & 1) return;  // a grid barrier of k_coll_prepare gave up
+    const int used = d.gmode[1];  // 0 when no large robot is due this step
+    if (used <= 0) return;
+    const int nbin = min(d.hstart[used - 1] + d.hcount[used - 1], d.ns);  // voxels binned this step
+    if (nbin <= 0) return;
+    const bool dense = d.gmode[0] != 0;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    ListScratch &S = scratch[wp];
+    if (!dense) {  // voxel by voxel, each CTA a contiguous range in cell order
+        const int per_cta = (nbin + gridDim.x - 1) / gridDim.x;
+        const int k1 = min(nbin, (blockIdx.x + 1) * per_cta);
+        for (int k = blockIdx.x * per_cta + wp; k < k1; k += kGridListWarps) list_voxel(d, k, nbin, false, lane, S.lst);
+        return;
+    }
+    // dense: each warp an equal contiguous range of the binned voxels (cell order), taken
+    // cell by cell (consecutive warps of a CTA take consecutive ranges: shared L1 lines)
+    const int R = d.gmode[0], w = 2 * R + 1, nruns = w * w;  // reach in cells, rows of the neighbourhood
+    const int nw = gridDim.x * kGridListWarps;
+    const int per_w = (nbin + nw - 1) / nw;
+    const int kend = min(nbin, (blockIdx.x * kGridListWarps + wp + 1) * per_w);
+    for (int k = (blockIdx.x * kGridListWarps + wp) * per_w; k < kend;) {
+        const int b = d.ccell[d.ssurf[k]].x;  // the bucket (cell) of voxel k
+        const int cnt = min(min(d.hfill[b], nbin), kend) - k;  // this warp's voxels of the cell
+        const int beg = k;
+        k += max(cnt, 1);
+        if (cnt <= 0) continue;
+        // the cell's robot (one robot per dense cell) and its coordinates
+        const int r = (int)d.vinfo[__float_as_int(d.spos[beg].w)].x;
+        const RobotP &rp = d.rp[r];
+        const GridP g = d.ggrid[r];
+        const int loc = b - g.base;
+        const int3 c = make_int3(loc % g.gx, (loc / g.gx) % g.gy, loc / (g.gx * g.gy));
+        int rb = 0, rl = 0;  // run `lane`: row (dz, dy) of the neighbourhood, cells x-R .. x+R
+        if (lane < nruns) {
+            const int z = c.z + lane / w - R, y = c.y + lane % w - R;
+            if (z >= 0 && z < g.gz && y >= 0 && y < g.gy) {
+                const int rw = g.base + (z * g.gy + y) * g.gx;
+                rb = d.hstart[rw + max(c.x - R, 0)];
+                rl = max(min(d.hfill[rw + min(c.x + R, g.gx - 1)], nbin) - rb, 0);  // bucket ends after the scatter
+            }
+        }
+        int ro = rl;  // inclusive, then exclusive prefix of the run lengths
 #pragma unroll
-                            for (int t = 0; t < 4; t++) {
-                                const int j = j0 + t;
-                                const float4 pu = pq[t];
-                                const int u = __float_as_int(pu.w);
-                                const float ex = pu.x - pv.x, ey = pu.y - pv.y, ez = pu.z - pv.z;
-                                bool acc = j < e && u != v && ex * ex + ey * ey + ez * ez <= cut2;
-                                if (acc) {
-                                    const short4 ik = d.sij[j];
-                                    if (!dense) {  // another cell in the same bucket, or another robot
-                                        const int3 cu = grid_cell(g, pu, false);
-                                        acc = cu.x == c.x + dx && cu.y == y && cu.z == z && (int)d.vinfo[u].x == r;
-                                    }
-                                    // is_neighbor depth 1 (VX3_VoxelyzeKernel.cu:651-680): a link joins them
-                                    // (a runtime link may join any two voxels: the face partners say)
-                                    const int ddx = ik.x - ij.x, ddy = ik.y - ij.y, ddz = ik.z - ij.z;
-                                    if (rp.attach) {
-                                        if (linked_to(d, v, u)) acc = false;
-                                    } else if (abs(ddx) + abs(ddy) + abs(ddz) == 1 &&
-                                               ((vi.y >> link_bit(ddx, ddy, ddz)) & 1u)) {
-                                        acc = false;
-                                    }
-                                    if ((ij.w & 1) && (ik.w & 1)) acc = false;  // both fixed
-                                }
-                                if (acc) {
-                                    if (nc < kNbrCap) my[nc * T] = u;
-                                    nc++;
-                                }
-                            }
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, ro, o);
+            if (lane >= o) ro += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, ro, 31);
+        ro -= rl;
+        const float cut = (float)(rp.cell_size + rp.skin) * 1.001f, cut2 = cut * cut;
+        const bool attach = rp.attach != 0;
+        for (int i0 = 0; i0 < cnt; i0 += 32) {  // the voxels, 32 at a time
+            const int m = min(32, cnt - i0);
+            if (lane < m) {
+                const int kk = beg + i0 + lane;
+                const float4 p = d.spos[kk];
+                S.s[lane] = d.ssurf[kk];
+                S.pv[lane] = p;
+                S.ij[lane] = d.sij[kk];
+                S.viy[lane] = d.vinfo[__float_as_int(p.w)].y;
+                S.nfound[lane] = 0;
+            }
+            __syncwarp();
+            for (int t0 = 0; t0 < total; t0 += 32) {  // candidate rounds
+                const int t = t0 + lane;
+                int run = 0;  // the last run starting at or before t (empty runs share the next one's start)
+                for (int i = 1; i < nruns; i++) run += __shfl_sync(0xffffffffu, ro, i) <= t ? 1 : 0;
+                const int j = __shfl_sync(0xffffffffu, rb, run) + (t - __shfl_sync(0xffffffffu, ro, run));
+                float4 pu = make_float4(0.f, 0.f, 0.f, 0.f);
+                short4 ik = make_short4(0, 0, 0, 0);
+                if (t < total) {
+                    pu = d.spos[j];
+                    ik = d.sij[j];
+                }
+                const int u = __float_as_int(pu.w);
+                for (int i = 0; i < m; i++) {
+                    const bool acc = t < total && list_pair(d, attach, __float_as_int(S.pv[i].w), S.pv[i], S.ij[i],
+                                                            S.viy[i], cut2, u, pu, ik);
+                    const unsigned hit = __ballot_sync(0xffffffffu, acc);
+                    if (hit) {
+                        const int n = S.nfound[i];
+                        if (acc) {
+                            const int q = n + __popc(hit & ((1u << lane) - 1u));
+                            if (q < kNbrCap) S.found[i][q] = u;
                         }
+                        __syncwarp();
+                        if (lane == 0) S.nfound[i] = n + __popc(hit);
+                        __syncwarp();
                     }
                 }
             }
+            for (int i = 0; i < m; i++) list_write(d, lane, S.s[i], r, S.pv[i], (float)rp.skin, S.nfound[i], S.found[i]);
         }
-        const bool overflow = nc > kNbrCap;
-        nc = min(nc, kNbrCap);
-        for (int a2 = 1; a2 < nc; a2++) {  // ascending voxel index
-            const int x = my[a2 * T];
-            int j = a2;
-            while (j > 0 && my[(j - 1) * T] > x) {
-                my[j * T] = my[(j - 1) * T];
-                j--;
-            }
-            my[j * T] = x;
-        }
-        int c3[3];
-        bool ov3 = false;
-#pragma unroll
-        for (int kk = 0; kk < 3; kk++) {
-            c3[kk] = __shfl_sync(0xffffffffu, nc, (tb + kk) & 31);
-            ov3 |= __shfl_sync(0xffffffffu, overflow ? 1 : 0, (tb + kk) & 31) != 0;
-        }
-        __syncwarp();
-        if (valid) {
-            int *out = d.nbr + s;
-            for (int j = 0; j < nc; j++) {
-                const int e = my[j * T];
-                int rank = j;
-#pragma unroll
-                for (int kk = 0; kk < 3; kk++) {
-                    if (kk == q) continue;
-                    const int *o = cand + (tid - q + kk);
-                    int m = 0;
-                    while (m < c3[kk] && o[m * T] < e) m++;
-                    rank += m;
-                }
-                if (rank < kNbrCap) out[rank * ns] = e;
-            }
-            if (q == 0) {
-                const int r = (int)d.vinfo[v].x;
-                const int total = c3[0] + c3[1] + c3[2];
-                d.nnb[s] = min(total, kNbrCap);
-                if (ov3 || total > kNbrCap) atomicOr(&d.status[r], 2);
-                const float lim = 0.49f * (float)d.rp[r].skin;  // rebuild when a voxel has moved farther than this
-                d.cref[s] = make_float4(pv.x, pv.y, pv.z, lim * lim);
-            }
-        }
-        __syncwarp();
     }
 }
 
@@ -1103,8 +1259,8 @@ __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_prepare(Dev d) {
     // a barrier gave up in an earlier launch and vx3g_status has not cleared it yet: the
     // arrival count may be stale, so no barrier of this launch could be trusted
     if (*(volatile int *)d.err & 1) return;
-    if (d.nhash) {  // robots too large for shared memory, if any is due
-        for (int s0 = 0; s0 < d.ns; s0 += gs) grid_box(d, s0 + gt);  // warp-uniform trip count
+    if (d.nhash) {  // robots too large for shared memory, if any is due (their lists: k_grid_list)
+        grid_boxes(d, gt, gs);
         if (!grid_barrier(d)) return;
         if (gt == 0) grid_params(d);
         if (!grid_barrier(d)) return;
@@ -1118,20 +1274,12 @@ __global__ void __launch_bounds__(kLocalListThreads, 1) k_coll_prepare(Dev d) {
         for (int b = blockIdx.x; b < used / 1024; b += gridDim.x) coll_scan_add(d, b, wsum);
         if (!grid_barrier(d)) return;
         for (int s = gt; s < d.ns; s += gs) grid_scatter(d, s);
-        if (!grid_barrier(d)) return;
-        grid_list(d, reinterpret_cast<int *>(lsm));
-        __syncthreads();  // the shared-memory path below reuses lsm
     }
     if (d.lmax) coll_list_robots(d, lsm, wsum);
 }
 
-// dynamic shared memory of k_coll_prepare: the shared-memory path's tables, or the
-// large-robot path's sub-lists (kNbrCap ints per thread), whichever is larger
-static size_t coll_prepare_smem(const Dev &d) {
-    size_t sm = d.lmax ? local_list_smem(d.lmax) : 0;
-    if (d.nhash) sm = std::max(sm, (size_t)kNbrCap * kLocalListThreads * sizeof(int));
-    return sm;
-}
+// dynamic shared memory of k_coll_prepare: the shared-memory path's tables
+static size_t coll_prepare_smem(const Dev &d) { return d.lmax ? local_list_smem(d.lmax) : 0; }
 
 cudaError_t init_collision(Dev &d) {
     d.cgrid = 0;
@@ -1147,6 +1295,13 @@ cudaError_t init_collision(Dev &d) {
         return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
     d.cgrid = nsm * occ;  // every CTA resident: the grid barrier's premise
+    d.glgrid = 0;
+    if (d.nhash) {  // k_grid_list: as many CTAs as fit at once
+        int gocc = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gocc, k_grid_list, kGridListThreads, 0)) != cudaSuccess)
+            return e;
+        d.glgrid = nsm * std::max(gocc, 1);
+    }
     return cudaSuccess;
 }
 
@@ -1247,7 +1402,9 @@ cudaError_t launch_coll_prepare(const Dev &d, cudaStream_t s) {
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_coll_prepare, d);
+    if ((e = cudaLaunchKernelEx(&cfg, k_coll_prepare, d)) != cudaSuccess) return e;
+    if (d.glgrid) k_grid_list<<<d.glgrid, kGridListThreads, 0, s>>>(d);  // the large robots' lists, if rebuilt
+    return cudaSuccess;
 }
 
 cudaError_t launch_collision(const Dev &d, cudaStream_t s) {

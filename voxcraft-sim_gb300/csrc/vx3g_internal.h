@@ -182,11 +182,12 @@ struct Dev {
     unsigned long long *lwork_ctr;  // (robots << 32) | chunks listed in lwork; cleared by the narrow phase
     int lmax;       // most collision-surface voxels of a robot on the shared-memory path (0: none)
     int cgrid;      // CTAs of the cooperative k_coll_prepare (all resident)
+    int glgrid;     // CTAs of k_grid_list (the lists of robots on the global hashed grid), 0: none
     int nhash;      // collision-surface voxels on the global hashed-grid path
     int *hcount, *hstart, *hfill, *hblock;  // bucket counts, starts, ends (after the scatter), segment sums
     unsigned *gbox;      // [NR][6] bounding-box accumulators of the large-robot grid (order-preserving keys)
     GridP *ggrid;        // [NR] that grid's corner, cell edge, size and first bucket
-    int *gmode;          // [3] dense grid (1) or hashed (0), buckets in use
+    int *gmode;          // [3] reach of a dense grid's neighbourhood in cells (1), 0 hashed; buckets in use
     float4 *spos;        // [NS] binned voxels in cell order: FP32 position, voxel index in w
     short4 *sij;         // [NS] their lattice coordinates, w = fixed
     int *ssurf;          // [NS] their collision-surface index
