@@ -173,9 +173,9 @@ __device__ bool make_link(const Dev &d, const RobotP &rp, int r, int v1, int v2,
     d.vnb[6 * (size_t)pos + 2 * axis + 1] = neg;
     const size_t sn = (size_t)(2 * axis) * d.nv + neg, sp = (size_t)(2 * axis + 1) * d.nv + pos;
     if (d.mixed) {
-        Slot<float> *S = (Slot<float> *)d.slots;
-        S[sn] = Slot<float>{{0, 0, 0}, {0, 0, 0}};
-        S[sp] = Slot<float>{{0, 0, 0}, {0, 0, 0}};
+        const V3<float> z{0, 0, 0};
+        store_slot_mx(d, 2 * axis, neg, z, z);
+        store_slot_mx(d, 2 * axis + 1, pos, z, z);
     } else {
         Slot<double> *S = (Slot<double> *)d.slots;
         S[sn] = Slot<double>{{0, 0, 0}, {0, 0, 0}};

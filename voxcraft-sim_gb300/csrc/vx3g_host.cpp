@@ -1240,12 +1240,18 @@ int vx3g_get_links(vx3g_ctx *c, float *strain, float *max_strain, double *local9
             std::fill(forces12 + 12 * l, forces12 + 12 * l + 12, 0.0);
         } else if (forces12) {
             const int a = (int)laxis[l];
-            const size_t sn = ((size_t)(2 * a) * nv + lends[l].x) * 6, sp = ((size_t)(2 * a + 1) * nv + lends[l].y) * 6;
+            const size_t in = (size_t)(2 * a) * nv + lends[l].x, ip = (size_t)(2 * a + 1) * nv + lends[l].y;
+            // the six components (force x, y, z, moment x, y, z) of slot i: FP64 Slot<double>;
+            // mixed precision: a 16-byte row {f, m.x} then, after all of those, an 8-byte row {m.y, m.z}
+            auto comp = [&](size_t i, int k) -> double {
+                if (fp64) return rd(sl, i * 6 + k);
+                return k < 4 ? rd(sl, i * 4 + k) : rd(sl, 24 * nv + i * 2 + (k - 4));
+            };
             for (int k = 0; k < 3; k++) {
-                forces12[12 * l + k] = rd(sl, sn + k);         // forceNeg
-                forces12[12 * l + 3 + k] = rd(sl, sp + k);     // forcePos
-                forces12[12 * l + 6 + k] = rd(sl, sn + 3 + k); // momentNeg
-                forces12[12 * l + 9 + k] = rd(sl, sp + 3 + k); // momentPos
+                forces12[12 * l + k] = comp(in, k);          // forceNeg
+                forces12[12 * l + 3 + k] = comp(ip, k);      // forcePos
+                forces12[12 * l + 6 + k] = comp(in, 3 + k);  // momentNeg
+                forces12[12 * l + 9 + k] = comp(ip, 3 + k);  // momentPos
             }
         }
     }

@@ -281,14 +281,11 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     d.strain[l] = sm;
     if (axialStrain > 100) atomicOr(&d.status[r], 1);
 
-    Slot<float> *S = (Slot<float> *)d.slots;
-    Slot<float> *sNeg = &S[(size_t)(2 * axis) * d.nv + e.x];
-    Slot<float> *sPos = &S[(size_t)(2 * axis + 1) * d.nv + e.y];
     uint32_t nfl = (fl & ~(LF_SMALL | LF_LVV)) | (small ? LF_SMALL : 0u);
     if (m.eps_fail != -1.0f && sm.y > m.eps_fail) {
         const V3<float> z{0, 0, 0};
-        store_slot(sNeg, z, z);
-        store_slot(sPos, z, z);
+        store_slot_mx(d, 2 * axis, e.x, z, z);
+        store_slot_mx(d, 2 * axis + 1, e.y, z, z);
         nfl |= lvv ? LF_LVV : 0u;
         if (nfl != fl) d.linfo[l].y = nfl;
         return;
@@ -323,9 +320,9 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     const Q4<float> angle2{w2, v2.x, v2.y, v2.z};
     fPos = qrotinv(angle2, fPos);
     mPos = qrotinv(angle2, mPos);
-    store_slot(sNeg, to_axis_original(axis, fNeg), to_axis_original(axis, mNeg));
-    store_slot(sPos, to_axis_original(axis, fPos), to_axis_original(axis, mPos));
-    if (fl & LF_RUNTIME) new_link_scale(d, l, sNeg, sPos);
+    store_slot_mx(d, 2 * axis, e.x, to_axis_original(axis, fNeg), to_axis_original(axis, mNeg));
+    store_slot_mx(d, 2 * axis + 1, e.y, to_axis_original(axis, fPos), to_axis_original(axis, mPos));
+    if (fl & LF_RUNTIME) new_link_scale_mx(d, l, 2 * axis, e.x, e.y);
     if (nfl != fl) d.linfo[l].y = nfl;
 }
 
@@ -428,13 +425,13 @@ template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &
         AM[2 * v + 1] = z4;
     } else if (dtf != 0.0f) {
         V3<float> Fs{0, 0, 0}, Ms{0, 0, 0};
-        const Slot<float> *S = (const Slot<float> *)d.slots;
 #pragma unroll
         for (int dir = 0; dir < 6; dir++) {
             if (fl & (1u << dir)) {
-                const Slot<float> s = S[(size_t)dir * d.nv + v];
-                Fs = add(Fs, V3<float>{s.f[0], s.f[1], s.f[2]});
-                Ms = add(Ms, V3<float>{s.m[0], s.m[1], s.m[2]});
+                V3<float> sf, sm;
+                load_slot_mx(d, dir, v, &sf, &sm);
+                Fs = add(Fs, sf);
+                Ms = add(Ms, sm);
             }
         }
         bool stat = (fl & VF_STATIC) != 0;

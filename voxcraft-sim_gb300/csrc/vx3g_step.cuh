@@ -145,6 +145,23 @@ template <class R> __device__ __forceinline__ V3<R> to_axis_original(int axis, V
     return v;
 }
 
+// Mixed-precision slots: the slot of (direction dir, voxel v) is split into a 16-byte row
+// {force x, y, z, moment x} and an 8-byte row {moment y, z}: six 16-byte rows per voxel
+// direction-major, then six 8-byte rows, in the same 24 bytes per slot as Slot<float>,
+// so that the link pass stores and the voxel pass loads each slot with two wide accesses
+__device__ __forceinline__ void store_slot_mx(const Dev &d, int dir, int v, V3<float> f, V3<float> m) {
+    const size_t i = (size_t)dir * d.nv + v;
+    reinterpret_cast<float4 *>(d.slots)[i] = make_float4(f.x, f.y, f.z, m.x);
+    reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(d.slots) + 6 * (size_t)d.nv)[i] = make_float2(m.y, m.z);
+}
+__device__ __forceinline__ void load_slot_mx(const Dev &d, int dir, int v, V3<float> *f, V3<float> *m) {
+    const size_t i = (size_t)dir * d.nv + v;
+    const float4 a = reinterpret_cast<const float4 *>(d.slots)[i];
+    const float2 b = reinterpret_cast<const float2 *>(reinterpret_cast<const float4 *>(d.slots) + 6 * (size_t)d.nv)[i];
+    *f = V3<float>{a.x, a.y, a.z};
+    *m = V3<float>{a.w, b.x, b.y};
+}
+
 template <class R> __device__ __forceinline__ void store_slot(Slot<R> *s, V3<R> f, V3<R> m) {
     Slot<R> o;
     o.f[0] = f.x; o.f[1] = f.y; o.f[2] = f.z;
@@ -288,6 +305,21 @@ template <class R> __device__ __forceinline__ void new_link_scale(const Dev &d, 
     for (int c = 0; c < 6; c++) {
         a[c] = a[c] * k;
         b[c] = b[c] * k;
+    }
+    d.lnew[l] = n - 1;
+}
+
+// the same for a runtime link's two mixed-precision slots (negative end: direction dneg)
+__device__ __forceinline__ void new_link_scale_mx(const Dev &d, int l, int dneg, int vneg, int vpos) {
+    const int n = d.lnew[l];
+    if (n == 0) return;
+    for (int e = 0; e < 2; e++) {
+        const size_t i = (size_t)(dneg + e) * d.nv + (e ? vpos : vneg);
+        volatile float *a = reinterpret_cast<volatile float *>(reinterpret_cast<float4 *>(d.slots) + i);
+        volatile float *b =
+            reinterpret_cast<volatile float *>(reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(d.slots) + 6 * (size_t)d.nv) + i);
+        for (int c = 0; c < 4; c++) a[c] = a[c] * 0.01f;
+        for (int c = 0; c < 2; c++) b[c] = b[c] * 0.01f;
     }
     d.lnew[l] = n - 1;
 }
