@@ -158,8 +158,10 @@ __device__ bool make_link(const Dev &d, const RobotP &rp, int r, int v1, int v2,
     d.linfo[l] = make_uint2((unsigned)r, (uint32_t)axis | LF_SMALL | LF_RUNTIME | ((uint32_t)lm << 8));
     const size_t NL = (size_t)d.nl;
     if (d.mixed) {
-        float *ls = (float *)d.lstate;
-        for (int k = 0; k < 9; k++) ls[k * NL + l] = 0.0f;
+        mixed_lstate_a(d)[l] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        mixed_lstate_b(d)[l] = make_float2(0.0f, 0.0f);
+        float *c = mixed_lstate_c(d);
+        for (int k = 0; k < 3; k++) c[k * NL + l] = 0.0f;
     } else {
         double *ls = (double *)d.lstate;
         for (int k = 0; k < 9; k++) ls[k * NL + l] = 0.0;

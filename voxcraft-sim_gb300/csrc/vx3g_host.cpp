@@ -1234,8 +1234,17 @@ int vx3g_get_links(vx3g_ctx *c, float *strain, float *max_strain, double *local9
         if (strain) strain[l] = sm[l].x;
         if (max_strain) max_strain[l] = sm[l].y;
         if (small) small[l] = ((li[l].y & LF_SMALL) ? 1 : 0) | ((li[l].y & LF_GONE) ? 2 : 0) | ((li[l].y & LF_LVV) ? 4 : 0);
-        if (local9)
-            for (int k = 0; k < 9; k++) local9[9 * l + k] = rd(ls, (size_t)k * nl + l);
+        if (local9) {  // pos2, angle1v, angle2v
+            if (fp64) {
+                for (int k = 0; k < 9; k++) local9[9 * l + k] = rd(ls, (size_t)k * nl + l);
+            } else {  // mixed: rows {pos2, angle2v.x}, {angle2v.y, angle2v.z}, then angle1v component-major
+                for (int k = 0; k < 3; k++) local9[9 * l + k] = rd(ls, 4 * l + k);
+                for (int k = 0; k < 3; k++) local9[9 * l + 3 + k] = rd(ls, 6 * nl + (size_t)k * nl + l);
+                local9[9 * l + 6] = rd(ls, 4 * l + 3);
+                local9[9 * l + 7] = rd(ls, 4 * nl + 2 * l);
+                local9[9 * l + 8] = rd(ls, 4 * nl + 2 * l + 1);
+            }
+        }
         if (forces12 && lends[l].x < 0) {  // an unused reserve slot
             std::fill(forces12 + 12 * l, forces12 + 12 * l + 12, 0.0);
         } else if (forces12) {

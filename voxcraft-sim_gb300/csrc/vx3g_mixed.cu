@@ -191,16 +191,22 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     // endpoint state: two dependent load levels instead of four (latency-bound kernel)
     const uint2 li = d.linfo[l];
     const int2 e = d.ends[l];
-    float *ls = (float *)d.lstate;
+    // link state (mixed precision): a 16-byte row {pos2, angle2v.x} and an 8-byte row
+    // {angle2v.y, angle2v.z} per link, then angle1v component-major (mixed_lstate_*)
+    float4 *lsA = mixed_lstate_a(d);
+    float2 *lsB = mixed_lstate_b(d);
+    float *lsC = mixed_lstate_c(d);
     const size_t NL = (size_t)d.nl;
-    const V3<float> oldPos2{ls[l], ls[NL + l], ls[2 * NL + l]};
+    const float4 sa = lsA[l];
+    const float2 sb = lsB[l];
+    const V3<float> oldPos2{sa.x, sa.y, sa.z};
     // angle1v is zero while a link is in the small-angle branch (the flag it entered
     // this step with says so); it is read and written only for large-angle links and
     // zeroed once when a link returns to the small branch
     const bool wasSmall = (li.y & LF_SMALL) != 0;
     V3<float> oldA1{0, 0, 0};
-    if (!wasSmall) oldA1 = V3<float>{ls[3 * NL + l], ls[4 * NL + l], ls[5 * NL + l]};
-    const V3<float> oldA2{ls[6 * NL + l], ls[7 * NL + l], ls[8 * NL + l]};
+    if (!wasSmall) oldA1 = V3<float>{lsC[l], lsC[NL + l], lsC[2 * NL + l]};
+    const V3<float> oldA2{sa.w, sb.x, sb.y};
     float2 sm = d.strain[l];
     pdl_wait_then_release();  // the previous voxel pass has moved the endpoints
     const float4 *P = reinterpret_cast<const float4 *>(d.pos);
@@ -266,11 +272,11 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     }
     const V3<float> a1v = small ? V3<float>{0, 0, 0} : rotvec_f(angle1.w, V3<float>{angle1.x, angle1.y, angle1.z});
     const V3<float> a2v = rotvec_f(w2, v2);
-    ls[l] = pos2.x; ls[NL + l] = pos2.y; ls[2 * NL + l] = pos2.z;
+    lsA[l] = make_float4(pos2.x, pos2.y, pos2.z, a2v.x);
+    lsB[l] = make_float2(a2v.y, a2v.z);
     if (!(small && wasSmall)) {
-        ls[3 * NL + l] = a1v.x; ls[4 * NL + l] = a1v.y; ls[5 * NL + l] = a1v.z;
+        lsC[l] = a1v.x; lsC[NL + l] = a1v.y; lsC[2 * NL + l] = a1v.z;
     }
-    ls[6 * NL + l] = a2v.x; ls[7 * NL + l] = a2v.y; ls[8 * NL + l] = a2v.z;
 
     const V3<float> dPos2 = scl(sub(pos2, oldPos2), 0.5f);
     const V3<float> dA1 = scl(sub(a1v, oldA1), 0.5f);

@@ -145,6 +145,18 @@ template <class R> __device__ __forceinline__ V3<R> to_axis_original(int axis, V
     return v;
 }
 
+// Mixed-precision link state, in the 36 bytes per link of nine floats: a 16-byte row
+// {pos2.x, pos2.y, pos2.z, angle2v.x} per link, an 8-byte row {angle2v.y, angle2v.z} per
+// link, then angle1v's three components, component-major (read and written only for
+// links in the large-angle branch)
+__device__ __forceinline__ float4 *mixed_lstate_a(const Dev &d) { return reinterpret_cast<float4 *>(d.lstate); }
+__device__ __forceinline__ float2 *mixed_lstate_b(const Dev &d) {
+    return reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(d.lstate) + d.nl);
+}
+__device__ __forceinline__ float *mixed_lstate_c(const Dev &d) {
+    return reinterpret_cast<float *>(reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(d.lstate) + d.nl) + d.nl);
+}
+
 // Mixed-precision slots: the slot of (direction dir, voxel v) is split into a 16-byte row
 // {force x, y, z, moment x} and an 8-byte row {moment y, z}: six 16-byte rows per voxel
 // direction-major, then six 8-byte rows, in the same 24 bytes per slot as Slot<float>,
