@@ -458,9 +458,14 @@ def main():
     value = vox_steps / (total_ms / 1e3)
     surf = b.surface()
     ns_coll = 0
+    global_grid = False  # some robot is listed on the global grid (k_grid_list launches every step)
     for i, r in enumerate(robots):
         if r.enable_collision:
-            ns_coll += int(np.count_nonzero((surf >= b.voxel_offset[i]) & (surf < b.voxel_offset[i + 1])))
+            ns_r = int(np.count_nonzero((surf >= b.voxel_offset[i]) & (surf < b.voxel_offset[i + 1])))
+            ns_coll += ns_r
+            # the library lists a robot in shared memory when it has at most 6144 collision-surface
+            # voxels and lattice coordinates below 512 (kLocalListMax)
+            global_grid |= ns_r > 6144 or max(r.grid.shape) + r.z_offset > 512
 
     # per-pass device times (after the measured run); the dominant kernel is the single
     # kernel with the largest time: the link pass, the voxel pass or the contact evaluation
@@ -476,8 +481,9 @@ def main():
     achieved = kernel_bytes[dom] / (kernel_ms[dom] / 1e3) / 1e9 if kernel_ms[dom] > 0 else 0.0
     traffic = ncu_traffic(args.workload, args.precision, dom)
     # link pass + voxel pass; collision: the displacement check, the cooperative list
-    # rebuild kernel (it returns at once unless a rebuild is due) and the contact evaluation
-    kernels_per_step = 2 + (3 if ns_coll else 0)
+    # rebuild kernel (it returns at once unless a rebuild is due), the global grid's list
+    # kernel (the same) and the contact evaluation
+    kernels_per_step = 2 + ((4 if global_grid else 3) if ns_coll else 0)
     shapes = [int(x) for x in b.launch_shapes()]
     b.close()
 

@@ -127,6 +127,7 @@ VMat to_vmat(const HostVMat &m, const vx3g_material &in) {
     v.is_measured = in.is_measured ? 1 : 0;
     v.nom_size = m.nom;
     v.thermal_on_after = in.thermal_on_after;
+    v.toa_pos = in.thermal_on_after > 0 ? 1 : 0;
     v.pacemaker = in.is_pacemaker ? 1 : 0;
     v.pace_period = in.pacemaker_period;
     v.sig_decay = in.signal_value_decay;
@@ -509,6 +510,8 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         rp.temp_amp = R.temp_amplitude;
         rp.temp_period = R.temp_period;
         rp.inv_period = R.temp_period > 0 ? 1.0 / R.temp_period : 0.0;
+        rp.cyc_rate = (float)(rp.inv_period * kCycle);
+        rp.amp_f = (float)R.temp_amplitude;
         rp.dt_frac = R.dt_frac;
         rp.voff = v0;
         rp.nv = nvr;
@@ -753,6 +756,17 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         (rc = c->upload(&d.phase, phase)) || (rc = c->upload(&d.vinfo, vinfo)) || (rc = c->upload(&d.ijk, c->ijk)) ||
         (rc = c->upload(&d.ends, c->ends)) || (rc = c->upload(&d.linfo, linfo)) || (rc = c->alloc(&d.strain, d.nl)))
         return rc;
+    d.tcyc = d.phc = nullptr;
+    if (d.mixed) {  // actuation cycles: the robots' (zero at time 0) and the voxels' phases
+        std::vector<float2> phc(phase.size());
+        for (size_t i = 0; i < phase.size(); i++) {
+            double cy = phase[i] * kCycle;
+            cy -= std::floor(cy);
+            phc[i].x = (float)cy;
+            phc[i].y = (float)(cy - (double)phc[i].x);
+        }
+        if ((rc = c->upload(&d.phc, phc)) || (rc = c->alloc(&d.tcyc, 2 * (size_t)d.nr))) return rc;
+    }
     const size_t rsz = c->precision == VX3G_PRECISION_FP64 ? sizeof(double) : sizeof(float);
     char *ls = nullptr, *sl = nullptr;
     if ((rc = c->alloc(&ls, 9 * (size_t)d.nl * rsz)) || (rc = c->alloc(&sl, 6 * (size_t)d.nv * 6 * rsz))) return rc;
@@ -1201,7 +1215,12 @@ int vx3g_get_voxel_aux(vx3g_ctx *c, float *tempe, int32_t *flags, double *contac
             // reference voxState bits: SURFACE(2, set for interior voxels), FLOOR_ENABLED(4), FLOOR_STATIC_FRICTION(8)
             flags[i] = (((f & VF_LINKMASK) == VF_LINKMASK) ? 2 : 0) | (rps[vi[i].x].floor ? 4 : 0) | ((f & VF_STATIC) ? 8 : 0);
         }
-        if (contact) { contact[3 * i] = ct[i].x; contact[3 * i + 1] = ct[i].y; contact[3 * i + 2] = ct[i].z; }
+        if (contact && c->d.mixed) {  // mixed precision: float4 per voxel in the first half of the buffer
+            const float4 f = reinterpret_cast<const float4 *>(ct.data())[i];
+            contact[3 * i] = f.x; contact[3 * i + 1] = f.y; contact[3 * i + 2] = f.z;
+        } else if (contact) {
+            contact[3 * i] = ct[i].x; contact[3 * i + 1] = ct[i].y; contact[3 * i + 2] = ct[i].z;
+        }
     }
     return VX3G_OK;
 }

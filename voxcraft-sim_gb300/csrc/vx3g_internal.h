@@ -7,7 +7,8 @@
 //             quat[v]   double4 {w, x, y, z}
 //             linmom[v] double4 {x, y, z, -}, angmom[v] double4 {x, y, z, -}
 //             vinfo[v]  uint2 {robot, flags | vmat<<8}
-//             contact[v] double4, tempe[v] float, phase[v] double, ijk[v] short4
+//             contact[v] double4 (float4 in mixed precision), tempe[v] float, phase[v] double,
+//             ijk[v] short4
 //   link l  : ends[l] int2 {neg, pos}, linfo[l] uint2 {robot, flags | lmat<<8},
 //             local state (pos2, angle1v, angle2v): 9 component-major arrays of R,
 //             strain[l] float2 {strain, maxStrain}
@@ -37,6 +38,10 @@ enum : uint32_t {
     LF_RUNTIME = 1u << 6,     // made by attachment, or a reserve slot for one (GONE until made)
 };
 
+// the actuation argument 2*3.1415926f*(t/period + phase) (gpu_update_temperature,
+// VX3_VoxelyzeKernel.cu:625-650) in cycles of 2*pi: (t/period + phase) * kCycle
+constexpr double kCycle = (double)(2 * 3.1415926f) * (1.0 / 6.283185307179586);
+
 // robot status bit (VX3G_ROBOT_LINK_CAPACITY): attachment found the robot's link reserve used up
 constexpr int kStatusLinkCapacity = 8;
 
@@ -54,6 +59,7 @@ struct VMat {  // one voxel material (global index), constants as the reference 
     int fixed, is_measured;
     double nom_size;
     double thermal_on_after;
+    int toa_pos;       // thermal_on_after > 0: only then is it compared with the time (in FP64)
     int pacemaker;     // isPaceMaker
     double pace_period, sig_decay, sig_delay, inactive;  // PaceMakerPeriod, signalValueDecay, signalTimeDelay, inactivePeriod
     int alm;           // Sticky material of a robot with EnableAttach: the link material of its runtime
@@ -73,6 +79,7 @@ struct LMat {  // one link material (global index), oriented: (negative end, pos
 
 struct RobotP {
     double vox_size, temp_amp, temp_period, inv_period, dt_frac;
+    float cyc_rate, amp_f;  // mixed precision: actuation cycles per second (inv_period * kCycle), amplitude
     double cell_size;      // upper bound of the envelope cutoff (bsa1+bsa2)*0.625
     double skin;           // Verlet skin of the contact-candidate lists
     double inv_list_cell;  // 1 / (cell_size + skin): grid used to build the lists
@@ -159,6 +166,10 @@ struct Dev {
     const RobotP *rp;
     float *dt;
     double *T;      // [2][NR] time, double-buffered by step parity
+    // mixed precision: [2][NR] the actuation cycles frac(T * inv_period * kCycle) as an FP32
+    // hi + lo pair, written with T; per voxel the phase cycles frac(phase * kCycle) as hi + lo
+    // (NULL in FP64)
+    float2 *tcyc, *phc;
     int *status;
     // materials
     const VMat *vmat;

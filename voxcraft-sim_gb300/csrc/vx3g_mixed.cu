@@ -1,7 +1,10 @@
 // vx3g_mixed.cu -- the mixed-precision step: FP32 link forces and moments,
 // compensated FP32 (hi + lo float pairs, two-sum arithmetic) for positions,
-// orientations and momenta.  No FP64 arithmetic runs per link; per voxel only the
-// actuation phase is reduced in FP64.
+// orientations and momenta.  No FP64 arithmetic runs per link or per voxel (the actuation
+// phase is reduced in FP64 once per robot and step).  Quotients and square roots on the
+// hot paths use the hardware reciprocal and reciprocal square root (__fdividef, rsqrtf:
+// within 2 ulp), fixed instructions, so every compiled launch shape computes the same
+// values; the FP64 step keeps the reference's correctly rounded operations.
 //
 // The link pass restates VX3_Link::orientLink/updateForces (src/VX3/VX3_Link.cu:90-218)
 // without the cancellations FP32 would suffer:
@@ -15,6 +18,8 @@
 // The voxel pass restates VX3_Voxel::timeStep (src/VX3/VX3_Voxel.cu:162-277) with the
 // same sums in FP32 and every accumulation (p += F dt, x += p dt/m, L += M dt,
 // q += (dq - 1) q) done as a two-sum into the hi/lo pair.
+#include <math_constants.h>
+
 #include "vx3g_step.cuh"
 
 namespace vx3g {
@@ -35,19 +40,18 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float x) {
     e += lo;
     quick_two_sum(s, e, hi, lo);
 }
-// (ah + al) - (bh + bl) rounded once, for nearby values
-__device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl) {
-    float s, e;
-    two_sum(ah, -bh, s, e);
-    return s + (e + (al - bl));
-}
-// (ah + al) - (bh + bl) - (ch + cl): the axial deviation of a link (a-b ~= c)
+// (ah + al) - (bh + bl) to FP32 accuracy: the rounding of ah - bh is at most half an ulp of
+// the difference itself (and none when ah and bh are within a factor 2), so no two-sum is
+// needed when nothing is subtracted from the result afterwards
+__device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl) { return (ah - bh) + (al - bl); }
+// (ah + al) - (bh + bl) - (ch + cl): the axial deviation of a link (a - b ~= c).  The
+// rounding of ah - bh is kept (two-sum): it can be as large as the deviation; s - ch is
+// exact (Sterbenz) while the link's strain lies between -50% and +100%, and otherwise
+// rounds a deviation as large as the rest length
 __device__ __forceinline__ float df_diff3(float ah, float al, float bh, float bl, float ch, float cl) {
     float s, e;
     two_sum(ah, -bh, s, e);
-    float s2, e2;
-    two_sum(s, -ch, s2, e2);
-    return s2 + (e2 + (e + ((al - bl) - cl)));
+    return (s - ch) + (e + ((al - bl) - cl));
 }
 
 // ToRotationVector (src/VX3/VX3_Quat3D.h:347-359) of a unit quaternion (w, v) in FP32.
@@ -61,9 +65,9 @@ __device__ __forceinline__ float df_diff3(float ah, float al, float bh, float bl
 __device__ __forceinline__ V3<float> rotvec_f(float w, V3<float> v) {
     const float s2 = v.x * v.x + v.y * v.y + v.z * v.z;
     if (!(s2 > 0.0f)) return V3<float>{0, 0, 0};
-    if (s2 < 2.4e-3f) return scl(v, 2.0f * sqrtf(2.0f / (1.0f + w)));
-    const float s = sqrtf(s2);
-    return scl(v, 2.0f * atan2f(s, w) / s);
+    if (s2 < 2.4e-3f) return scl(v, 2.82842712f * rsqrtf(1.0f + w));
+    const float is = rsqrtf(s2);  // s2 >= 2.4e-3 here
+    return scl(v, 2.0f * atan2f(s2 * is, w) * is);
 }
 
 // FromAngleToPosX (src/VX3/VX3_Quat3D.h:384-432) in FP32: the rotation taking r to
@@ -77,7 +81,7 @@ __device__ __forceinline__ V3<float> rotvec_f(float w, V3<float> v) {
 // are the reference's.
 __device__ __forceinline__ Q4<float> from_angle_to_posx_f(Q4<float> q, V3<float> r) {
     if (r.x == 0 && r.y == 0 && r.z == 0) return q;
-    const float yx = r.y / r.x, zx = r.z / r.x;
+    const float yx = __fdividef(r.y, r.x), zx = __fdividef(r.z, r.x);
     const float SA = 1.732e-2f;
     if (yx < SA && yx > -SA && zx < SA && zx > -SA) {
         q.x = 0;
@@ -90,7 +94,7 @@ __device__ __forceinline__ Q4<float> from_angle_to_posx_f(Q4<float> q, V3<float>
     const float nx = r.x * il, ny = r.y * il, nz = r.z * il;
     const float t = 2.0f * (1.0f + nx);
     if (!(t > 0.0f)) return Q4<float>{0, 0, 1, 0};
-    const float c = sqrtf(t), ic = __frcp_rn(c);
+    const float ic = rsqrtf(t), c = t * ic;
     return Q4<float>{0.5f * c, 0, nz * ic, -ny * ic};
 }
 
@@ -137,14 +141,17 @@ template <bool ATTACH> __global__ void __launch_bounds__(256) k_coll_eval_mixed(
             const float oz = sg * df_diff(puH.z, puL.z, pvH.z, pvL.z);
             const float bu = puH.w;
             const float wd = (bv + bu) * 0.625f;
-            const float dist = sqrtf(ox * ox + oy * oy + oz * oz);
+            // |offset| and its reciprocal from one hardware reciprocal square root (coincident
+            // voxels, d2 = 0, give dist = NaN and are skipped; the reference's force is NaN there)
+            const float d2 = ox * ox + oy * oy + oz * oz;
+            const float inv = rsqrtf(d2);
+            const float dist = d2 * inv;
             if (!(dist <= wd)) continue;
             const float rel = wd - dist;
             if (!(rel > 0)) continue;
             const float4 wu = R[3 * u + 2];
-            const float pstiff = 2.0f / (1.0f / pvL.w + 1.0f / puL.w);
+            const float pstiff = __fdividef(2.0f * pvL.w * puL.w, pvL.w + puL.w);  // 2 / (1/a + 1/b)
             const float dampC = 0.5f * (wv.w + wu.w);
-            const float inv = 1.0f / dist;
             const float ux = ox * inv, uy = oy * inv, uz = oz * inv;
             const float w1x = wv.x, w1y = wv.y, w1z = wv.z;
             const float w2x = wu.x, w2y = wu.y, w2z = wu.z;
@@ -164,7 +171,7 @@ template <bool ATTACH> __global__ void __launch_bounds__(256) k_coll_eval_mixed(
             acc.z += sg * uz * f;
         }
     }
-    d.contact[v] = make_double4(acc.x, acc.y, acc.z, 0.0);
+    reinterpret_cast<float4 *>(d.contact)[v] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
 
 void launch_coll_eval_mixed(const Dev &d, cudaStream_t s) {
@@ -267,8 +274,9 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
         const Q4<float> a2 = qmul(angle1, Q4<float>{w2, v2.x, v2.y, v2.z});
         w2 = a2.w;
         v2 = V3<float>{a2.x, a2.y, a2.z};
-        const float len2 = sqrtf(px * px + py * py + pz * pz);
-        pos2 = V3<float>{(pxm * (px + L) + py * py + pz * pz) / (len2 + L), 0, 0};  // |pos2| - L
+        const float l2 = px * px + py * py + pz * pz;
+        const float len2 = l2 > 0.0f ? l2 * rsqrtf(l2) : 0.0f;
+        pos2 = V3<float>{__fdividef(pxm * (px + L) + py * py + pz * pz, len2 + L), 0, 0};  // |pos2| - L
     }
     const V3<float> a1v = small ? V3<float>{0, 0, 0} : rotvec_f(angle1.w, V3<float>{angle1.x, angle1.y, angle1.z});
     const V3<float> a2v = rotvec_f(w2, v2);
@@ -281,7 +289,9 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     const V3<float> dPos2 = scl(sub(pos2, oldPos2), 0.5f);
     const V3<float> dA1 = scl(sub(a1v, oldA1), 0.5f);
     const V3<float> dA2 = scl(sub(a2v, oldA2), 0.5f);
-    const float axialStrain = pos2.x / L;
+    // FP32 quotients in the hot paths use the hardware reciprocal (__fdividef: within 2 ulp, one
+    // fixed instruction pair, so every launch shape computes the same value)
+    const float axialStrain = __fdividef(pos2.x, L);
     sm.x = axialStrain;
     const float stress = link_stress(d, m, l, axialStrain, &sm.y);  // updateStrain (VX3_Link.cu:220-260)
     d.strain[l] = sm;
@@ -304,9 +314,10 @@ __device__ __forceinline__ void links_mixed_body(const Dev &d, int l) {
     if (lvv) {
         const V3<float> posCalc{m.sqA1 * dPos2.x, m.sqB1 * dPos2.y - m.sqB2xFMp * (dA1.z + dA2.z),
                                 m.sqB1 * dPos2.z + m.sqB2xFMp * (dA1.y + dA2.y)};
-        const float dtf = d.dt[r];
-        const float dmN = m.dmcN / (m.fixN ? 0.0f : dtf);
-        const float dmP = m.dmcP / (m.fixP ? 0.0f : dtf);
+        // dampingMultiplier / dt, infinite for a Fixed end (its numerator over a zero time step)
+        const float idt = __fdividef(1.0f, d.dt[r]);
+        const float dmN = m.dmcN * (m.fixN ? CUDART_INF_F : idt);
+        const float dmP = m.dmcP * (m.fixP ? CUDART_INF_F : idt);
         fNeg = add(fNeg, scl(posCalc, dmN));
         fPos = sub(fPos, scl(posCalc, dmP));
         mNeg = sub(mNeg, scl(V3<float>{-m.sqA2xIp * (dA2.x - dA1.x), m.sqB2xFMp * dPos2.z + m.sqB3xIp * (2 * dA1.y + dA2.y),
@@ -340,22 +351,49 @@ __device__ __forceinline__ void base_size_df(const VMat &m, float te, float &hi,
     quick_two_sum(p, err, hi, lo);
 }
 
-// temperature at time t (gpu_update_temperature, VX3_VoxelyzeKernel.cu:625-650): the phase
-// 2*3.1415926f*(t/P + phase) reduced to cycles c in FP64 and split into c_hi + c_lo
-// (two floats); sin(2 pi c) = sin(2 pi c_hi) + 2 pi c_lo cos(2 pi c_hi), the second
-// term dropping (2 pi c_lo)^2 / 2 < 1e-13.  The FP32 sine alone would carry the
-// rounding of c (up to 3.7e-7 rad of phase); with the correction the temperature is
-// within about one FP32 rounding of the FP64 step's.
-__device__ __forceinline__ float temperature_f(const RobotP &rp, double phase, double t) {
-    double c = (t * rp.inv_period + phase) * ((double)(2 * 3.1415926f) * (1.0 / 6.283185307179586));
-    c -= floor(c);
-    const float ch = (float)c;
-    const float cl = (float)(c - (double)ch);
+// temperature at the end of a step (gpu_update_temperature, VX3_VoxelyzeKernel.cu:625-650)
+// from the cycles of the phase 2*3.1415926f*(t/P + phase) / (2 pi): the robot's cycles at
+// the step's start tc and the voxel's phase cycles ph, each frac(.) reduced in FP64 once
+// (by the writer of the robot's time, and at create) and held as FP32 hi + lo pairs, plus
+// the step's dt * cycles per second (about 5e-4 cycles, rounded to 3e-11).  The sum c_hi +
+// c_lo is formed with two-sums, and sin(2 pi c) = sin(2 pi c_hi) + 2 pi c_lo cos(2 pi c_hi),
+// the second term dropping (2 pi c_lo)^2 / 2 < 1e-13.  The FP32 sine of a rounded c alone
+// would carry up to 3.7e-7 rad of phase; with the correction the temperature is within
+// about one FP32 rounding of the FP64 step's, and no FP64 arithmetic runs per voxel.
+__device__ __forceinline__ float temperature_mx(const RobotP &rp, float2 tc, float2 ph, float dtf) {
+    float s, e;
+    two_sum(tc.x, ph.x, s, e);
+    s -= floorf(s);  // exact: s lies in [0, 2]
+    e += (tc.y + ph.y) + dtf * rp.cyc_rate;
+    float ch, cl;
+    two_sum(s, e, ch, cl);
     float sn, cs;
     sincospif(2.0f * ch, &sn, &cs);
-    float T = (float)rp.temp_amp * fmaf(6.28318531f * cl, cs, sn);
+    float T = rp.amp_f * fmaf(6.28318531f * cl, cs, sn);
     if (!rp.expansion && T > 0) T = 0;
     return T;
+}
+
+// frac(c) as an FP32 hi + lo pair
+__device__ __forceinline__ float2 cycles_df(double c) {
+    c -= floor(c);
+    const float h = (float)c;
+    return make_float2(h, (float)(c - (double)h));
+}
+
+// The FP64 arithmetic of the mixed voxel pass, kept out of line: if-converted into the
+// pass, it would issue in every warp (GB300 runs FP64 at about 1/64 of the FP32 rate).
+// The robot's time and actuation cycles of the next step (one thread per robot):
+__device__ __noinline__ void advance_time(const Dev &d, const RobotP &rp, int r, int parity, float dtf, int st) {
+    const double Tcur = d.T[(size_t)parity * d.nr + r];
+    const double Tn = (st == 0) ? Tcur + dtf : Tcur;
+    d.T[(size_t)(parity ^ 1) * d.nr + r] = Tn;
+    d.tcyc[(size_t)(parity ^ 1) * d.nr + r] = cycles_df(Tn * rp.inv_period * kCycle);
+}
+// a material with TurnOnThermalExpansionAfterThisManySeconds > 0: is expansion on at the
+// end of this step?
+__device__ __noinline__ bool thermal_on(const Dev &d, double toa, int r, int parity, float dtf) {
+    return !(toa > d.T[(size_t)parity * d.nr + r] + dtf);
 }
 
 __global__ void k_init_temperature_mixed(Dev d) {
@@ -365,7 +403,8 @@ __global__ void k_init_temperature_mixed(Dev d) {
     const VMat m = d.vmat[vi.y >> 8];
     const RobotP &rp = d.rp[vi.x];
     float te = d.tempe[v];
-    if (rp.vary_temp && rp.temp_period > 0 && !(m.thermal_on_after > 0.0) && !m.fixed) te = temperature_f(rp, d.phase[v], 0.0);
+    if (rp.vary_temp && rp.temp_period > 0 && !(m.thermal_on_after > 0.0) && !m.fixed)
+        te = temperature_mx(rp, make_float2(0.0f, 0.0f), d.phc[v], 0.0f);
     float4 *P = reinterpret_cast<float4 *>(d.pos);
     base_size_df(m, te, P[2 * v].w, P[2 * v + 1].w);
     d.tempe[v] = te;
@@ -398,10 +437,9 @@ template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &
     pdl_wait_then_release();  // the link pass (or the contact evaluation) of this step is done
     const int r = (int)vi.x;
     const RobotP &rp = d.rp[r];
-    const double Tcur = d.T[(size_t)parity * d.nr + r];
     const int st = d.status[r];
     const float dtf = d.dt[r];
-    if (!BC && v == rp.voff) d.T[(size_t)(parity ^ 1) * d.nr + r] = (st == 0) ? Tcur + dtf : Tcur;
+    if (!BC && v == rp.voff) advance_time(d, rp, r, parity, dtf, st);
     if (st != 0) return;
     uint32_t fl = vi.y;
     if (fl & VF_FIXED) return;
@@ -409,7 +447,6 @@ template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &
     const VMat m = d.vmat[fl >> 8];
     const bool actuated = rp.vary_temp && rp.temp_period > 0;
     float *tcur = d.tempe + (size_t)parity * d.nv, *tnext = d.tempe + (size_t)(parity ^ 1) * d.nv;
-    const double tn = Tcur + dtf;
     const int xi = BC ? d.vext[v] : -1;  // boundary-condition external
     const int dof = BC ? d.ext[xi].dof : 0;
     if (BC && dtf != 0.0f && dof == EXT_ALL) {  // isFixedAll (VX3_Voxel.cu:167-173)
@@ -449,8 +486,8 @@ template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &
         F = sub(F, scl(vel, m.c_glob));
         F.z += m.grav_force;
         if (rp.collision) {
-            const double4 c = d.contact[v];
-            F = sub(F, V3<float>{(float)c.x, (float)c.y, (float)c.z});
+            const float4 c = reinterpret_cast<const float4 *>(d.contact)[v];
+            F = sub(F, V3<float>{c.x, c.y, c.z});
         }
         if (rp.cilia) {  // CiliaForce * Cilia (VX3_Voxel.cu:376), evaluated in FP64 by k_extra_forces
             const double4 c = d.cfv[v];
@@ -470,7 +507,10 @@ template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &
                 if (stat) {
                     if (F.x * F.x + F.y * F.y > (m.mu_s * normal) * (m.mu_s * normal)) stat = false;
                 } else {
-                    F = sub(F, scl(normalized(V3<float>{vel.x, vel.y, 0}), m.mu_k * normal));
+                    // the horizontal velocity's direction (normalized(): unchanged when zero)
+                    const float h2 = vel.x * vel.x + vel.y * vel.y;
+                    const float k = h2 > 0.0f ? rsqrtf(h2) : 1.0f;
+                    F = sub(F, scl(V3<float>{vel.x * k, vel.y * k, 0}, m.mu_k * normal));
                 }
             } else {
                 stat = false;
@@ -511,7 +551,13 @@ template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &
         float dw, sfac;
         if (m2 * m2 < 5.328e-15f) {
             dw = -0.5f * m2;
-            sfac = 1.0f - m2 / 6.0f;
+            sfac = 1.0f - m2 * (1.0f / 6.0f);
+        } else if (m2 < 0.25f) {
+            // |theta| < 0.5 rad: cos|theta| - 1 and sin|theta| / |theta| as their Taylor series in
+            // m2 = |theta|^2, truncated where the next term is below 3e-10 (no square root,
+            // sine or division; the same values to FP32 rounding)
+            dw = m2 * (-0.5f + m2 * (1.0f / 24 + m2 * (-1.0f / 720 + m2 * (1.0f / 40320 - m2 * (1.0f / 3628800)))));
+            sfac = 1.0f + m2 * (-1.0f / 6 + m2 * (1.0f / 120 + m2 * (-1.0f / 5040 + m2 * (1.0f / 362880))));
         } else {
             const float mm = sqrtf(m2);
             float sn, cs;
@@ -564,7 +610,8 @@ template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &
     }
     if (actuated) {  // next step's temperature and base size
         float te = tcur[v];
-        if (!(m.thermal_on_after > tn)) te = temperature_f(rp, d.phase[v], tn);
+        if (!m.toa_pos || thermal_on(d, m.thermal_on_after, r, parity, dtf))
+            te = temperature_mx(rp, d.tcyc[(size_t)parity * d.nr + r], d.phc[v], dtf);
         base_size_df(m, te, pH.w, pL.w);
         tnext[v] = te;
     }

@@ -129,20 +129,18 @@ template <class R> __device__ __forceinline__ Q4<R> from_angle_to_posx(Q4<R> q, 
 }
 
 // VX3_Link.h:134-191 (bond-local +X frame and back)
+// written as per-component selects (no branches: a warp's links mix the three axes)
 template <class R> __device__ __forceinline__ V3<R> to_axis_x(int axis, V3<R> v) {
-    if (axis == 1) return V3<R>{v.y, -v.x, v.z};
-    if (axis == 2) return V3<R>{v.z, v.y, -v.x};
-    return v;
+    const bool a1 = axis == 1, a2 = axis == 2;
+    return V3<R>{a1 ? v.y : (a2 ? v.z : v.x), a1 ? -v.x : v.y, a2 ? -v.x : v.z};
 }
 template <class R> __device__ __forceinline__ Q4<R> to_axis_xq(int axis, Q4<R> q) {
-    if (axis == 1) return Q4<R>{q.w, q.y, -q.x, q.z};
-    if (axis == 2) return Q4<R>{q.w, q.z, q.y, -q.x};
-    return q;
+    const bool a1 = axis == 1, a2 = axis == 2;
+    return Q4<R>{q.w, a1 ? q.y : (a2 ? q.z : q.x), a1 ? -q.x : q.y, a2 ? -q.x : q.z};
 }
 template <class R> __device__ __forceinline__ V3<R> to_axis_original(int axis, V3<R> v) {
-    if (axis == 1) return V3<R>{-v.y, v.x, v.z};
-    if (axis == 2) return V3<R>{-v.z, v.y, v.x};
-    return v;
+    const bool a1 = axis == 1, a2 = axis == 2;
+    return V3<R>{a1 ? -v.y : (a2 ? -v.z : v.x), a1 ? v.x : v.y, a2 ? v.x : v.z};
 }
 
 // Mixed-precision link state, in the 36 bytes per link of nine floats: a 16-byte row
