@@ -559,11 +559,11 @@ template <bool BC> __device__ __forceinline__ void voxels_mixed_body(const Dev &
             dw = m2 * (-0.5f + m2 * (1.0f / 24 + m2 * (-1.0f / 720 + m2 * (1.0f / 40320 - m2 * (1.0f / 3628800)))));
             sfac = 1.0f + m2 * (-1.0f / 6 + m2 * (1.0f / 120 + m2 * (-1.0f / 5040 + m2 * (1.0f / 362880))));
         } else {
-            const float mm = sqrtf(m2);
+            const float im = rsqrtf(m2);  // 1 / |theta|, m2 >= 0.25 here
             float sn, cs;
-            sincosf(0.5f * mm, &sn, &cs);
+            sincospif(m2 * im * 0.159154943f, &sn, &cs);  // sin, cos of |theta| / 2
             dw = -2.0f * sn * sn;
-            sfac = 2.0f * sn * cs / mm;
+            sfac = 2.0f * sn * cs * im;
         }
         const Q4<float> delta = qmul(Q4<float>{dw, th.x * sfac, th.y * sfac, th.z * sfac}, o);
         df_add(qH.x, qL.x, delta.w);
