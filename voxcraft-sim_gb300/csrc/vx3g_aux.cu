@@ -407,10 +407,10 @@ __device__ __forceinline__ void coll_check(const Dev &d, int s) {
         const float4 h = P[0], l = P[1];
         const float4 lm = reinterpret_cast<const float4 *>(d.linmom)[2 * (size_t)v];
         const VMat &m = d.vmat[d.vinfo[v].y >> 8];
-        float4 *R = d.crec + 3 * (size_t)v;
+        float4 *R = d.crec + 2 * (size_t)v;
         R[0] = make_float4(h.x, h.y, h.z, h.w + l.w);
         R[1] = make_float4(l.x, l.y, l.z, m.pstiff);
-        R[2] = make_float4(lm.x * m.mass_inv, lm.y * m.mass_inv, lm.z * m.mass_inv, m.c_col);
+        d.crec[2 * (size_t)d.nv + v] = make_float4(lm.x * m.mass_inv, lm.y * m.mass_inv, lm.z * m.mass_inv, m.c_col);
     }
     if (d.any_dyn) {  // robots whose surface follows their link table
         const uint2 vi = d.vinfo[v];

@@ -179,9 +179,10 @@ struct Dev {
     int4 *ccell;    // x: the bucket of a collision-surface voxel in the large-robot grid (-1: not binned)
     float4 *cposf;  // FP32 position per collision-surface voxel, written by the displacement check
     // mixed precision: per voxel, the contact record of the collision-surface voxels for this
-    // step, written by the displacement check: [3v] {position hi x, y, z; base size},
-    // [3v+1] {position lo x, y, z; penetrationStiffness}, [3v+2] {velocity (linMom hi / m);
-    // collision damping} -- one contiguous read per contact candidate (NULL in FP64)
+    // step, written by the displacement check: [2v] {position hi x, y, z; base size},
+    // [2v+1] {position lo x, y, z; penetrationStiffness} -- one aligned 32-byte sector per
+    // contact candidate, four voxels to a cache line -- and [2NV+v] {velocity (linMom hi /
+    // m); collision damping}, read for the candidates in contact (NULL in FP64)
     float4 *crec;
     unsigned *cpk;  // per collision-surface voxel: packed lattice word (kPackMask, kPackFixed; shared-memory path)
     float4 *cref;   // position at the last list build (w: squared displacement that forces a rebuild)

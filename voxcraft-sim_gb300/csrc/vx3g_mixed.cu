@@ -129,11 +129,11 @@ template <bool ATTACH> __global__ void __launch_bounds__(256) k_coll_eval_mixed(
     const bool att = ATTACH && d.rp[r].attach && d.acnt[r] > 0;
     V3<float> acc{0, 0, 0};
     if (n) {
-        const float4 pvH = R[3 * v], pvL = R[3 * v + 1], wv = R[3 * v + 2];
+        const float4 pvH = R[2 * v], pvL = R[2 * v + 1], wv = R[2 * d.nv + v];
         const float bv = pvH.w;  // baseSizeAverage = baseSize (isotropic)
         for (int k = 0; k < n; k++) {
             const int u = lst[k * ns];  // partner voxel, ascending
-            const float4 puH = R[3 * u], puL = R[3 * u + 1];
+            const float4 puH = R[2 * u], puL = R[2 * u + 1];  // one 32-byte sector
             // offset from the later surface voxel (voxel1) to the earlier one (voxel2)
             const float sg = u < v ? 1.0f : -1.0f;
             const float ox = sg * df_diff(puH.x, puL.x, pvH.x, pvL.x);
@@ -149,7 +149,7 @@ template <bool ATTACH> __global__ void __launch_bounds__(256) k_coll_eval_mixed(
             if (!(dist <= wd)) continue;
             const float rel = wd - dist;
             if (!(rel > 0)) continue;
-            const float4 wu = R[3 * u + 2];
+            const float4 wu = R[2 * d.nv + u];
             const float pstiff = __fdividef(2.0f * pvL.w * puL.w, pvL.w + puL.w);  // 2 / (1/a + 1/b)
             const float dampC = 0.5f * (wv.w + wu.w);
             const float ux = ox * inv, uy = oy * inv, uz = oz * inv;
