@@ -726,7 +726,7 @@ int build(vx3g_ctx *c, const vx3g_batch_desc *desc) {
         // keeps a wider skin than one rebuilt in shared memory, trading longer candidate lists
         // for fewer rebuilds (measured on the 64^3 body and the 256-robot batch)
         if (rp.ns > 0 && !rp.lchunks) {
-            rp.skin = 0.4 * R.vox_size;
+            rp.skin = 0.5 * R.vox_size;
             rp.inv_list_cell = 1.0 / (rp.cell_size + rp.skin);
         }
     }
