@@ -69,6 +69,14 @@ def cases():
     out["bern5_force_field"] = (
         wl.bernoulli_body(rng, (5, 4, 3), 0.8, ffmats, random_phase=True, temp_vary=True, temp_amplitude=20.0,
                           force_field=ff, z_offset=1), 300, 100)
+    # TurnOnThermalExpansionAfterThisManySeconds: two of three actuated materials start
+    # expanding later, at about step 129 and step 241 (dt = 2.49e-5 s)
+    rng = np.random.default_rng(17)
+    tmats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=5e5, nu=0.35, cte=0.01, thermal_on_after=0.0032),
+             wl.Material(E=8e5, nu=0.35, cte=0.008, thermal_on_after=0.006)]
+    out["bern5_thermal_delay"] = (
+        wl.bernoulli_body(rng, (5, 5, 4), 0.8, tmats, random_phase=True, temp_vary=True, temp_amplitude=30.0,
+                          enable_expansion=1, z_offset=1), 300, 100)
     # EnableCilia: per-voxel BaseCiliaForce/ShiftCiliaForce, a negative Cilia and a turn-on time
     rng = np.random.default_rng(9)
     cmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),
@@ -245,7 +253,8 @@ def nonlinear(r):
 def robot_record(r):
     g, ph = r.padded()
     mats = np.array([[m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress, m.fixed, m.is_measured,
-                      m.cilia, m.cilia_on_after, m.remove_after, m.sticky] for m in r.materials], np.float64)
+                      m.cilia, m.cilia_on_after, m.remove_after, m.sticky, m.thermal_on_after] for m in r.materials],
+                    np.float64)
     settings = dict(vox_size=r.vox_size, dt_frac=r.dt_frac, bond_damping=r.bond_damping, col_damping=r.col_damping,
                     slow_damping=r.slow_damping, gravity=r.gravity, grav_acc=r.grav_acc, floor=r.floor,
                     temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,

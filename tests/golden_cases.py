@@ -25,7 +25,8 @@ def load(name):
     mats = [wl.Material(E=m[0], nu=m[1], rho=m[2], cte=m[3], mu_static=m[4], mu_kinetic=m[5], fail_stress=m[6],
                         fixed=int(m[7]), is_measured=int(m[8]),
                         cilia=float(m[9]) if len(m) > 9 else 0.0, cilia_on_after=float(m[10]) if len(m) > 10 else 0.0,
-                        remove_after=float(m[11]) if len(m) > 11 else 0.0, sticky=int(m[12]) if len(m) > 12 else 0)
+                        remove_after=float(m[11]) if len(m) > 11 else 0.0, sticky=int(m[12]) if len(m) > 12 else 0,
+                        thermal_on_after=float(m[13]) if len(m) > 13 else 0.0)
             for m in d["materials"]]
     if "models" in d.files:  # MatModel 2/3 parameters per palette entry
         for m, md in zip(mats, json.loads(str(d["models"]))):

@@ -250,7 +250,7 @@ def robot_struct(robot):
         n, e, s = m.ss_arrays()
         ss_keep.append((e, s))
         mats[i] = VxoMaterial(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic,
-                              m.fail_stress, m.mat_model(), m.fixed, m.is_measured, 0.0,
+                              m.fail_stress, m.mat_model(), m.fixed, m.is_measured, m.thermal_on_after,
                               m.cilia, m.cilia_on_after, m.remove_after, m.plastic_mod, m.yield_stress,
                               n, None if e is None else _P(e), None if s is None else _P(s),
                               int(m.is_pacemaker), m.pacemaker_period, m.signal_value_decay, m.signal_time_delay,

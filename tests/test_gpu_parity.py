@@ -153,6 +153,10 @@ def test_both_list_builds_match_oracle():
     assert np.all(m.status() == 0)
     rel = np.linalg.norm(m.com() - b.com(), axis=1) / np.linalg.norm(b.com(), axis=1)
     assert np.all(rel <= 1e-5), rel
+    # the mixed step's contact forces (FP32, read back through the same getter) follow the FP64 ones
+    cf, cm = b.voxel_aux()["contact"], m.voxel_aux()["contact"]
+    assert np.count_nonzero(np.abs(cm).sum(1)) > 0
+    np.testing.assert_allclose(cm, cf, rtol=0, atol=1e-2 * np.abs(cf).max())
 
 
 def _ff(*trees):
@@ -304,6 +308,33 @@ def test_nonlinear_materials_mixed_matches_fp64(name):
     np.testing.assert_allclose(lm["maxstrain"], lf["maxstrain"], rtol=0, atol=1e-5)
     with pytest.raises(abi.Vx3gError, match="not implemented"):
         abi.Batch([robot], abi.PRECISION_FP64).record(10, 5)
+
+
+def test_thermal_delay_mixed_matches_fp64():
+    """TurnOnThermalExpansionAfterThisManySeconds: the delayed materials keep their initial
+    temperature until their turn-on time in both precisions, switch on in the same step,
+    and the mixed step's temperatures (the actuation phase carried as FP32 cycles) stay
+    within 1e-4 degrees of the FP64 step's; COM within 1e-5 relative."""
+    robot, d = golden_cases.load("bern5_thermal_delay")
+    g, _ = robot.padded()
+    cells = g.reshape(-1)
+    mat = cells[cells > 0] - 1
+    f = abi.Batch([robot], abi.PRECISION_FP64)
+    m = abi.Batch([robot], abi.PRECISION_MIXED)
+    for snap in (100, 200, 300):
+        f.step(100)
+        m.step(100)
+        tf, tm = f.voxel_aux()["tempe"], m.voxel_aux()["tempe"]
+        np.testing.assert_allclose(tf, d[f"s{snap}_tempe"], rtol=0, atol=1e-4)
+        for k, m_on in enumerate(robot.materials):
+            sel = mat == k
+            on = m_on.thermal_on_after <= float(d[f"s{snap}_time"][0])
+            assert np.any(tf[sel] != 0) == on, (snap, k)
+            assert np.array_equal(tm[sel] != 0, tf[sel] != 0), (snap, k)
+        np.testing.assert_allclose(tm, tf, rtol=0, atol=1e-4)
+    assert np.all(f.status() == 0) and np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - f.com(), axis=1) / np.linalg.norm(f.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
 
 
 def test_signals_mixed_matches_fp64():

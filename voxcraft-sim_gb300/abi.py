@@ -157,7 +157,7 @@ def robot_desc(robot):
         n, e, s = m.ss_arrays()
         ss_keep.append((e, s))
         mats[i] = Material(m.E, m.nu, m.rho, m.cte, m.mu_static, m.mu_kinetic, m.fail_stress,
-                           m.mat_model(), int(m.fixed), int(m.is_measured), 0.0,
+                           m.mat_model(), int(m.fixed), int(m.is_measured), float(m.thermal_on_after),
                            float(m.cilia), float(m.cilia_on_after), float(m.remove_after),
                            float(m.plastic_mod), float(m.yield_stress), n, _P(e), _P(s),
                            int(m.is_pacemaker), float(m.pacemaker_period), float(m.signal_value_decay),

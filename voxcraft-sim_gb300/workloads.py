@@ -36,6 +36,7 @@ class Material:
     cilia: float = 0.0         # Cilia (scale of the cilia force)
     cilia_on_after: float = 0.0  # TurnOnCiliaAfterThisManySeconds
     remove_after: float = 0.0  # RemoveFromSimulationAfterThisManySeconds (SecondaryExperiment; 0: never)
+    thermal_on_after: float = 0.0  # TurnOnThermalExpansionAfterThisManySeconds (actuation starts then)
     name: str = "mat"
     model: Optional[int] = None  # MatModel (0 linear, 1 linear+failure, 2 bilinear, 3 data points);
                                  # None: 0 without fail_stress, 1 with
@@ -376,6 +377,8 @@ def to_vxa(r: Robot) -> str:
             f"<Cilia>{_fmt(m.cilia)}</Cilia><TurnOnCiliaAfterThisManySeconds>{_fmt(m.cilia_on_after)}"
             "</TurnOnCiliaAfterThisManySeconds>"
             f"<RemoveFromSimulationAfterThisManySeconds>{_fmt(m.remove_after)}</RemoveFromSimulationAfterThisManySeconds>"
+            f"<TurnOnThermalExpansionAfterThisManySeconds>{_fmt(m.thermal_on_after)}"
+            "</TurnOnThermalExpansionAfterThisManySeconds>"
             f"<uStatic>{_fmt(m.mu_static)}</uStatic><uDynamic>{_fmt(m.mu_kinetic)}</uDynamic>"
             f"<Fixed>{int(m.fixed)}</Fixed><Sticky>{int(m.sticky)}</Sticky><isMeasured>{int(m.is_measured)}</isMeasured>"
             f"<isPaceMaker>{int(m.is_pacemaker)}</isPaceMaker><PaceMakerPeriod>{_fmt(m.pacemaker_period)}</PaceMakerPeriod>"
