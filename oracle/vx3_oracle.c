@@ -606,6 +606,17 @@ void *vxo_create(const vxo_robot *r) {
     for (int i = 0; i < S->nvm; i++) vmat_import(&S->vm[i], &r->materials[i], r);
     S->mat_removed = (int *)calloc(S->nvm ? S->nvm : 1, sizeof(int));
 
+    /* initial temperature with Thermal/TempEnabled: CVX_Sim::UpdateMatTemps at import
+     * (VXA/VX_Sim.cpp:467-478) sets every voxel to CVX_Environment::UpdateCurTemp(0) - TempBase
+     * (old/VX_Environment.cpp:327-346): TempBase + TempAmplitude without VaryTempEnabled,
+     * TempBase + TempAmplitude*sin(0) with it, 0 for a TempPeriod of 0; VX3_Voxel takes it over
+     * (VX3_Voxel.cu:12) and, without varying temperature, keeps it */
+    float temp0 = 0.0f;
+    if (r->temp_enabled) {
+        const double cur = r->vary_temp ? (r->temp_period == 0 ? 0.0 : r->temp_base + r->temp_amplitude * sin(0.0))
+                                        : r->temp_base + r->temp_amplitude;
+        temp0 = (float)((float)cur - r->temp_base);
+    }
     int *vid = (int *)malloc(sizeof(int) * (ncell ? ncell : 1));
     S->nv = 0;
     for (int c = 0; c < ncell; c++) vid[c] = r->lattice[c] > 0 ? S->nv++ : -1;
@@ -625,7 +636,7 @@ void *vxo_create(const vxo_robot *r) {
         v->pos = V(x * r->vox_size, y * r->vox_size, z * r->vox_size);
         v->orient = qident();
         v->flags = F_STATIC | (r->floor_enabled ? F_FLOOR : 0);
-        v->tempe = 0.0f;
+        v->tempe = temp0;
         v->prevDt = 0.0f;
         v->phase = r->phase ? r->phase[c] : 0.0;
         v->attach_ok = 1; /* VX3_Voxel.h:302 */

@@ -77,6 +77,15 @@ def cases():
     out["bern5_thermal_delay"] = (
         wl.bernoulli_body(rng, (5, 5, 4), 0.8, tmats, random_phase=True, temp_vary=True, temp_amplitude=30.0,
                           enable_expansion=1, z_offset=1), 300, 100)
+    # Thermal/TempEnabled without VaryTempEnabled: every voxel starts at TempBase + TempAmplitude, so
+    # one material of a two-material block is expanded by 20% from the start (a bimetal that bends
+    # as it drops)
+    smats = [wl.Material(E=5e5, nu=0.35, cte=0.01), wl.Material(E=5e5, nu=0.35, cte=0.0)]
+    sgrid = np.ones((3, 4, 6), np.uint8)
+    sgrid[:, :2, :] = 2
+    out["bimetal_static_expansion"] = (
+        wl.Robot(grid=sgrid, materials=smats, temp_enabled=True, temp_amplitude=20.0, enable_expansion=1,
+                 z_offset=1), 300, 100)
     # EnableCilia: per-voxel BaseCiliaForce/ShiftCiliaForce, a negative Cilia and a turn-on time
     rng = np.random.default_rng(9)
     cmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),
@@ -258,7 +267,8 @@ def robot_record(r):
     settings = dict(vox_size=r.vox_size, dt_frac=r.dt_frac, bond_damping=r.bond_damping, col_damping=r.col_damping,
                     slow_damping=r.slow_damping, gravity=r.gravity, grav_acc=r.grav_acc, floor=r.floor,
                     temp_vary=r.temp_vary, temp_amplitude=r.temp_amplitude, temp_period=r.temp_period,
-                    temp_base=r.temp_base, enable_expansion=r.enable_expansion, enable_collision=r.enable_collision,
+                    temp_base=r.temp_base, temp_enabled=r.temp_enabled, enable_expansion=r.enable_expansion,
+                    enable_collision=r.enable_collision,
                     volume_effects=r.volume_effects, force_field=r.force_field, enable_cilia=r.enable_cilia,
                     enable_detach=r.enable_detach, secondary_experiment=r.secondary_experiment,
                     enable_signals=r.enable_signals, enable_attach=r.enable_attach, safety_guard=r.safety_guard,

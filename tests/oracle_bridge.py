@@ -258,7 +258,7 @@ def robot_struct(robot):
     Z, Y, X = g.shape
     r = VxoRobot(X, Y, Z, _P(lattice), None if phase is None else _P(phase), len(robot.materials), mats,
                  robot.vox_size, robot.dt_frac, robot.grav_acc, int(robot.floor),
-                 robot.temp_amplitude, robot.temp_period, robot.temp_base, 0, int(robot.temp_vary),
+                 robot.temp_amplitude, robot.temp_period, robot.temp_base, int(robot.temp_enabled), int(robot.temp_vary),
                  int(robot.enable_expansion), int(robot.enable_collision), int(robot.volume_effects),
                  robot.bond_damping, robot.col_damping, robot.slow_damping)
     progs = _force_field_tokens(robot)

@@ -337,6 +337,22 @@ def test_thermal_delay_mixed_matches_fp64():
     assert np.all(rel <= 1e-5), rel
 
 
+def test_static_expansion_mixed_matches_fp64():
+    """Thermal/TempEnabled without VaryTempEnabled: every voxel starts, and stays, at
+    TempAmplitude above TempBase (a bimetal block, one material expanded by 20%, bends as it
+    drops); the mixed step follows the FP64 one (COM within 1e-5 relative)."""
+    robot, d = golden_cases.load("bimetal_static_expansion")
+    f = abi.Batch([robot], abi.PRECISION_FP64)
+    m = abi.Batch([robot], abi.PRECISION_MIXED)
+    f.step(300)
+    m.step(300)
+    assert np.all(f.voxel_aux()["tempe"] == np.float32(robot.temp_amplitude))
+    assert np.all(m.voxel_aux()["tempe"] == np.float32(robot.temp_amplitude))
+    assert np.all(f.status() == 0) and np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - f.com(), axis=1) / np.linalg.norm(f.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
+
+
 def test_signals_mixed_matches_fp64():
     """EnableSignals with shifting cilia: the mixed-precision context carries the same
     signals (they depend on time, links and materials only) and follows the FP64 COM

@@ -170,7 +170,8 @@ def robot_desc(robot):
             le = np.concatenate([np.zeros((robot.z_offset,) + le.shape[1:]), le], axis=0)
         log10E = np.ascontiguousarray(le.reshape(-1).astype(np.float64))
     d = RobotDesc(X, Y, Z, _P(lattice), _P(phase), len(robot.materials), mats, robot.vox_size, robot.dt_frac,
-                  robot.grav_acc, int(robot.floor), robot.temp_amplitude, robot.temp_period, robot.temp_base, 0,
+                  robot.grav_acc, int(robot.floor), robot.temp_amplitude, robot.temp_period, robot.temp_base,
+                  int(robot.temp_enabled),
                   int(robot.temp_vary), int(robot.enable_expansion), int(robot.enable_collision),
                   int(robot.volume_effects), robot.bond_damping, robot.col_damping, robot.slow_damping,
                   _P(log10E))

@@ -104,6 +104,8 @@ class Robot:
     temp_amplitude: float = 0.0
     temp_period: float = 0.2
     temp_base: float = 25.0
+    temp_enabled: bool = False            # Environment/Thermal/TempEnabled: without VaryTempEnabled, every voxel
+                                          # starts (and stays) at TempBase + TempAmplitude (static expansion)
     enable_expansion: int = 0
     enable_collision: bool = False
     volume_effects: bool = True
@@ -355,7 +357,7 @@ def to_vxa(r: Robot) -> str:
            _bcs_xml(r),
            f"<Gravity><GravEnabled>{int(r.gravity)}</GravEnabled><GravAcc>{_fmt(r.grav_acc)}</GravAcc>"
            f"<FloorEnabled>{int(r.floor)}</FloorEnabled></Gravity>",
-           "<Thermal><TempEnabled>0</TempEnabled>"
+           f"<Thermal><TempEnabled>{int(r.temp_enabled)}</TempEnabled>"
            f"<TempAmplitude>{_fmt(r.temp_amplitude)}</TempAmplitude><TempBase>{_fmt(r.temp_base)}</TempBase>"
            f"<VaryTempEnabled>{int(r.temp_vary)}</VaryTempEnabled><TempPeriod>{_fmt(r.temp_period)}</TempPeriod>"
            "</Thermal>",
