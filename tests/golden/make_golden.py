@@ -86,6 +86,16 @@ def cases():
     out["bimetal_static_expansion"] = (
         wl.Robot(grid=sgrid, materials=smats, temp_enabled=True, temp_amplitude=20.0, enable_expansion=1,
                  z_offset=1), 300, 100)
+    # Settings every other case leaves at their defaults: global (slow) damping, bond and
+    # collision damping other than 1, DtFrac 0.5 and a weaker gravity, on an actuated,
+    # self-colliding body
+    rng = np.random.default_rng(19)
+    dmats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=3e5, nu=0.3, cte=0.005, mu_static=0.6,
+                                                                mu_kinetic=0.3)]
+    dmp = wl.bernoulli_body(rng, (6, 5, 4), 0.75, dmats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                            enable_collision=True, enable_expansion=1, z_offset=1)
+    dmp.slow_damping, dmp.bond_damping, dmp.col_damping, dmp.dt_frac, dmp.grav_acc = 0.05, 0.4, 0.7, 0.5, -5.0
+    out["bern6_damping_settings"] = (dmp, 300, 100)
     # EnableCilia: per-voxel BaseCiliaForce/ShiftCiliaForce, a negative Cilia and a turn-on time
     rng = np.random.default_rng(9)
     cmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),

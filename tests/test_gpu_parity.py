@@ -353,6 +353,22 @@ def test_static_expansion_mixed_matches_fp64():
     assert np.all(rel <= 1e-5), rel
 
 
+def test_damping_settings_mixed_matches_fp64():
+    """Global (slow) damping, bond and collision damping other than 1, DtFrac 0.5 and a weaker
+    gravity on an actuated, self-colliding body: the mixed step follows the FP64 one (COM
+    within 1e-5 relative, contact forces on the same voxels)."""
+    robot, d = golden_cases.load("bern6_damping_settings")
+    f = abi.Batch([robot], abi.PRECISION_FP64)
+    m = abi.Batch([robot], abi.PRECISION_MIXED)
+    f.step(300)
+    m.step(300)
+    assert np.all(f.status() == 0) and np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - f.com(), axis=1) / np.linalg.norm(f.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
+    cf, cm = f.voxel_aux()["contact"], m.voxel_aux()["contact"]
+    assert np.array_equal(np.abs(cf).sum(1) > 0, np.abs(cm).sum(1) > 0)
+
+
 def test_signals_mixed_matches_fp64():
     """EnableSignals with shifting cilia: the mixed-precision context carries the same
     signals (they depend on time, links and materials only) and follows the FP64 COM
