@@ -96,6 +96,21 @@ def cases():
                             enable_collision=True, enable_expansion=1, z_offset=1)
     dmp.slow_damping, dmp.bond_damping, dmp.col_damping, dmp.dt_frac, dmp.grav_acc = 0.05, 0.4, 0.7, 0.5, -5.0
     out["bern6_damping_settings"] = (dmp, 300, 100)
+    # Material properties every other case leaves alike: densities 400 and 2500 kg/m^3,
+    # Poisson's ratios 0.45 and 0.2, a material left out of the centre of mass (isMeasured 0)
+    # and a Fixed one, on an actuated, self-colliding body
+    rng = np.random.default_rng(23)
+    pmats = [wl.Material(E=6e5, nu=0.45, rho=400.0, cte=0.01),
+             wl.Material(E=2e6, nu=0.2, rho=2500.0, cte=0.004, is_measured=0),
+             wl.Material(E=1e6, nu=0.35, rho=1500.0, cte=0.008),
+             wl.Material(E=1e6, nu=0.35, fixed=1)]
+    pg = wl.bernoulli_body(rng, (6, 5, 4), 0.8, pmats[:3], random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                           enable_collision=True, enable_expansion=1, z_offset=1)
+    occ = np.argwhere(pg.grid[1:] > 0)  # two voxels above the body's bottom layer held Fixed
+    for z, y, x in occ[rng.choice(len(occ), 2, replace=False)]:
+        pg.grid[z + 1, y, x] = 4
+    pg.materials = pmats
+    out["bern6_density_measured_fixed"] = (pg, 300, 100)
     # EnableCilia: per-voxel BaseCiliaForce/ShiftCiliaForce, a negative Cilia and a turn-on time
     rng = np.random.default_rng(9)
     cmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),

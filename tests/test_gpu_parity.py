@@ -60,6 +60,7 @@ def test_fp64_against_reference_golden(name):
         np.testing.assert_allclose(aux["contact"], d[f"s{snap}_contact"], rtol=1e-6, atol=1e-9)
         np.testing.assert_allclose(lk["strain"], d[f"s{snap}_strain"], rtol=0, atol=1e-6)
         np.testing.assert_allclose(b.time()[0], d[f"s{snap}_time"][0], rtol=1e-12)
+        np.testing.assert_allclose(b.com()[0], d[f"s{snap}_com"], rtol=1e-12)  # measured voxels only
         assert np.float32(b.dt()[0]) == d[f"s{snap}_dt"][0]
         if f"s{snap}_signal" in d.files:  # EnableSignals: localSignal per voxel
             np.testing.assert_allclose(b.signals(), d[f"s{snap}_signal"], rtol=1e-12, atol=0)
@@ -353,11 +354,14 @@ def test_static_expansion_mixed_matches_fp64():
     assert np.all(rel <= 1e-5), rel
 
 
-def test_damping_settings_mixed_matches_fp64():
-    """Global (slow) damping, bond and collision damping other than 1, DtFrac 0.5 and a weaker
-    gravity on an actuated, self-colliding body: the mixed step follows the FP64 one (COM
-    within 1e-5 relative, contact forces on the same voxels)."""
-    robot, d = golden_cases.load("bern6_damping_settings")
+@pytest.mark.parametrize("name", ["bern6_damping_settings", "bern6_density_measured_fixed"])
+def test_settings_mixed_matches_fp64(name):
+    """Settings every other case leaves at their defaults -- global (slow) damping, bond and
+    collision damping other than 1, DtFrac 0.5 and a weaker gravity; densities, Poisson's
+    ratios, a material left out of the centre of mass and Fixed voxels -- on actuated,
+    self-colliding bodies: the mixed step follows the FP64 one (COM within 1e-5 relative,
+    contact forces on the same voxels)."""
+    robot, d = golden_cases.load(name)
     f = abi.Batch([robot], abi.PRECISION_FP64)
     m = abi.Batch([robot], abi.PRECISION_MIXED)
     f.step(300)

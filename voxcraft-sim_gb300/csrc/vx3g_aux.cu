@@ -1333,7 +1333,8 @@ __global__ void k_coll_eval(Dev d) {
     }
     if (s >= d.ns) return;
     const int v = d.csurf[s];
-    const int r = (int)d.vinfo[v].x;
+    const uint2 vi = d.vinfo[v];
+    const int r = (int)vi.x;
     if (d.cflag[1 + r]) d.cflag[1 + r] = 0;
     if (d.status[r] != 0) return;
     const int n = d.nnb[s];
@@ -1344,6 +1345,10 @@ __global__ void k_coll_eval(Dev d) {
     // (a link makes its robot rebuild its lists in the next step)
     const bool att = d.narob && d.rp[r].attach && d.acnt[r] > 0;
     V3<double> acc{0, 0, 0};
+    if (!runs_force(d, d.rp[r].bcs, v, vi.y)) {  // its contactForce is never cleared: the pairs add to it
+        const double4 c = d.contact[v];
+        acc = V3<double>{c.x, c.y, c.z};
+    }
     if (n) {
         const float4 pf = pos_f(d, v);
         const double4 pv = load_state(d, d.pos, v);

@@ -128,6 +128,10 @@ template <bool ATTACH> __global__ void __launch_bounds__(256) k_coll_eval_mixed(
     // pairs linked by this step's attachment: contact added, then taken back
     const bool att = ATTACH && d.rp[r].attach && d.acnt[r] > 0;
     V3<float> acc{0, 0, 0};
+    if (!runs_force(d, d.rp[r].bcs, v, vi.y)) {  // its contactForce is never cleared: the pairs add to it
+        const float4 c = reinterpret_cast<const float4 *>(d.contact)[v];
+        acc = V3<float>{c.x, c.y, c.z};
+    }
     if (n) {
         const float4 pvH = R[2 * v], pvL = R[2 * v + 1], wv = R[2 * d.nv + v];
         const float bv = pvH.w;  // baseSizeAverage = baseSize (isotropic)

@@ -143,6 +143,16 @@ template <class R> __device__ __forceinline__ V3<R> to_axis_original(int axis, V
     return V3<R>{a1 ? -v.y : (a2 ? -v.z : v.x), a1 ? v.x : v.y, a2 ? v.x : v.z};
 }
 
+// The voxel runs VX3_Voxel::force() in its timeStep (VX3_Voxel.cu:162-176): not of a Fixed
+// material, not fixed in all DOFs by a boundary condition.  force() clears the voxel's
+// contactForce (VX3_Voxel.cu:373-374); on those two kinds of voxel the contacts add up over the
+// steps.  (A removed voxel, also flagged VF_FIXED, has no contacts and reports none.)
+__device__ __forceinline__ bool runs_force(const Dev &d, int bcs, int v, uint32_t vflags) {
+    if ((vflags & VF_FIXED) && d.vmat[vflags >> 8].fixed) return false;
+    if (bcs && d.vext[v] >= 0 && d.ext[d.vext[v]].dof == EXT_ALL) return false;
+    return true;
+}
+
 // Mixed-precision link state, in the 36 bytes per link of nine floats: a 16-byte row
 // {pos2.x, pos2.y, pos2.z, angle2v.x} per link, an 8-byte row {angle2v.y, angle2v.z} per
 // link, then angle1v's three components, component-major (read and written only for
