@@ -111,6 +111,13 @@ def cases():
         pg.grid[z + 1, y, x] = 4
     pg.materials = pmats
     out["bern6_density_measured_fixed"] = (pg, 300, 100)
+    # A robot of one voxel (no links: the time step from the voxel's own stiffness), actuated,
+    # dropped onto the floor, where it sticks and slips as it breathes
+    one = wl.Robot(grid=np.ones((1, 1, 1), np.uint8), materials=[wl.Material(E=1e6, nu=0.35, cte=0.01,
+                                                                             mu_static=0.4, mu_kinetic=0.2)],
+                   phase=np.full((1, 1, 1), 0.3), temp_vary=True, temp_amplitude=39.0, enable_expansion=1,
+                   z_offset=1)
+    out["voxel1_actuated_drop"] = (one, 1500, 500)
     # EnableCilia: per-voxel BaseCiliaForce/ShiftCiliaForce, a negative Cilia and a turn-on time
     rng = np.random.default_rng(9)
     cmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),

@@ -94,6 +94,36 @@ def test_fp64_batch_matches_oracle_per_step():
         np.testing.assert_allclose(b.com()[i], s.com(), rtol=1e-12)
 
 
+def test_batch_with_linkless_robot_matches_oracle():
+    """A robot of one voxel (no links) between two others in one batch, FP64 and mixed:
+    the batch's link offsets skip it, its time step comes from its own stiffness, and every
+    robot follows the oracle (FP64 within the position bar; mixed COM within 1e-5)."""
+    rng = np.random.default_rng(41)
+    mats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=3e5, nu=0.35, cte=0.01)]
+    one = wl.Robot(grid=np.ones((1, 1, 1), np.uint8), materials=[wl.Material(E=5e5, nu=0.35, cte=0.01)],
+                   phase=np.full((1, 1, 1), 0.7), temp_vary=True, temp_amplitude=39.0, enable_expansion=1,
+                   z_offset=1)
+    robots = [wl.bernoulli_body(rng, (4, 3, 3), 0.8, mats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                                enable_collision=True, z_offset=1),
+              one, wl.solid_block(3)]
+    b = abi.Batch(robots, abi.PRECISION_FP64)
+    assert b.link_offset[1] == b.link_offset[2]  # no links of its own
+    sims = [ob.oracle_sim(r) for r in robots]
+    for _ in range(4):
+        b.step(50)
+        st = b.state()
+        for i, (r, s) in enumerate(zip(robots, sims)):
+            s.step(50)
+            err = np.max(np.abs(_robot_slice(b, i, st["pos"]) - s.voxels()["pos"]))
+            assert err <= POS_TOL * r.vox_size, f"robot {i}: {err:.3e}"
+            assert np.float32(b.dt()[i]) == np.float32(s.dt())
+    m = abi.Batch(robots, abi.PRECISION_MIXED)
+    m.step(200)
+    assert np.all(b.status() == 0) and np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - b.com(), axis=1) / np.linalg.norm(b.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
+
+
 def test_batch_invariance_and_determinism():
     robots = _seeded_batch(5, n=4)
     together = abi.Batch(robots, abi.PRECISION_FP64)
