@@ -118,6 +118,14 @@ def cases():
                    phase=np.full((1, 1, 1), 0.3), temp_vary=True, temp_amplitude=39.0, enable_expansion=1,
                    z_offset=1)
     out["voxel1_actuated_drop"] = (one, 1500, 500)
+    # A lattice of 2.5 cm voxels (every other case uses 1 cm): masses, stiffnesses, the
+    # collision cutoff and the floor scale with it
+    rng = np.random.default_rng(29)
+    vmats = [wl.Material(E=1e6, nu=0.35, cte=0.01), wl.Material(E=4e5, nu=0.35, cte=0.01)]
+    big = wl.bernoulli_body(rng, (5, 5, 4), 0.8, vmats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                            enable_collision=True, enable_expansion=1, z_offset=1)
+    big.vox_size = 0.025
+    out["bern5_voxsize_25mm"] = (big, 300, 100)
     # EnableCilia: per-voxel BaseCiliaForce/ShiftCiliaForce, a negative Cilia and a turn-on time
     rng = np.random.default_rng(9)
     cmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),
