@@ -126,6 +126,15 @@ def cases():
                             enable_collision=True, enable_expansion=1, z_offset=1)
     big.vox_size = 0.025
     out["bern5_voxsize_25mm"] = (big, 300, 100)
+    # Link failure with Poisson's ratio (the failure stress of the volume-effects model) and
+    # detach: an actuated block whose softer links fail and leave the lattice
+    rng = np.random.default_rng(31)
+    fmats = [wl.Material(E=2e5, nu=0.3, fail_stress=3000.0, cte=0.01, mu_static=0.3, mu_kinetic=0.2),
+             wl.Material(E=6e5, nu=0.4, cte=0.005)]
+    fb = wl.bernoulli_body(rng, (4, 4, 4), 1.0, fmats, random_phase=True, temp_vary=True, temp_amplitude=39.0,
+                           enable_collision=True, enable_expansion=1, z_offset=0)
+    fb.enable_detach = True
+    out["block4_fail_poisson_detach"] = (fb, 300, 100)
     # EnableCilia: per-voxel BaseCiliaForce/ShiftCiliaForce, a negative Cilia and a turn-on time
     rng = np.random.default_rng(9)
     cmats = [wl.Material(E=1e6, nu=0.35, cte=0.01, cilia=1.0),
