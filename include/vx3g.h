@@ -236,7 +236,9 @@ int vx3g_get_state(vx3g_ctx *ctx, double *pos, double *orient, double *linmom, d
 int vx3g_set_state(vx3g_ctx *ctx, const double *pos, const double *orient, const double *linmom,
                    const double *angmom);
 /* tempe: float per voxel; flags: reference voxel bool-state bits (FLOOR_ENABLED 4,
- * FLOOR_STATIC_FRICTION 8); contact: 3 doubles per voxel (last step's contact force). */
+ * FLOOR_STATIC_FRICTION 8); contact: 3 doubles per voxel (last step's contact force; on a
+ * voxel of a Fixed material or with all DOFs fixed by a boundary condition, which never
+ * reaches VX3_Voxel::force() where the reference clears it, the sum over all steps so far). */
 int vx3g_get_voxel_aux(vx3g_ctx *ctx, float *tempe, int32_t *flags, double *contact);
 /* Link state in the reference's link order (each robot's lattice links, then its runtime
  * links in creation order, then its unused reserve, reported as gone): strain, maxStrain (float),
