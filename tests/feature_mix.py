@@ -34,3 +34,39 @@ def robot(seed):
         robot.force_field = [("mtMUL", C(2e-3), ("mtSIN", ("mtMUL", C(40.0), V("t")))), None,
                              ("mtMUL", C(-0.2), ("mtSUB", V("z"), C(0.02)))]
     return robot
+
+
+def robot_settings(seed):
+    """Seeded random robots over the settings the fixed workloads leave at their defaults:
+    densities, Poisson's ratios, CTEs, friction, isMeasured, thermal turn-on delays, Fixed
+    voxels, lattice size, DtFrac, global/bond/collision damping, gravity, and a static
+    temperature (TempEnabled without VaryTempEnabled) for the robots that do not actuate."""
+    rng = np.random.default_rng(2000 + seed)
+    nmat = int(rng.integers(2, 5))
+    mats = []
+    for k in range(nmat):
+        mats.append(wl.Material(E=float(10 ** rng.uniform(4.5, 6.5)), nu=float(rng.choice([0.0, 0.2, 0.35, 0.45])),
+                                rho=float(rng.choice([400.0, 1000.0, 2500.0])),
+                                cte=float(rng.choice([0.0, 0.005, 0.01])), mu_static=float(rng.uniform(0.2, 1.0)),
+                                mu_kinetic=float(rng.uniform(0.05, 0.3)), is_measured=int(rng.choice([1, 1, 0])),
+                                thermal_on_after=float(rng.choice([0.0, 0.0, 0.002]))))
+    vary = seed % 2 == 0
+    dims = tuple(int(x) for x in rng.integers(3, 7, size=3))
+    robot = wl.bernoulli_body(rng, dims, 0.85, mats, random_phase=True, temp_vary=vary,
+                              temp_amplitude=float(rng.uniform(10, 40) if vary else rng.uniform(5, 25)),
+                              enable_collision=seed % 4 < 2, enable_expansion=int(seed % 3 != 1),
+                              z_offset=int(rng.integers(0, 2)))
+    robot.temp_enabled = not vary
+    robot.volume_effects = seed % 4 != 3
+    robot.vox_size = float(rng.choice([0.005, 0.01, 0.02]))
+    robot.dt_frac = float(rng.uniform(0.4, 0.95))
+    robot.slow_damping = float(rng.choice([0.0, 0.02, 0.1]))
+    robot.bond_damping = float(rng.uniform(0.3, 1.2))
+    robot.col_damping = float(rng.uniform(0.5, 1.5))
+    robot.grav_acc = float(rng.choice([-9.81, -4.0]))
+    if seed % 3 == 0:  # one or two voxels of a Fixed material
+        robot.materials = mats + [wl.Material(E=1e6, nu=0.35, fixed=1)]
+        occ = np.argwhere(robot.grid > 0)
+        for z, y, x in occ[rng.choice(len(occ), min(2, len(occ) - 1), replace=False)]:
+            robot.grid[z, y, x] = len(robot.materials)
+    return robot

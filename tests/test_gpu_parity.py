@@ -611,6 +611,31 @@ def test_full_size_single_body_properties():
     assert np.all(runs[0].status() == 0)
 
 
+def test_settings_mix_batch_matches_oracle():
+    """Eight seeded robots over densities, Poisson's ratios, isMeasured, thermal delays,
+    Fixed voxels, lattice sizes, DtFrac, damping, gravity and static temperature, in one
+    batch: the FP64 kernels follow the oracle robot by robot (positions within 1e-6 voxel
+    sizes, centres of mass to 1e-12), and the mixed kernels follow the FP64 ones (COM within
+    1e-5 relative)."""
+    import feature_mix
+    robots = [feature_mix.robot_settings(s) for s in range(8)]
+    b = abi.Batch(robots, abi.PRECISION_FP64)
+    sims = [ob.oracle_sim(r) for r in robots]
+    for _ in range(4):
+        b.step(60)
+        pos, com = b.state()["pos"], b.com()
+        for i, (r, s) in enumerate(zip(robots, sims)):
+            s.step(60)
+            err = np.max(np.abs(_robot_slice(b, i, pos) - s.voxels()["pos"]))
+            assert err <= POS_TOL * r.vox_size, f"robot {i}: {err:.3e}"
+            np.testing.assert_allclose(com[i], s.com(), rtol=1e-12, atol=1e-15)
+    m = abi.Batch(robots, abi.PRECISION_MIXED)
+    m.step(240)
+    assert np.all(b.status() == 0) and np.all(m.status() == 0)
+    rel = np.linalg.norm(m.com() - b.com(), axis=1) / np.linalg.norm(b.com(), axis=1)
+    assert np.all(rel <= 1e-5), rel
+
+
 def test_fp64_feature_mix_batch_matches_oracle():
     """Eight seeded robots combining collision, detach, material removal, cilia and
     force fields, in one batch: the FP64 kernels follow the oracle robot by robot
