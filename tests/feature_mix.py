@@ -70,3 +70,37 @@ def robot_settings(seed):
         for z, y, x in occ[rng.choice(len(occ), min(2, len(occ) - 1), replace=False)]:
             robot.grid[z, y, x] = len(robot.materials)
     return robot
+
+
+def robot_dynamic(seed):
+    """Seeded random robots over the run-time features together: pacemaker signals driving
+    cilia, boundary-condition regions (fixed DOFs, forces, torques, displacements),
+    attachment of Sticky materials, detach, on actuated, self-colliding bodies."""
+    rng = np.random.default_rng(3000 + seed)
+    sticky = seed % 2 == 0
+    mats = [wl.Material(E=float(10 ** rng.uniform(5.0, 6.3)), nu=0.0 if sticky else 0.35, cte=0.01,
+                        sticky=int(sticky), cilia=float(rng.choice([0.0, 0.6])),
+                        fail_stress=float(rng.choice([0.0, 4000.0])) if not sticky else 0.0,
+                        is_pacemaker=int(seed % 3 == 0), pacemaker_period=0.002,
+                        mu_static=float(rng.uniform(0.3, 1.0)), mu_kinetic=float(rng.uniform(0.05, 0.3))),
+            wl.Material(E=float(10 ** rng.uniform(5.0, 6.3)), nu=0.0, cte=float(rng.choice([0.0, 0.01])),
+                        sticky=int(sticky), cilia=float(rng.choice([0.0, -0.4])))]
+    dims = tuple(int(x) for x in rng.integers(4, 7, size=3))
+    robot = wl.bernoulli_body(rng, dims, 0.8, mats, random_phase=True, temp_vary=True,
+                              temp_amplitude=float(rng.uniform(20, 39)), enable_collision=True, enable_expansion=1,
+                              z_offset=int(rng.integers(0, 2)))
+    robot.volume_effects = not sticky
+    robot.enable_attach = sticky
+    robot.safety_guard = int(rng.choice([0, 20]))
+    robot.enable_detach = not sticky
+    robot.enable_signals = seed % 3 != 2
+    robot.enable_cilia = True
+    robot.cilia_base = 1e-2 * rng.standard_normal(robot.grid.shape + (3,))
+    robot.cilia_shift = 5e-3 * rng.standard_normal(robot.grid.shape + (3,))
+    if seed % 4 < 2:  # a fixed slab at one end, a pushed region at the other
+        robot.bcs = [wl.BCRegion(prim=0, dof_fixed=int(rng.choice([7, 63])), x=0.0, y=0.0, z=0.0, dx=0.2, dy=1.0,
+                                 dz=1.0),
+                     wl.BCRegion(prim=0, dof_fixed=0, x=0.75, y=0.0, z=0.0, dx=0.25, dy=1.0, dz=1.0,
+                                 force=(0.0, 0.0, float(rng.uniform(-0.05, 0.05))),
+                                 torque=(float(rng.uniform(-1e-4, 1e-4)), 0.0, 0.0))]
+    return robot

@@ -636,6 +636,28 @@ def test_settings_mix_batch_matches_oracle():
     assert np.all(rel <= 1e-5), rel
 
 
+def test_dynamic_mix_batch_matches_oracle():
+    """Eight seeded robots over pacemaker signals driving cilia, boundary-condition regions,
+    attachment of Sticky materials and detach, in one FP64 batch: each follows the oracle
+    (positions within 1e-6 voxel sizes, the same surface sets and runtime links)."""
+    import feature_mix
+    robots = [feature_mix.robot_dynamic(s) for s in range(8)]
+    b = abi.Batch(robots, abi.PRECISION_FP64)
+    sims = [ob.oracle_sim(r) for r in robots]
+    off = b.voxel_offset
+    for _ in range(4):
+        b.step(60)
+        pos, surf, used = b.state()["pos"], b.surface(), b.links_in_use()
+        for i, (r, s) in enumerate(zip(robots, sims)):
+            s.step(60)
+            err = np.max(np.abs(_robot_slice(b, i, pos) - s.voxels()["pos"]))
+            assert err <= POS_TOL * r.vox_size, f"robot {i}: {err:.3e}"
+            mine = surf[(surf >= off[i]) & (surf < off[i + 1])] - off[i]
+            assert np.array_equal(mine, s.surface()), f"robot {i}: surface"
+            assert used[i] == s.counts()[1], f"robot {i}: links in use"
+    assert np.all(b.status() == 0)
+
+
 def test_fp64_feature_mix_batch_matches_oracle():
     """Eight seeded robots combining collision, detach, material removal, cilia and
     force fields, in one batch: the FP64 kernels follow the oracle robot by robot
