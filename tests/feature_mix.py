@@ -104,3 +104,29 @@ def robot_dynamic(seed):
                                  force=(0.0, 0.0, float(rng.uniform(-0.05, 0.05))),
                                  torque=(float(rng.uniform(-1e-4, 1e-4)), 0.0, 0.0))]
     return robot
+
+
+def robot_models(seed):
+    """Seeded random robots mixing the stress-strain models: bilinear (elastic-plastic,
+    with or without failure), data-point curves and linear materials (with or without
+    failure), Poisson's ratio on or off, on actuated bodies, some self-colliding."""
+    rng = np.random.default_rng(4000 + seed)
+    nu = float(rng.choice([0.0, 0.3]))
+    E1 = float(10 ** rng.uniform(4.8, 5.5))
+    ys = float(rng.uniform(50.0, 200.0))
+    bil = wl.Material(E=E1, nu=nu, cte=0.01, model=2, plastic_mod=E1 * float(rng.uniform(0.1, 0.5)),
+                      yield_stress=ys, fail_stress=float(rng.choice([-1.0, 6.0 * ys])))
+    s1 = float(rng.uniform(0.001, 0.003))
+    s2, s3 = s1 * float(rng.uniform(2.0, 4.0)), 0.0
+    s3 = s2 * float(rng.uniform(2.0, 4.0))
+    k1 = float(10 ** rng.uniform(4.8, 5.3))
+    f1 = k1 * s1
+    f2 = f1 + 0.5 * k1 * (s2 - s1)
+    f3 = f2 + 0.2 * k1 * (s3 - s2)
+    dat = wl.Material(E=0, nu=nu, cte=0.01, model=3, ss_strain=(0.0, s1, s2, s3), ss_stress=(0.0, f1, f2, f3))
+    lin = wl.Material(E=float(10 ** rng.uniform(4.8, 5.5)), nu=nu, cte=float(rng.choice([0.0, 0.01])),
+                      fail_stress=float(rng.choice([0.0, 800.0])))
+    dims = tuple(int(x) for x in rng.integers(4, 7, size=3))
+    return wl.bernoulli_body(rng, dims, 0.85, [bil, dat, lin], random_phase=True, temp_vary=True,
+                             temp_amplitude=float(rng.uniform(5.0, 12.0)), temp_period=0.02, enable_expansion=1,
+                             enable_collision=seed % 2 == 0, z_offset=1, volume_effects=nu > 0 or seed % 3 == 0)

@@ -658,6 +658,24 @@ def test_dynamic_mix_batch_matches_oracle():
     assert np.all(b.status() == 0)
 
 
+def test_models_mix_batch_matches_oracle():
+    """Eight seeded robots mixing bilinear (plastic), data-point and linear materials with
+    failure and Poisson's ratio, in one FP64 batch: each follows the oracle (positions
+    within 1e-6 voxel sizes)."""
+    import feature_mix
+    robots = [feature_mix.robot_models(s) for s in range(8)]
+    b = abi.Batch(robots, abi.PRECISION_FP64)
+    sims = [ob.oracle_sim(r) for r in robots]
+    for _ in range(4):
+        b.step(60)
+        pos = b.state()["pos"]
+        for i, (r, s) in enumerate(zip(robots, sims)):
+            s.step(60)
+            err = np.max(np.abs(_robot_slice(b, i, pos) - s.voxels()["pos"]))
+            assert err <= POS_TOL * r.vox_size, f"robot {i}: {err:.3e}"
+    assert np.all(b.status() == 0)
+
+
 def test_fp64_feature_mix_batch_matches_oracle():
     """Eight seeded robots combining collision, detach, material removal, cilia and
     force fields, in one batch: the FP64 kernels follow the oracle robot by robot

@@ -5,7 +5,8 @@ actuation, self-collision, detach, material removal, cilia, force fields -- and
 over the settings the fixed workloads leave at their defaults (densities, Poisson's
 ratios, isMeasured, thermal delays, Fixed voxels, lattice size, DtFrac, damping,
 gravity, static temperature) and over the run-time features together (signals,
-boundary conditions, attachment, detach), compared bit for bit: positions, orientations,
+boundary conditions, attachment, detach) and the stress-strain models together (bilinear
+with plastic unloading, data-point curves, failure, Poisson's ratio), compared bit for bit: positions, orientations,
 momenta, temperatures, contact forces, surface sets, time and centre of mass.  Skipped where the reference build is absent."""
 
 import numpy as np
@@ -18,7 +19,7 @@ pytestmark = pytest.mark.skipif(not ob.ref_available(), reason="reference host b
 
 
 @pytest.mark.parametrize("gen,seed", [("robot", s) for s in range(8)] + [("robot_settings", s) for s in range(8)]
-                         + [("robot_dynamic", s) for s in range(8)])
+                         + [("robot_dynamic", s) for s in range(8)] + [("robot_models", s) for s in range(8)])
 def test_oracle_matches_reference_build(gen, seed):
     robot = getattr(feature_mix, gen)(seed)
     a, b = ob.ref_sim(robot), ob.oracle_sim(robot)
